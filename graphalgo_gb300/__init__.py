@@ -1,0 +1,402 @@
+"""graphalgo_gb300: GB300-native masked SpGEMM C<M> = A*B over CSR graphs.
+
+Python binding (ctypes) over the C ABI in ``include/graphalgo_gb300.h``;
+the kernels live in ``graphalgo_gb300/_lib/libgraphalgo_gb300.so``, built
+in-tree by ``graphalgo_gb300.build.build()``. There is no CPU fallback: if the
+library is missing, ``lib()`` raises, and if no CUDA device is usable,
+``Context()`` raises.
+
+The entry points mirror the reference's (UAlex322/GraphAlgo) operator API:
+``mxm_masked`` for mxmm_msa / mxmm_mca / mxmm_heap / mxmm_naive
+(include/matrix_la.h:700-1277), ``mxm_cmask`` for mxmm_msa_cmask (788-891),
+``mxm_spd`` (241-270), ``tc`` for triangle_counting_masked_sandia
+(src/main.cpp:65-86), ``ktruss`` for k_truss (src/main.cpp:90-146) and ``bc``
+for betweenness_centrality_batch (include/betweenness_centrality.h:125-237).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence, Tuple
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libgraphalgo_gb300.so")
+
+# dtypes
+INT32, INT64, FP32, FP64, UINT8 = 0, 1, 2, 3, 4
+# algorithms
+MSA, MCA, HEAP, NAIVE, DOT = 0, 1, 2, 3, 4
+ALGOS = {"msa": MSA, "mca": MCA, "heap": HEAP, "naive": NAIVE, "dot": DOT}
+# options
+OPT_DEVICE_LOOPS, OPT_PROFILE, OPT_FAIL_ALLOC_AFTER = 1, 2, 3
+# status codes
+OK, ERR_INVALID_ARG, ERR_INVALID_CSR, ERR_SHAPE, ERR_DTYPE, ERR_CUDA, ERR_OOM, ERR_NO_DEVICE, \
+    ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_ADMISSION = range(11)
+
+_NP = {INT32: np.int32, INT64: np.int64, FP32: np.float32, FP64: np.float64, UINT8: np.uint8}
+_DT = {np.dtype(v): k for k, v in _NP.items()}
+
+_i64 = ctypes.c_int64
+_p = ctypes.c_void_p
+_int = ctypes.c_int
+
+
+class GaError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+        self.msg = msg
+
+
+class KernelStat(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 48), ("launches", ctypes.c_int64), ("total_ms", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load the CUDA library (raises when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with graphalgo_gb300.build.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    L.ga_last_error.restype = ctypes.c_char_p
+    L.ga_status_string.restype = ctypes.c_char_p
+    L.ga_host_free.restype = None
+    for name in ("ga_gen_rmat",):
+        getattr(L, name).argtypes = [_int, _int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_uint64, ctypes.POINTER(_i64), ctypes.POINTER(_i64),
+                                     ctypes.POINTER(_p), ctypes.POINTER(_p)]
+    L.ga_gen_er.argtypes = [_i64, _i64, ctypes.c_uint64, ctypes.POINTER(_i64), ctypes.POINTER(_i64),
+                            ctypes.POINTER(_p), ctypes.POINTER(_p)]
+    L.ga_gen_knn.argtypes = [_i64, _int, _int, ctypes.c_uint64, ctypes.POINTER(_i64), ctypes.POINTER(_i64),
+                             ctypes.POINTER(_p), ctypes.POINTER(_p)]
+    L.ga_ctx_set_option.argtypes = [_p, _int, _i64]
+    _lib = L
+    return L
+
+
+def device_count() -> int:
+    c = _int(0)
+    lib().ga_device_count(ctypes.byref(c))
+    return int(c.value)
+
+
+def _check(rc: int, ctx: Optional["Context"] = None):
+    if rc != OK:
+        L = lib()
+        msg = L.ga_last_error(ctx.handle).decode() if ctx is not None and ctx.handle else ""
+        if not msg:
+            msg = L.ga_status_string(rc).decode()
+        raise GaError(rc, msg)
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(_p)
+
+
+class Context:
+    """One CUDA context handle (device, stream, memory pool)."""
+
+    def __init__(self, device: int = 0, stream: Optional[int] = None):
+        self.handle = _p()
+        _check(lib().ga_ctx_create(int(device), _p(stream) if stream else None, ctypes.byref(self.handle)))
+
+    def close(self):
+        if self.handle:
+            lib().ga_ctx_destroy(self.handle)
+            self.handle = _p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        _check(lib().ga_ctx_sync(self.handle), self)
+
+    def stream(self) -> int:
+        s = _p()
+        _check(lib().ga_ctx_stream(self.handle, ctypes.byref(s)), self)
+        return int(s.value or 0)
+
+    def set_option(self, option: int, value: int):
+        _check(lib().ga_ctx_set_option(self.handle, int(option), int(value)), self)
+
+    def timer_start(self):
+        _check(lib().ga_timer_start(self.handle), self)
+
+    def timer_stop(self) -> float:
+        ms = ctypes.c_double()
+        _check(lib().ga_timer_stop(self.handle, ctypes.byref(ms)), self)
+        return float(ms.value)
+
+    def kernel_stats(self) -> dict:
+        n = _int()
+        _check(lib().ga_ctx_kernel_stats(self.handle, None, 0, ctypes.byref(n)), self)
+        arr = (KernelStat * max(1, n.value))()
+        _check(lib().ga_ctx_kernel_stats(self.handle, arr, n.value, ctypes.byref(n)), self)
+        return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].total_ms)) for i in range(n.value)}
+
+    def reset_kernel_stats(self):
+        _check(lib().ga_ctx_reset_kernel_stats(self.handle), self)
+
+    def mem_info(self) -> Tuple[int, int]:
+        f, t = _i64(), _i64()
+        _check(lib().ga_mem_info(self.handle, ctypes.byref(f), ctypes.byref(t)), self)
+        return int(f.value), int(t.value)
+
+
+class Csr:
+    """Device-resident CSR matrix (the reference's spMtx<T>)."""
+
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self.handle = handle
+
+    @classmethod
+    def upload(cls, ctx: Context, m: int, n: int, rst, col, val=None, dtype: Optional[int] = None) -> "Csr":
+        rst = np.ascontiguousarray(rst, dtype=np.int32)
+        col = np.ascontiguousarray(col, dtype=np.int32)
+        if val is not None:
+            val = np.ascontiguousarray(val)
+            if dtype is None:
+                dtype = _DT[val.dtype]
+            val = np.ascontiguousarray(val, dtype=_NP[dtype])
+        elif dtype is None:
+            dtype = INT32
+        h = _p()
+        _check(lib().ga_csr_upload(ctx.handle, _i64(m), _i64(n), _i64(len(col)), _ptr(rst), _ptr(col), _ptr(val),
+                                   int(dtype), ctypes.byref(h)), ctx)
+        return cls(ctx, h)
+
+    def info(self) -> Tuple[int, int, int, int]:
+        m, n, z, d = _i64(), _i64(), _i64(), _int()
+        _check(lib().ga_csr_info(self.handle, ctypes.byref(m), ctypes.byref(n), ctypes.byref(z), ctypes.byref(d)))
+        return int(m.value), int(n.value), int(z.value), int(d.value)
+
+    @property
+    def shape(self):
+        m, n, _, _ = self.info()
+        return m, n
+
+    @property
+    def nnz(self) -> int:
+        return self.info()[2]
+
+    @property
+    def dtype(self) -> int:
+        return self.info()[3]
+
+    def download(self):
+        m, n, z, d = self.info()
+        rst = np.empty(m + 1, np.int32)
+        col = np.empty(z, np.int32)
+        val = np.empty(z, _NP[d])
+        _check(lib().ga_csr_download(self.ctx.handle, self.handle, _ptr(rst), _ptr(col), _ptr(val)), self.ctx)
+        return rst, col, val
+
+    def device_ptrs(self):
+        r, c, v = _p(), _p(), _p()
+        _check(lib().ga_csr_device_ptrs(self.handle, ctypes.byref(r), ctypes.byref(c), ctypes.byref(v)))
+        return int(r.value or 0), int(c.value or 0), int(v.value or 0)
+
+    def free(self):
+        if self.handle:
+            lib().ga_csr_free(self.ctx.handle, self.handle)
+            self.handle = _p()
+
+    def __del__(self):
+        try:
+            if self.handle and self.ctx.handle:
+                self.free()
+        except Exception:
+            pass
+
+
+class Dense:
+    """Device-resident row-major dense matrix (the reference's denseMtx<T>)."""
+
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self.handle = handle
+
+    @classmethod
+    def create(cls, ctx: Context, m: int, n: int, dtype: int = FP64, values: Optional[np.ndarray] = None):
+        h = _p()
+        vals = None if values is None else np.ascontiguousarray(values, dtype=_NP[dtype])
+        _check(lib().ga_dense_create(ctx.handle, _i64(m), _i64(n), int(dtype), _ptr(vals), ctypes.byref(h)), ctx)
+        return cls(ctx, h)
+
+    @classmethod
+    def from_csr(cls, A: Csr):
+        h = _p()
+        _check(lib().ga_dense_from_csr(A.ctx.handle, A.handle, ctypes.byref(h)), A.ctx)
+        return cls(A.ctx, h)
+
+    def info(self):
+        m, n, d = _i64(), _i64(), _int()
+        _check(lib().ga_dense_info(self.handle, ctypes.byref(m), ctypes.byref(n), ctypes.byref(d)))
+        return int(m.value), int(n.value), int(d.value)
+
+    def download(self) -> np.ndarray:
+        m, n, d = self.info()
+        out = np.empty((m, n), _NP[d])
+        _check(lib().ga_dense_download(self.ctx.handle, self.handle, _ptr(out)), self.ctx)
+        return out
+
+    def free(self):
+        if self.handle:
+            lib().ga_dense_free(self.ctx.handle, self.handle)
+            self.handle = _p()
+
+    def __del__(self):
+        try:
+            if self.handle and self.ctx.handle:
+                self.free()
+        except Exception:
+            pass
+
+
+def _algo(a) -> int:
+    return ALGOS[a] if isinstance(a, str) else int(a)
+
+
+def _new(ctx, fn, *args) -> Csr:
+    h = _p()
+    _check(fn(ctx.handle, *args, ctypes.byref(h)), ctx)
+    return Csr(ctx, h)
+
+
+# ------------------------------------------------------------- operations
+def mxm_masked(algo, A: Csr, B: Csr, M: Csr) -> Csr:
+    return _new(A.ctx, lib().ga_mxm_masked, _algo(algo), A.handle, B.handle, M.handle)
+
+
+def mxm_masked_vals(algo, A: Csr, B: Csr, M: Csr, d_cvals: int):
+    _check(lib().ga_mxm_masked_vals(A.ctx.handle, _algo(algo), A.handle, B.handle, M.handle, _p(d_cvals)), A.ctx)
+
+
+def mxm_cmask(A: Csr, B: Csr, M: Csr) -> Csr:
+    return _new(A.ctx, lib().ga_mxm_cmask, A.handle, B.handle, M.handle)
+
+
+def mxm_spd(A: Csr, B: Dense, M: Csr, C: Dense):
+    _check(lib().ga_mxm_spd(A.ctx.handle, A.handle, B.handle, M.handle, C.handle), A.ctx)
+
+
+def add_nointersect(A: Csr, B: Csr) -> Csr:
+    return _new(A.ctx, lib().ga_add_nointersect, A.handle, B.handle)
+
+
+def ewise_mult_masked(A: Dense, B: Dense, M: Csr, C: Dense):
+    _check(lib().ga_ewise_mult_masked(A.ctx.handle, A.handle, B.handle, M.handle, C.handle), A.ctx)
+
+
+def fuse_ewise_mult_add(A: Dense, B: Dense, C: Dense):
+    _check(lib().ga_fuse_ewise_mult_add(A.ctx.handle, A.handle, B.handle, C.handle), A.ctx)
+
+
+def transpose(A: Csr) -> Csr:
+    return _new(A.ctx, lib().ga_transpose, A.handle)
+
+
+def extract_lower(A: Csr) -> Csr:
+    return _new(A.ctx, lib().ga_extract_lower, A.handle)
+
+
+def extract_upper(A: Csr) -> Csr:
+    return _new(A.ctx, lib().ga_extract_upper, A.handle)
+
+
+def symm_from_lower(L: Csr) -> Csr:
+    return _new(L.ctx, lib().ga_symm_from_lower, L.handle)
+
+
+def adjacency(A: Csr) -> Csr:
+    return _new(A.ctx, lib().ga_adjacency, A.handle)
+
+
+def convert(A: Csr, dtype: int) -> Csr:
+    h = _p()
+    _check(lib().ga_csr_convert(A.ctx.handle, A.handle, int(dtype), ctypes.byref(h)), A.ctx)
+    return Csr(A.ctx, h)
+
+
+def tc(algo, A: Csr, per_row: bool = True):
+    m = A.shape[0]
+    total = _i64()
+    rows = np.zeros(m, np.int64) if per_row else None
+    _check(lib().ga_tc(A.ctx.handle, _algo(algo), A.handle, ctypes.byref(total), _ptr(rows)), A.ctx)
+    return int(total.value), rows
+
+
+def tc_lu(algo, A: Csr) -> int:
+    total = _i64()
+    _check(lib().ga_tc_lu(A.ctx.handle, _algo(algo), A.handle, ctypes.byref(total)), A.ctx)
+    return int(total.value)
+
+
+def tc_vertex(algo, A: Csr) -> np.ndarray:
+    out = np.zeros(A.shape[0], np.int32)
+    _check(lib().ga_tc_vertex(A.ctx.handle, _algo(algo), A.handle, _ptr(out)), A.ctx)
+    return out
+
+
+def ktruss(algo, A: Csr, k: int) -> Tuple[Csr, int]:
+    h = _p()
+    it = _int()
+    _check(lib().ga_ktruss(A.ctx.handle, _algo(algo), A.handle, int(k), ctypes.byref(h), ctypes.byref(it)), A.ctx)
+    return Csr(A.ctx, h), int(it.value)
+
+
+def bc(A: Csr, sources: Sequence[int]) -> np.ndarray:
+    src = np.ascontiguousarray(sources, dtype=np.int32)
+    out = np.zeros(A.shape[0], np.float64)
+    _check(lib().ga_bc(A.ctx.handle, A.handle, _ptr(src), _i64(len(src)), _ptr(out)), A.ctx)
+    return out
+
+
+# ------------------------------------------------------------- generators
+def _take_host(ptr: _p, count: int) -> np.ndarray:
+    if count > 0:
+        buf = (ctypes.c_int32 * count).from_address(ptr.value)
+        out = np.frombuffer(buf, dtype=np.int32).copy()
+    else:
+        out = np.zeros(0, np.int32)
+    lib().ga_host_free(ptr)
+    return out
+
+
+def _gen(fn, *args):
+    m, z = _i64(), _i64()
+    r, c = _p(), _p()
+    _check(fn(*args, ctypes.byref(m), ctypes.byref(z), ctypes.byref(r), ctypes.byref(c)))
+    return int(m.value), _take_host(r, int(m.value) + 1), _take_host(c, int(z.value))
+
+
+def gen_rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19, seed: int = 1):
+    """Seeded R-MAT graph: (m, rst, col), symmetric, sorted, no loops or duplicates."""
+    return _gen(lib().ga_gen_rmat, int(scale), int(edge_factor), float(a), float(b), float(c), int(seed))
+
+
+def gen_er(n: int, edges: int, seed: int = 1):
+    """Seeded Erdos-Renyi G(n, m) graph with `edges` undirected edges."""
+    return _gen(lib().ga_gen_er, int(n), int(edges), int(seed))
+
+
+def gen_knn(n: int, dim: int, k: int = 30, seed: int = 1):
+    """Seeded k-NN graph of n Gaussian points in `dim` dimensions, symmetrised."""
+    return _gen(lib().ga_gen_knn, int(n), int(dim), int(k), int(seed))

@@ -1,0 +1,453 @@
+// Batched betweenness centrality (betweenness_centrality_batch,
+// include/betweenness_centrality.h:125-237) with FP64 path counts and
+// dependencies, device-resident from the first frontier to the scores.
+//
+// Layout (vertex x source pairs, ns = number of sources):
+//  * an append-only entry store (source index, sigma, bcu = 1 + delta), one
+//    record per discovered (vertex, source) pair, grouped per (level, vertex);
+//  * per level, a list of frontier rows (vertex, first entry, length) - the
+//    reference's Sigmas[d];
+//  * a visited bitmap per vertex (ns bits) - the reference's Numsp pattern;
+//  * a dense m x ns FP64 matrix W used by the backward sweep.
+// Forward level (Front<!Numsp> = A^T * Front, matrix_la.h:800-891 fused with
+// add_nointersect, matrix_la.h:337-372): one warp per unvisited vertex pulls
+// the frontier entries of its in-neighbours into a shared-memory accumulator
+// over the sources, skips sources already visited, and appends the new
+// frontier row to the store (stream compaction by atomic reservation).
+// Backward level k (betweenness_centrality.h:203-218): W<S[k]> = bcu/sigma,
+// then for every row of S[k-1]: acc = A * W restricted to its sources,
+// bcu += acc * sigma, and bc[v] += acc * sigma (the final row sum,
+// betweenness_centrality.h:220-228, accumulated as it is produced).
+// Both sweeps run as device loops (CUDA-graph WHILE nodes).
+#include "ga_device.cuh"
+#include "ga_loop.cuh"
+
+namespace ga {
+
+constexpr int kBcThreads = 256;
+constexpr int kBcWarps = kBcThreads / 32;
+constexpr int kBcMaxSources = 1024;
+
+struct BcState {
+    int32_t d;        // current forward level
+    int32_t depth;    // number of non-empty levels (forward result)
+    int32_t k;        // backward level
+    int32_t done;
+    int32_t entries;  // entries appended so far (store size)
+    int32_t rows;     // frontier rows appended so far
+    int32_t overflow;
+};
+
+struct BcArgs {
+    const int32_t* atr; const int32_t* atc; const double* atv;  // A^T (in-neighbours)
+    const int32_t* ar; const int32_t* ac; const double* av;     // A (out-neighbours)
+    int64_t m;
+    int ns, words;                                              // sources, 32-bit words per vertex
+    const int32_t* sources;
+    BcState* st;
+    int32_t* level_rows;    // level_rows[d] = first row of level d
+    int32_t* cur_start[2];  // per vertex, per parity: first entry of its frontier row
+    int32_t* cur_len[2];
+    uint32_t* vbits;        // m x words
+    int32_t* vcnt;          // sources that reached each vertex
+    int32_t* es; double* ev; double* ed;  // store: source, sigma, bcu
+    int32_t* rv; int32_t* rs; int32_t* rl; // rows: vertex, start, length
+    int64_t cap_entries, cap_rows;
+    double* W;              // m x ns
+    uint32_t* inlvl;        // m bits: vertex has entries at the level being swept
+    double* bc;
+};
+
+__global__ void k_bc_init(BcArgs p) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < p.ns; j += gridDim.x * blockDim.x) {
+        int v = p.sources[j];
+        p.es[j] = j;
+        p.ev[j] = 1.0;
+        p.ed[j] = 1.0;
+        atomicOr(&p.vbits[(size_t)v * p.words + (j >> 5)], 1u << (j & 31));
+        atomicAdd(&p.vcnt[v], 1);
+        p.cur_start[0][v] = j;
+        p.cur_len[0][v] = 1;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        p.st->d = 0; p.st->depth = 0; p.st->k = 0; p.st->done = 0;
+        p.st->entries = p.ns; p.st->rows = 0; p.st->overflow = 0;
+        p.level_rows[0] = 0;
+    }
+}
+
+// One forward level: dynamic per-warp shared memory = acc[ns] doubles +
+// touched[words] + visited[words] + 32-entry flattening scratch.
+template <bool UNIT>
+__global__ void __launch_bounds__(kBcThreads) k_bc_forward(BcArgs p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned FULL = 0xffffffffu;
+    const size_t per_warp = (size_t)p.ns * sizeof(double) + 2 * (size_t)p.words * sizeof(uint32_t) +
+                            32 * (2 * sizeof(int) + sizeof(double));
+    unsigned char* base = smem + wid * ((per_warp + 15) & ~(size_t)15);
+    double* acc = reinterpret_cast<double*>(base);
+    uint32_t* touched = reinterpret_cast<uint32_t*>(base + (size_t)p.ns * sizeof(double));
+    uint32_t* vis = touched + p.words;
+    int* s_incl = reinterpret_cast<int*>(vis + p.words);
+    int* s_off = s_incl + 32;
+    double* s_a = reinterpret_cast<double*>(s_off + 32);
+
+    const int d = p.st->d;
+    if (p.st->done) return;
+    const int par = d & 1;
+    const int32_t* curS = p.cur_start[par];
+    const int32_t* curL = p.cur_len[par];
+    int32_t* nxtS = p.cur_start[par ^ 1];
+    int32_t* nxtL = p.cur_len[par ^ 1];
+
+    for (int s = lane; s < p.ns; s += 32) acc[s] = 0.0;
+    if (lane < p.words) touched[lane] = 0u;
+    __syncwarp();
+
+    const int64_t warps = (int64_t)gridDim.x * kBcWarps;
+    for (int64_t v = (int64_t)blockIdx.x * kBcWarps + wid; v < p.m; v += warps) {
+        if (p.vcnt[v] >= p.ns) {
+            if (lane == 0) nxtL[v] = 0;
+            continue;
+        }
+        if (lane < p.words) vis[lane] = p.vbits[(size_t)v * p.words + lane];
+        __syncwarp();
+        const int32_t ab = p.atr[v], ae = p.atr[v + 1];
+        for (int32_t g = ab; g < ae; g += 32) {
+            int32_t t = g + lane;
+            int len = 0, bs = 0;
+            double a = 0.0;
+            if (t < ae) {
+                int32_t u = __ldg(p.atc + t);
+                len = curL[u];
+                if (len) {
+                    bs = curS[u];
+                    a = UNIT ? 1.0 : __ldg(p.atv + t);
+                }
+            }
+            int incl = warp_incl_scan(len);
+            int total = __shfl_sync(FULL, incl, 31);
+            if (total == 0) continue;
+            s_incl[lane] = incl;
+            s_off[lane] = bs - (incl - len);
+            s_a[lane] = a;
+            __syncwarp();
+            int q = 0;
+            for (int x = lane; x < total; x += 32) {
+                while (s_incl[q] <= x) ++q;
+                int32_t j = x + s_off[q];
+                int s = p.es[j];
+                if (!(vis[s >> 5] & (1u << (s & 31)))) {
+                    atomicAdd(&acc[s], s_a[q] * p.ev[j]);
+                    atomicOr(&touched[s >> 5], 1u << (s & 31));
+                }
+            }
+            __syncwarp();
+        }
+        // new frontier row of v: its touched sources, in source order
+        uint32_t word = lane < p.words ? touched[lane] : 0u;
+        int cnt = __popc(word);
+        int excl = warp_incl_scan(cnt) - cnt;
+        int count = __shfl_sync(FULL, excl + cnt, 31);
+        if (count == 0) {
+            if (lane == 0) nxtL[v] = 0;
+            continue;
+        }
+        int start = 0;
+        if (lane == 0) {
+            start = atomicAdd(&p.st->entries, count);
+            int r = atomicAdd(&p.st->rows, 1);
+            if ((int64_t)start + count > p.cap_entries || (int64_t)r >= p.cap_rows) {
+                atomicExch(&p.st->overflow, 1);
+                start = -1;
+            } else {
+                p.rv[r] = (int32_t)v; p.rs[r] = start; p.rl[r] = count;
+                p.vcnt[v] += count;
+            }
+            nxtS[v] = start;
+            nxtL[v] = start < 0 ? 0 : count;
+        }
+        start = __shfl_sync(FULL, start, 0);
+        if (start >= 0 && word) {
+            int pos = start + excl;
+            uint32_t w = word;
+            while (w) {
+                int b = __ffs(w) - 1;
+                w &= w - 1;
+                int s = lane * 32 + b;
+                p.es[pos] = s;
+                p.ev[pos] = acc[s];
+                p.ed[pos] = 1.0;
+                ++pos;
+            }
+            p.vbits[(size_t)v * p.words + lane] = vis[lane] | word;
+        }
+        __syncwarp();
+        // reset the accumulator for the next vertex
+        for (int s = lane; s < p.ns; s += 32) acc[s] = 0.0;
+        if (lane < p.words) touched[lane] = 0u;
+        __syncwarp();
+    }
+}
+
+__global__ void k_bc_forward_finalize(BcArgs p, LoopCtl ctl) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    BcState* st = p.st;
+    bool more = false;
+    if (!st->done) {
+        const int d = st->d;
+        if (st->overflow || st->rows == p.level_rows[d]) {
+            st->depth = d;
+            st->done = 1;
+        } else {
+            p.level_rows[d + 1] = st->rows;
+            st->d = d + 1;
+            if ((int64_t)st->d > p.m) { st->depth = st->d; st->done = 1; }
+            else more = true;
+        }
+    }
+    if (!more) st->k = st->depth - 1;
+    loop_continue(ctl, more);
+}
+
+// W<S[k]> = bcu / sigma and mark the level's vertices (set = true), or clear
+// both again (set = false).
+__global__ void k_bc_set_w(BcArgs p, bool set) {
+    const int k = p.st->k;
+    if (k < 1) return;
+    const int lane = threadIdx.x & 31;
+    const int32_t r0 = p.level_rows[k], r1 = p.level_rows[k + 1];
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t r = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); r < r1; r += warps) {
+        const int32_t v = p.rv[r], s0 = p.rs[r], n = p.rl[r];
+        double* wrow = p.W + (size_t)v * p.ns;
+        for (int e = lane; e < n; e += 32) {
+            int s = p.es[s0 + e];
+            wrow[s] = set ? p.ed[s0 + e] / p.ev[s0 + e] : 0.0;
+        }
+        if (lane == 0) {
+            if (set) atomicOr(&p.inlvl[v >> 5], 1u << (v & 31));
+            else atomicAnd(&p.inlvl[v >> 5], ~(1u << (v & 31)));
+        }
+    }
+}
+
+// Rows of S[k-1]: acc_s = sum_w A[v][w] * W[w][s] over out-neighbours w that
+// sit at level k; bcu += acc*sigma; bc[v] += sum_s acc*sigma.
+template <bool UNIT>
+__global__ void __launch_bounds__(kBcThreads) k_bc_backward(BcArgs p) {
+    const int k = p.st->k;
+    if (k < 1) return;
+    const int lane = threadIdx.x & 31;
+    const int32_t r0 = p.level_rows[k - 1], r1 = p.level_rows[k];
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    constexpr int PER = 4;  // entries per lane per pass
+    for (int64_t r = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); r < r1; r += warps) {
+        const int32_t v = p.rv[r], e0 = p.rs[r], n = p.rl[r];
+        const int32_t ab = p.ar[v], ae = p.ar[v + 1];
+        double vsum = 0.0;
+        for (int base = 0; base < n; base += 32 * PER) {
+            int s[PER];
+            double acc[PER];
+#pragma unroll
+            for (int u = 0; u < PER; ++u) {
+                int e = base + u * 32 + lane;
+                s[u] = e < n ? p.es[e0 + e] : -1;
+                acc[u] = 0.0;
+            }
+            for (int32_t t = ab; t < ae; ++t) {
+                const int32_t w = __ldg(p.ac + t);
+                if (!(__ldg(p.inlvl + (w >> 5)) & (1u << (w & 31)))) continue;
+                const double a = UNIT ? 1.0 : __ldg(p.av + t);
+                const double* wrow = p.W + (size_t)w * p.ns;
+#pragma unroll
+                for (int u = 0; u < PER; ++u)
+                    if (s[u] >= 0) acc[u] += a * wrow[s[u]];
+            }
+#pragma unroll
+            for (int u = 0; u < PER; ++u) {
+                int e = base + u * 32 + lane;
+                if (e < n) {
+                    double c = acc[u] * p.ev[e0 + e];
+                    p.ed[e0 + e] += c;
+                    vsum += c;
+                }
+            }
+        }
+        vsum = warp_sum<double>(vsum);
+        if (lane == 0 && vsum != 0.0) atomicAdd(&p.bc[v], vsum);
+    }
+}
+
+__global__ void k_bc_backward_finalize(BcArgs p, LoopCtl ctl) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    BcState* st = p.st;
+    if (st->k >= 1) st->k -= 1;
+    loop_continue(ctl, st->k >= 1);
+}
+
+// checks: self-loops, symmetric pattern and values, unit values
+__global__ void k_bc_checks(const int32_t* __restrict__ r, const int32_t* __restrict__ c,
+                            const double* __restrict__ v, int64_t m, int* __restrict__ flags) {
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int lane = threadIdx.x & 31;
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < m; i += warps) {
+        int bad_loop = 0, asym = 0, nonunit = 0;
+        for (int32_t q = r[i] + lane; q < r[i + 1]; q += 32) {
+            int32_t j = c[q];
+            if (j == (int32_t)i) bad_loop = 1;
+            if (v[q] != 1.0) nonunit = 1;
+            int32_t jb = r[j], jn = r[j + 1] - jb;
+            int pos = lower_bound_i32(c + jb, jn, (int32_t)i);
+            if (pos >= jn || c[jb + pos] != (int32_t)i || v[jb + pos] != v[q]) asym = 1;
+        }
+        int f = (bad_loop ? 1 : 0) | (asym ? 2 : 0) | (nonunit ? 4 : 0);
+        f = __reduce_or_sync(0xffffffffu, f);
+        if (lane == 0 && f) atomicOr(flags, f);
+    }
+}
+
+__global__ void k_bc_check_sources(const int32_t* __restrict__ src, int ns, int64_t m, int* __restrict__ mark,
+                                   int* __restrict__ flags) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < ns; j += gridDim.x * blockDim.x) {
+        int v = src[j];
+        if (v < 0 || (int64_t)v >= m) { atomicOr(flags, 8); continue; }
+        if (atomicAdd(&mark[v], 1) != 0) atomicOr(flags, 16);
+    }
+}
+
+static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t nsrc, double* d_bc) {
+    GA_REQUIRE(A->m == A->n, GA_ERR_SHAPE, "non-square matrix; BC is only for square matrices");
+    GA_REQUIRE(nsrc >= 0 && nsrc <= kBcMaxSources, GA_ERR_INVALID_ARG, "BC: between 0 and 1024 sources per batch");
+    const int64_t m = A->m;
+    GA_CUDA(cudaMemsetAsync(d_bc, 0, sizeof(double) * (m ? m : 1), ctx->stream));
+    if (m == 0 || nsrc == 0) return;
+    const int ns = (int)nsrc;
+    const int words = (ns + 31) / 32;
+    GA_REQUIRE(m * (int64_t)(ns + 1) < INT32_MAX, GA_ERR_UNSUPPORTED, "BC: m x sources exceeds the int32 entry range");
+    ProfScope whole(ctx, "bc");
+    // FP64 copy of A (the algebra's values) and checks
+    ga_csr Ad = copy_csr(ctx, A, GA_FP64);
+    ga_csr AT = nullptr;
+    try {
+        DBuf<int> flags(ctx, 1), mark(ctx, (size_t)m);
+        GA_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int), ctx->stream));
+        GA_CUDA(cudaMemsetAsync(mark.p, 0, sizeof(int) * m, ctx->stream));
+        k_bc_checks<<<grid_for(m * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(
+            Ad->rst, Ad->col, static_cast<const double*>(Ad->val), m, flags.p);
+        post_launch("bc_checks");
+        k_bc_check_sources<<<grid_for(ns, 256, 64), 256, 0, ctx->stream>>>(d_sources, ns, m, mark.p, flags.p);
+        post_launch("bc_check_sources");
+        const int f = read_i32(ctx, flags.p);
+        GA_REQUIRE(!(f & 1), GA_ERR_INVALID_ARG, "BC: the graph has self-loops");
+        GA_REQUIRE(!(f & 8), GA_ERR_INVALID_ARG, "BC: source index out of range");
+        GA_REQUIRE(!(f & 16), GA_ERR_INVALID_ARG, "BC: sources must be distinct");
+        const bool symmetric = !(f & 2);
+        const bool unit = !(f & 4);
+        if (!symmetric) AT = transpose_csr(ctx, Ad);
+        ga_csr ATu = symmetric ? Ad : AT;
+
+        const int64_t cap_entries = m * (int64_t)ns + ns;
+        const int64_t cap_rows = cap_entries;
+        BcArgs p;
+        p.atr = ATu->rst; p.atc = ATu->col; p.atv = static_cast<const double*>(ATu->val);
+        p.ar = Ad->rst; p.ac = Ad->col; p.av = static_cast<const double*>(Ad->val);
+        p.m = m; p.ns = ns; p.words = words; p.sources = d_sources;
+        DBuf<BcState> st(ctx, 1);
+        DBuf<int32_t> level_rows(ctx, (size_t)m + 2);
+        DBuf<int32_t> cs0(ctx, m), cs1(ctx, m), cl0(ctx, m), cl1(ctx, m), vcnt(ctx, m);
+        DBuf<uint32_t> vbits(ctx, (size_t)m * words), inlvl(ctx, (size_t)(m + 31) / 32);
+        DBuf<int32_t> es(ctx, (size_t)cap_entries);
+        DBuf<double> ev(ctx, (size_t)cap_entries), ed(ctx, (size_t)cap_entries);
+        DBuf<int32_t> rv(ctx, (size_t)cap_rows), rs(ctx, (size_t)cap_rows), rl(ctx, (size_t)cap_rows);
+        DBuf<double> W(ctx, (size_t)m * ns);
+        GA_CUDA(cudaMemsetAsync(cl0.p, 0, sizeof(int32_t) * m, ctx->stream));
+        GA_CUDA(cudaMemsetAsync(cl1.p, 0, sizeof(int32_t) * m, ctx->stream));
+        GA_CUDA(cudaMemsetAsync(vcnt.p, 0, sizeof(int32_t) * m, ctx->stream));
+        GA_CUDA(cudaMemsetAsync(vbits.p, 0, sizeof(uint32_t) * m * words, ctx->stream));
+        GA_CUDA(cudaMemsetAsync(inlvl.p, 0, sizeof(uint32_t) * ((m + 31) / 32), ctx->stream));
+        GA_CUDA(cudaMemsetAsync(W.p, 0, sizeof(double) * m * ns, ctx->stream));
+        p.st = st.p; p.level_rows = level_rows.p;
+        p.cur_start[0] = cs0.p; p.cur_start[1] = cs1.p; p.cur_len[0] = cl0.p; p.cur_len[1] = cl1.p;
+        p.vbits = vbits.p; p.vcnt = vcnt.p;
+        p.es = es.p; p.ev = ev.p; p.ed = ed.p;
+        p.rv = rv.p; p.rs = rs.p; p.rl = rl.p;
+        p.cap_entries = cap_entries; p.cap_rows = cap_rows;
+        p.W = W.p; p.inlvl = inlvl.p; p.bc = d_bc;
+
+        k_bc_init<<<grid_for(ns, 256, 64), 256, 0, ctx->stream>>>(p);
+        post_launch("bc_init");
+
+        const size_t per_warp = (size_t)ns * sizeof(double) + 2 * (size_t)words * sizeof(uint32_t) +
+                                32 * (2 * sizeof(int) + sizeof(double));
+        const size_t smem = kBcWarps * ((per_warp + 15) & ~(size_t)15);
+        auto fwd = unit ? k_bc_forward<true> : k_bc_forward<false>;
+        GA_CUDA(cudaFuncSetAttribute(fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 1;
+        GA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd, kBcThreads, smem));
+        if (per_sm < 1) per_sm = 1;
+        const int grid_fwd = ctx->num_sms * per_sm;
+        const int grid_rows = ctx->num_sms * 8;
+        {
+            ProfScope ps(ctx, "bc_forward_loop");
+            run_device_loop(ctx, [&](const LoopCtl& ctl) {
+                fwd<<<grid_fwd, kBcThreads, smem, ctx->stream>>>(p);
+                post_launch("bc_forward");
+                k_bc_forward_finalize<<<1, 32, 0, ctx->stream>>>(p, ctl);
+                post_launch("bc_forward_finalize");
+            }, m + 2);
+        }
+        {
+            ProfScope ps(ctx, "bc_backward_loop");
+            auto bwd = unit ? k_bc_backward<true> : k_bc_backward<false>;
+            run_device_loop(ctx, [&](const LoopCtl& ctl) {
+                k_bc_set_w<<<grid_rows, 256, 0, ctx->stream>>>(p, true);
+                post_launch("bc_set_w");
+                bwd<<<grid_rows, kBcThreads, 0, ctx->stream>>>(p);
+                post_launch("bc_backward");
+                k_bc_set_w<<<grid_rows, 256, 0, ctx->stream>>>(p, false);
+                post_launch("bc_clear_w");
+                k_bc_backward_finalize<<<1, 32, 0, ctx->stream>>>(p, ctl);
+                post_launch("bc_backward_finalize");
+            }, m + 2);
+        }
+        BcState hs;
+        GA_CUDA(cudaMemcpyAsync(&hs, st.p, sizeof(BcState), cudaMemcpyDeviceToHost, ctx->stream));
+        GA_CUDA(cudaStreamSynchronize(ctx->stream));
+        GA_REQUIRE(!hs.overflow, GA_ERR_INVALID_ARG, "BC: entry store overflow");
+    } catch (...) {
+        csr_destroy(ctx, AT);
+        csr_destroy(ctx, Ad);
+        throw;
+    }
+    csr_destroy(ctx, AT);
+    csr_destroy(ctx, Ad);
+}
+
+}  // namespace ga
+
+using namespace ga;
+
+extern "C" {
+
+int ga_bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t nsrc, double* d_bc) {
+    if (!ctx || !A || !d_bc || (nsrc > 0 && !d_sources)) return GA_ERR_INVALID_ARG;
+    GA_API_BODY(ctx, bc_device(ctx, A, d_sources, nsrc, d_bc));
+}
+
+int ga_bc(ga_ctx ctx, ga_csr A, const int32_t* sources, int64_t nsrc, double* bc) {
+    if (!ctx || !A || !bc || (nsrc > 0 && !sources)) return GA_ERR_INVALID_ARG;
+    GA_API_BODY(ctx, {
+        DBuf<int32_t> src(ctx, nsrc > 0 ? (size_t)nsrc : 1);
+        DBuf<double> out(ctx, A->m > 0 ? (size_t)A->m : 1);
+        if (nsrc > 0)
+            GA_CUDA(cudaMemcpyAsync(src.p, sources, sizeof(int32_t) * nsrc, cudaMemcpyHostToDevice, ctx->stream));
+        bc_device(ctx, A, src.p, nsrc, out.p);
+        if (A->m)
+            GA_CUDA(cudaMemcpyAsync(bc, out.p, sizeof(double) * A->m, cudaMemcpyDeviceToHost, ctx->stream));
+        GA_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+}  // extern "C"

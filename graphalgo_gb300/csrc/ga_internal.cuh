@@ -1,0 +1,196 @@
+// Internal declarations shared by the CUDA translation units of
+// libgraphalgo_gb300.so. Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+#include <map>
+#include <stdexcept>
+
+#include "../../include/graphalgo_gb300.h"
+
+namespace ga {
+
+// ------------------------------------------------------------------ errors
+struct Error {
+    int code;
+    std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string& msg);
+void check_cuda(cudaError_t e, const char* what, const char* file, int line);
+#define GA_CUDA(expr) ::ga::check_cuda((expr), #expr, __FILE__, __LINE__)
+#define GA_REQUIRE(cond, code, msg) \
+    do {                            \
+        if (!(cond)) ::ga::fail((code), (msg)); \
+    } while (0)
+
+// --------------------------------------------------------------- device info
+constexpr int kWarp = 32;
+constexpr int32_t kEmpty = -1;  // empty hash-table key
+
+// ------------------------------------------------------------------ context
+struct PendingTiming {
+    const char* name;
+    cudaEvent_t start, stop;
+};
+
+struct KStat {
+    int64_t launches = 0;
+    double total_ms = 0.0;
+};
+
+}  // namespace ga
+
+struct ga_ctx_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int num_sms = 0;
+    int cc_major = 0, cc_minor = 0;
+    size_t smem_optin = 0;  // max dynamic shared memory per block (opt-in)
+    cudaMemPool_t pool = nullptr;
+    std::string last_error;
+    // options
+    bool device_loops = true;
+    bool profile = false;
+    int64_t fail_alloc_after = -1;  // fault injection
+    // profiling
+    std::vector<ga::PendingTiming> pending;
+    std::vector<cudaEvent_t> event_pool;
+    std::map<std::string, ga::KStat> kstats;
+    cudaEvent_t timer_start = nullptr, timer_stop = nullptr;
+    // pinned host word for small read-backs
+    int64_t* h_pinned = nullptr;
+    bool capturing = false;
+};
+
+struct ga_csr_s {
+    int64_t m = 0, n = 0, nnz = 0;
+    ga_dtype dtype = GA_INT32;
+    int32_t* rst = nullptr;
+    int32_t* col = nullptr;
+    void* val = nullptr;
+    size_t cap = 0;  // allocated entries of col/val
+};
+
+struct ga_dense_s {
+    int64_t m = 0, n = 0;
+    ga_dtype dtype = GA_FP64;
+    void* val = nullptr;
+};
+
+namespace ga {
+
+size_t dtype_size(ga_dtype t);
+bool dtype_valid(int t);
+
+// -------------------------------------------------------------- allocation
+void* dalloc(ga_ctx ctx, size_t bytes);
+void dfree(ga_ctx ctx, void* p);
+
+template <typename T>
+T* dalloc_t(ga_ctx ctx, size_t count) {
+    return static_cast<T*>(dalloc(ctx, count * sizeof(T)));
+}
+
+// RAII device buffer, freed stream-ordered on the context's stream.
+template <typename T>
+struct DBuf {
+    ga_ctx ctx = nullptr;
+    T* p = nullptr;
+    size_t count = 0;
+    DBuf() = default;
+    DBuf(ga_ctx c, size_t n) : ctx(c), p(dalloc_t<T>(c, n)), count(n) {}
+    ~DBuf() {
+        if (p) dfree(ctx, p);
+    }
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : ctx(o.ctx), p(o.p), count(o.count) { o.p = nullptr; }
+    DBuf& operator=(DBuf&& o) noexcept {
+        if (this != &o) {
+            if (p) dfree(ctx, p);
+            ctx = o.ctx; p = o.p; count = o.count; o.p = nullptr;
+        }
+        return *this;
+    }
+    T* release() {
+        T* r = p;
+        p = nullptr;
+        return r;
+    }
+};
+
+// CSR handle helpers
+ga_csr csr_alloc(ga_ctx ctx, int64_t m, int64_t n, int64_t nnz, ga_dtype dt);
+void csr_destroy(ga_ctx ctx, ga_csr A);
+
+// ------------------------------------------------------------- profiling
+// Begin/end a named kernel region on the context stream (no-op unless the
+// GA_OPT_PROFILE option is on and no graph capture is running).
+void prof_begin(ga_ctx ctx, const char* name);
+void prof_end(ga_ctx ctx);
+struct ProfScope {
+    ga_ctx ctx;
+    ProfScope(ga_ctx c, const char* name) : ctx(c) { prof_begin(c, name); }
+    ~ProfScope() { prof_end(ctx); }
+};
+void post_launch(const char* name);
+
+// ------------------------------------------------------------- primitives
+// Exclusive prefix sum of `n` int32 counts into out[0..n] (out[n] = total).
+// in and out may alias. Launch sizes depend only on n (graph-capturable).
+void scan_exclusive_i32(ga_ctx ctx, const int32_t* in, int32_t* out, int64_t n);
+// Same for int64.
+void scan_exclusive_i64(ga_ctx ctx, const int64_t* in, int64_t* out, int64_t n);
+// Scratch bytes needed by the scans above for n elements.
+size_t scan_scratch_bytes(int64_t n);
+
+// Fills `count` values of type `dt` with 1.
+void fill_ones(ga_ctx ctx, void* vals, int64_t count, ga_dtype dt);
+
+// Validates a device CSR; throws GA_ERR_INVALID_CSR when malformed.
+void validate_csr(ga_ctx ctx, const int32_t* rst, const int32_t* col, int64_t m, int64_t n, int64_t nnz);
+
+// device-side transpose (counting sort; rows of the result sorted)
+ga_csr transpose_csr(ga_ctx ctx, ga_csr A);
+ga_csr extract_tri(ga_ctx ctx, ga_csr A, bool lower);
+ga_csr copy_csr(ga_ctx ctx, ga_csr A, ga_dtype to);
+
+// Masked SpGEMM into caller-provided value storage aligned with M.
+void mxm_masked_into(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals);
+ga_csr mxm_cmask(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M);
+size_t mxm_scratch_bytes(int64_t m, int64_t mask_nnz);
+void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals, void* scratch);
+void scan_exclusive_i32_scratch(ga_ctx ctx, const int32_t* in, int32_t* out, int64_t n, void* scratch);
+
+// Read one device value to the host (synchronises the stream).
+int64_t read_i64(ga_ctx ctx, const int64_t* d);
+int32_t read_i32(ga_ctx ctx, const int32_t* d);
+
+int grid_for(int64_t work, int block, int max_blocks = 1 << 20);
+
+}  // namespace ga
+
+// Entry-point wrapper: runs `body`, maps ga::Error / std::bad_alloc / other
+// exceptions to status codes and records the message on the context.
+#define GA_API_BODY(ctx, ...)                                        \
+    do {                                                             \
+        try {                                                        \
+            __VA_ARGS__;                                             \
+            return GA_OK;                                            \
+        } catch (const ::ga::Error& e) {                             \
+            if (ctx) (ctx)->last_error = e.msg;                      \
+            return e.code;                                           \
+        } catch (const std::bad_alloc&) {                            \
+            if (ctx) (ctx)->last_error = "host allocation failed";   \
+            return GA_ERR_OOM;                                       \
+        } catch (const std::exception& e) {                          \
+            if (ctx) (ctx)->last_error = e.what();                   \
+            return GA_ERR_INVALID_ARG;                               \
+        }                                                            \
+    } while (0)

@@ -1,0 +1,241 @@
+/*
+ * graphalgo_gb300 — GB300-native (sm_103a) masked sparse matrix-matrix
+ * multiply C<M> = A*B over CSR graphs, and its callers (triangle counting,
+ * k-truss, batched betweenness centrality).
+ *
+ * C ABI. Plain pointers and sizes; every call returns an int status (GA_OK = 0)
+ * and ga_last_error(ctx) gives the message. No C++ exception crosses it.
+ *
+ * Drop-in for UAlex322/GraphAlgo's masked-SpGEMM path. The reference's plugin
+ * seam is the function-pointer type
+ *     template<T> using mxmOp = void(*)(bool, const spMtx<T>&, const spMtx<T>&,
+ *                                       const spMtx<T>&, spMtx<T>&);
+ * (src/main.cpp:11-12); include/graphalgo_gb300.hpp re-exposes those exact
+ * signatures on top of this ABI. Each entry point below names the reference
+ * function it replaces.
+ *
+ * Data model. A CSR matrix (the reference's spMtx<T>, include/matrix.h:23-33)
+ * lives in device memory behind a ga_csr handle: int32 row starts (m+1),
+ * int32 column indices sorted strictly ascending within each row, values of
+ * one ga_dtype. Masks are structural (only the pattern of M matters), as in
+ * every reference entry point. Dense matrices (denseMtx<T>,
+ * include/matrix.h:561-666) are row-major behind a ga_dense handle.
+ *
+ * Threading. One ga_ctx per host thread. Calls are ordered on the context's
+ * CUDA stream; functions that return host results synchronise that stream.
+ */
+#ifndef GRAPHALGO_GB300_H
+#define GRAPHALGO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GA_API __attribute__((visibility("default")))
+
+typedef struct ga_ctx_s* ga_ctx;
+typedef struct ga_csr_s* ga_csr;
+typedef struct ga_dense_s* ga_dense;
+
+/* value types (the reference's T: int for graphs, float/double for BC) */
+typedef enum {
+    GA_INT32 = 0,
+    GA_INT64 = 1,
+    GA_FP32 = 2,
+    GA_FP64 = 3,
+    GA_UINT8 = 4
+} ga_dtype;
+
+/* masked-SpGEMM variants: the reference's four mxmOp implementations,
+ * plus the dot-product (sorted-list intersection) form used by TC */
+typedef enum {
+    GA_MSA = 0,   /* mxmm_msa,   include/matrix_la.h:700-749 */
+    GA_MCA = 1,   /* mxmm_mca,   include/matrix_la.h:586-641 */
+    GA_HEAP = 2,  /* mxmm_heap,  include/matrix_la.h:1013-1084 (a warp-cooperative sorted merge here) */
+    GA_NAIVE = 3, /* mxmm_naive, include/matrix_la.h:1139-1277 */
+    GA_DOT = 4    /* triangle counting only: warp sorted-list intersections */
+} ga_algo;
+
+/* status codes */
+enum {
+    GA_OK = 0,
+    GA_ERR_INVALID_ARG = 1,
+    GA_ERR_INVALID_CSR = 2, /* unsorted / out-of-range / malformed CSR */
+    GA_ERR_SHAPE = 3,       /* dimensions do not agree */
+    GA_ERR_DTYPE = 4,       /* value types do not agree or are unsupported */
+    GA_ERR_CUDA = 5,        /* a CUDA runtime call failed */
+    GA_ERR_OOM = 6,         /* device allocation failed (or was injected) */
+    GA_ERR_NO_DEVICE = 7,   /* no CUDA device / the kernels are not loadable */
+    GA_ERR_TIMEOUT = 8,     /* a bounded device wait expired */
+    GA_ERR_UNSUPPORTED = 9,
+    GA_ERR_ADMISSION = 10   /* request refused: HBM bound exceeded */
+};
+
+/* ------------------------------------------------------------------ context */
+/* stream may be NULL (the context creates its own non-blocking stream) or a
+ * cudaStream_t owned by the caller. */
+GA_API int ga_ctx_create(int device, void* stream, ga_ctx* out);
+GA_API int ga_ctx_destroy(ga_ctx ctx);
+GA_API const char* ga_last_error(ga_ctx ctx);
+GA_API const char* ga_status_string(int status);
+GA_API int ga_ctx_sync(ga_ctx ctx);
+GA_API int ga_ctx_stream(ga_ctx ctx, void** stream);
+GA_API int ga_device_count(int* count);
+GA_API int ga_version(int* major, int* minor);
+
+/* Context options. GA_OPT_DEVICE_LOOPS (default 1): run the k-truss and BC
+ * iteration loops as CUDA graphs with device-side WHILE conditions (no host
+ * round trip per iteration); 0 runs the same kernels from a host loop.
+ * GA_OPT_PROFILE: when 1, each kernel launch is bracketed by CUDA events and
+ * ga_ctx_kernel_stats reports per-kernel totals. GA_OPT_FAIL_ALLOC_AFTER:
+ * fault injection for tests — the N-th device allocation from now on fails
+ * with GA_ERR_OOM (-1 disables). */
+enum { GA_OPT_DEVICE_LOOPS = 1, GA_OPT_PROFILE = 2, GA_OPT_FAIL_ALLOC_AFTER = 3 };
+GA_API int ga_ctx_set_option(ga_ctx ctx, int option, int64_t value);
+
+/* Per-kernel timing collected while GA_OPT_PROFILE is on. Writes up to `cap`
+ * records; *count receives the number of distinct kernels. */
+typedef struct {
+    char name[48];
+    int64_t launches;
+    double total_ms;
+} ga_kernel_stat;
+GA_API int ga_ctx_kernel_stats(ga_ctx ctx, ga_kernel_stat* out, int cap, int* count);
+GA_API int ga_ctx_reset_kernel_stats(ga_ctx ctx);
+
+/* Stream-ordered device timer: ga_timer_start records an event on the
+ * context's stream; ga_timer_stop records another, synchronises and returns
+ * the elapsed milliseconds. */
+GA_API int ga_timer_start(ga_ctx ctx);
+GA_API int ga_timer_stop(ga_ctx ctx, double* ms);
+
+/* Free / total device memory as the CUDA runtime sees it. */
+GA_API int ga_mem_info(ga_ctx ctx, int64_t* free_bytes, int64_t* total_bytes);
+
+/* --------------------------------------------------------------- CSR handle */
+/* Upload a host CSR (spMtx::Rst/Col/Val). val may be NULL: all ones.
+ * The pattern is validated on the device (monotone row starts, in-range and
+ * strictly ascending columns); a malformed matrix gives GA_ERR_INVALID_CSR.
+ * Replaces the spMtx constructors / copy (include/matrix.h:56-80). */
+GA_API int ga_csr_upload(ga_ctx ctx, int64_t m, int64_t n, int64_t nnz,
+                         const int32_t* rst, const int32_t* col, const void* val,
+                         ga_dtype dtype, ga_csr* out);
+/* Same from device pointers (copied on the device); no host traffic. */
+GA_API int ga_csr_from_device(ga_ctx ctx, int64_t m, int64_t n, int64_t nnz,
+                              const int32_t* d_rst, const int32_t* d_col, const void* d_val,
+                              ga_dtype dtype, ga_csr* out);
+GA_API int ga_csr_info(ga_csr A, int64_t* m, int64_t* n, int64_t* nnz, int* dtype);
+/* Copy back into caller-allocated host arrays (rst: m+1, col/val: nnz).
+ * Any of the three may be NULL to skip it. */
+GA_API int ga_csr_download(ga_ctx ctx, ga_csr A, int32_t* rst, int32_t* col, void* val);
+GA_API int ga_csr_device_ptrs(ga_csr A, void** rst, void** col, void** val);
+GA_API int ga_csr_free(ga_ctx ctx, ga_csr A);
+/* Deep copy, optionally converting the value type
+ * (convertType, include/matrix.h:668-677). */
+GA_API int ga_csr_convert(ga_ctx ctx, ga_csr A, ga_dtype dtype, ga_csr* out);
+
+/* ------------------------------------------------------------- dense handle */
+GA_API int ga_dense_create(ga_ctx ctx, int64_t m, int64_t n, ga_dtype dtype, const void* host_vals,
+                           ga_dense* out);
+GA_API int ga_dense_download(ga_ctx ctx, ga_dense D, void* host_vals);
+GA_API int ga_dense_info(ga_dense D, int64_t* m, int64_t* n, int* dtype);
+GA_API int ga_dense_device_ptr(ga_dense D, void** vals);
+GA_API int ga_dense_free(ga_ctx ctx, ga_dense D);
+/* Dense copy of a sparse matrix, zero-filled elsewhere
+ * (denseMtx(const spMtx&), include/matrix.h:585-596). */
+GA_API int ga_dense_from_csr(ga_ctx ctx, ga_csr A, ga_dense* out);
+
+/* -------------------------------------------------------- masked SpGEMM */
+/* C<M> = A*B, structural mask: C has M's pattern (row starts and columns of
+ * M), values sum_k A[i][k]*B[k][j] or an explicit 0.
+ * Replaces mxmm_msa / mxmm_mca / mxmm_heap / mxmm_naive
+ * (include/matrix_la.h:700-713, 586-599, 1013-1028, 1139-1277).
+ * A, B share a dtype; M may have any dtype. *C is a new handle. */
+GA_API int ga_mxm_masked(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, ga_csr* C);
+/* Same, writing only the values into a caller-provided device array aligned
+ * with M's pattern (length nnz(M), A's dtype). No allocation of C. */
+GA_API int ga_mxm_masked_vals(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals);
+
+/* C<!M> = A*B: the structural product minus M's pattern, columns sorted.
+ * Replaces mxmm_msa_cmask (include/matrix_la.h:788-891). An empty M gives
+ * the unmasked product. */
+GA_API int ga_mxm_cmask(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M, ga_csr* C);
+
+/* Dense C<M> = A*B with B and C dense (m x n); C is zero outside M.
+ * Replaces mxmm_spd (include/matrix_la.h:241-270). C may not alias B. */
+GA_API int ga_mxm_spd(ga_ctx ctx, ga_csr A, ga_dense B, ga_csr M, ga_dense C);
+
+/* ------------------------------------------------------ element-wise helpers */
+/* Union of two matrices with disjoint patterns (include/matrix_la.h:337-372). */
+GA_API int ga_add_nointersect(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr* C);
+/* Dense C<M> = A .* B, zero elsewhere (include/matrix_la.h:200-219). */
+GA_API int ga_ewise_mult_masked(ga_ctx ctx, ga_dense A, ga_dense B, ga_csr M, ga_dense C);
+/* Dense C += A .* B (include/matrix_la.h:192-198). */
+GA_API int ga_fuse_ewise_mult_add(ga_ctx ctx, ga_dense A, ga_dense B, ga_dense C);
+
+/* ------------------------------------------------------------ graph prep */
+GA_API int ga_transpose(ga_ctx ctx, ga_csr A, ga_csr* AT);          /* matrix_la.h:166-190 */
+GA_API int ga_extract_lower(ga_ctx ctx, ga_csr A, ga_csr* L);       /* matrix.h:736-763 */
+GA_API int ga_extract_upper(ga_ctx ctx, ga_csr A, ga_csr* U);       /* matrix.h:765-792 */
+GA_API int ga_symm_from_lower(ga_ctx ctx, ga_csr L, ga_csr* S);     /* matrix.h:700-734 */
+/* All values set to 1 as int32 (build_adjacency_matrix, matrix.h:679-698). */
+GA_API int ga_adjacency(ga_ctx ctx, ga_csr A, ga_csr* adj);
+
+/* ------------------------------------------------------------ algorithms */
+/* Triangle count of an undirected graph given as symmetric adjacency A.
+ * algo GA_MSA/MCA/HEAP/NAIVE: C<L> = L*L with that variant, L = strict lower
+ * triangle of A, total = sum of C (triangle_counting_masked_sandia,
+ * src/main.cpp:65-86); GA_DOT: the same counts by warp-level sorted-list
+ * intersections. per_row (host, length m, may be NULL) receives the row sums
+ * of C<L> = L*L: triangles whose largest vertex is that row. Values of A are
+ * ignored (the reference CLI makes them 1, src/main.cpp:335). */
+GA_API int ga_tc(ga_ctx ctx, ga_algo algo, ga_csr A, int64_t* total, int64_t* per_row);
+/* Device-result variant: writes the total into d_total (int64, device) and
+ * per-row counts into d_per_row (device, length m, may be NULL); no sync. */
+GA_API int ga_tc_device(ga_ctx ctx, ga_algo algo, ga_csr A, int64_t* d_total, int64_t* d_per_row);
+/* Other TC forms: C<A> = L*U summed and halved (triangle_counting_masked_lu,
+ * src/main.cpp:40-62), and per-vertex counts (A*A<A> row sums)/2
+ * (triangle_counting_vertex, src/main.cpp:14-37; per_vertex has length m). */
+GA_API int ga_tc_lu(ga_ctx ctx, ga_algo algo, ga_csr A, int64_t* total);
+GA_API int ga_tc_vertex(ga_ctx ctx, ga_algo algo, ga_csr A, int32_t* per_vertex);
+
+/* k-truss (src/main.cpp:90-146): iterate Tmp<C> = C*C with the chosen
+ * variant, keep entries >= k-2 as 1, stop when nnz is unchanged. The loop
+ * stays on the device. *C is the returned matrix; *iters the iteration count
+ * the reference prints (0 if it did not converge within m iterations).
+ * A must be int32. */
+GA_API int ga_ktruss(ga_ctx ctx, ga_algo algo, ga_csr A, int k, ga_csr* C, int* iters);
+
+/* Batched betweenness centrality (betweenness_centrality_batch,
+ * include/betweenness_centrality.h:125-237) for an explicit list of distinct
+ * sources, path counts and dependencies in FP64. bc (host, length m). The
+ * reference itself uses sources 0..batch-1. A must be square without
+ * self-loops; values are used as the reference's algebra uses them. */
+GA_API int ga_bc(ga_ctx ctx, ga_csr A, const int32_t* sources, int64_t nsrc, double* bc);
+/* Device-result variant (bc: device array of length m, overwritten). */
+GA_API int ga_bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t nsrc, double* d_bc);
+
+/* ------------------------------------------------------ synthetic graphs */
+/* Seeded generators producing sorted, duplicate-free, loop-free symmetric
+ * int32 CSR on the host (arrays allocated with malloc; free with
+ * ga_host_free). R-MAT and Erdos-Renyi output depends only on the seed;
+ * the k-NN points use the C library's log/cos and so the host's libm.
+ *  R-MAT: scale, edge factor, quadrant probabilities a, b, c (d = 1-a-b-c).
+ *  Erdos-Renyi G(n, m): m distinct undirected edges.
+ *  k-NN: n points i.i.d. N(0,1) in dim dimensions, k nearest neighbours by
+ *  Euclidean distance (self excluded), symmetrised by union. */
+GA_API int ga_gen_rmat(int scale, int edge_factor, double a, double b, double c, uint64_t seed,
+                       int64_t* m, int64_t* nnz, int32_t** rst, int32_t** col);
+GA_API int ga_gen_er(int64_t n, int64_t edges, uint64_t seed, int64_t* m, int64_t* nnz, int32_t** rst,
+                     int32_t** col);
+GA_API int ga_gen_knn(int64_t n, int dim, int k, uint64_t seed, int64_t* m, int64_t* nnz, int32_t** rst,
+                      int32_t** col);
+GA_API void ga_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GRAPHALGO_GB300_H */
