@@ -1,0 +1,427 @@
+#!/usr/bin/env python3
+"""Benchmark: masked SpGEMM GFLOP/s on the k-truss sweep of an R-MAT graph.
+
+Workload (one step): the k-truss sweep k = 3, 4, ... up to the largest k with
+a non-empty truss, on a seeded R-MAT graph (scale 18, edge factor 16,
+a/b/c/d = 0.57/0.19/0.19/0.05, symmetrised, loops and duplicates removed,
+int32 CSR, 262,144 vertices, 7.6M stored entries). Each k runs the
+reference's k_truss (src/main.cpp:90-146: Tmp<C> = C*C with the MSA masked
+SpGEMM, prune below k-2, repeat until nnz is unchanged) through the C ABI;
+k starts from the (k-1)-truss, which contains it (same edge sets as starting
+from A). value = 2 * (Gustavson products of every support product) / time,
+inputs resident in HBM, L2 flushed (256 MiB write) between steps.
+
+e2e: the same sweep through the public API from pinned host buffers: upload
+A, run the sweep, download every k-truss (row starts and columns).
+
+cpu_baseline / --impl reference: the oracle port of the reference's k_truss
+(oracle/oracle.c, OpenMP over all host cores) on a bounded sample of the same
+workload - the k = 3 stage from A - reported in the same unit.
+
+Multi-GPU: the path does not shard; --gpus N under torchrun runs N
+independent replicas (one per rank) and reports their aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "masked SpGEMM GFLOP/s & HBM % of peak; batched/served req/s, p50/p99 vs plain"
+UNIT = "GFLOP/s"
+HBM_FALLBACK_GBS = 6800.0
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--scale", type=int, default=18)
+    ap.add_argument("--edge-factor", type=int, default=16)
+    ap.add_argument("--seed", type=int, default=42)
+    ap.add_argument("--algo", default="msa", choices=["msa", "mca", "heap"])
+    ap.add_argument("--kmin", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-reps", type=int, default=2)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- plumbing
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = td
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling (200 ms) during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.out.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, val in zip(names, parts[5:9]):
+                    if val.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            v = json.load(f).get("hbm_gbs")
+        if v:
+            return float(v), "measured"
+    except Exception:
+        pass
+    return HBM_FALLBACK_GBS, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per Gustavson product of the MSA kernel from the committed
+    ncu summary (profiles/mxm_msa_rmat18_support.md), or None."""
+    p = os.path.join(ROOT, "profiles", "mxm_msa_rmat18_support.md")
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_product:"):
+                    return float(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+def workload_config(args, m, nnz, kmax):
+    return {"workload": f"k-truss sweep k={args.kmin}..{kmax} (k_max), R-MAT scale {args.scale}",
+            "graph": f"R-MAT scale {args.scale}, edge factor {args.edge_factor}, a/b/c/d=0.57/0.19/0.19/0.05, "
+                     f"seed {args.seed}, symmetrised, no loops/duplicates",
+            "vertices": m, "stored_entries": nnz, "variant": args.algo, "k_range": [args.kmin, kmax],
+            "k_start": "each k starts from the (k-1)-truss",
+            "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas only"}
+
+
+def cpu_sample(A_host, reps: int):
+    """Oracle port (OpenMP, all host threads) on the k=3 stage from A."""
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_num_threads(threads)
+    times, prod = [], 0
+    for _ in range(max(1, reps)):
+        t0 = time.perf_counter()
+        _, _, prod = oracle.ktruss(A_host, 3, with_products=True)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    return {"value": 2.0 * prod / t / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"k=3 stage of the sweep from A (k_truss, {prod:.4g} Gustavson products), "
+                      f"median of {len(times)} runs, {t:.3f} s each"}
+
+
+# --------------------------------------------------------------- GPU arm
+def sweep(ga, ctx, A, algo, kmin, sink=None, per_k=None):
+    """k-truss sweep from A: C_k = k_truss(C_{k-1}, k) until the truss is empty."""
+    cur, k, out = A, kmin, []
+    while True:
+        if per_k is not None:
+            ctx.work_counters(reset=True)
+        C, it = ga.ktruss(algo, cur, k)
+        nnz = C.nnz
+        out.append((k, it, nnz))
+        if per_k is not None:
+            per_k[k] = ctx.work_counters()
+        if sink is not None:
+            sink(k, C)
+        if cur is not A:
+            cur.free()
+        cur = C
+        if nnz == 0:
+            break
+        k += 1
+    if cur is not A:
+        cur.free()
+    return out
+
+
+def run_gpu(args, dist: Dist):
+    import graphalgo_gb300 as ga
+    from graphalgo_gb300 import build as gbuild
+    gbuild.build()
+    ctx = ga.Context(dist.local_rank)
+
+    m, rst, col = ga.gen_rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, args.seed)
+    nnz = len(col)
+    val = np.ones(nnz, np.int32)
+    A = ga.Csr.upload(ctx, m, m, rst, col, val)
+
+    # warm-up (also fixes k_max)
+    shape = None
+    for _ in range(max(1, args.warmup)):
+        shape = sweep(ga, ctx, A, args.algo, args.kmin)
+    kmax = shape[-1][0] - 1 if len(shape) > 1 else args.kmin
+
+    # ------------------------------------------------------- timed region
+    sampler = ClockSampler(dist.local_rank)
+    ctx.work_counters(reset=True)
+    dist.barrier()
+    ctx.sync()
+    sampler.start()
+    step_ms = []
+    for _ in range(args.steps):
+        ctx.flush_l2()
+        ctx.timer_start()
+        sweep(ga, ctx, A, args.algo, args.kmin)
+        step_ms.append(ctx.timer_stop())
+    ctx.sync()
+    clocks = sampler.stop()
+    dist.barrier()
+    wc = ctx.work_counters(reset=True)
+    total_ms = sum(step_ms)
+    flops = 2.0 * wc["products"]
+    t_max = dist.max(total_ms)
+    flops_all = dist.sum(flops)
+    value = flops_all / (t_max * 1e-3) / 1e9
+
+    # ----------------------------------- per-kernel profile of one step
+    ctx.set_option(ga.OPT_DEVICE_LOOPS, 0)
+    ctx.set_option(ga.OPT_PROFILE, 1)
+    ctx.reset_kernel_stats()
+    ctx.work_counters(reset=True)
+    l0 = ga.kernel_launches()
+    ctx.flush_l2()
+    per_k = {}
+    sweep(ga, ctx, A, args.algo, args.kmin, per_k=per_k)
+    ctx.sync()
+    launches_per_step = ga.kernel_launches() - l0
+    stats = ctx.kernel_stats()
+    prof_ctr = {key: sum(v[key] for v in per_k.values()) for key in next(iter(per_k.values()))}
+    ctx.set_option(ga.OPT_PROFILE, 0)
+    ctx.set_option(ga.OPT_DEVICE_LOOPS, 1)
+    kname = {"msa": "mxm_msa", "mca": "mxm_mca", "heap": "mxm_heap_merge"}[args.algo]
+    k_launches, k_ms = stats.get(kname, (0, 0.0))
+    # algorithmic bytes of the Gustavson model, int32 values (s = 4):
+    # 4(m+1)*2 + nnz(A)*(4+4) + nnz(A)*8 + P*(4+4) + nnz(M)*4 + nnz(C)*4
+    bytes_model = (8 * prof_ctr["rows"] + 16 * prof_ctr["a_entries"] + 8 * prof_ctr["products"]
+                   + 8 * prof_ctr["mask_entries"])
+    peak, peak_kind = measured_peak_hbm()
+    achieved = bytes_model / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
+    tpp = profile_traffic()
+    traffic = (tpp * prof_ctr["products"] / max(1, k_launches)) if tpp is not None else None
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "kernel": kname, "peak_kind": peak_kind,
+                "bytes_per_launch": bytes_model / max(1, k_launches),
+                "avg_launch_ms": k_ms / max(1, k_launches),
+                "kernel_share_of_step": k_ms / (total_ms / args.steps) if total_ms else None}
+
+    # ---------------------------------------------------------- e2e
+    e2e = None
+    if not args.no_e2e:
+        rst_h = np.ascontiguousarray(rst, np.int32)
+        col_h = np.ascontiguousarray(col, np.int32)
+        val_h = np.ascontiguousarray(val, np.int32)
+        res_rst = np.empty((len(shape), m + 1), np.int32)
+        res_col = np.empty(sum(s[2] for s in shape) + 1, np.int32)
+        pinned = [rst_h, col_h, val_h, res_rst, res_col]
+        for a in pinned:
+            ga.host_register(a)
+        try:
+            d2h = 0
+
+            def sink_factory():
+                state = {"i": 0, "off": 0}
+
+                def sink(k, C):
+                    nonlocal d2h
+                    z = C.nnz
+                    r = res_rst[state["i"]]
+                    c = res_col[state["off"]:state["off"] + z]
+                    ga.lib().ga_csr_download(ctx.handle, C.handle, r.ctypes.data_as(ga._p),
+                                             c.ctypes.data_as(ga._p), None)
+                    d2h += (m + 1) * 4 + z * 4
+                    state["i"] += 1
+                    state["off"] += z
+                return sink
+
+            e2e_ms = []
+            ctx.work_counters(reset=True)
+            dist.barrier()
+            for _ in range(args.steps):
+                ctx.flush_l2()
+                d2h = 0
+                ctx.timer_start()
+                Ad = ga.Csr.upload(ctx, m, m, rst_h, col_h, val_h)
+                sweep(ga, ctx, Ad, args.algo, args.kmin, sink=sink_factory())
+                Ad.free()
+                e2e_ms.append(ctx.timer_stop())
+            wce = ctx.work_counters(reset=True)
+            e2e_t = dist.max(sum(e2e_ms))
+            e2e = {"value": dist.sum(2.0 * wce["products"]) / (e2e_t * 1e-3) / 1e9, "unit": UNIT,
+                   "h2d_bytes_per_step": int(rst_h.nbytes + col_h.nbytes + val_h.nbytes),
+                   "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t / args.steps}
+        finally:
+            for a in pinned:
+                ga.host_unregister(a)
+
+    # ------------------------------------------------- support variants
+    variants = {}
+    for algo in ("msa", "mca", "heap"):
+        ctx.work_counters(reset=True)
+        ctx.flush_l2()
+        ctx.timer_start()
+        C = ga.mxm_masked(algo, A, A, A)
+        ms = ctx.timer_stop()
+        C.free()
+        variants[algo] = {"ms": ms, "gflops": 2.0 * ctx.work_counters()["products"] / ms / 1e6}
+
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        import oracle
+        cpu = cpu_sample(oracle.Csr(m, m, rst, col, val), args.cpu_reps)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": workload_config(args, m, nnz, kmax),
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": int(launches_per_step * args.steps), "clocks": clocks,
+        "work": {"products_per_step": wc["products"] / args.steps, "k_max": kmax,
+                 "support_products_k3": per_k.get(args.kmin, {}).get("products")},
+        "support_variants": variants,
+    }
+    ctx.close()
+    return line
+
+
+# --------------------------------------------------------- reference arm
+def run_reference(args, dist: Dist):
+    if dist.rank != 0:
+        return None
+    import graphalgo_gb300 as ga  # host-side generator only (no GPU use)
+    from graphalgo_gb300 import build as gbuild
+    import oracle
+    gbuild.build()
+    m, rst, col = ga.gen_rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, args.seed)
+    A = oracle.Csr(m, m, rst, col, np.ones(len(col), np.int32))
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_num_threads(threads)
+    prod = 0
+    for _ in range(args.warmup):
+        oracle.ktruss(A, 3)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, _, prod = oracle.ktruss(A, 3, with_products=True)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = 2.0 * prod * args.steps / total / 1e9
+    sample = (f"k=3 stage of the k-truss sweep from A ({prod:.4g} Gustavson products) per step, "
+              f"oracle port of k_truss on {threads} host threads")
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic", "impl": "reference",
+            "config": workload_config(args, m, len(col), None),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse_args()
+    dist = Dist()
+    try:
+        line = run_reference(args, dist) if args.impl == "reference" else run_gpu(args, dist)
+        if dist.rank == 0 and line is not None:
+            print(json.dumps(line), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

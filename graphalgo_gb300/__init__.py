@@ -158,6 +158,32 @@ class Context:
         _check(lib().ga_mem_info(self.handle, ctypes.byref(f), ctypes.byref(t)), self)
         return int(f.value), int(t.value)
 
+    def work_counters(self, reset: bool = False) -> dict:
+        """Masked-SpGEMM work since the last reset: products P, mask entries,
+        launches, A entries and rows (device counters)."""
+        out = (ctypes.c_int64 * 5)()
+        _check(lib().ga_ctx_work_counters(self.handle, out, int(bool(reset))), self)
+        return dict(zip(("products", "mask_entries", "launches", "a_entries", "rows"), (int(x) for x in out)))
+
+    def flush_l2(self):
+        _check(lib().ga_ctx_flush_l2(self.handle), self)
+
+
+def kernel_launches() -> int:
+    """Kernel launches issued by the library in this process (host count)."""
+    f = lib().ga_kernel_launches
+    f.restype = ctypes.c_int64
+    return int(f())
+
+
+def host_register(a: np.ndarray) -> None:
+    """Page-lock a numpy array's memory for fast asynchronous copies."""
+    _check(lib().ga_host_register(a.ctypes.data_as(_p), ctypes.c_size_t(a.nbytes)))
+
+
+def host_unregister(a: np.ndarray) -> None:
+    _check(lib().ga_host_unregister(a.ctypes.data_as(_p)))
+
 
 class Csr:
     """Device-resident CSR matrix (the reference's spMtx<T>)."""

@@ -306,7 +306,7 @@ static ga_csr ktruss(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out) 
         const int64_t cap = A->nnz > 0 ? A->nnz : 1;
         DBuf<int32_t> sup(ctx, (size_t)cap), cnt(ctx, (size_t)m + 1), tr(ctx, (size_t)m + 1), tc(ctx, (size_t)cap);
         DBuf<unsigned char> scan_scr(ctx, scan_scratch_bytes(m));
-        DBuf<unsigned char> mxm_scr(ctx, mxm_scratch_bytes(m, cap));
+        DBuf<unsigned char> mxm_scr(ctx, mxm_scratch_bytes(m, m, cap));
         DBuf<KtState> st(ctx, 1);
         KtState h0 = {};
         h0.nnz = (int32_t)A->nnz;
@@ -317,7 +317,7 @@ static ga_csr ktruss(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out) 
         auto body = [&](const LoopCtl& ctl) {
             // Tmp<C> = C*C, values aligned with C's pattern
             if (algo == GA_NAIVE) mxm_masked_into(ctx, algo, C, C, C, sup.p);
-            else mxm_masked_launch(ctx, algo, C, C, C, sup.p, mxm_scr.p);
+            else mxm_masked_launch(ctx, algo, C, C, C, sup.p, mxm_scr.p, cap);
             k_kt_count<<<grid_rows, 256, 0, ctx->stream>>>(C->rst, sup.p, m, k, cnt.p);
             post_launch("kt_count");
             scan_exclusive_i32_scratch(ctx, cnt.p, tr.p, m, scan_scr.p);

@@ -1,6 +1,7 @@
 // Context, memory, handles, validation, profiling and timing.
 #include "ga_internal.cuh"
 
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <cstdlib>
@@ -23,7 +24,10 @@ void check_cuda(cudaError_t e, const char* what, const char* file, int line) {
     fail(code, buf);
 }
 
+static std::atomic<int64_t> g_launches{0};
+
 void post_launch(const char* name) {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         char buf[256];
@@ -95,8 +99,8 @@ void csr_destroy(ga_ctx ctx, ga_csr A) {
 }
 
 // ---------------------------------------------------------------- profiling
-void prof_begin(ga_ctx ctx, const char* name) {
-    if (!ctx->profile || ctx->capturing) return;
+int prof_begin(ga_ctx ctx, const char* name) {
+    if (!ctx->profile || ctx->capturing) return -1;
     cudaEvent_t a, b;
     if (ctx->event_pool.size() >= 2) {
         a = ctx->event_pool.back(); ctx->event_pool.pop_back();
@@ -107,11 +111,12 @@ void prof_begin(ga_ctx ctx, const char* name) {
     }
     GA_CUDA(cudaEventRecord(a, ctx->stream));
     ctx->pending.push_back(PendingTiming{name, a, b});
+    return (int)ctx->pending.size() - 1;
 }
 
-void prof_end(ga_ctx ctx) {
-    if (!ctx->profile || ctx->capturing || ctx->pending.empty()) return;
-    cudaEventRecord(ctx->pending.back().stop, ctx->stream);
+void prof_end(ga_ctx ctx, int token) {
+    if (token < 0 || token >= (int)ctx->pending.size()) return;
+    cudaEventRecord(ctx->pending[token].stop, ctx->stream);
 }
 
 static void prof_collect(ga_ctx ctx) {
@@ -266,6 +271,8 @@ int ga_ctx_create(int device, void* stream, ga_ctx* out) {
         uint64_t threshold = UINT64_MAX;  // keep freed blocks cached in the pool
         GA_CUDA(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &threshold));
         GA_CUDA(cudaMallocHost((void**)&ctx->h_pinned, 64));
+        GA_CUDA(cudaMalloc((void**)&ctx->d_counters, sizeof(unsigned long long) * GA_CTR_COUNT));
+        GA_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * GA_CTR_COUNT, ctx->stream));
         GA_CUDA(cudaEventCreate(&ctx->timer_start));
         GA_CUDA(cudaEventCreate(&ctx->timer_stop));
         *out = ctx;
@@ -274,6 +281,7 @@ int ga_ctx_create(int device, void* stream, ga_ctx* out) {
         int code = e.code;
         // the caller has no context to query; keep the message on stderr
         fprintf(stderr, "graphalgo_gb300: ga_ctx_create: %s\n", e.msg.c_str());
+        if (ctx->d_counters) cudaFree(ctx->d_counters);
         if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
         if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
@@ -293,8 +301,54 @@ int ga_ctx_destroy(ga_ctx ctx) {
     if (ctx->timer_start) cudaEventDestroy(ctx->timer_start);
     if (ctx->timer_stop) cudaEventDestroy(ctx->timer_stop);
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+    if (ctx->d_counters) cudaFree(ctx->d_counters);
+    if (ctx->l2_flush) cudaFree(ctx->l2_flush);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
+    return GA_OK;
+}
+
+int64_t ga_kernel_launches(void) { return ga::g_launches.load(std::memory_order_relaxed); }
+
+int ga_ctx_work_counters(ga_ctx ctx, int64_t* out, int reset) {
+    if (!ctx || !out) return GA_ERR_INVALID_ARG;
+    GA_API_BODY(ctx, {
+        unsigned long long h[GA_CTR_COUNT];
+        GA_CUDA(cudaMemcpyAsync(h, ctx->d_counters, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+        GA_CUDA(cudaStreamSynchronize(ctx->stream));
+        for (int i = 0; i < GA_CTR_COUNT; ++i) out[i] = (int64_t)h[i];
+        if (reset) GA_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(h), ctx->stream));
+    });
+}
+
+int ga_ctx_flush_l2(ga_ctx ctx) {
+    if (!ctx) return GA_ERR_INVALID_ARG;
+    GA_API_BODY(ctx, {
+        if (!ctx->l2_flush) {
+            ctx->l2_flush_bytes = (size_t)256 << 20;
+            GA_CUDA(cudaMalloc(&ctx->l2_flush, ctx->l2_flush_bytes));
+        }
+        GA_CUDA(cudaMemsetAsync(ctx->l2_flush, ctx->l2_flush_bytes & 0xff, ctx->l2_flush_bytes, ctx->stream));
+    });
+}
+
+int ga_host_register(void* ptr, size_t bytes) {
+    if (!ptr || !bytes) return GA_ERR_INVALID_ARG;
+    cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return GA_ERR_CUDA;
+    }
+    return GA_OK;
+}
+
+int ga_host_unregister(void* ptr) {
+    if (!ptr) return GA_ERR_INVALID_ARG;
+    cudaError_t e = cudaHostUnregister(ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return GA_ERR_CUDA;
+    }
     return GA_OK;
 }
 

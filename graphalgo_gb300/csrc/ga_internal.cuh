@@ -66,6 +66,11 @@ struct ga_ctx_s {
     // pinned host word for small read-backs
     int64_t* h_pinned = nullptr;
     bool capturing = false;
+    // device work counters (GA_CTR_*), accumulated by the masked-SpGEMM binning
+    unsigned long long* d_counters = nullptr;
+    // scratch written to evict the L2 between benchmark steps
+    void* l2_flush = nullptr;
+    size_t l2_flush_bytes = 0;
 };
 
 struct ga_csr_s {
@@ -132,12 +137,13 @@ void csr_destroy(ga_ctx ctx, ga_csr A);
 // ------------------------------------------------------------- profiling
 // Begin/end a named kernel region on the context stream (no-op unless the
 // GA_OPT_PROFILE option is on and no graph capture is running).
-void prof_begin(ga_ctx ctx, const char* name);
-void prof_end(ga_ctx ctx);
+int prof_begin(ga_ctx ctx, const char* name);  // returns a token for prof_end (-1: off)
+void prof_end(ga_ctx ctx, int token);
 struct ProfScope {
     ga_ctx ctx;
-    ProfScope(ga_ctx c, const char* name) : ctx(c) { prof_begin(c, name); }
-    ~ProfScope() { prof_end(ctx); }
+    int token;
+    ProfScope(ga_ctx c, const char* name) : ctx(c), token(prof_begin(c, name)) {}
+    ~ProfScope() { prof_end(ctx, token); }
 };
 void post_launch(const char* name);
 
@@ -164,8 +170,9 @@ ga_csr copy_csr(ga_ctx ctx, ga_csr A, ga_dtype to);
 // Masked SpGEMM into caller-provided value storage aligned with M.
 void mxm_masked_into(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals);
 ga_csr mxm_cmask(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M);
-size_t mxm_scratch_bytes(int64_t m, int64_t mask_nnz);
-void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals, void* scratch);
+size_t mxm_scratch_bytes(int64_t m, int64_t n, int64_t mask_nnz);
+void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals, void* scratch,
+                       int64_t cap_nnz);
 void scan_exclusive_i32_scratch(ga_ctx ctx, const int32_t* in, int32_t* out, int64_t n, void* scratch);
 
 // Read one device value to the host (synchronises the stream).

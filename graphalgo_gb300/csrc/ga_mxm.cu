@@ -2,25 +2,29 @@
 //
 // Design (one pass, no symbolic phase: the output pattern is M's):
 //  1. k_row_bin: one warp per output row computes the mask length m_i and the
-//     Gustavson product count P_i = sum_{k in A_i} nnz(B_k); rows with an
-//     empty mask are skipped, rows with no products get explicit zeros, the
-//     rest go to a warp queue (short mask rows, few products) or a CTA queue
-//     (long mask rows or many products; mask rows longer than kCtaSlots are
-//     split into slot chunks, each chunk restricted to its column range).
+//     Gustavson product count P_i = sum_{k in A_i} nnz(B_k). Rows with an
+//     empty mask are skipped, rows without products get explicit zeros, short
+//     light rows (m_i <= kWarpSlots, P_i <= kWarpMaxFlops) go to a warp
+//     queue, all others to a CTA queue as windows of at most kCtaSlots mask
+//     slots spanning fewer than kWinCols columns (heavy rows first).
 //  2. k_mxm_masked: a persistent kernel (one wave of CTAs sized by occupancy)
-//     drains the CTA queue, then each warp drains the warp queue. Per row the
+//     drains the CTA queue, then every warp drains the warp queue. The
 //     accumulator is indexed by mask slot and lives in shared memory.
-//     The column -> slot lookup is the variant:
-//       GA_MSA  : open-addressing hash of the mask row in shared memory;
-//       GA_MCA  : binary search of the sorted mask row in shared memory
-//                 (the reference MCA walks the mask row, matrix_la.h:625-632);
+//     Column -> slot lookup per variant:
+//       GA_MSA  : a dense bitmap of the window's mask columns in shared memory
+//                 (the reference MSA keeps a dense state array over the
+//                 columns, matrix_la.h:681-749); a set bit is resolved to its
+//                 slot by binary search. Warp rows use a 4096-bit hashed filter.
+//       GA_MCA  : binary search of the sorted mask row in shared memory (the
+//                 reference MCA walks the mask row, matrix_la.h:625-632);
 //       GA_HEAP : warp-cooperative sorted merge of each B row against the
 //                 mask row (replaces the priority-queue merge,
 //                 matrix_la.h:1030-1084).
-//     MSA and MCA flatten the products of 32 A entries across the warp's
-//     lanes (a warp scan of the B row lengths, then each lane walks the
-//     flattened index), so hub rows of B keep every lane busy and B's column
-//     stream is read coalesced.
+//     Work distribution inside a CTA item: warps take the row's A entries 32
+//     at a time; B rows of up to kLongSeg entries are flattened over the
+//     warp's lanes (warp scan of the lengths, lanes walk the flattened index);
+//     longer B rows (hubs) go to a shared list and are cut into kChunk-entry
+//     pieces that all warps of the CTA stream coalesced.
 // Integer results are exact and equal across variants; floating-point sums
 // are accumulated with shared-memory atomics (order not fixed).
 #include "ga_device.cuh"
@@ -29,18 +33,26 @@ namespace ga {
 
 constexpr int kMxmThreads = 512;
 constexpr int kMxmWarps = kMxmThreads / 32;
-constexpr int kCtaSlots = 4096;      // mask slots per CTA work item
-constexpr int kCtaTblBits = 13;      // 8192-entry hash table
-constexpr int kWarpSlots = 128;      // mask slots per warp row
-constexpr int kWarpTblBits = 8;      // 256-entry hash table
-constexpr int64_t kWarpMaxFlops = 1 << 16;  // rows above this go to a CTA
+constexpr int kCtaSlots = 4096;            // mask slots per CTA work item
+constexpr int kWinCols = 1 << 18;          // column span of a CTA work item
+constexpr int kWinWords = kWinCols / 32;   // dense bitmap words
+constexpr int kWarpSlots = 256;            // mask slots per warp row
+constexpr int kWarpTblBits = 9;            // warp-row hash table: 512 entries
+constexpr int kFilterBits = 12;            // warp-row filter: 4096 bits
+constexpr int64_t kWarpMaxFlops = 32768;   // rows above this go to a CTA
+constexpr int64_t kHeavyFlops = 1 << 20;   // CTA items scheduled first
+constexpr int kLongSeg = 256;              // B rows longer than this are shared by the CTA
+constexpr int kLongCap = 1024;             // long B rows listed per item
+constexpr int kChunk = 1024;               // entries per long-row piece
 
 struct MxmQueue {
     int32_t warp_count;
-    int32_t cta_count;
+    int32_t heavy_count;   // CTA items at the front of the item array
+    int32_t normal_count;  // CTA items at the back
     int32_t warp_next;
     int32_t cta_next;
-    unsigned long long flops;  // total products (reported)
+    int32_t pad;
+    unsigned long long flops;
 };
 
 template <typename T, typename A>
@@ -52,12 +64,15 @@ struct MxmArgs {
     int64_t m;
     MxmQueue* q;
     int32_t* warp_rows;
-    int2* cta_items;
+    int4* cta_items;          // (row, first slot, end slot, unused)
+    int32_t cta_cap;
+    unsigned long long* ctr;  // context work counters (GA_CTR_*)
 };
 
 __global__ void k_reset_queue(MxmQueue* q) {
     if (threadIdx.x == 0) {
-        q->warp_count = 0; q->cta_count = 0; q->warp_next = 0; q->cta_next = 0; q->flops = 0ull;
+        q->warp_count = 0; q->heavy_count = 0; q->normal_count = 0;
+        q->warp_next = 0; q->cta_next = 0; q->flops = 0ull;
     }
 }
 
@@ -66,12 +81,18 @@ template <typename T, typename A>
 __global__ void k_row_bin(MxmArgs<T, A> p) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    unsigned long long my_flops = 0;
+    unsigned long long my_flops = 0, my_mask = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(&p.ctr[GA_CTR_LAUNCHES], 1ull);
+        atomicAdd(&p.ctr[GA_CTR_A_ENTRIES], (unsigned long long)(p.ar[p.m] - p.ar[0]));
+        atomicAdd(&p.ctr[GA_CTR_ROWS], (unsigned long long)p.m);
+    }
     for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < p.m; i += warps) {
-        int32_t mb = p.mr[i], me = p.mr[i + 1];
-        int32_t mi = me - mb;
+        const int32_t mb = p.mr[i], me = p.mr[i + 1];
+        const int32_t mi = me - mb;
         if (mi == 0) continue;
-        int32_t ab = p.ar[i], ae = p.ar[i + 1];
+        if (lane == 0) my_mask += (unsigned long long)mi;
+        const int32_t ab = p.ar[i], ae = p.ar[i + 1];
         long long f = 0;
         for (int32_t t = ab + lane; t < ae; t += 32) {
             int32_t k = p.ac[t];
@@ -88,179 +109,379 @@ __global__ void k_row_bin(MxmArgs<T, A> p) {
                 int pos = atomicAdd(&p.q->warp_count, 1);
                 p.warp_rows[pos] = (int32_t)i;
             } else {
-                int chunks = (mi + kCtaSlots - 1) / kCtaSlots;
-                int pos = atomicAdd(&p.q->cta_count, chunks);
-                for (int c = 0; c < chunks; ++c) p.cta_items[pos + c] = make_int2((int)i, c);
+                const int32_t* mcol = p.mc + mb;
+                const bool heavy = f >= kHeavyFlops;
+                int s0 = 0;
+                while (s0 < mi) {
+                    int s1 = min(mi, s0 + kCtaSlots);
+                    const int32_t c0 = mcol[s0];
+                    if (mcol[s1 - 1] - c0 >= kWinCols) {
+                        const int64_t lim = (int64_t)c0 + (kWinCols - 1);
+                        s1 = s0 + upper_bound_i32(mcol + s0, s1 - s0, (int32_t)(lim < INT32_MAX ? lim : INT32_MAX));
+                    }
+                    int pos;
+                    if (heavy) pos = atomicAdd(&p.q->heavy_count, 1);
+                    else pos = p.cta_cap - 1 - atomicAdd(&p.q->normal_count, 1);
+                    p.cta_items[pos] = make_int4((int)i, s0, s1, 0);
+                    s0 = s1;
+                }
             }
         }
     }
-    if (lane == 0 && my_flops) atomicAdd(&p.q->flops, my_flops);
+    if (lane == 0 && my_flops) {
+        atomicAdd(&p.q->flops, my_flops);
+        atomicAdd(&p.ctr[GA_CTR_PRODUCTS], my_flops);
+    }
+    if (lane == 0 && my_mask) atomicAdd(&p.ctr[GA_CTR_MASK_ENTRIES], my_mask);
 }
 
 // ------------------------------------------------------------------ lookups
-enum { LK_HASH = 0, LK_BSEARCH = 1, LK_MERGE = 2 };
+// MODE: how a product's column finds its mask slot.
+enum { MD_DENSE = 0, MD_HASHED = 1, MD_BSEARCH = 2, MD_MERGE = 3 };
 
-struct SlotTable {
-    int32_t* keys;    // hash keys (LK_HASH) or sorted mask columns (others)
-    uint16_t* slots;  // hash payload (LK_HASH)
-    int bits;
-    int ns;           // slots in this item
-    int32_t lo, hi;   // column range of the item
+// The mask columns of one work item, staged in shared memory.
+struct SlotView {
+    const int32_t* mcol;    // MD_BSEARCH / MD_MERGE: sorted mask columns
+    const uint32_t* bits;   // MD_DENSE: bitmap over [lo, lo + kWinCols)
+    const uint16_t* wbase;  // MD_DENSE: slot of the first mask column of each bitmap word
+    const uint32_t* filt;   // MD_HASHED: 4096-bit filter of hashed columns
+    const int32_t* hkeys;   // MD_HASHED: open-addressing table (2^kWarpTblBits)
+    const uint8_t* hslot;
+    int ns;
+    int32_t lo, hi;
 };
 
-template <int LK>
-__device__ __forceinline__ int slot_of(const SlotTable& t, int32_t c) {
-    if (LK == LK_HASH) {
-        return hash_find<uint16_t>(t.keys, t.slots, t.bits, c);
+template <int MD>
+__device__ __forceinline__ int slot_of(const SlotView& v, int32_t c) {
+    if (MD == MD_DENSE) {
+        // dense state over the window: a set bit is a mask column, and its
+        // slot is the word's first slot plus the set bits below it
+        const uint32_t d = (uint32_t)(c - v.lo);
+        if (d > (uint32_t)(v.hi - v.lo)) return -1;
+        const uint32_t w = v.bits[d >> 5];
+        const uint32_t b = d & 31;
+        if (!((w >> b) & 1u)) return -1;
+        return (int)v.wbase[d >> 5] + __popc(w & ((1u << b) - 1u));
+    } else if (MD == MD_HASHED) {
+        const uint32_t h = hash_col(c);
+        const uint32_t f = h >> (32 - kFilterBits);
+        if (!((v.filt[f >> 5] >> (f & 31)) & 1u)) return -1;
+        const uint32_t mask = (1u << kWarpTblBits) - 1u;
+        uint32_t pos = h >> (32 - kWarpTblBits);
+        while (true) {
+            const int32_t key = v.hkeys[pos];
+            if (key == c) return (int)v.hslot[pos];
+            if (key == kEmpty) return -1;
+            pos = (pos + 1) & mask;
+        }
     } else {
-        if (c < t.lo || c > t.hi) return -1;
-        int pos = lower_bound_i32(t.keys, t.ns, c);
-        return (pos < t.ns && t.keys[pos] == c) ? pos : -1;
+        if (c < v.lo || c > v.hi) return -1;
+        const int pos = lower_bound_i32(v.mcol, v.ns, c);
+        return (pos < v.ns && v.mcol[pos] == c) ? pos : -1;
     }
 }
 
-// Products of A entries [t, t+32) (lane-strided group) for one output row,
-// flattened over the warp. s_incl/s_off/s_a are this warp's 32-entry scratch.
-template <int LK, typename T, typename A>
-__device__ __forceinline__ void group_products(const MxmArgs<T, A>& p, int32_t t_first, int32_t t_end,
-                                               const SlotTable& tbl, A* acc, bool clip, int* s_incl, int* s_off,
-                                               A* s_a) {
+template <int MD, typename T, typename A>
+__device__ __forceinline__ void add_product(const MxmArgs<T, A>& p, const SlotView& v, A* acc, int32_t j, int32_t c,
+                                            A a) {
+    const int slot = slot_of<MD>(v, c);
+    if (slot >= 0) atomic_add_acc<A>(&acc[slot], a * to_acc<T, A>(__ldg(p.bv + j)));
+}
+
+// B-row range of A entry t, optionally clipped to the item's column window.
+template <typename T, typename A>
+__device__ __forceinline__ void b_range(const MxmArgs<T, A>& p, int32_t t, bool clip, int32_t lo, int32_t hi,
+                                        int32_t& bs, int32_t& be) {
+    const int32_t k = __ldg(p.ac + t);
+    bs = __ldg(p.br + k);
+    be = __ldg(p.br + k + 1);
+    if (clip) {
+        const int n = be - bs;
+        const int l = lower_bound_i32(p.bc + bs, n, lo);
+        const int h = upper_bound_i32(p.bc + bs, n, hi);
+        be = bs + h;
+        bs = bs + l;
+    }
+}
+
+// Flattened products of the 32 A entries starting at t_first (one per lane).
+// Non-empty B rows are compacted; for each window of 32 consecutive product
+// indices the segment ends falling inside it form one 32-bit mask (a warp OR
+// reduction), so every lane finds its B row with a popcount - no per-lane
+// search loop. Lanes whose B row is long may hand it to the CTA's long list.
+template <int MD, typename T, typename A, bool PUSH>
+__device__ __forceinline__ void group_products(const MxmArgs<T, A>& p, int32_t t_first, int32_t t_end, bool clip,
+                                               const SlotView& v, A* acc, int* s_incl, int* s_off, A* s_a,
+                                               int* s_nlong, int32_t* s_lbs, int32_t* s_lend, A* s_la) {
+    const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    int32_t t = t_first + lane;
+    const int32_t t = t_first + lane;
     int len = 0;
     int32_t bs = 0;
     A av = (A)0;
     if (t < t_end) {
-        int32_t k = p.ac[t];
-        av = to_acc<T, A>(p.av[t]);
-        bs = p.br[k];
-        int32_t be = p.br[k + 1];
-        if (clip) {
-            int n = be - bs;
-            int lo = lower_bound_i32(p.bc + bs, n, tbl.lo);
-            int hi = upper_bound_i32(p.bc + bs, n, tbl.hi);
-            be = bs + hi;
-            bs = bs + lo;
-        }
+        int32_t be;
+        b_range(p, t, clip, v.lo, v.hi, bs, be);
+        av = to_acc<T, A>(__ldg(p.av + t));
         len = be - bs;
+        if (PUSH && len > kLongSeg) {
+            const int slot = atomicAdd(s_nlong, 1);
+            if (slot < kLongCap) {
+                s_lbs[slot] = bs;
+                s_lend[slot] = be;
+                s_la[slot] = av;
+                len = 0;
+            }
+        }
     }
-    int incl = warp_incl_scan(len);
-    int total = __shfl_sync(0xffffffffu, incl, 31);
-    s_incl[lane] = incl;
-    s_off[lane] = bs - (incl - len);
-    s_a[lane] = av;
+    const unsigned nz = __ballot_sync(FULL, len > 0);
+    if (nz == 0) return;
+    const int nseg = __popc(nz);
+    const int incl = warp_incl_scan(len);
+    const int total = __shfl_sync(FULL, incl, 31);
+    if (len > 0) {
+        const int rank = __popc(nz & ((1u << lane) - 1u));
+        s_incl[rank] = incl;
+        s_off[rank] = bs - (incl - len);
+        s_a[rank] = av;
+    }
     __syncwarp();
-    int q = 0;
-    for (int pidx = lane; pidx < total; pidx += 32) {
-        while (s_incl[q] <= pidx) ++q;
-        int32_t j = pidx + s_off[q];
-        int32_t c = __ldg(p.bc + j);
-        int slot = slot_of<LK>(tbl, c);
-        if (slot >= 0) atomic_add_acc<A>(&acc[slot], s_a[q] * to_acc<T, A>(__ldg(p.bv + j)));
+    const int my_end = lane < nseg ? s_incl[lane] - 1 : INT32_MAX;  // last product of segment `lane`
+    const unsigned lt = (1u << lane) - 1u;
+    int q_base = 0;
+    int base = 0;
+    for (; base + 32 < total; base += 64) {
+        const int e0 = my_end - base, e1 = my_end - base - 32;
+        const unsigned bm0 = __reduce_or_sync(FULL, (e0 >= 0 && e0 < 32) ? (1u << e0) : 0u);
+        const unsigned bm1 = __reduce_or_sync(FULL, (e1 >= 0 && e1 < 32) ? (1u << e1) : 0u);
+        const int q0 = q_base + __popc(bm0 & lt);
+        const int q1 = q_base + __popc(bm0) + __popc(bm1 & lt);
+        const int x1 = base + 32 + lane;
+        const int32_t j0 = base + lane + s_off[q0];
+        const int32_t c0 = __ldg(p.bc + j0);
+        int32_t j1 = 0, c1 = 0;
+        if (x1 < total) {
+            j1 = x1 + s_off[q1];
+            c1 = __ldg(p.bc + j1);
+        }
+        add_product<MD, T, A>(p, v, acc, j0, c0, s_a[q0]);
+        if (x1 < total) add_product<MD, T, A>(p, v, acc, j1, c1, s_a[q1]);
+        q_base += __popc(bm0) + __popc(bm1);
+    }
+    if (base < total) {
+        const int e0 = my_end - base;
+        const unsigned bm0 = __reduce_or_sync(FULL, (e0 >= 0 && e0 < 32) ? (1u << e0) : 0u);
+        const int x = base + lane;
+        if (x < total) {
+            const int q = q_base + __popc(bm0 & lt);
+            const int32_t j = x + s_off[q];
+            add_product<MD, T, A>(p, v, acc, j, __ldg(p.bc + j), s_a[q]);
+        }
     }
     __syncwarp();
 }
 
-// Warp-cooperative sorted merge of B row k (columns [bs, be)) against the
-// item's sorted mask columns; matches add a*b into the slot accumulator.
+// Stream B entries [j0, j1) of one row with scalar head/tail and int4 body.
+template <int MD, typename T, typename A>
+__device__ __forceinline__ void stream_row(const MxmArgs<T, A>& p, const SlotView& v, A* acc, int32_t j0,
+                                           int32_t j1, A a) {
+    const int lane = threadIdx.x & 31;
+    int32_t ja = (j0 + 3) & ~3;
+    if (ja > j1) ja = j1;
+    if (j0 + lane < ja) add_product<MD, T, A>(p, v, acc, j0 + lane, __ldg(p.bc + j0 + lane), a);
+    const int32_t groups = (j1 - ja) >> 2;
+    const int4* b4 = reinterpret_cast<const int4*>(p.bc + ja);
+    int32_t g = lane;
+    for (; g + 32 < groups; g += 64) {
+        const int4 x = __ldg(b4 + g);
+        const int4 y = __ldg(b4 + g + 32);
+        const int32_t j = ja + 4 * g, jy = j + 128;
+        add_product<MD, T, A>(p, v, acc, j, x.x, a);
+        add_product<MD, T, A>(p, v, acc, j + 1, x.y, a);
+        add_product<MD, T, A>(p, v, acc, j + 2, x.z, a);
+        add_product<MD, T, A>(p, v, acc, j + 3, x.w, a);
+        add_product<MD, T, A>(p, v, acc, jy, y.x, a);
+        add_product<MD, T, A>(p, v, acc, jy + 1, y.y, a);
+        add_product<MD, T, A>(p, v, acc, jy + 2, y.z, a);
+        add_product<MD, T, A>(p, v, acc, jy + 3, y.w, a);
+    }
+    if (g < groups) {
+        const int4 x = __ldg(b4 + g);
+        const int32_t j = ja + 4 * g;
+        add_product<MD, T, A>(p, v, acc, j, x.x, a);
+        add_product<MD, T, A>(p, v, acc, j + 1, x.y, a);
+        add_product<MD, T, A>(p, v, acc, j + 2, x.z, a);
+        add_product<MD, T, A>(p, v, acc, j + 3, x.w, a);
+    }
+    const int32_t jt = ja + 4 * groups;
+    if (jt + lane < j1) add_product<MD, T, A>(p, v, acc, jt + lane, __ldg(p.bc + jt + lane), a);
+}
+
+// Warp-cooperative sorted merge of B row [bs, be) against the item's sorted
+// mask columns; matches add a*b into the slot accumulator.
 template <typename T, typename A>
-__device__ __forceinline__ void merge_row(const MxmArgs<T, A>& p, int32_t bs, int32_t be, A av,
-                                          const SlotTable& tbl, A* acc) {
+__device__ __forceinline__ void merge_row(const MxmArgs<T, A>& p, int32_t bs, int32_t be, A av, const SlotView& v,
+                                          A* acc) {
     const int lane = threadIdx.x & 31;
     const unsigned FULL = 0xffffffffu;
     if (bs >= be) return;
-    int32_t x0 = __ldg(p.bc + bs);
-    int yc = lower_bound_i32(tbl.keys, tbl.ns, x0);
+    const int32_t x0 = __ldg(p.bc + bs);
+    int yc = lower_bound_i32(v.mcol, v.ns, x0);
     int32_t xb = bs;
-    while (xb < be && yc < tbl.ns) {
-        int32_t x = (xb + lane < be) ? __ldg(p.bc + xb + lane) : INT32_MAX;
-        int32_t y = (yc + lane < tbl.ns) ? tbl.keys[yc + lane] : INT32_MAX;
+    while (xb < be && yc < v.ns) {
+        const int32_t x = (xb + lane < be) ? __ldg(p.bc + xb + lane) : INT32_MAX;
+        const int32_t y = (yc + lane < v.ns) ? v.mcol[yc + lane] : INT32_MAX;
         int r = 0;
 #pragma unroll
         for (int step = 16; step >= 1; step >>= 1) {
-            int32_t yy = __shfl_sync(FULL, y, r + step - 1);
+            const int32_t yy = __shfl_sync(FULL, y, r + step - 1);
             if (yy < x) r += step;
         }
-        int32_t y31 = __shfl_sync(FULL, y, 31);
+        const int32_t y31 = __shfl_sync(FULL, y, 31);
         if (r == 31 && y31 < x) r = 32;
-        int32_t yr = __shfl_sync(FULL, y, r & 31);
+        const int32_t yr = __shfl_sync(FULL, y, r & 31);
         if (r < 32 && yr == x && x != INT32_MAX)
             atomic_add_acc<A>(&acc[yc + r], av * to_acc<T, A>(__ldg(p.bv + xb + lane)));
-        int32_t x31 = __shfl_sync(FULL, x, 31);
+        const int32_t x31 = __shfl_sync(FULL, x, 31);
         if (x31 <= y31) xb += 32; else yc += 32;
     }
 }
 
-template <typename A>
+// Shared-memory layout per variant (MD of the CTA phase: MD_DENSE for MSA).
+template <int MD, typename A>
 struct MxmSmem {
+    static constexpr bool dense = MD == MD_DENSE;
+    // CTA phase
+    static constexpr size_t off_acc = 0;
+    static constexpr size_t off_lbs = off_acc + (size_t)kCtaSlots * sizeof(A);
+    static constexpr size_t off_lend = off_lbs + (size_t)kLongCap * 4;
+    static constexpr size_t off_lchunk = off_lend + (size_t)kLongCap * 4;
+    static constexpr size_t off_la = off_lchunk + (size_t)(kLongCap + 8) * 4;
+    static constexpr size_t off_key = off_la + (size_t)kLongCap * sizeof(A);  // bits+wbase or mcol
+    static constexpr size_t off_wbase = off_key + (size_t)kWinWords * 4;
     static constexpr size_t cta_bytes =
-        (size_t)(1 << kCtaTblBits) * sizeof(int32_t) + (size_t)(1 << kCtaTblBits) * sizeof(uint16_t) +
-        (size_t)kCtaSlots * sizeof(A);
-    static constexpr size_t warp_one = (size_t)(1 << kWarpTblBits) * sizeof(int32_t) +
-                                       (size_t)(1 << kWarpTblBits) * sizeof(uint16_t) + (size_t)kWarpSlots * sizeof(A);
+        dense ? off_wbase + (size_t)kWinWords * 2 : off_key + (size_t)kCtaSlots * 4;
+    // warp phase (per warp): acc, hashed filter + table (MSA) or mcol (others)
+    static constexpr size_t w_acc = 0;
+    static constexpr size_t w_filt = w_acc + (size_t)kWarpSlots * sizeof(A);
+    static constexpr size_t w_hkeys = w_filt + (size_t)(1 << kFilterBits) / 8;
+    static constexpr size_t w_hslot = w_hkeys + (size_t)(1 << kWarpTblBits) * 4;
+    static constexpr size_t w_mcol = w_filt;
+    static constexpr size_t warp_one =
+        dense ? w_hslot + (size_t)(1 << kWarpTblBits) : w_mcol + (size_t)kWarpSlots * 4;
     static constexpr size_t warp_bytes = warp_one * kMxmWarps;
+    static constexpr size_t region = cta_bytes > warp_bytes ? cta_bytes : warp_bytes;
+    // per-warp flattening scratch (both phases)
     static constexpr size_t scratch_bytes = (size_t)kMxmWarps * 32 * (2 * sizeof(int) + sizeof(A));
-    static constexpr size_t total = (cta_bytes > warp_bytes ? cta_bytes : warp_bytes) + scratch_bytes;
+    static constexpr size_t total = region + scratch_bytes;
 };
 
-template <int LK, typename T, typename A>
+template <int MD, typename T, typename A>
 __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) {
     extern __shared__ __align__(16) unsigned char smem[];
-    using SM = MxmSmem<A>;
+    using SM = MxmSmem<MD, A>;
+    constexpr bool DENSE = MD == MD_DENSE;
+    constexpr int WMD = DENSE ? MD_HASHED : MD;  // warp-row lookup
+    const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int* s_incl = reinterpret_cast<int*>(smem + (SM::total - SM::scratch_bytes)) + wid * 32;
-    int* s_off = reinterpret_cast<int*>(smem + (SM::total - SM::scratch_bytes)) + kMxmWarps * 32 + wid * 32;
-    A* s_a = reinterpret_cast<A*>(smem + (SM::total - SM::scratch_bytes) + (size_t)kMxmWarps * 32 * 2 * sizeof(int)) +
-             wid * 32;
-    __shared__ int s_item;
+    unsigned char* scr = smem + SM::region;
+    int* s_incl = reinterpret_cast<int*>(scr) + wid * 32;
+    int* s_off = reinterpret_cast<int*>(scr) + kMxmWarps * 32 + wid * 32;
+    A* s_a = reinterpret_cast<A*>(scr + (size_t)kMxmWarps * 32 * 2 * sizeof(int)) + wid * 32;
+    __shared__ int s_item, s_nlong, s_nchunks, s_chunk_next;
 
     // ------------------------------------------------------------ CTA items
     {
-        const int TBL = 1 << kCtaTblBits;
-        int32_t* keys = reinterpret_cast<int32_t*>(smem);
-        uint16_t* slots = reinterpret_cast<uint16_t*>(smem + TBL * sizeof(int32_t));
-        A* acc = reinterpret_cast<A*>(smem + TBL * (sizeof(int32_t) + sizeof(uint16_t)));
-        for (int t = threadIdx.x; t < TBL; t += blockDim.x) keys[t] = kEmpty;
-        const int ncta = p.q->cta_count;
+        A* acc = reinterpret_cast<A*>(smem + SM::off_acc);
+        int32_t* lbs = reinterpret_cast<int32_t*>(smem + SM::off_lbs);
+        int32_t* lend = reinterpret_cast<int32_t*>(smem + SM::off_lend);
+        int32_t* lchunk = reinterpret_cast<int32_t*>(smem + SM::off_lchunk);
+        A* la = reinterpret_cast<A*>(smem + SM::off_la);
+        uint32_t* bits = reinterpret_cast<uint32_t*>(smem + SM::off_key);
+        uint16_t* wbase = reinterpret_cast<uint16_t*>(smem + SM::off_wbase);
+        int32_t* mcol = reinterpret_cast<int32_t*>(smem + SM::off_key);
+        if (DENSE)
+            for (int t = threadIdx.x; t < kWinWords; t += blockDim.x) bits[t] = 0u;
+        const int nheavy = p.q->heavy_count;
+        const int ncta = nheavy + p.q->normal_count;
         while (true) {
-            if (threadIdx.x == 0) s_item = atomicAdd(&p.q->cta_next, 1);
+            if (threadIdx.x == 0) {
+                s_item = atomicAdd(&p.q->cta_next, 1);
+                s_nlong = 0;
+            }
             __syncthreads();
             const int it = s_item;
             if (it >= ncta) break;
-            const int2 item = p.cta_items[it];
+            const int4 item = p.cta_items[it < nheavy ? it : p.cta_cap - 1 - (it - nheavy)];
             const int64_t i = item.x;
             const int32_t mb = p.mr[i], mi = p.mr[i + 1] - mb;
-            const int s0 = item.y * kCtaSlots;
-            const int ns = min(kCtaSlots, mi - s0);
-            const int32_t* mcol = p.mc + mb + s0;
-            SlotTable tbl;
-            tbl.keys = keys; tbl.slots = slots; tbl.bits = kCtaTblBits; tbl.ns = ns;
-            tbl.lo = __ldg(mcol); tbl.hi = __ldg(mcol + ns - 1);
-            if (LK == LK_HASH) {
-                for (int s = threadIdx.x; s < ns; s += blockDim.x)
-                    hash_insert<uint16_t>(keys, slots, kCtaTblBits, __ldg(mcol + s), (uint16_t)s);
-            } else {
-                for (int s = threadIdx.x; s < ns; s += blockDim.x) keys[s] = __ldg(mcol + s);
+            const int s0 = item.y, ns = item.z - item.y;
+            const int32_t* gcol = p.mc + mb + s0;
+            SlotView v;
+            v.mcol = mcol; v.bits = bits; v.wbase = wbase; v.filt = nullptr; v.hkeys = nullptr; v.hslot = nullptr;
+            v.ns = ns;
+            v.lo = __ldg(gcol); v.hi = __ldg(gcol + ns - 1);
+            for (int s = threadIdx.x; s < ns; s += blockDim.x) {
+                const int32_t c = __ldg(gcol + s);
+                acc[s] = (A)0;
+                if (DENSE) {
+                    const uint32_t d = (uint32_t)(c - v.lo);
+                    atomicOr(&bits[d >> 5], 1u << (d & 31));
+                    if (s == 0 || ((uint32_t)(__ldg(gcol + s - 1) - v.lo) >> 5) != (d >> 5)) wbase[d >> 5] = (uint16_t)s;
+                } else {
+                    mcol[s] = c;
+                }
             }
-            for (int s = threadIdx.x; s < ns; s += blockDim.x) acc[s] = (A)0;
             __syncthreads();
-            const bool clip = mi > kCtaSlots;
+            const bool clip = ns < mi;
             const int32_t ab = p.ar[i], ae = p.ar[i + 1];
-            if (LK == LK_MERGE) {
+            if (MD == MD_MERGE) {
                 for (int32_t t = ab + wid; t < ae; t += kMxmWarps) {
-                    int32_t k = __ldg(p.ac + t);
-                    A av = to_acc<T, A>(__ldg(p.av + t));
-                    int32_t bs = __ldg(p.br + k), be = __ldg(p.br + k + 1);
-                    merge_row<T, A>(p, bs, be, av, tbl, acc);
+                    int32_t bs, be;
+                    b_range(p, t, clip, v.lo, v.hi, bs, be);
+                    merge_row<T, A>(p, bs, be, to_acc<T, A>(__ldg(p.av + t)), v, acc);
                 }
             } else {
+                // phase A: short B rows flattened per warp, long ones listed
                 for (int32_t g = ab + wid * 32; g < ae; g += kMxmWarps * 32)
-                    group_products<LK, T, A>(p, g, ae, tbl, acc, clip, s_incl, s_off, s_a);
+                    group_products<MD, T, A, true>(p, g, ae, clip, v, acc, s_incl, s_off, s_a, &s_nlong, lbs, lend, la);
+                __syncthreads();
+                // phase B: long B rows cut into kChunk pieces shared by all warps
+                const int nlong = min(s_nlong, kLongCap);
+                if (nlong > 0) {
+                    if (wid == 0) {
+                        int running = 0;
+                        for (int base = 0; base < nlong; base += 32) {
+                            const int x = base + lane;
+                            const int c = x < nlong ? (lend[x] - lbs[x] + kChunk - 1) / kChunk : 0;
+                            const int incl = warp_incl_scan(c);
+                            if (x < nlong) lchunk[x + 1] = running + incl;
+                            running += __shfl_sync(FULL, incl, 31);
+                        }
+                        if (lane == 0) {
+                            lchunk[0] = 0;
+                            s_nchunks = running;
+                            s_chunk_next = 0;
+                        }
+                    }
+                    __syncthreads();
+                    const int nch = s_nchunks;
+                    while (true) {
+                        int c = 0;
+                        if (lane == 0) c = atomicAdd(&s_chunk_next, 1);
+                        c = __shfl_sync(FULL, c, 0);
+                        if (c >= nch) break;
+                        const int seg = upper_bound_i32(lchunk + 1, nlong, c);
+                        const int32_t j0 = lbs[seg] + (c - lchunk[seg]) * kChunk;
+                        const int32_t j1 = min(lend[seg], j0 + kChunk);
+                        stream_row<MD, T, A>(p, v, acc, j0, j1, la[seg]);
+                    }
+                }
             }
             __syncthreads();
-            for (int s = threadIdx.x; s < ns; s += blockDim.x) p.cv[mb + s0 + s] = from_acc<T, A>(acc[s]);
-            if (LK == LK_HASH) {
-                for (int t = threadIdx.x; t < TBL; t += blockDim.x) keys[t] = kEmpty;
+            for (int s = threadIdx.x; s < ns; s += blockDim.x) {
+                p.cv[mb + s0 + s] = from_acc<T, A>(acc[s]);
+                if (DENSE) bits[(uint32_t)(__ldg(gcol + s) - v.lo) >> 5] = 0u;
             }
             __syncthreads();
         }
@@ -268,77 +489,100 @@ __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) 
 
     // ----------------------------------------------------------- warp rows
     {
-        const int TBL = 1 << kWarpTblBits;
         unsigned char* base = smem + wid * SM::warp_one;
-        int32_t* keys = reinterpret_cast<int32_t*>(base);
-        uint16_t* slots = reinterpret_cast<uint16_t*>(base + TBL * sizeof(int32_t));
-        A* acc = reinterpret_cast<A*>(base + TBL * (sizeof(int32_t) + sizeof(uint16_t)));
-        for (int t = lane; t < TBL; t += 32) keys[t] = kEmpty;
+        A* acc = reinterpret_cast<A*>(base + SM::w_acc);
+        uint32_t* filt = reinterpret_cast<uint32_t*>(base + SM::w_filt);
+        int32_t* hkeys = reinterpret_cast<int32_t*>(base + SM::w_hkeys);
+        uint8_t* hslot = reinterpret_cast<uint8_t*>(base + SM::w_hslot);
+        int32_t* mcol = reinterpret_cast<int32_t*>(base + SM::w_mcol);
+        constexpr int FW = (1 << kFilterBits) / 32;
+        constexpr int TBL = 1 << kWarpTblBits;
+        if (DENSE) {
+            for (int t = lane; t < FW; t += 32) filt[t] = 0u;
+            for (int t = lane; t < TBL; t += 32) hkeys[t] = kEmpty;
+        }
         __syncwarp();
         const int nwarp = p.q->warp_count;
         while (true) {
             int r = 0;
             if (lane == 0) r = atomicAdd(&p.q->warp_next, 1);
-            r = __shfl_sync(0xffffffffu, r, 0);
+            r = __shfl_sync(FULL, r, 0);
             if (r >= nwarp) break;
             const int64_t i = p.warp_rows[r];
             const int32_t mb = p.mr[i], mi = p.mr[i + 1] - mb;
-            const int32_t* mcol = p.mc + mb;
-            SlotTable tbl;
-            tbl.keys = keys; tbl.slots = slots; tbl.bits = kWarpTblBits; tbl.ns = mi;
-            tbl.lo = __ldg(mcol); tbl.hi = __ldg(mcol + mi - 1);
-            if (LK == LK_HASH) {
-                for (int s = lane; s < mi; s += 32)
-                    hash_insert<uint16_t>(keys, slots, kWarpTblBits, __ldg(mcol + s), (uint16_t)s);
-            } else {
-                for (int s = lane; s < mi; s += 32) keys[s] = __ldg(mcol + s);
+            const int32_t* gcol = p.mc + mb;
+            SlotView v;
+            v.mcol = mcol; v.bits = nullptr; v.wbase = nullptr; v.filt = filt; v.hkeys = hkeys; v.hslot = hslot;
+            v.ns = mi;
+            v.lo = __ldg(gcol); v.hi = __ldg(gcol + mi - 1);
+            for (int s = lane; s < mi; s += 32) {
+                const int32_t c = __ldg(gcol + s);
+                acc[s] = (A)0;
+                if (DENSE) {
+                    const uint32_t h = hash_col(c);
+                    const uint32_t f = h >> (32 - kFilterBits);
+                    atomicOr(&filt[f >> 5], 1u << (f & 31));
+                    hash_insert<uint8_t>(hkeys, hslot, kWarpTblBits, c, (uint8_t)s);
+                } else {
+                    mcol[s] = c;
+                }
             }
-            for (int s = lane; s < mi; s += 32) acc[s] = (A)0;
             __syncwarp();
             const int32_t ab = p.ar[i], ae = p.ar[i + 1];
-            if (LK == LK_MERGE) {
+            if (MD == MD_MERGE) {
                 for (int32_t t = ab; t < ae; ++t) {
-                    int32_t k = __ldg(p.ac + t);
-                    A av = to_acc<T, A>(__ldg(p.av + t));
-                    merge_row<T, A>(p, __ldg(p.br + k), __ldg(p.br + k + 1), av, tbl, acc);
+                    int32_t bs, be;
+                    b_range(p, t, false, 0, 0, bs, be);
+                    merge_row<T, A>(p, bs, be, to_acc<T, A>(__ldg(p.av + t)), v, acc);
                 }
             } else {
                 for (int32_t g = ab; g < ae; g += 32)
-                    group_products<LK, T, A>(p, g, ae, tbl, acc, false, s_incl, s_off, s_a);
+                    group_products<WMD, T, A, false>(p, g, ae, false, v, acc, s_incl, s_off, s_a, nullptr, nullptr,
+                                                     nullptr, nullptr);
             }
             __syncwarp();
             for (int s = lane; s < mi; s += 32) p.cv[mb + s] = from_acc<T, A>(acc[s]);
-            if (LK == LK_HASH) {
-                for (int t = lane; t < TBL; t += 32) keys[t] = kEmpty;
+            if (DENSE) {
+                for (int t = lane; t < FW; t += 32) filt[t] = 0u;
+                for (int t = lane; t < TBL; t += 32) hkeys[t] = kEmpty;
             }
             __syncwarp();
         }
     }
 }
 
+static int64_t cta_item_cap(int64_t m, int64_t n, int64_t mask_nnz) {
+    // windows per row <= ceil(m_i / kCtaSlots) + ceil(n / kWinCols), and <= m_i
+    const int64_t per_row = 1 + (n + kWinCols - 1) / kWinCols;
+    int64_t cap = m * per_row + mask_nnz / kCtaSlots + 1;
+    if (cap > mask_nnz + 1) cap = mask_nnz + 1;
+    return cap;
+}
+
 // Launch the masked product for one value type and lookup variant.
 template <int LK, typename T>
 static void launch_masked(ga_ctx ctx, ga_csr A_, ga_csr B_, ga_csr M_, T* cv, MxmQueue* q, int32_t* warp_rows,
-                          int2* cta_items) {
+                          int4* cta_items, int32_t cta_cap) {
     using Ac = typename Acc<T>::type;
     MxmArgs<T, Ac> p;
     p.ar = A_->rst; p.ac = A_->col; p.av = static_cast<const T*>(A_->val);
     p.br = B_->rst; p.bc = B_->col; p.bv = static_cast<const T*>(B_->val);
     p.mr = M_->rst; p.mc = M_->col;
-    p.cv = cv; p.m = M_->m; p.q = q; p.warp_rows = warp_rows; p.cta_items = cta_items;
+    p.cv = cv; p.m = M_->m; p.q = q; p.warp_rows = warp_rows; p.cta_items = cta_items; p.cta_cap = cta_cap;
+    p.ctr = ctx->d_counters;
     {
         ProfScope ps(ctx, "mxm_row_bin");
         int grid = grid_for(p.m * 32, 256, ctx->num_sms * 16);
         k_row_bin<T, Ac><<<grid, 256, 0, ctx->stream>>>(p);
         post_launch("mxm_row_bin");
     }
-    const size_t smem = MxmSmem<Ac>::total;
+    const size_t smem = MxmSmem<LK, Ac>::total;
     auto kern = k_mxm_masked<LK, T, Ac>;
     GA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     GA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMxmThreads, smem));
     if (per_sm < 1) per_sm = 1;
-    const char* name = LK == LK_HASH ? "mxm_msa" : LK == LK_BSEARCH ? "mxm_mca" : "mxm_heap_merge";
+    const char* name = LK == MD_DENSE ? "mxm_msa" : LK == MD_BSEARCH ? "mxm_mca" : "mxm_heap_merge";
     ProfScope ps(ctx, name);
     kern<<<ctx->num_sms * per_sm, kMxmThreads, smem, ctx->stream>>>(p);
     post_launch(name);
@@ -346,28 +590,30 @@ static void launch_masked(ga_ctx ctx, ga_csr A_, ga_csr B_, ga_csr M_, T* cv, Mx
 
 void naive_masked_into(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M, void* d_cvals);
 
-size_t mxm_scratch_bytes(int64_t m, int64_t mask_nnz) {
-    const int64_t cap_cta = m + mask_nnz / kCtaSlots + 1;
-    return 256 + sizeof(int32_t) * (size_t)(m + 1) + sizeof(int2) * (size_t)cap_cta + 64;
+size_t mxm_scratch_bytes(int64_t m, int64_t n, int64_t mask_nnz) {
+    return 256 + sizeof(int32_t) * (size_t)(m + 1) + 16 + sizeof(int4) * (size_t)cta_item_cap(m, n, mask_nnz);
 }
 
 // Non-allocating launch (usable inside captured loops): `scratch` holds
-// mxm_scratch_bytes(M->m, max nnz(M)) bytes. Resets the queue itself.
-void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals, void* scratch) {
+// mxm_scratch_bytes(M->m, M->n, max nnz(M)) bytes; `cap_nnz` is that max.
+void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals, void* scratch,
+                       int64_t cap_nnz) {
     GA_REQUIRE(algo == GA_MSA || algo == GA_MCA || algo == GA_HEAP, GA_ERR_INVALID_ARG, "mxm: unknown algorithm");
     unsigned char* s = static_cast<unsigned char*>(scratch);
     MxmQueue* q = reinterpret_cast<MxmQueue*>(s);
     int32_t* warp_rows = reinterpret_cast<int32_t*>(s + 256);
     size_t off = 256 + sizeof(int32_t) * (size_t)(M->m + 1);
     off = (off + 15) & ~(size_t)15;
-    int2* cta_items = reinterpret_cast<int2*>(s + off);
+    int4* cta_items = reinterpret_cast<int4*>(s + off);
+    const int64_t cap = cta_item_cap(M->m, M->n, cap_nnz);
+    GA_REQUIRE(cap < INT32_MAX, GA_ERR_UNSUPPORTED, "mxm: too many work items");
     k_reset_queue<<<1, 32, 0, ctx->stream>>>(q);
     post_launch("mxm_reset_queue");
     GA_DISPATCH_DTYPE(A->dtype, T, {
         T* cv = static_cast<T*>(d_cvals);
-        if (algo == GA_MSA) launch_masked<LK_HASH, T>(ctx, A, B, M, cv, q, warp_rows, cta_items);
-        else if (algo == GA_MCA) launch_masked<LK_BSEARCH, T>(ctx, A, B, M, cv, q, warp_rows, cta_items);
-        else launch_masked<LK_MERGE, T>(ctx, A, B, M, cv, q, warp_rows, cta_items);
+        if (algo == GA_MSA) launch_masked<MD_DENSE, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, (int32_t)cap);
+        else if (algo == GA_MCA) launch_masked<MD_BSEARCH, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, (int32_t)cap);
+        else launch_masked<MD_MERGE, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, (int32_t)cap);
     });
 }
 
@@ -380,8 +626,8 @@ void mxm_masked_into(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, voi
         naive_masked_into(ctx, A, B, M, d_cvals);
         return;
     }
-    DBuf<unsigned char> scratch(ctx, mxm_scratch_bytes(M->m, M->nnz));
-    mxm_masked_launch(ctx, algo, A, B, M, d_cvals, scratch.p);
+    DBuf<unsigned char> scratch(ctx, mxm_scratch_bytes(M->m, M->n, M->nnz));
+    mxm_masked_launch(ctx, algo, A, B, M, d_cvals, scratch.p, M->nnz);
 }
 
 }  // namespace ga

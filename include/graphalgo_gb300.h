@@ -115,6 +115,28 @@ GA_API int ga_timer_stop(ga_ctx ctx, double* ms);
 /* Free / total device memory as the CUDA runtime sees it. */
 GA_API int ga_mem_info(ga_ctx ctx, int64_t* free_bytes, int64_t* total_bytes);
 
+/* Work counters accumulated on the device by every masked-SpGEMM launch of
+ * this context (MSA / MCA / HEAP): Gustavson products P = sum over A entries
+ * (i,k) of nnz(B_k), mask entries, launches, A entries and rows. They feed
+ * the GFLOP/s (2P) and byte models. out has GA_CTR_COUNT entries; reset != 0
+ * zeroes them after reading. Synchronises the stream. */
+enum { GA_CTR_PRODUCTS = 0, GA_CTR_MASK_ENTRIES = 1, GA_CTR_LAUNCHES = 2, GA_CTR_A_ENTRIES = 3,
+       GA_CTR_ROWS = 4, GA_CTR_COUNT = 5 };
+GA_API int ga_ctx_work_counters(ga_ctx ctx, int64_t* out, int reset);
+
+/* Kernel launches issued by this library in this process so far (counted on
+ * the host; a launch captured into a CUDA graph counts once, when captured). */
+GA_API int64_t ga_kernel_launches(void);
+
+/* Writes a device buffer larger than the L2 cache (256 MiB) on the context
+ * stream, so the next timed step starts with a cold L2. */
+GA_API int ga_ctx_flush_l2(ga_ctx ctx);
+
+/* Page-lock (or release) host memory the caller owns, for fast async copies
+ * (cudaHostRegister / cudaHostUnregister). */
+GA_API int ga_host_register(void* ptr, size_t bytes);
+GA_API int ga_host_unregister(void* ptr);
+
 /* --------------------------------------------------------------- CSR handle */
 /* Upload a host CSR (spMtx::Rst/Col/Val). val may be NULL: all ones.
  * The pattern is validated on the device (monotone row starts, in-range and

@@ -221,18 +221,24 @@ def tc_sandia(A: Csr):
     return int(total), rows
 
 
-def ktruss(A: Csr, k: int):
-    """(pattern CSR, iterations) of main.cpp:90-146."""
+def ktruss(A: Csr, k: int, with_products: bool = False):
+    """(pattern CSR, iterations) of main.cpp:90-146; with_products adds the
+    Gustavson product count of all its support products."""
     cr, cc, cv = _p(), _p(), _p()
     cnz = _i64()
     it = ctypes.c_int()
+    prod = _i64()
     val = _c(A.val, np.int32) if A.val is not None else None
-    lib().or_ktruss(_i64(A.m), _ptr(_c(A.rst, np.int32)), _ptr(_c(A.col, np.int32)), _ptr(val), int(k),
-                    ctypes.byref(cr), ctypes.byref(cc), ctypes.byref(cv), ctypes.byref(cnz), ctypes.byref(it))
+    lib().or_ktruss_ex(_i64(A.m), _ptr(_c(A.rst, np.int32)), _ptr(_c(A.col, np.int32)), _ptr(val), int(k),
+                       ctypes.byref(cr), ctypes.byref(cc), ctypes.byref(cv), ctypes.byref(cnz), ctypes.byref(it),
+                       ctypes.byref(prod))
     free = lib().or_free
     rst = _take(cr, A.m + 1, np.int32, free)
     z = int(cnz.value)
-    return Csr(A.m, A.n, rst, _take(cc, z, np.int32, free), _take(cv, z, np.int32, free)), int(it.value)
+    C = Csr(A.m, A.n, rst, _take(cc, z, np.int32, free), _take(cv, z, np.int32, free))
+    if with_products:
+        return C, int(it.value), int(prod.value)
+    return C, int(it.value)
 
 
 def bc_batch(A: Csr, sources) -> np.ndarray:

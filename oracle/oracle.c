@@ -345,8 +345,22 @@ int64_t or_tc_sandia(int64_t m, const int* rst, const int* col, int64_t* rows) {
  * keep entries with Tmp >= k-2 as 1 (106-117), stop when the count is unchanged
  * (120-123; the returned matrix is C, whose values are A's when that happens at
  * the first iteration), else swap (126). At most m iterations (100). */
+/* Gustavson products P = sum over entries (i,j) of C of nnz(C_j) */
+static int64_t products_of(int64_t m, const int* cr, const int* cc) {
+    int64_t p = 0;
+    for (int64_t i = 0; i < m; ++i)
+        for (int q = cr[i]; q < cr[i + 1]; ++q) p += cr[cc[q] + 1] - cr[cc[q]];
+    return p;
+}
+
 int or_ktruss(int64_t m, const int* rst, const int* col, const int* val, int k,
               int** cr_out, int** cc_out, int** cv_out, int64_t* cnz_out, int* iters) {
+    return or_ktruss_ex(m, rst, col, val, k, cr_out, cc_out, cv_out, cnz_out, iters, NULL);
+}
+
+int or_ktruss_ex(int64_t m, const int* rst, const int* col, const int* val, int k,
+                 int** cr_out, int** cc_out, int** cv_out, int64_t* cnz_out, int* iters, int64_t* products) {
+    int64_t prod = 0;
     int64_t nnz = rst[m];
     int* cr = (int*)xmalloc(sizeof(int) * ((size_t)m + 1));
     int* cc = (int*)xmalloc(sizeof(int) * (size_t)nnz);
@@ -360,6 +374,7 @@ int or_ktruss(int64_t m, const int* rst, const int* col, const int* val, int k,
     int* tr = (int*)xmalloc(sizeof(int) * ((size_t)m + 1));
     int* tc = (int*)xmalloc(sizeof(int) * (size_t)(nnz ? nnz : 1));
     for (int64_t t = 0; t < m; ++t) {
+        if (products) prod += products_of(m, cr, cc);
         or_mxm_masked_i32(m, m, cr, cc, cv, cr, cc, cv, cr, cc, tv);
         int64_t p = 0;
         tr[0] = 0;
@@ -378,6 +393,7 @@ int or_ktruss(int64_t m, const int* rst, const int* col, const int* val, int k,
     }
     free(tv); free(tr); free(tc);
     *cr_out = cr; *cc_out = cc; *cv_out = cv; *cnz_out = cnz; *iters = total;
+    if (products) *products = prod;
     return 0;
 }
 

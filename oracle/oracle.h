@@ -72,6 +72,10 @@ int64_t or_tc_sandia(int64_t m, const int* rst, const int* col, int64_t* rows);
  * reference prints. */
 int or_ktruss(int64_t m, const int* rst, const int* col, const int* val, int k,
               int** cr, int** cc, int** cv, int64_t* cnz, int* iters);
+/* Same, also returning the Gustavson product count summed over the
+ * iterations' support products (products may be NULL). */
+int or_ktruss_ex(int64_t m, const int* rst, const int* col, const int* val, int k,
+                 int** cr, int** cc, int** cv, int64_t* cnz, int* iters, int64_t* products);
 
 /* Batched betweenness centrality in FP64 over an explicit source list.
  * val may be NULL (all ones). bc has length m. */
