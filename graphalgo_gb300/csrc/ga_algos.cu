@@ -179,6 +179,7 @@ static ga_csr adjacency_of(ga_ctx ctx, ga_csr A) {
     if (A->nnz)
         GA_CUDA(cudaMemcpyAsync(C->col, A->col, sizeof(int32_t) * A->nnz, cudaMemcpyDeviceToDevice, ctx->stream));
     fill_ones(ctx, C->val, A->nnz, GA_INT32);
+    C->unit = 1;
     return C;
 }
 
@@ -312,12 +313,14 @@ static ga_csr ktruss(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out) 
         h0.nnz = (int32_t)A->nnz;
         h0.first_vals = 1;
         GA_CUDA(cudaMemcpyAsync(st.p, &h0, sizeof(KtState), cudaMemcpyHostToDevice, ctx->stream));
+        // C's values are A's at the first iteration and ones afterwards
+        const bool unit = csr_unit_values(ctx, A);
         const int grid_rows = grid_for(m * 32, 256, ctx->num_sms * 16);
         const int grid_copy = grid_for(m + cap, 256, ctx->num_sms * 8);
         auto body = [&](const LoopCtl& ctl) {
             // Tmp<C> = C*C, values aligned with C's pattern
             if (algo == GA_NAIVE) mxm_masked_into(ctx, algo, C, C, C, sup.p);
-            else mxm_masked_launch(ctx, algo, C, C, C, sup.p, mxm_scr.p, cap);
+            else mxm_masked_launch(ctx, algo, C, C, C, sup.p, mxm_scr.p, cap, unit);
             k_kt_count<<<grid_rows, 256, 0, ctx->stream>>>(C->rst, sup.p, m, k, cnt.p);
             post_launch("kt_count");
             scan_exclusive_i32_scratch(ctx, cnt.p, tr.p, m, scan_scr.p);
@@ -343,6 +346,7 @@ static ga_csr ktruss(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out) 
         GA_CUDA(cudaMemcpyAsync(&hs, st.p, sizeof(KtState), cudaMemcpyDeviceToHost, ctx->stream));
         GA_CUDA(cudaStreamSynchronize(ctx->stream));
         C->nnz = hs.nnz;
+        C->unit = unit ? 1 : -1;
         if (iters_out) *iters_out = hs.iters;
     } catch (...) {
         csr_destroy(ctx, C);

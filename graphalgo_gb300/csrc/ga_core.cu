@@ -447,6 +447,7 @@ static int upload_impl(ga_ctx ctx, int64_t m, int64_t n, int64_t nnz, const int3
                     GA_CUDA(cudaMemcpyAsync(A->val, val, es * nnz, kind, ctx->stream));
                 } else {
                     fill_ones(ctx, A->val, nnz, dtype);
+                    A->unit = 1;
                 }
             }
             validate_csr(ctx, A->rst, A->col, m, n, nnz);

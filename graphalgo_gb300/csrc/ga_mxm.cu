@@ -181,11 +181,36 @@ __device__ __forceinline__ int slot_of(const SlotView& v, int32_t c) {
     }
 }
 
-template <int MD, typename T, typename A>
-__device__ __forceinline__ void add_product(const MxmArgs<T, A>& p, const SlotView& v, A* acc, int32_t j, int32_t c,
-                                            A a) {
+// B value of entry j in the accumulator type (1 without a load when B's
+// values are known to be all ones).
+template <bool UB, typename T, typename A>
+__device__ __forceinline__ A bval(const MxmArgs<T, A>& p, int32_t j) {
+    return UB ? (A)1 : to_acc<T, A>(__ldg(p.bv + j));
+}
+
+template <int MD, typename A>
+__device__ __forceinline__ void add_product(const SlotView& v, A* acc, int32_t c, A prod) {
     const int slot = slot_of<MD>(v, c);
-    if (slot >= 0) atomic_add_acc<A>(&acc[slot], a * to_acc<T, A>(__ldg(p.bv + j)));
+    if (slot >= 0) atomic_add_acc<A>(&acc[slot], prod);
+}
+
+// Four consecutive values starting at a 16-byte aligned index.
+template <typename T> struct Vec4 { T x, y, z, w; };
+template <typename T>
+__device__ __forceinline__ Vec4<T> load4(const T* ptr) {
+    Vec4<T> r;
+    if (sizeof(T) == 4) {
+        const int4 t = __ldg(reinterpret_cast<const int4*>(ptr));
+        memcpy(&r, &t, 16);
+    } else if (sizeof(T) == 8) {
+        const int4 a = __ldg(reinterpret_cast<const int4*>(ptr));
+        const int4 b = __ldg(reinterpret_cast<const int4*>(ptr) + 1);
+        memcpy(&r, &a, 16);
+        memcpy(reinterpret_cast<char*>(&r) + 16, &b, 16);
+    } else {
+        r.x = __ldg(ptr); r.y = __ldg(ptr + 1); r.z = __ldg(ptr + 2); r.w = __ldg(ptr + 3);
+    }
+    return r;
 }
 
 // B-row range of A entry t, optionally clipped to the item's column window.
@@ -209,7 +234,7 @@ __device__ __forceinline__ void b_range(const MxmArgs<T, A>& p, int32_t t, bool 
 // indices the segment ends falling inside it form one 32-bit mask (a warp OR
 // reduction), so every lane finds its B row with a popcount - no per-lane
 // search loop. Lanes whose B row is long may hand it to the CTA's long list.
-template <int MD, typename T, typename A, bool PUSH>
+template <int MD, bool UB, typename T, typename A, bool PUSH>
 __device__ __forceinline__ void group_products(const MxmArgs<T, A>& p, int32_t t_first, int32_t t_end, bool clip,
                                                const SlotView& v, A* acc, int* s_incl, int* s_off, A* s_a,
                                                int* s_nlong, int32_t* s_lbs, int32_t* s_lend, A* s_la) {
@@ -259,13 +284,16 @@ __device__ __forceinline__ void group_products(const MxmArgs<T, A>& p, int32_t t
         const int x1 = base + 32 + lane;
         const int32_t j0 = base + lane + s_off[q0];
         const int32_t c0 = __ldg(p.bc + j0);
-        int32_t j1 = 0, c1 = 0;
+        const A b0 = bval<UB, T, A>(p, j0);
+        int32_t c1 = 0;
+        A b1 = (A)0;
         if (x1 < total) {
-            j1 = x1 + s_off[q1];
+            const int32_t j1 = x1 + s_off[q1];
             c1 = __ldg(p.bc + j1);
+            b1 = bval<UB, T, A>(p, j1);
         }
-        add_product<MD, T, A>(p, v, acc, j0, c0, s_a[q0]);
-        if (x1 < total) add_product<MD, T, A>(p, v, acc, j1, c1, s_a[q1]);
+        add_product<MD, A>(v, acc, c0, s_a[q0] * b0);
+        if (x1 < total) add_product<MD, A>(v, acc, c1, s_a[q1] * b1);
         q_base += __popc(bm0) + __popc(bm1);
     }
     if (base < total) {
@@ -275,46 +303,61 @@ __device__ __forceinline__ void group_products(const MxmArgs<T, A>& p, int32_t t
         if (x < total) {
             const int q = q_base + __popc(bm0 & lt);
             const int32_t j = x + s_off[q];
-            add_product<MD, T, A>(p, v, acc, j, __ldg(p.bc + j), s_a[q]);
+            add_product<MD, A>(v, acc, __ldg(p.bc + j), s_a[q] * bval<UB, T, A>(p, j));
         }
     }
     __syncwarp();
 }
 
-// Stream B entries [j0, j1) of one row with scalar head/tail and int4 body.
-template <int MD, typename T, typename A>
+// Stream B entries [j0, j1) of one row with scalar head/tail and a
+// 16-byte vector body (columns, and values unless they are all ones).
+template <int MD, bool UB, typename T, typename A>
 __device__ __forceinline__ void stream_row(const MxmArgs<T, A>& p, const SlotView& v, A* acc, int32_t j0,
                                            int32_t j1, A a) {
     const int lane = threadIdx.x & 31;
     int32_t ja = (j0 + 3) & ~3;
     if (ja > j1) ja = j1;
-    if (j0 + lane < ja) add_product<MD, T, A>(p, v, acc, j0 + lane, __ldg(p.bc + j0 + lane), a);
+    if (j0 + lane < ja) add_product<MD, A>(v, acc, __ldg(p.bc + j0 + lane), a * bval<UB, T, A>(p, j0 + lane));
     const int32_t groups = (j1 - ja) >> 2;
-    const int4* b4 = reinterpret_cast<const int4*>(p.bc + ja);
     int32_t g = lane;
     for (; g + 32 < groups; g += 64) {
-        const int4 x = __ldg(b4 + g);
-        const int4 y = __ldg(b4 + g + 32);
         const int32_t j = ja + 4 * g, jy = j + 128;
-        add_product<MD, T, A>(p, v, acc, j, x.x, a);
-        add_product<MD, T, A>(p, v, acc, j + 1, x.y, a);
-        add_product<MD, T, A>(p, v, acc, j + 2, x.z, a);
-        add_product<MD, T, A>(p, v, acc, j + 3, x.w, a);
-        add_product<MD, T, A>(p, v, acc, jy, y.x, a);
-        add_product<MD, T, A>(p, v, acc, jy + 1, y.y, a);
-        add_product<MD, T, A>(p, v, acc, jy + 2, y.z, a);
-        add_product<MD, T, A>(p, v, acc, jy + 3, y.w, a);
+        const Vec4<int32_t> x = load4<int32_t>(p.bc + j);
+        const Vec4<int32_t> y = load4<int32_t>(p.bc + jy);
+        if (UB) {
+            add_product<MD, A>(v, acc, x.x, a); add_product<MD, A>(v, acc, x.y, a);
+            add_product<MD, A>(v, acc, x.z, a); add_product<MD, A>(v, acc, x.w, a);
+            add_product<MD, A>(v, acc, y.x, a); add_product<MD, A>(v, acc, y.y, a);
+            add_product<MD, A>(v, acc, y.z, a); add_product<MD, A>(v, acc, y.w, a);
+        } else {
+            const Vec4<T> bx = load4<T>(p.bv + j);
+            const Vec4<T> by = load4<T>(p.bv + jy);
+            add_product<MD, A>(v, acc, x.x, a * to_acc<T, A>(bx.x));
+            add_product<MD, A>(v, acc, x.y, a * to_acc<T, A>(bx.y));
+            add_product<MD, A>(v, acc, x.z, a * to_acc<T, A>(bx.z));
+            add_product<MD, A>(v, acc, x.w, a * to_acc<T, A>(bx.w));
+            add_product<MD, A>(v, acc, y.x, a * to_acc<T, A>(by.x));
+            add_product<MD, A>(v, acc, y.y, a * to_acc<T, A>(by.y));
+            add_product<MD, A>(v, acc, y.z, a * to_acc<T, A>(by.z));
+            add_product<MD, A>(v, acc, y.w, a * to_acc<T, A>(by.w));
+        }
     }
     if (g < groups) {
-        const int4 x = __ldg(b4 + g);
         const int32_t j = ja + 4 * g;
-        add_product<MD, T, A>(p, v, acc, j, x.x, a);
-        add_product<MD, T, A>(p, v, acc, j + 1, x.y, a);
-        add_product<MD, T, A>(p, v, acc, j + 2, x.z, a);
-        add_product<MD, T, A>(p, v, acc, j + 3, x.w, a);
+        const Vec4<int32_t> x = load4<int32_t>(p.bc + j);
+        if (UB) {
+            add_product<MD, A>(v, acc, x.x, a); add_product<MD, A>(v, acc, x.y, a);
+            add_product<MD, A>(v, acc, x.z, a); add_product<MD, A>(v, acc, x.w, a);
+        } else {
+            const Vec4<T> bx = load4<T>(p.bv + j);
+            add_product<MD, A>(v, acc, x.x, a * to_acc<T, A>(bx.x));
+            add_product<MD, A>(v, acc, x.y, a * to_acc<T, A>(bx.y));
+            add_product<MD, A>(v, acc, x.z, a * to_acc<T, A>(bx.z));
+            add_product<MD, A>(v, acc, x.w, a * to_acc<T, A>(bx.w));
+        }
     }
     const int32_t jt = ja + 4 * groups;
-    if (jt + lane < j1) add_product<MD, T, A>(p, v, acc, jt + lane, __ldg(p.bc + jt + lane), a);
+    if (jt + lane < j1) add_product<MD, A>(v, acc, __ldg(p.bc + jt + lane), a * bval<UB, T, A>(p, jt + lane));
 }
 
 // Warp-cooperative sorted merge of B row [bs, be) against the item's sorted
@@ -376,7 +419,7 @@ struct MxmSmem {
     static constexpr size_t total = region + scratch_bytes;
 };
 
-template <int MD, typename T, typename A>
+template <int MD, bool UB, typename T, typename A>
 __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) {
     extern __shared__ __align__(16) unsigned char smem[];
     using SM = MxmSmem<MD, A>;
@@ -444,7 +487,7 @@ __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) 
             } else {
                 // phase A: short B rows flattened per warp, long ones listed
                 for (int32_t g = ab + wid * 32; g < ae; g += kMxmWarps * 32)
-                    group_products<MD, T, A, true>(p, g, ae, clip, v, acc, s_incl, s_off, s_a, &s_nlong, lbs, lend, la);
+                    group_products<MD, UB, T, A, true>(p, g, ae, clip, v, acc, s_incl, s_off, s_a, &s_nlong, lbs, lend, la);
                 __syncthreads();
                 // phase B: long B rows cut into kChunk pieces shared by all warps
                 const int nlong = min(s_nlong, kLongCap);
@@ -474,7 +517,7 @@ __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) 
                         const int seg = upper_bound_i32(lchunk + 1, nlong, c);
                         const int32_t j0 = lbs[seg] + (c - lchunk[seg]) * kChunk;
                         const int32_t j1 = min(lend[seg], j0 + kChunk);
-                        stream_row<MD, T, A>(p, v, acc, j0, j1, la[seg]);
+                        stream_row<MD, UB, T, A>(p, v, acc, j0, j1, la[seg]);
                     }
                 }
             }
@@ -537,7 +580,7 @@ __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) 
                 }
             } else {
                 for (int32_t g = ab; g < ae; g += 32)
-                    group_products<WMD, T, A, false>(p, g, ae, false, v, acc, s_incl, s_off, s_a, nullptr, nullptr,
+                    group_products<WMD, UB, T, A, false>(p, g, ae, false, v, acc, s_incl, s_off, s_a, nullptr, nullptr,
                                                      nullptr, nullptr);
             }
             __syncwarp();
@@ -560,7 +603,7 @@ static int64_t cta_item_cap(int64_t m, int64_t n, int64_t mask_nnz) {
 }
 
 // Launch the masked product for one value type and lookup variant.
-template <int LK, typename T>
+template <int LK, bool UB, typename T>
 static void launch_masked(ga_ctx ctx, ga_csr A_, ga_csr B_, ga_csr M_, T* cv, MxmQueue* q, int32_t* warp_rows,
                           int4* cta_items, int32_t cta_cap) {
     using Ac = typename Acc<T>::type;
@@ -577,7 +620,7 @@ static void launch_masked(ga_ctx ctx, ga_csr A_, ga_csr B_, ga_csr M_, T* cv, Mx
         post_launch("mxm_row_bin");
     }
     const size_t smem = MxmSmem<LK, Ac>::total;
-    auto kern = k_mxm_masked<LK, T, Ac>;
+    auto kern = k_mxm_masked<LK, UB, T, Ac>;
     GA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     GA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMxmThreads, smem));
@@ -596,8 +639,9 @@ size_t mxm_scratch_bytes(int64_t m, int64_t n, int64_t mask_nnz) {
 
 // Non-allocating launch (usable inside captured loops): `scratch` holds
 // mxm_scratch_bytes(M->m, M->n, max nnz(M)) bytes; `cap_nnz` is that max.
+// unit_b: B's values are all ones (no value loads).
 void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals, void* scratch,
-                       int64_t cap_nnz) {
+                       int64_t cap_nnz, bool unit_b) {
     GA_REQUIRE(algo == GA_MSA || algo == GA_MCA || algo == GA_HEAP, GA_ERR_INVALID_ARG, "mxm: unknown algorithm");
     unsigned char* s = static_cast<unsigned char*>(scratch);
     MxmQueue* q = reinterpret_cast<MxmQueue*>(s);
@@ -611,9 +655,16 @@ void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, v
     post_launch("mxm_reset_queue");
     GA_DISPATCH_DTYPE(A->dtype, T, {
         T* cv = static_cast<T*>(d_cvals);
-        if (algo == GA_MSA) launch_masked<MD_DENSE, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, (int32_t)cap);
-        else if (algo == GA_MCA) launch_masked<MD_BSEARCH, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, (int32_t)cap);
-        else launch_masked<MD_MERGE, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, (int32_t)cap);
+        const int32_t c32 = (int32_t)cap;
+        if (algo == GA_MSA) {
+            if (unit_b) launch_masked<MD_DENSE, true, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32);
+            else launch_masked<MD_DENSE, false, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32);
+        } else if (algo == GA_MCA) {
+            if (unit_b) launch_masked<MD_BSEARCH, true, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32);
+            else launch_masked<MD_BSEARCH, false, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32);
+        } else {
+            launch_masked<MD_MERGE, false, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32);
+        }
     });
 }
 
@@ -626,8 +677,9 @@ void mxm_masked_into(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, voi
         naive_masked_into(ctx, A, B, M, d_cvals);
         return;
     }
+    const bool unit_b = csr_unit_values(ctx, B);
     DBuf<unsigned char> scratch(ctx, mxm_scratch_bytes(M->m, M->n, M->nnz));
-    mxm_masked_launch(ctx, algo, A, B, M, d_cvals, scratch.p, M->nnz);
+    mxm_masked_launch(ctx, algo, A, B, M, d_cvals, scratch.p, M->nnz, unit_b);
 }
 
 }  // namespace ga

@@ -137,6 +137,31 @@ void fill_ones(ga_ctx ctx, void* vals, int64_t count, ga_dtype dt) {
     post_launch("fill");
 }
 
+template <typename T>
+__global__ void k_any_not_one(const T* __restrict__ v, int64_t n, int* __restrict__ flag) {
+    bool bad = false;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        bad |= v[i] != (T)1;
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+bool csr_unit_values(ga_ctx ctx, ga_csr A) {
+    if (A->unit >= 0) return A->unit == 1;
+    if (A->nnz == 0) {
+        A->unit = 1;
+        return true;
+    }
+    DBuf<int> flag(ctx, 1);
+    GA_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), ctx->stream));
+    GA_DISPATCH_DTYPE(A->dtype, T, {
+        k_any_not_one<T><<<grid_for(A->nnz, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+            static_cast<const T*>(A->val), A->nnz, flag.p);
+    });
+    post_launch("unit_check");
+    A->unit = read_i32(ctx, flag.p) ? 0 : 1;
+    return A->unit == 1;
+}
+
 template <typename S, typename D>
 __global__ void k_convert(const S* __restrict__ s, D* __restrict__ d, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -519,6 +544,7 @@ int ga_adjacency(ga_ctx ctx, ga_csr A, ga_csr* adj) {
                 GA_CUDA(cudaMemcpyAsync(C->col, A->col, sizeof(int32_t) * A->nnz, cudaMemcpyDeviceToDevice,
                                         ctx->stream));
             fill_ones(ctx, C->val, A->nnz, GA_INT32);
+            C->unit = 1;
         } catch (...) {
             csr_destroy(ctx, C);
             throw;
