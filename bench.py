@@ -58,6 +58,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-reps", type=int, default=2)
+    ap.add_argument("--support-only", action="store_true",
+                    help="profiling case: only the first support product, --reps times")
+    ap.add_argument("--reps", type=int, default=2)
     return ap.parse_args()
 
 
@@ -164,17 +167,38 @@ def measured_peak_hbm():
 
 
 def profile_traffic():
-    """DRAM bytes per Gustavson product of the MSA kernel from the committed
-    ncu summary (profiles/mxm_msa_rmat18_support.md), or None."""
+    """DRAM bytes per mask entry of the MSA kernel from the committed ncu
+    summary (profiles/mxm_msa_rmat18_support.md), or None."""
     p = os.path.join(ROOT, "profiles", "mxm_msa_rmat18_support.md")
     try:
         with open(p) as f:
             for line in f:
-                if line.startswith("dram_bytes_per_product:"):
+                if line.startswith("dram_bytes_per_mask_entry:"):
                     return float(line.split(":", 1)[1].strip())
     except OSError:
         pass
     return None
+
+
+def run_support_only(args):
+    """Small profiling case: the sweep's first support product C<A> = A*A,
+    repeated --reps times (used for ncu captures of the dominant kernel)."""
+    import graphalgo_gb300 as ga
+    from graphalgo_gb300 import build as gbuild
+    gbuild.build()
+    ctx = ga.Context(0)
+    m, rst, col = ga.gen_rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, args.seed)
+    A = ga.Csr.upload(ctx, m, m, rst, col, np.ones(len(col), np.int32))
+    for _ in range(args.reps):
+        ctx.work_counters(reset=True)
+        ctx.timer_start()
+        C = ga.mxm_masked(args.algo, A, A, A)
+        ms = ctx.timer_stop()
+        C.free()
+        wc = ctx.work_counters()
+        print(json.dumps({"support_ms": ms, "products": wc["products"], "mask_entries": wc["mask_entries"],
+                          "gflops": 2.0 * wc["products"] / ms / 1e6}), flush=True)
+    ctx.close()
 
 
 def workload_config(args, m, nnz, kmax):
@@ -290,8 +314,8 @@ def run_gpu(args, dist: Dist):
                    + 8 * prof_ctr["mask_entries"])
     peak, peak_kind = measured_peak_hbm()
     achieved = bytes_model / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
-    tpp = profile_traffic()
-    traffic = (tpp * prof_ctr["products"] / max(1, k_launches)) if tpp is not None else None
+    tpe = profile_traffic()
+    traffic = (tpe * prof_ctr["mask_entries"] / max(1, k_launches)) if tpe is not None else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                 "kernel": kname, "peak_kind": peak_kind,
@@ -414,6 +438,9 @@ def run_reference(args, dist: Dist):
 
 def main():
     args = parse_args()
+    if args.support_only:
+        run_support_only(args)
+        return
     dist = Dist()
     try:
         line = run_reference(args, dist) if args.impl == "reference" else run_gpu(args, dist)

@@ -1,0 +1,161 @@
+#!/usr/bin/env python3
+"""Regenerates the golden fixtures in this directory from the UNMODIFIED
+reference (UAlex322/GraphAlgo), compiled from its own sources into
+oracle/_ref/libref.so by oracle/build_ref.sh.
+
+Inputs are seeded synthetic graphs made here with numpy (independent of the
+product's generators). Outputs come from the reference's own functions:
+  mxmm_msa / mxmm_mca / mxmm_heap (C.Val zero-filled first) / mxmm_naive,
+  mxmm_msa_cmask, triangle_counting_masked_sandia and the row sums of its
+  C<L> = L*L, k_truss (edge sets and printed iteration counts), and the
+  batched BC both as shipped (FP32, sources 0..b-1) and with the reference's
+  templates instantiated at double for an explicit source list.
+For the four Matrix-Market graphs shipped with the reference only the
+known answers (triangles, k-truss edge counts and iterations) are stored;
+the graphs themselves are not copied.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+
+REF_GRAPHS = "/root/reference/graphs"
+
+
+def csr_from_dense(D, V=None, dtype=np.int32):
+    m, n = D.shape
+    rst = np.zeros(m + 1, np.int32)
+    rst[1:] = np.cumsum((D != 0).sum(1))
+    r, c = np.nonzero(D)
+    val = (V[r, c] if V is not None else np.ones(len(c))).astype(dtype)
+    return oracle.Csr(m, n, rst, c.astype(np.int32), val)
+
+
+def sym_graph(n, p, rng):
+    U = np.triu(rng.random((n, n)) < p, 1)
+    return csr_from_dense(U | U.T)
+
+
+def rmat_graph(scale, ef, rng, a=0.57, b=0.19, c=0.19):
+    n = 1 << scale
+    e = n * ef
+    u = np.zeros(e, np.int64)
+    v = np.zeros(e, np.int64)
+    for _ in range(scale):
+        r = rng.random(e)
+        bu = (r >= a + b).astype(np.int64)
+        bv = (((r >= a) & (r < a + b)) | (r >= a + b + c)).astype(np.int64)
+        u = (u << 1) | bu
+        v = (v << 1) | bv
+    keep = u != v
+    D = np.zeros((n, n), bool)
+    D[u[keep], v[keep]] = True
+    D = D | D.T
+    return csr_from_dense(D)
+
+
+def knn_graph(n, dim, k, rng):
+    X = rng.standard_normal((n, dim))
+    d2 = ((X[:, None, :] - X[None, :, :]) ** 2).sum(-1)
+    np.fill_diagonal(d2, np.inf)
+    nb = np.argsort(d2, axis=1, kind="stable")[:, :k]
+    D = np.zeros((n, n), bool)
+    D[np.repeat(np.arange(n), k), nb.ravel()] = True
+    return csr_from_dense(D | D.T)
+
+
+def pack(prefix, C, out):
+    out[prefix + "_rst"] = C.rst
+    out[prefix + "_col"] = C.col
+    out[prefix + "_val"] = C.val
+
+
+def main():
+    if oracle.build_ref() is None:
+        raise SystemExit("reference sources not available; cannot regenerate fixtures")
+    rng = np.random.default_rng(20261203)
+    graphs = {
+        "er300": sym_graph(300, 0.05, rng),
+        "rmat9": rmat_graph(9, 8, rng),
+        "knn200": knn_graph(200, 5, 12, rng),
+        "dense40": sym_graph(40, 0.6, rng),
+    }
+    out = {}
+    meta = {"graphs": {}, "mxm": []}
+    for name, G in graphs.items():
+        pack(f"{name}_A", G, out)
+        total, rows = oracle.ref_tc(G)
+        out[f"{name}_tc_rows"] = rows
+        kt = []
+        k = 3
+        while True:
+            R, it = oracle.ref_ktruss(G, k)
+            pack(f"{name}_k{k}", R, out)
+            kt.append({"k": k, "nnz": int(R.nnz), "iters": it})
+            if R.nnz == 0:
+                break
+            k += 1
+        sources = rng.choice(G.m, min(24, G.m), replace=False).astype(np.int32)
+        out[f"{name}_bc_sources"] = sources
+        out[f"{name}_bc_f64"] = oracle.ref_bc_f64(G, sources)
+        b = min(16, G.m)
+        out[f"{name}_bc_f32_batch"] = oracle.ref_bc_f32(G, b)
+        sq = oracle.ref_mxm(0, G, G, G)
+        out[f"{name}_sq_val"] = sq.val
+        meta["graphs"][name] = {"m": G.m, "nnz": int(G.nnz), "triangles": total, "ktruss": kt,
+                                "bc_f32_batch": b}
+    # random square matrices with int and double values for the four variants
+    for t in range(4):
+        n = int(rng.integers(20, 70))
+        for dt, tag in ((np.int32, "i32"), (np.float64, "f64")):
+            mats = []
+            for dens in (0.15, 0.15, 0.4):
+                D = rng.random((n, n)) < dens
+                V = rng.integers(-3, 4, (n, n)) if dt == np.int32 else rng.standard_normal((n, n))
+                mats.append(csr_from_dense(D, V, dt))
+            A, B, M = mats
+            key = f"mxm{t}_{tag}"
+            for nm, X in zip("ABM", mats):
+                pack(f"{key}_{nm}", X, out)
+            for algo in range(4):
+                out[f"{key}_algo{algo}_val"] = oracle.ref_mxm(algo, A, B, M).val
+            pack(f"{key}_cmask", oracle.ref_cmask(A, B, M), out)
+            meta["mxm"].append(key)
+    np.savez_compressed(os.path.join(HERE, "synthetic.npz"), **out)
+    with open(os.path.join(HERE, "synthetic.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    # known answers on the reference's own graphs
+    known = {}
+    if os.path.isdir(REF_GRAPHS):
+        for g in sorted(os.listdir(REF_GRAPHS)):
+            if not g.endswith(".mtx"):
+                continue
+            G = oracle.ref_read_mtx(os.path.join(REF_GRAPHS, g))
+            total, _ = oracle.ref_tc(G)
+            kt = []
+            k = 3
+            while True:
+                R, it = oracle.ref_ktruss(G, k)
+                kt.append([k, int(R.nnz), it])
+                if R.nnz == 0:
+                    break
+                k += 1
+            known[g[:-4]] = {"m": G.m, "nnz": int(G.nnz), "triangles": total, "ktruss": kt}
+        with open(os.path.join(HERE, "reference_graphs.json"), "w") as f:
+            json.dump(known, f, indent=1)
+    print("wrote", sorted(os.listdir(HERE)))
+
+
+if __name__ == "__main__":
+    main()

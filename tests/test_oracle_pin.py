@@ -1,0 +1,147 @@
+"""Pins the CPU oracle (oracle/oracle.c) to the reference.
+
+1. Against the committed golden fixtures (generated from the unmodified
+   reference by tests/golden/make_golden.py) - runs everywhere.
+2. Against the live reference library (oracle/_ref) on fresh seeded inputs -
+   runs where the reference sources were available at build time.
+3. Against the known answers on the reference's own Matrix-Market graphs -
+   runs where those graphs are present.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from graphs import random_csr, random_graph
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden")
+REF_GRAPHS = "/root/reference/graphs"
+
+
+@pytest.fixture(scope="module")
+def gold():
+    oracle.build()
+    data = np.load(os.path.join(GOLD, "synthetic.npz"))
+    with open(os.path.join(GOLD, "synthetic.json")) as f:
+        meta = json.load(f)
+    return data, meta
+
+
+def _csr(data, key, m=None, n=None):
+    rst = data[key + "_rst"]
+    mm = len(rst) - 1
+    return oracle.Csr(mm if m is None else m, mm if n is None else n, rst, data[key + "_col"], data[key + "_val"])
+
+
+def test_golden_tc_and_rows(gold):
+    data, meta = gold
+    for name, info in meta["graphs"].items():
+        G = _csr(data, f"{name}_A")
+        total, rows = oracle.tc_sandia(G)
+        assert total == info["triangles"], name
+        assert np.array_equal(rows, data[f"{name}_tc_rows"]), name
+
+
+def test_golden_ktruss(gold):
+    data, meta = gold
+    for name, info in meta["graphs"].items():
+        G = _csr(data, f"{name}_A")
+        for kt in info["ktruss"]:
+            C, it = oracle.ktruss(G, kt["k"])
+            R = _csr(data, f"{name}_k{kt['k']}")
+            assert it == kt["iters"], (name, kt)
+            assert np.array_equal(C.rst, R.rst) and np.array_equal(C.col, R.col), (name, kt)
+            assert np.array_equal(C.val, R.val), (name, kt)
+
+
+def test_golden_square_and_bc(gold):
+    data, meta = gold
+    for name, info in meta["graphs"].items():
+        G = _csr(data, f"{name}_A")
+        assert np.array_equal(oracle.mxm_masked(G, G, G), data[f"{name}_sq_val"]), name
+        bc = oracle.bc_batch(G, data[f"{name}_bc_sources"])
+        ref = data[f"{name}_bc_f64"]
+        assert np.all(np.abs(bc - ref) <= 1e-12 * np.maximum(np.abs(ref), 1.0)), name
+        # the shipped FP32 reference agrees to single precision
+        b = info["bc_f32_batch"]
+        bc32 = oracle.bc_batch(G, np.arange(b, dtype=np.int32))
+        r32 = data[f"{name}_bc_f32_batch"].astype(np.float64)
+        assert np.all(np.abs(bc32 - r32) <= 1e-4 * np.maximum(np.abs(bc32), 1.0)), name
+
+
+def test_golden_mxm_variants_and_cmask(gold):
+    data, meta = gold
+    for key in meta["mxm"]:
+        A, B, M = (_csr(data, f"{key}_{x}") for x in "ABM")
+        got = oracle.mxm_masked(A, B, M)
+        for algo in range(4):
+            ref = data[f"{key}_algo{algo}_val"]
+            if key.endswith("i32"):
+                assert np.array_equal(got, ref), (key, algo)
+            else:
+                assert np.allclose(got, ref, rtol=1e-12, atol=1e-12), (key, algo)
+        C = oracle.mxm_cmask(A, B, M)
+        R = _csr(data, f"{key}_cmask")
+        assert np.array_equal(C.rst, R.rst) and np.array_equal(C.col, R.col), key
+        if key.endswith("i32"):
+            assert np.array_equal(C.val, R.val), key
+        else:
+            assert np.allclose(C.val, R.val, rtol=1e-12, atol=1e-12), key
+
+
+needs_ref = pytest.mark.skipif(not oracle.ref_available(), reason="reference library not built here")
+
+
+@needs_ref
+def test_live_reference_random_mxm_and_cmask():
+    rng = np.random.default_rng(99)
+    for trial in range(15):
+        n = int(rng.integers(1, 60))
+        for dt in (np.int32, np.float64):
+            A = random_csr(n, n, rng.random() * 0.3, rng, dt)
+            B = random_csr(n, n, rng.random() * 0.3, rng, dt)
+            M = random_csr(n, n, rng.random() * 0.5, rng, dt)
+            got = oracle.mxm_masked(A, B, M)
+            for algo in range(4):
+                R = oracle.ref_mxm(algo, A, B, M)
+                assert np.array_equal(R.rst, M.rst) and np.array_equal(R.col, M.col)
+                if dt == np.int32:
+                    assert np.array_equal(R.val, got), algo
+                else:
+                    assert np.allclose(R.val, got, rtol=1e-12, atol=1e-12), algo
+            C, R = oracle.mxm_cmask(A, B, M), oracle.ref_cmask(A, B, M)
+            assert np.array_equal(C.rst, R.rst) and np.array_equal(C.col, R.col)
+
+
+@needs_ref
+def test_live_reference_graph_algorithms():
+    rng = np.random.default_rng(100)
+    for n, p in ((30, 0.3), (120, 0.08), (200, 0.05)):
+        G = random_graph(n, p, rng)
+        assert oracle.tc_sandia(G)[0] == oracle.ref_tc(G)[0]
+        for k in (3, 4, 5):
+            C, it = oracle.ktruss(G, k)
+            R, rit = oracle.ref_ktruss(G, k)
+            assert it == rit and np.array_equal(C.col, R.col) and np.array_equal(C.rst, R.rst)
+        src = rng.choice(n, 10, replace=False).astype(np.int32)
+        assert np.allclose(oracle.bc_batch(G, src), oracle.ref_bc_f64(G, src), rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.skipif(not (oracle.ref_available() and os.path.isdir(REF_GRAPHS)),
+                    reason="reference graphs not present")
+def test_reference_graph_known_answers():
+    with open(os.path.join(GOLD, "reference_graphs.json")) as f:
+        known = json.load(f)
+    # the table of known answers measured on the reference (triangles, k-truss)
+    assert known["G43"]["triangles"] == 1392 and known["yeast_30NN"]["triangles"] == 180175
+    assert known["iris_dataset_30NN"]["triangles"] == 25972 and known["cage3"]["triangles"] == 3
+    for name, info in known.items():
+        G = oracle.ref_read_mtx(os.path.join(REF_GRAPHS, name + ".mtx"))
+        assert G.nnz == info["nnz"]
+        assert oracle.tc_sandia(G)[0] == info["triangles"], name
+        for k, nnz, iters in info["ktruss"]:
+            C, it = oracle.ktruss(G, k)
+            assert (C.nnz, it) == (nnz, iters), (name, k)
