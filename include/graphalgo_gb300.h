@@ -181,6 +181,31 @@ GA_API int ga_mxm_masked(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M,
  * with M's pattern (length nnz(M), A's dtype). No allocation of C. */
 GA_API int ga_mxm_masked_vals(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals);
 
+/* Allocation-free C<M> = A*B (no counterpart in the reference). For callers
+ * that cannot allocate device memory when they need the product - code
+ * running while a CUDA graph is being captured, where cudaMalloc is not
+ * allowed, or an application that keeps the whole device-memory budget in
+ * its own arena. Every argument is a device pointer the caller owns: CSR
+ * arrays of A (m x k), B (k x n) and the mask M (m x n, mask_nnz entries,
+ * structural), and c_val (mask_nnz values of `dtype`, aligned with M's
+ * pattern). No context and no allocation: the kernel's scratch lives in one
+ * fixed 16 MiB device array inside this library, which every GPU that loads
+ * the library keeps until the process exits. algo is GA_MSA, GA_MCA or
+ * GA_HEAP; b_unit != 0 promises that B's values are all 1 (they are then not
+ * read). The work runs on `stream` (NULL: the default stream) and is not
+ * synchronised. Returns GA_ERR_INVALID_ARG when the scratch this shape needs
+ * - 256 + 4(m+1) + 16 + 16 min(m(1 + ceil(n/2^18)) + mask_nnz/4096 + 1,
+ * mask_nnz + 1) bytes - exceeds 16 MiB (about 460k rows when n <= 2^18).
+ * The first call on a device looks up the array's device address for that
+ * device; make that first call before any stream capture. Calls share the
+ * array: two calls whose work overlaps on the GPU race with each other, so
+ * order them on one stream (each call clears what must start at zero). */
+GA_API int ga_mxm_masked_noalloc(void* stream, ga_algo algo, int64_t m, int64_t k, int64_t n,
+                                 const int32_t* a_rst, const int32_t* a_col, const void* a_val,
+                                 const int32_t* b_rst, const int32_t* b_col, const void* b_val,
+                                 const int32_t* m_rst, const int32_t* m_col, int64_t mask_nnz,
+                                 ga_dtype dtype, int b_unit, void* c_val);
+
 /* C<!M> = A*B: the structural product minus M's pattern, columns sorted.
  * Replaces mxmm_msa_cmask (include/matrix_la.h:788-891). An empty M gives
  * the unmasked product. */
