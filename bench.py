@@ -58,9 +58,12 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-reps", type=int, default=2)
-    ap.add_argument("--support-only", action="store_true",
-                    help="profiling case: only the first support product, --reps times")
+    ap.add_argument("--case", choices=["support", "tc", "bc"], default=None,
+                    help="profiling case instead of the benchmark: support product, TC or BC, --reps times")
     ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--sources", type=int, default=64)
+    ap.add_argument("--host-loops", action="store_true",
+                    help="run the k-truss loop from the host (kernels launched one by one, e.g. for ncu)")
     return ap.parse_args()
 
 
@@ -180,24 +183,39 @@ def profile_traffic():
     return None
 
 
-def run_support_only(args):
-    """Small profiling case: the sweep's first support product C<A> = A*A,
-    repeated --reps times (used for ncu captures of the dominant kernel)."""
+def run_case(args):
+    """Small profiling cases on the bench's R-MAT graph, --reps times each
+    (used for ncu captures): `support` = the sweep's first support product
+    C<A> = A*A; `tc` = triangle count with the dot-product kernel; `bc` =
+    batched BC over --sources seeded sources."""
     import graphalgo_gb300 as ga
     from graphalgo_gb300 import build as gbuild
     gbuild.build()
     ctx = ga.Context(0)
+    ctx.set_option(ga.OPT_DEVICE_LOOPS, 0 if args.host_loops else 1)
     m, rst, col = ga.gen_rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, args.seed)
     A = ga.Csr.upload(ctx, m, m, rst, col, np.ones(len(col), np.int32))
+    rng = np.random.default_rng(args.seed)
+    src = rng.choice(m, min(args.sources, m), replace=False).astype(np.int32)
     for _ in range(args.reps):
         ctx.work_counters(reset=True)
         ctx.timer_start()
-        C = ga.mxm_masked(args.algo, A, A, A)
-        ms = ctx.timer_stop()
-        C.free()
-        wc = ctx.work_counters()
-        print(json.dumps({"support_ms": ms, "products": wc["products"], "mask_entries": wc["mask_entries"],
-                          "gflops": 2.0 * wc["products"] / ms / 1e6}), flush=True)
+        if args.case == "support":
+            C = ga.mxm_masked(args.algo, A, A, A)
+            ms = ctx.timer_stop()
+            C.free()
+            wc = ctx.work_counters()
+            rec = {"support_ms": ms, "products": wc["products"], "mask_entries": wc["mask_entries"],
+                   "gflops": 2.0 * wc["products"] / ms / 1e6}
+        elif args.case == "tc":
+            total, _ = ga.tc("dot", A, per_row=False)
+            ms = ctx.timer_stop()
+            rec = {"tc_ms": ms, "triangles": total}
+        else:
+            ga.bc(A, src)
+            ms = ctx.timer_stop()
+            rec = {"bc_ms": ms, "sources": len(src), "gteps": len(src) * len(col) / 2 / ms / 1e6}
+        print(json.dumps(rec), flush=True)
     ctx.close()
 
 
@@ -257,6 +275,8 @@ def run_gpu(args, dist: Dist):
     from graphalgo_gb300 import build as gbuild
     gbuild.build()
     ctx = ga.Context(dist.local_rank)
+    loops = 0 if args.host_loops else 1
+    ctx.set_option(ga.OPT_DEVICE_LOOPS, loops)
 
     m, rst, col = ga.gen_rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, args.seed)
     nnz = len(col)
@@ -305,12 +325,14 @@ def run_gpu(args, dist: Dist):
     stats = ctx.kernel_stats()
     prof_ctr = {key: sum(v[key] for v in per_k.values()) for key in next(iter(per_k.values()))}
     ctx.set_option(ga.OPT_PROFILE, 0)
-    ctx.set_option(ga.OPT_DEVICE_LOOPS, 1)
+    ctx.set_option(ga.OPT_DEVICE_LOOPS, loops)
     kname = {"msa": "mxm_msa", "mca": "mxm_mca", "heap": "mxm_heap_merge"}[args.algo]
     k_launches, k_ms = stats.get(kname, (0, 0.0))
     # algorithmic bytes of the Gustavson model, int32 values (s = 4):
-    # 4(m+1)*2 + nnz(A)*(4+4) + nnz(A)*8 + P*(4+4) + nnz(M)*4 + nnz(C)*4
-    bytes_model = (8 * prof_ctr["rows"] + 16 * prof_ctr["a_entries"] + 8 * prof_ctr["products"]
+    # 4(m+1)*2 + nnz(A)*(4+4) + nnz(A)*8 + P*(4+4) + nnz(M)*4 + nnz(C)*4,
+    # with P the products the kernel processed (the support of a symmetric C
+    # evaluates its upper triangle and mirrors it)
+    bytes_model = (8 * prof_ctr["rows"] + 16 * prof_ctr["a_entries"] + 8 * prof_ctr["executed"]
                    + 8 * prof_ctr["mask_entries"])
     peak, peak_kind = measured_peak_hbm()
     achieved = bytes_model / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
@@ -395,7 +417,8 @@ def run_gpu(args, dist: Dist):
         "config": workload_config(args, m, nnz, kmax),
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(launches_per_step * args.steps), "clocks": clocks,
-        "work": {"products_per_step": wc["products"] / args.steps, "k_max": kmax,
+        "work": {"products_per_step": wc["products"] / args.steps,
+                 "executed_products_per_step": wc["executed"] / args.steps, "k_max": kmax,
                  "support_products_k3": per_k.get(args.kmin, {}).get("products")},
         "support_variants": variants,
     }
@@ -438,8 +461,8 @@ def run_reference(args, dist: Dist):
 
 def main():
     args = parse_args()
-    if args.support_only:
-        run_support_only(args)
+    if args.case:
+        run_case(args)
         return
     dist = Dist()
     try:

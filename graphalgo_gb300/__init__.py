@@ -159,11 +159,13 @@ class Context:
         return int(f.value), int(t.value)
 
     def work_counters(self, reset: bool = False) -> dict:
-        """Masked-SpGEMM work since the last reset: products P, mask entries,
-        launches, A entries and rows (device counters)."""
-        out = (ctypes.c_int64 * 5)()
+        """Masked-SpGEMM work since the last reset: Gustavson products P of the
+        requested products, mask entries, launches, A entries, rows, and the
+        products the kernels actually processed (device counters)."""
+        out = (ctypes.c_int64 * 6)()
         _check(lib().ga_ctx_work_counters(self.handle, out, int(bool(reset))), self)
-        return dict(zip(("products", "mask_entries", "launches", "a_entries", "rows"), (int(x) for x in out)))
+        return dict(zip(("products", "mask_entries", "launches", "a_entries", "rows", "executed"),
+                        (int(x) for x in out)))
 
     def flush_l2(self):
         _check(lib().ga_ctx_flush_l2(self.handle), self)

@@ -68,76 +68,69 @@ void run_device_loop(ga_ctx ctx, const std::function<void(const LoopCtl&)>& body
 
 // ==================================================== triangle counting
 constexpr int kTcThreads = 256;
-constexpr int kTcWarps = kTcThreads / 32;
-constexpr int kTcRowSmem = 1024;  // L row entries staged in shared memory per warp
+constexpr int kTcChunk = 8;  // edges (i, j) of one L row per work unit
 
-// Dot-product form over L (strict lower triangle, rows sorted): for each row
-// i and each j in L_i, |L_i ∩ L_j| counted by warp-level sorted-list
-// intersection. Only the prefix L_i[0..t) (entries < j) can meet L_j. The
+// Work units of the dot-product kernel: (row i, first edge t0) for t0 = 1,
+// 1 + kTcChunk, ... < |L_i| (edge t = 0 has no smaller neighbour to meet).
+__global__ void k_tc_unit_count(const int32_t* __restrict__ lr, int64_t m, int32_t* __restrict__ cnt) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t ln = lr[i + 1] - lr[i];
+        cnt[i] = ln > 1 ? (ln - 1 + kTcChunk - 1) / kTcChunk : 0;
+    }
+}
+
+__global__ void k_tc_unit_fill(const int32_t* __restrict__ cnt, const int32_t* __restrict__ offs, int64_t m,
+                               int2* __restrict__ units) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        for (int32_t u = 0; u < cnt[i]; ++u) units[offs[i] + u] = make_int2((int)i, 1 + u * kTcChunk);
+}
+
+// Dot-product form over L (strict lower triangle, rows sorted): for an edge
+// (i, j) = (i, L_i[t]), |L_i[0..t) ∩ L_j| by warp-level sorted-list
+// intersection - only the prefix L_i[0..t) (entries < j) can meet L_j. The
 // shorter list is walked 32 entries at a time, one per lane, each lane
 // binary-searches the longer one, and __ballot_sync/__popc count the hits.
-// Rows are fetched dynamically so hub rows do not stall a static schedule.
-// per_row[i] = triangles whose largest vertex is i (the row sums of the
-// reference's C<L> = L*L).
+// Each warp takes work units of kTcChunk edges, so the edges of a hub row
+// spread over many warps. per_row[i] = triangles whose largest vertex is i
+// (the row sums of the reference's C<L> = L*L).
 __global__ void __launch_bounds__(kTcThreads) k_tc_dot(const int32_t* __restrict__ lr, const int32_t* __restrict__ lc,
-                                                       int64_t m, int* __restrict__ next_row,
+                                                       const int2* __restrict__ units, int32_t nunits,
                                                        unsigned long long* __restrict__ total,
-                                                       int64_t* __restrict__ per_row) {
-    __shared__ int32_t buf[kTcWarps][kTcRowSmem];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+                                                       unsigned long long* __restrict__ per_row) {
+    const int lane = threadIdx.x & 31;
     const unsigned FULL = 0xffffffffu;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     unsigned long long acc_total = 0;
-    while (true) {
-        int i = 0;
-        if (lane == 0) i = atomicAdd(next_row, 1);
-        i = __shfl_sync(FULL, i, 0);
-        if (i >= m) break;
+    for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < nunits; u += warps) {
+        const int2 unit = units[u];
+        const int32_t i = unit.x;
         const int32_t lb = lr[i], ln = lr[i + 1] - lb;
-        const int32_t* Li;
-        if (ln <= kTcRowSmem) {
-            for (int t = lane; t < ln; t += 32) buf[wid][t] = lc[lb + t];
-            __syncwarp();
-            Li = buf[wid];
-        } else {
-            Li = lc + lb;
-        }
-        long long cnt = 0;
-        for (int t = 1; t < ln; ++t) {
-            const int32_t j = Li[t];
+        const int32_t* Li = lc + lb;
+        const int t1 = min(ln, unit.y + kTcChunk);
+        unsigned long long cnt = 0;
+        for (int t = unit.y; t < t1; ++t) {
+            const int32_t j = __ldg(Li + t);
             const int32_t jb = lr[j], jn = lr[j + 1] - jb;
             if (jn == 0) continue;
-            if (jn <= t) {
-                for (int base = 0; base < jn; base += 32) {
-                    int q = base + lane;
-                    bool hit = false;
-                    if (q < jn) {
-                        int32_t x = __ldg(lc + jb + q);
-                        int p = lower_bound_i32(Li, t, x);
-                        hit = p < t && Li[p] == x;
-                    }
-                    unsigned bal = __ballot_sync(FULL, hit);
-                    cnt += __popc(bal);
+            const bool walk_j = jn <= t;  // walk the shorter list
+            const int32_t* W = walk_j ? lc + jb : Li;
+            const int32_t* S = walk_j ? Li : lc + jb;
+            const int wn = walk_j ? jn : t, sn = walk_j ? t : jn;
+            for (int base = 0; base < wn; base += 32) {
+                const int q = base + lane;
+                bool hit = false;
+                if (q < wn) {
+                    const int32_t x = __ldg(W + q);
+                    const int p = lower_bound_i32(S, sn, x);
+                    hit = p < sn && __ldg(S + p) == x;
                 }
-            } else {
-                const int32_t* Lj = lc + jb;
-                for (int base = 0; base < t; base += 32) {
-                    int q = base + lane;
-                    bool hit = false;
-                    if (q < t) {
-                        int32_t x = Li[q];
-                        int p = lower_bound_i32(Lj, jn, x);
-                        hit = p < jn && __ldg(Lj + p) == x;
-                    }
-                    unsigned bal = __ballot_sync(FULL, hit);
-                    cnt += __popc(bal);
-                }
+                cnt += __popc(__ballot_sync(FULL, hit));
             }
         }
-        if (lane == 0) {
-            if (per_row) per_row[i] = cnt;
-            acc_total += (unsigned long long)cnt;
+        if (lane == 0 && cnt) {
+            if (per_row) atomicAdd(&per_row[i], cnt);
+            acc_total += cnt;
         }
-        __syncwarp();
     }
     if (lane == 0 && acc_total) atomicAdd(total, acc_total);
 }
@@ -197,11 +190,19 @@ static void tc_device(ga_ctx ctx, ga_algo algo, ga_csr A, int64_t* d_total, int6
     ga_csr L0 = extract_tri(ctx, A, true);
     CsrGuard g0(ctx, L0);
     if (algo == GA_DOT) {
-        DBuf<int> next(ctx, 1);
-        GA_CUDA(cudaMemsetAsync(next.p, 0, sizeof(int), ctx->stream));
-        if (d_per_row) GA_CUDA(cudaMemsetAsync(d_per_row, 0, sizeof(int64_t) * A->m, ctx->stream));
+        const int64_t m = A->m;
+        DBuf<int32_t> ucnt(ctx, (size_t)m + 1), uoff(ctx, (size_t)m + 1);
+        k_tc_unit_count<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(L0->rst, m, ucnt.p);
+        post_launch("tc_unit_count");
+        scan_exclusive_i32(ctx, ucnt.p, uoff.p, m);
+        const int32_t nunits = read_i32(ctx, uoff.p + m);
+        DBuf<int2> units(ctx, (size_t)nunits + 1);
+        k_tc_unit_fill<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(ucnt.p, uoff.p, m, units.p);
+        post_launch("tc_unit_fill");
+        if (d_per_row) GA_CUDA(cudaMemsetAsync(d_per_row, 0, sizeof(int64_t) * m, ctx->stream));
         ProfScope ps(ctx, "tc_dot");
-        k_tc_dot<<<ctx->num_sms * 8, kTcThreads, 0, ctx->stream>>>(L0->rst, L0->col, A->m, next.p, tot, d_per_row);
+        k_tc_dot<<<grid_for((int64_t)nunits * 32, kTcThreads, ctx->num_sms * 16), kTcThreads, 0, ctx->stream>>>(
+            L0->rst, L0->col, units.p, nunits, tot, reinterpret_cast<unsigned long long*>(d_per_row));
         post_launch("tc_dot");
         return;
     }
@@ -239,9 +240,11 @@ __global__ void k_kt_count(const int32_t* __restrict__ cr, const int32_t* __rest
 }
 
 // Keep entries with support >= k-2, in order (ballot compaction per row).
+// Optionally records each old entry's new position (-1 when dropped) and
+// the row of each new entry.
 __global__ void k_kt_compact(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
                              const int32_t* __restrict__ sup, const int32_t* __restrict__ tr, int64_t m, int k,
-                             int32_t* __restrict__ tc) {
+                             int32_t* __restrict__ tc, int32_t* __restrict__ pos_new, int32_t* __restrict__ trow) {
     const int lane = threadIdx.x & 31;
     const unsigned FULL = 0xffffffffu;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -252,7 +255,12 @@ __global__ void k_kt_compact(const int32_t* __restrict__ cr, const int32_t* __re
             int32_t q = base + lane;
             bool keep = q < e && sup[q] >= k - 2;
             unsigned bal = __ballot_sync(FULL, keep);
-            if (keep) tc[o + __popc(bal & ((1u << lane) - 1u))] = cc[q];
+            const int32_t dst = o + __popc(bal & ((1u << lane) - 1u));
+            if (keep) {
+                tc[dst] = cc[q];
+                if (trow) trow[dst] = (int32_t)i;
+            }
+            if (pos_new && q < e) pos_new[q] = keep ? dst : -1;
             o += __popc(bal);
         }
     }
@@ -291,6 +299,65 @@ __global__ void k_kt_copyback(const KtState* st, const int32_t* __restrict__ tr,
     }
 }
 
+// Position of the first entry of row i with column >= i (rows sorted).
+__global__ void k_upper_start(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc, int64_t m,
+                              int32_t* __restrict__ ust) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t b = cr[i], n = cr[i + 1] - b;
+        ust[i] = b + lower_bound_i32(cc + b, n, (int32_t)i);
+    }
+}
+
+// Row index of every entry.
+__global__ void k_expand_rows(const int32_t* __restrict__ cr, int64_t m, int32_t* __restrict__ row_of) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < m; i += warps)
+        for (int32_t q = cr[i] + lane; q < cr[i + 1]; q += 32) row_of[q] = (int32_t)i;
+}
+
+// Position of each entry's mirror (j, i) in a symmetric pattern.
+__global__ void k_mirror_index(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
+                               const int32_t* __restrict__ row_of, int64_t nnz, int32_t* __restrict__ mir) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t i = row_of[q], j = cc[q];
+        const int32_t jb = cr[j], jn = cr[j + 1] - jb;
+        mir[q] = jb + lower_bound_i32(cc + jb, jn, i);
+    }
+}
+
+// The support of a symmetric C is symmetric: lower entries (column below the
+// row) take the value computed for their mirror in the upper triangle.
+__global__ void k_gather_lower(const KtState* st, const int32_t* __restrict__ cc, const int32_t* __restrict__ row_of,
+                               const int32_t* __restrict__ mir, int32_t* __restrict__ sup) {
+    const int64_t nnz = st->nnz;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x)
+        if (cc[q] < row_of[q]) sup[q] = sup[mir[q]];
+}
+
+// Mirror positions after a prune: a kept entry's mirror is kept too (equal
+// support), so its new mirror is the mirror's new position.
+__global__ void k_mirror_update(const KtState* st, const int32_t* __restrict__ pos_new,
+                                const int32_t* __restrict__ mir, int32_t* __restrict__ mir_new) {
+    const int64_t nnz = st->nnz;  // before the prune
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t p = pos_new[q];
+        if (p >= 0) mir_new[p] = pos_new[mir[q]];
+    }
+}
+
+// Row index and mirror arrays follow C when the iteration swapped.
+__global__ void k_kt_copyback_aux(const KtState* st, const int32_t* __restrict__ trow,
+                                  const int32_t* __restrict__ mir_new, int32_t* __restrict__ row_of,
+                                  int32_t* __restrict__ mir) {
+    if (!st->swapped) return;
+    const int64_t nnz = st->nnz;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x) {
+        row_of[q] = trow[q];
+        mir[q] = mir_new[q];
+    }
+}
+
 static ga_csr ktruss(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out) {
     GA_REQUIRE(A->m == A->n, GA_ERR_SHAPE, "k-truss needs a square matrix");
     GA_REQUIRE(A->dtype == GA_INT32, GA_ERR_DTYPE, "k-truss needs int32 values (spMtx<int>)");
@@ -315,22 +382,59 @@ static ga_csr ktruss(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out) 
         GA_CUDA(cudaMemcpyAsync(st.p, &h0, sizeof(KtState), cudaMemcpyHostToDevice, ctx->stream));
         // C's values are A's at the first iteration and ones afterwards
         const bool unit = csr_unit_values(ctx, A);
+        // For a symmetric A every C stays symmetric, and so does its support:
+        // only the upper triangle (columns >= i) is multiplied, the lower
+        // triangle is mirrored. Same values, about half the products.
+        const bool upper = algo != GA_NAIVE && csr_is_symmetric(ctx, A);
+        const size_t aux = upper ? (size_t)cap : 1;
+        DBuf<int32_t> ust(ctx, upper ? (size_t)m + 1 : 1);
+        DBuf<int32_t> row_of(ctx, aux), mir(ctx, aux), pos_new(ctx, aux), trow(ctx, aux), mir_new(ctx, aux);
+        ga_csr_s Cu;  // C with row starts moved to the upper part
         const int grid_rows = grid_for(m * 32, 256, ctx->num_sms * 16);
         const int grid_copy = grid_for(m + cap, 256, ctx->num_sms * 8);
+        const int grid_ent = grid_for(cap, 256, ctx->num_sms * 16);
+        if (upper) {
+            // row of every entry and the position of its mirror, kept up to
+            // date through the prunes
+            k_expand_rows<<<grid_rows, 256, 0, ctx->stream>>>(C->rst, m, row_of.p);
+            post_launch("kt_expand_rows");
+            k_mirror_index<<<grid_ent, 256, 0, ctx->stream>>>(C->rst, C->col, row_of.p, C->nnz, mir.p);
+            post_launch("kt_mirror_index");
+        }
         auto body = [&](const LoopCtl& ctl) {
             // Tmp<C> = C*C, values aligned with C's pattern
-            if (algo == GA_NAIVE) mxm_masked_into(ctx, algo, C, C, C, sup.p);
-            else mxm_masked_launch(ctx, algo, C, C, C, sup.p, mxm_scr.p, cap, unit);
+            if (algo == GA_NAIVE) {
+                mxm_masked_into(ctx, algo, C, C, C, sup.p);
+            } else if (upper) {
+                k_upper_start<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(C->rst, C->col, m, ust.p);
+                post_launch("kt_upper_start");
+                Cu = *C;
+                Cu.rst = ust.p;
+                mxm_masked_launch(ctx, algo, C, C, &Cu, sup.p, mxm_scr.p, cap, unit, C->rst + 1);
+                k_gather_lower<<<grid_ent, 256, 0, ctx->stream>>>(st.p, C->col, row_of.p, mir.p, sup.p);
+                post_launch("kt_gather_lower");
+            } else {
+                mxm_masked_launch(ctx, algo, C, C, C, sup.p, mxm_scr.p, cap, unit);
+            }
             k_kt_count<<<grid_rows, 256, 0, ctx->stream>>>(C->rst, sup.p, m, k, cnt.p);
             post_launch("kt_count");
             scan_exclusive_i32_scratch(ctx, cnt.p, tr.p, m, scan_scr.p);
-            k_kt_compact<<<grid_rows, 256, 0, ctx->stream>>>(C->rst, C->col, sup.p, tr.p, m, k, tc.p);
+            k_kt_compact<<<grid_rows, 256, 0, ctx->stream>>>(C->rst, C->col, sup.p, tr.p, m, k, tc.p,
+                                                             upper ? pos_new.p : nullptr, upper ? trow.p : nullptr);
             post_launch("kt_compact");
+            if (upper) {
+                k_mirror_update<<<grid_ent, 256, 0, ctx->stream>>>(st.p, pos_new.p, mir.p, mir_new.p);
+                post_launch("kt_mirror_update");
+            }
             k_kt_finalize<<<1, 32, 0, ctx->stream>>>(st.p, tr.p, m, ctl);
             post_launch("kt_finalize");
             k_kt_copyback<<<grid_copy, 256, 0, ctx->stream>>>(st.p, tr.p, tc.p, m, C->rst, C->col,
                                                               static_cast<int32_t*>(C->val));
             post_launch("kt_copyback");
+            if (upper) {
+                k_kt_copyback_aux<<<grid_ent, 256, 0, ctx->stream>>>(st.p, trow.p, mir_new.p, row_of.p, mir.p);
+                post_launch("kt_copyback_aux");
+            }
         };
         const bool saved = ctx->device_loops;
         if (algo == GA_NAIVE) ctx->device_loops = false;  // naive allocates per call
@@ -347,6 +451,7 @@ static ga_csr ktruss(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out) 
         GA_CUDA(cudaStreamSynchronize(ctx->stream));
         C->nnz = hs.nnz;
         C->unit = unit ? 1 : -1;
+        C->sym = upper ? 1 : -1;  // pruning a symmetric matrix by a symmetric support keeps it symmetric
         if (iters_out) *iters_out = hs.iters;
     } catch (...) {
         csr_destroy(ctx, C);

@@ -56,6 +56,8 @@ struct BcArgs {
     double* W;              // m x ns
     uint32_t* inlvl;        // m bits: vertex has entries at the level being swept
     double* bc;
+    const int32_t* heavy_in;  // vertices with more than kBcHeavyDeg in-neighbours
+    int nheavy_in;
 };
 
 __global__ void k_bc_init(BcArgs p) {
@@ -76,25 +78,139 @@ __global__ void k_bc_init(BcArgs p) {
     }
 }
 
+// Vertices with more than kBcHeavyDeg neighbours are handled by a whole CTA
+// (their neighbour lists are split over the CTA's warps).
+constexpr int kBcHeavyDeg = 1024;
+
+// Frontier entries of the in-neighbours in group [g, g+32) of vertex v,
+// flattened over the warp (segment found by ballot/OR + popcount), added to
+// acc for sources v has not reached yet.
+template <bool UNIT>
+__device__ __forceinline__ void bc_pull_group(const BcArgs& p, const int32_t* curS, const int32_t* curL, int32_t g,
+                                              int32_t ae, const uint32_t* vis, double* acc, uint32_t* touched,
+                                              int* s_incl, int* s_off, double* s_a) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int32_t t = g + lane;
+    int len = 0, bs = 0;
+    double a = 0.0;
+    if (t < ae) {
+        const int32_t u = __ldg(p.atc + t);
+        len = curL[u];
+        if (len) {
+            bs = curS[u];
+            a = UNIT ? 1.0 : __ldg(p.atv + t);
+        }
+    }
+    const unsigned nz = __ballot_sync(FULL, len > 0);
+    if (nz == 0) return;
+    const int nseg = __popc(nz);
+    const int incl = warp_incl_scan(len);
+    const int total = __shfl_sync(FULL, incl, 31);
+    if (len > 0) {
+        const int rank = __popc(nz & ((1u << lane) - 1u));
+        s_incl[rank] = incl;
+        s_off[rank] = bs - (incl - len);
+        s_a[rank] = a;
+    }
+    __syncwarp();
+    const int my_end = lane < nseg ? s_incl[lane] - 1 : INT32_MAX;
+    const unsigned lt = (1u << lane) - 1u;
+    int q_base = 0;
+    for (int base = 0; base < total; base += 32) {
+        const int e = my_end - base;
+        const unsigned bm = __reduce_or_sync(FULL, (e >= 0 && e < 32) ? (1u << e) : 0u);
+        const int x = base + lane;
+        if (x < total) {
+            const int q = q_base + __popc(bm & lt);
+            const int32_t j = x + s_off[q];
+            const int s = p.es[j];
+            if (!(vis[s >> 5] & (1u << (s & 31)))) {
+                atomicAdd(&acc[s], s_a[q] * p.ev[j]);
+                atomicOr(&touched[s >> 5], 1u << (s & 31));
+            }
+        }
+        q_base += __popc(bm);
+    }
+    __syncwarp();
+}
+
+// Appends v's new frontier row (its touched sources, in source order) by one
+// warp; resets acc/touched.
+__device__ __forceinline__ void bc_emit_row(const BcArgs& p, int64_t v, int32_t* nxtS, int32_t* nxtL,
+                                            const uint32_t* vis, double* acc, uint32_t* touched) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t word = lane < p.words ? touched[lane] : 0u;
+    const int cnt = __popc(word);
+    const int excl = warp_incl_scan(cnt) - cnt;
+    const int count = __shfl_sync(FULL, excl + cnt, 31);
+    if (count == 0) {
+        if (lane == 0) nxtL[v] = 0;
+        return;
+    }
+    int start = 0;
+    if (lane == 0) {
+        start = atomicAdd(&p.st->entries, count);
+        const int r = atomicAdd(&p.st->rows, 1);
+        if ((int64_t)start + count > p.cap_entries || (int64_t)r >= p.cap_rows) {
+            atomicExch(&p.st->overflow, 1);
+            start = -1;
+        } else {
+            p.rv[r] = (int32_t)v; p.rs[r] = start; p.rl[r] = count;
+            p.vcnt[v] += count;
+        }
+        nxtS[v] = start;
+        nxtL[v] = start < 0 ? 0 : count;
+    }
+    start = __shfl_sync(FULL, start, 0);
+    if (start >= 0 && word) {
+        int pos = start + excl;
+        uint32_t w = word;
+        while (w) {
+            const int b = __ffs(w) - 1;
+            w &= w - 1;
+            const int s = lane * 32 + b;
+            p.es[pos] = s;
+            p.ev[pos] = acc[s];
+            p.ed[pos] = 1.0;
+            ++pos;
+        }
+        p.vbits[(size_t)v * p.words + lane] = vis[lane] | word;
+    }
+    __syncwarp();
+    for (int s = lane; s < p.ns; s += 32) acc[s] = 0.0;
+    if (lane < p.words) touched[lane] = 0u;
+    __syncwarp();
+}
+
 // One forward level: dynamic per-warp shared memory = acc[ns] doubles +
-// touched[words] + visited[words] + 32-entry flattening scratch.
+// touched[words] + visited[words] + 32-entry flattening scratch. Heavy
+// vertices first, one per CTA with all warps pulling into warp 0's
+// accumulator; then the rest, one per warp.
 template <bool UNIT>
 __global__ void __launch_bounds__(kBcThreads) k_bc_forward(BcArgs p) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const unsigned FULL = 0xffffffffu;
-    const size_t per_warp = (size_t)p.ns * sizeof(double) + 2 * (size_t)p.words * sizeof(uint32_t) +
-                            32 * (2 * sizeof(int) + sizeof(double));
-    unsigned char* base = smem + wid * ((per_warp + 15) & ~(size_t)15);
-    double* acc = reinterpret_cast<double*>(base);
-    uint32_t* touched = reinterpret_cast<uint32_t*>(base + (size_t)p.ns * sizeof(double));
-    uint32_t* vis = touched + p.words;
-    int* s_incl = reinterpret_cast<int*>(vis + p.words);
-    int* s_off = s_incl + 32;
-    double* s_a = reinterpret_cast<double*>(s_off + 32);
+    const size_t per_warp = ((size_t)p.ns * sizeof(double) + 2 * (size_t)p.words * sizeof(uint32_t) +
+                             32 * (2 * sizeof(int) + sizeof(double)) + 15) & ~(size_t)15;
+    auto region = [&](int w, double*& acc, uint32_t*& touched, uint32_t*& vis, int*& s_incl, int*& s_off,
+                      double*& s_a) {
+        unsigned char* base = smem + w * per_warp;
+        acc = reinterpret_cast<double*>(base);
+        touched = reinterpret_cast<uint32_t*>(base + (size_t)p.ns * sizeof(double));
+        vis = touched + p.words;
+        s_incl = reinterpret_cast<int*>(vis + p.words);
+        s_off = s_incl + 32;
+        s_a = reinterpret_cast<double*>(s_off + 32);
+    };
+    double* acc; uint32_t* touched; uint32_t* vis; int* s_incl; int* s_off; double* s_a;
+    region(wid, acc, touched, vis, s_incl, s_off, s_a);
+    double* acc0; uint32_t* touched0; uint32_t* vis0; int* i0; int* o0; double* a0;
+    region(0, acc0, touched0, vis0, i0, o0, a0);
 
-    const int d = p.st->d;
     if (p.st->done) return;
+    const int d = p.st->d;
     const int par = d & 1;
     const int32_t* curS = p.cur_start[par];
     const int32_t* curL = p.cur_len[par];
@@ -103,91 +219,39 @@ __global__ void __launch_bounds__(kBcThreads) k_bc_forward(BcArgs p) {
 
     for (int s = lane; s < p.ns; s += 32) acc[s] = 0.0;
     if (lane < p.words) touched[lane] = 0u;
-    __syncwarp();
+    __syncthreads();
+
+    // heavy vertices: the CTA's warps split the in-neighbours
+    for (int h = blockIdx.x; h < p.nheavy_in; h += gridDim.x) {
+        const int64_t v = p.heavy_in[h];
+        const bool active = p.vcnt[v] < p.ns;  // uniform over the CTA
+        if (active) {
+            if (wid == 0 && lane < p.words) vis0[lane] = p.vbits[(size_t)v * p.words + lane];
+            __syncthreads();
+            const int32_t ab = p.atr[v], ae = p.atr[v + 1];
+            for (int32_t g = ab + wid * 32; g < ae; g += kBcWarps * 32)
+                bc_pull_group<UNIT>(p, curS, curL, g, ae, vis0, acc0, touched0, s_incl, s_off, s_a);
+            __syncthreads();
+            if (wid == 0) bc_emit_row(p, v, nxtS, nxtL, vis0, acc0, touched0);
+        } else if (threadIdx.x == 0) {
+            nxtL[v] = 0;
+        }
+        __syncthreads();
+    }
 
     const int64_t warps = (int64_t)gridDim.x * kBcWarps;
     for (int64_t v = (int64_t)blockIdx.x * kBcWarps + wid; v < p.m; v += warps) {
+        const int32_t ab = p.atr[v], ae = p.atr[v + 1];
+        if (ae - ab > kBcHeavyDeg) continue;  // done above
         if (p.vcnt[v] >= p.ns) {
             if (lane == 0) nxtL[v] = 0;
             continue;
         }
         if (lane < p.words) vis[lane] = p.vbits[(size_t)v * p.words + lane];
         __syncwarp();
-        const int32_t ab = p.atr[v], ae = p.atr[v + 1];
-        for (int32_t g = ab; g < ae; g += 32) {
-            int32_t t = g + lane;
-            int len = 0, bs = 0;
-            double a = 0.0;
-            if (t < ae) {
-                int32_t u = __ldg(p.atc + t);
-                len = curL[u];
-                if (len) {
-                    bs = curS[u];
-                    a = UNIT ? 1.0 : __ldg(p.atv + t);
-                }
-            }
-            int incl = warp_incl_scan(len);
-            int total = __shfl_sync(FULL, incl, 31);
-            if (total == 0) continue;
-            s_incl[lane] = incl;
-            s_off[lane] = bs - (incl - len);
-            s_a[lane] = a;
-            __syncwarp();
-            int q = 0;
-            for (int x = lane; x < total; x += 32) {
-                while (s_incl[q] <= x) ++q;
-                int32_t j = x + s_off[q];
-                int s = p.es[j];
-                if (!(vis[s >> 5] & (1u << (s & 31)))) {
-                    atomicAdd(&acc[s], s_a[q] * p.ev[j]);
-                    atomicOr(&touched[s >> 5], 1u << (s & 31));
-                }
-            }
-            __syncwarp();
-        }
-        // new frontier row of v: its touched sources, in source order
-        uint32_t word = lane < p.words ? touched[lane] : 0u;
-        int cnt = __popc(word);
-        int excl = warp_incl_scan(cnt) - cnt;
-        int count = __shfl_sync(FULL, excl + cnt, 31);
-        if (count == 0) {
-            if (lane == 0) nxtL[v] = 0;
-            continue;
-        }
-        int start = 0;
-        if (lane == 0) {
-            start = atomicAdd(&p.st->entries, count);
-            int r = atomicAdd(&p.st->rows, 1);
-            if ((int64_t)start + count > p.cap_entries || (int64_t)r >= p.cap_rows) {
-                atomicExch(&p.st->overflow, 1);
-                start = -1;
-            } else {
-                p.rv[r] = (int32_t)v; p.rs[r] = start; p.rl[r] = count;
-                p.vcnt[v] += count;
-            }
-            nxtS[v] = start;
-            nxtL[v] = start < 0 ? 0 : count;
-        }
-        start = __shfl_sync(FULL, start, 0);
-        if (start >= 0 && word) {
-            int pos = start + excl;
-            uint32_t w = word;
-            while (w) {
-                int b = __ffs(w) - 1;
-                w &= w - 1;
-                int s = lane * 32 + b;
-                p.es[pos] = s;
-                p.ev[pos] = acc[s];
-                p.ed[pos] = 1.0;
-                ++pos;
-            }
-            p.vbits[(size_t)v * p.words + lane] = vis[lane] | word;
-        }
-        __syncwarp();
-        // reset the accumulator for the next vertex
-        for (int s = lane; s < p.ns; s += 32) acc[s] = 0.0;
-        if (lane < p.words) touched[lane] = 0u;
-        __syncwarp();
+        for (int32_t g = ab; g < ae; g += 32)
+            bc_pull_group<UNIT>(p, curS, curL, g, ae, vis, acc, touched, s_incl, s_off, s_a);
+        bc_emit_row(p, v, nxtS, nxtL, vis, acc, touched);
     }
 }
 
@@ -233,43 +297,114 @@ __global__ void k_bc_set_w(BcArgs p, bool set) {
     }
 }
 
+constexpr int kBcPer = 4;  // row entries per lane per pass of the backward sweep
+
+// acc[u] += sum over out-neighbours t in [t0, t1) step `stride` (groups of
+// 32 fetched together, level-k neighbours picked by ballot) of
+// A[v][w] * W[w][s[u]].
+template <bool UNIT>
+__device__ __forceinline__ void bc_push_range(const BcArgs& p, int32_t t0, int32_t t1, int32_t stride,
+                                              const int (&s)[kBcPer], double (&acc)[kBcPer]) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    for (int32_t g = t0; g < t1; g += stride) {
+        const int32_t t = g + lane;
+        int32_t w = -1;
+        double a = 0.0;
+        if (t < t1) {
+            const int32_t x = __ldg(p.ac + t);
+            if (__ldg(p.inlvl + (x >> 5)) & (1u << (x & 31))) {
+                w = x;
+                a = UNIT ? 1.0 : __ldg(p.av + t);
+            }
+        }
+        unsigned hits = __ballot_sync(FULL, w >= 0);
+        while (hits) {
+            const int src = __ffs(hits) - 1;
+            hits &= hits - 1;
+            const int32_t ww = __shfl_sync(FULL, w, src);
+            const double aa = __shfl_sync(FULL, a, src);
+            const double* wrow = p.W + (size_t)ww * p.ns;
+#pragma unroll
+            for (int u = 0; u < kBcPer; ++u)
+                if (s[u] >= 0) acc[u] += aa * wrow[s[u]];
+        }
+    }
+}
+
 // Rows of S[k-1]: acc_s = sum_w A[v][w] * W[w][s] over out-neighbours w that
-// sit at level k; bcu += acc*sigma; bc[v] += sum_s acc*sigma.
+// sit at level k; bcu += acc*sigma; bc[v] += sum_s acc*sigma. Rows of heavy
+// vertices are shared by all warps of a CTA, the others take one warp.
 template <bool UNIT>
 __global__ void __launch_bounds__(kBcThreads) k_bc_backward(BcArgs p) {
+    __shared__ double sacc[kBcMaxSources];
+    __shared__ double s_vsum;
     const int k = p.st->k;
     if (k < 1) return;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int32_t r0 = p.level_rows[k - 1], r1 = p.level_rows[k];
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    constexpr int PER = 4;  // entries per lane per pass
-    for (int64_t r = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); r < r1; r += warps) {
-        const int32_t v = p.rv[r], e0 = p.rs[r], n = p.rl[r];
+
+    // heavy rows: each warp takes every 8th group of 32 neighbours
+    for (int64_t r = r0 + blockIdx.x; r < r1; r += gridDim.x) {
+        const int32_t v = p.rv[r];
         const int32_t ab = p.ar[v], ae = p.ar[v + 1];
-        double vsum = 0.0;
-        for (int base = 0; base < n; base += 32 * PER) {
-            int s[PER];
-            double acc[PER];
+        if (ae - ab <= kBcHeavyDeg) continue;  // uniform over the CTA
+        const int32_t e0 = p.rs[r], n = p.rl[r];
+        for (int e = threadIdx.x; e < n; e += blockDim.x) sacc[e] = 0.0;
+        if (threadIdx.x == 0) s_vsum = 0.0;
+        __syncthreads();
+        for (int base = 0; base < n; base += 32 * kBcPer) {
+            int s[kBcPer];
+            double acc[kBcPer];
 #pragma unroll
-            for (int u = 0; u < PER; ++u) {
-                int e = base + u * 32 + lane;
+            for (int u = 0; u < kBcPer; ++u) {
+                const int e = base + u * 32 + lane;
                 s[u] = e < n ? p.es[e0 + e] : -1;
                 acc[u] = 0.0;
             }
-            for (int32_t t = ab; t < ae; ++t) {
-                const int32_t w = __ldg(p.ac + t);
-                if (!(__ldg(p.inlvl + (w >> 5)) & (1u << (w & 31)))) continue;
-                const double a = UNIT ? 1.0 : __ldg(p.av + t);
-                const double* wrow = p.W + (size_t)w * p.ns;
+            bc_push_range<UNIT>(p, ab + wid * 32, ae, kBcWarps * 32, s, acc);
 #pragma unroll
-                for (int u = 0; u < PER; ++u)
-                    if (s[u] >= 0) acc[u] += a * wrow[s[u]];
+            for (int u = 0; u < kBcPer; ++u) {
+                const int e = base + u * 32 + lane;
+                if (e < n && acc[u] != 0.0) atomicAdd(&sacc[e], acc[u]);
             }
+        }
+        __syncthreads();
+        double part = 0.0;
+        for (int e = threadIdx.x; e < n; e += blockDim.x) {
+            const double c = sacc[e] * p.ev[e0 + e];
+            p.ed[e0 + e] += c;
+            part += c;
+        }
+        part = warp_sum<double>(part);
+        if (lane == 0 && part != 0.0) atomicAdd(&s_vsum, part);
+        __syncthreads();
+        if (threadIdx.x == 0 && s_vsum != 0.0) atomicAdd(&p.bc[v], s_vsum);
+        __syncthreads();
+    }
+
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t r = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); r < r1; r += warps) {
+        const int32_t v = p.rv[r];
+        const int32_t ab = p.ar[v], ae = p.ar[v + 1];
+        if (ae - ab > kBcHeavyDeg) continue;  // done above
+        const int32_t e0 = p.rs[r], n = p.rl[r];
+        double vsum = 0.0;
+        for (int base = 0; base < n; base += 32 * kBcPer) {
+            int s[kBcPer];
+            double acc[kBcPer];
 #pragma unroll
-            for (int u = 0; u < PER; ++u) {
-                int e = base + u * 32 + lane;
+            for (int u = 0; u < kBcPer; ++u) {
+                const int e = base + u * 32 + lane;
+                s[u] = e < n ? p.es[e0 + e] : -1;
+                acc[u] = 0.0;
+            }
+            bc_push_range<UNIT>(p, ab, ae, 32, s, acc);
+#pragma unroll
+            for (int u = 0; u < kBcPer; ++u) {
+                const int e = base + u * 32 + lane;
                 if (e < n) {
-                    double c = acc[u] * p.ev[e0 + e];
+                    const double c = acc[u] * p.ev[e0 + e];
                     p.ed[e0 + e] += c;
                     vsum += c;
                 }
@@ -306,6 +441,12 @@ __global__ void k_bc_checks(const int32_t* __restrict__ r, const int32_t* __rest
         f = __reduce_or_sync(0xffffffffu, f);
         if (lane == 0 && f) atomicOr(flags, f);
     }
+}
+
+__global__ void k_bc_heavy(const int32_t* __restrict__ r, int64_t m, int32_t* __restrict__ out,
+                           int* __restrict__ count) {
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < m; v += (int64_t)gridDim.x * blockDim.x)
+        if (r[v + 1] - r[v] > kBcHeavyDeg) out[atomicAdd(count, 1)] = (int32_t)v;
 }
 
 __global__ void k_bc_check_sources(const int32_t* __restrict__ src, int ns, int64_t m, int* __restrict__ mark,
@@ -375,6 +516,14 @@ static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t ns
         p.rv = rv.p; p.rs = rs.p; p.rl = rl.p;
         p.cap_entries = cap_entries; p.cap_rows = cap_rows;
         p.W = W.p; p.inlvl = inlvl.p; p.bc = d_bc;
+        // vertices whose in-neighbour lists are split over a CTA
+        DBuf<int32_t> heavy(ctx, (size_t)m + 1);
+        DBuf<int> nheavy(ctx, 1);
+        GA_CUDA(cudaMemsetAsync(nheavy.p, 0, sizeof(int), ctx->stream));
+        k_bc_heavy<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(ATu->rst, m, heavy.p, nheavy.p);
+        post_launch("bc_heavy");
+        p.heavy_in = heavy.p;
+        p.nheavy_in = read_i32(ctx, nheavy.p);
 
         k_bc_init<<<grid_for(ns, 256, 64), 256, 0, ctx->stream>>>(p);
         post_launch("bc_init");

@@ -81,6 +81,7 @@ struct ga_csr_s {
     void* val = nullptr;
     size_t cap = 0;  // allocated entries of col/val
     int unit = -1;   // all values equal 1: -1 unknown, 0 no, 1 yes
+    int sym = -1;    // pattern and values symmetric: -1 unknown, 0 no, 1 yes
 };
 
 struct ga_dense_s {
@@ -173,10 +174,13 @@ void mxm_masked_into(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, voi
 ga_csr mxm_cmask(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M);
 size_t mxm_scratch_bytes(int64_t m, int64_t n, int64_t mask_nnz);
 void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals, void* scratch,
-                       int64_t cap_nnz, bool unit_b);
+                       int64_t cap_nnz, bool unit_b, const int32_t* mask_row_end = nullptr);
 // True when every stored value of A equals 1 (computed once per handle and
 // cached; synchronises the stream the first time).
 bool csr_unit_values(ga_ctx ctx, ga_csr A);
+// True when A is square and every (i, j, v) has a matching (j, i, v)
+// (synchronises the stream).
+bool csr_is_symmetric(ga_ctx ctx, ga_csr A);
 void scan_exclusive_i32_scratch(ga_ctx ctx, const int32_t* in, int32_t* out, int64_t n, void* scratch);
 
 // Read one device value to the host (synchronises the stream).

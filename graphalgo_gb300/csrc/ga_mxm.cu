@@ -60,6 +60,7 @@ struct MxmArgs {
     const int32_t* ar; const int32_t* ac; const T* av;
     const int32_t* br; const int32_t* bc; const T* bv;
     const int32_t* mr; const int32_t* mc;
+    const int32_t* mre;  // optional mask row ends (row i's mask is [mr[i], mre[i])); nullptr: mr[i+1]
     T* cv;
     int64_t m;
     MxmQueue* q;
@@ -88,7 +89,7 @@ __global__ void k_row_bin(MxmArgs<T, A> p) {
         atomicAdd(&p.ctr[GA_CTR_ROWS], (unsigned long long)p.m);
     }
     for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < p.m; i += warps) {
-        const int32_t mb = p.mr[i], me = p.mr[i + 1];
+        const int32_t mb = p.mr[i], me = p.mre ? p.mre[i] : p.mr[i + 1];
         const int32_t mi = me - mb;
         if (mi == 0) continue;
         if (lane == 0) my_mask += (unsigned long long)mi;
@@ -234,10 +235,11 @@ __device__ __forceinline__ void b_range(const MxmArgs<T, A>& p, int32_t t, bool 
 // indices the segment ends falling inside it form one 32-bit mask (a warp OR
 // reduction), so every lane finds its B row with a popcount - no per-lane
 // search loop. Lanes whose B row is long may hand it to the CTA's long list.
+// Returns the number of products it processed (warp-uniform).
 template <int MD, bool UB, typename T, typename A, bool PUSH>
-__device__ __forceinline__ void group_products(const MxmArgs<T, A>& p, int32_t t_first, int32_t t_end, bool clip,
-                                               const SlotView& v, A* acc, int* s_incl, int* s_off, A* s_a,
-                                               int* s_nlong, int32_t* s_lbs, int32_t* s_lend, A* s_la) {
+__device__ __forceinline__ int group_products(const MxmArgs<T, A>& p, int32_t t_first, int32_t t_end, bool clip,
+                                              const SlotView& v, A* acc, int* s_incl, int* s_off, A* s_a,
+                                              int* s_nlong, int32_t* s_lbs, int32_t* s_lend, A* s_la) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int32_t t = t_first + lane;
@@ -260,7 +262,7 @@ __device__ __forceinline__ void group_products(const MxmArgs<T, A>& p, int32_t t
         }
     }
     const unsigned nz = __ballot_sync(FULL, len > 0);
-    if (nz == 0) return;
+    if (nz == 0) return 0;
     const int nseg = __popc(nz);
     const int incl = warp_incl_scan(len);
     const int total = __shfl_sync(FULL, incl, 31);
@@ -307,6 +309,7 @@ __device__ __forceinline__ void group_products(const MxmArgs<T, A>& p, int32_t t
         }
     }
     __syncwarp();
+    return total;
 }
 
 // Stream B entries [j0, j1) of one row with scalar head/tail and a
@@ -432,6 +435,7 @@ __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) 
     int* s_off = reinterpret_cast<int*>(scr) + kMxmWarps * 32 + wid * 32;
     A* s_a = reinterpret_cast<A*>(scr + (size_t)kMxmWarps * 32 * 2 * sizeof(int)) + wid * 32;
     __shared__ int s_item, s_nlong, s_nchunks, s_chunk_next;
+    unsigned long long executed = 0;  // products this warp processed (warp-uniform)
 
     // ------------------------------------------------------------ CTA items
     {
@@ -457,7 +461,7 @@ __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) 
             if (it >= ncta) break;
             const int4 item = p.cta_items[it < nheavy ? it : p.cta_cap - 1 - (it - nheavy)];
             const int64_t i = item.x;
-            const int32_t mb = p.mr[i], mi = p.mr[i + 1] - mb;
+            const int32_t mb = p.mr[i], mi = (p.mre ? p.mre[i] : p.mr[i + 1]) - mb;
             const int s0 = item.y, ns = item.z - item.y;
             const int32_t* gcol = p.mc + mb + s0;
             SlotView v;
@@ -476,18 +480,22 @@ __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) 
                 }
             }
             __syncthreads();
-            const bool clip = ns < mi;
+            // a window that does not span the whole row, or a mask restricted
+            // to part of the row, only meets B entries inside [lo, hi]
+            const bool clip = ns < mi || p.mre != nullptr;
             const int32_t ab = p.ar[i], ae = p.ar[i + 1];
             if (MD == MD_MERGE) {
                 for (int32_t t = ab + wid; t < ae; t += kMxmWarps) {
                     int32_t bs, be;
                     b_range(p, t, clip, v.lo, v.hi, bs, be);
                     merge_row<T, A>(p, bs, be, to_acc<T, A>(__ldg(p.av + t)), v, acc);
+                    executed += (unsigned long long)(be - bs);
                 }
             } else {
                 // phase A: short B rows flattened per warp, long ones listed
                 for (int32_t g = ab + wid * 32; g < ae; g += kMxmWarps * 32)
-                    group_products<MD, UB, T, A, true>(p, g, ae, clip, v, acc, s_incl, s_off, s_a, &s_nlong, lbs, lend, la);
+                    executed += (unsigned long long)group_products<MD, UB, T, A, true>(
+                        p, g, ae, clip, v, acc, s_incl, s_off, s_a, &s_nlong, lbs, lend, la);
                 __syncthreads();
                 // phase B: long B rows cut into kChunk pieces shared by all warps
                 const int nlong = min(s_nlong, kLongCap);
@@ -518,6 +526,7 @@ __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) 
                         const int32_t j0 = lbs[seg] + (c - lchunk[seg]) * kChunk;
                         const int32_t j1 = min(lend[seg], j0 + kChunk);
                         stream_row<MD, UB, T, A>(p, v, acc, j0, j1, la[seg]);
+                        executed += (unsigned long long)(j1 - j0);
                     }
                 }
             }
@@ -552,7 +561,8 @@ __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) 
             r = __shfl_sync(FULL, r, 0);
             if (r >= nwarp) break;
             const int64_t i = p.warp_rows[r];
-            const int32_t mb = p.mr[i], mi = p.mr[i + 1] - mb;
+            const int32_t mb = p.mr[i], mi = (p.mre ? p.mre[i] : p.mr[i + 1]) - mb;
+            const bool clip = p.mre != nullptr;
             const int32_t* gcol = p.mc + mb;
             SlotView v;
             v.mcol = mcol; v.bits = nullptr; v.wbase = nullptr; v.filt = filt; v.hkeys = hkeys; v.hslot = hslot;
@@ -575,13 +585,14 @@ __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) 
             if (MD == MD_MERGE) {
                 for (int32_t t = ab; t < ae; ++t) {
                     int32_t bs, be;
-                    b_range(p, t, false, 0, 0, bs, be);
+                    b_range(p, t, clip, v.lo, v.hi, bs, be);
                     merge_row<T, A>(p, bs, be, to_acc<T, A>(__ldg(p.av + t)), v, acc);
+                    executed += (unsigned long long)(be - bs);
                 }
             } else {
                 for (int32_t g = ab; g < ae; g += 32)
-                    group_products<WMD, UB, T, A, false>(p, g, ae, false, v, acc, s_incl, s_off, s_a, nullptr, nullptr,
-                                                     nullptr, nullptr);
+                    executed += (unsigned long long)group_products<WMD, UB, T, A, false>(
+                        p, g, ae, clip, v, acc, s_incl, s_off, s_a, nullptr, nullptr, nullptr, nullptr);
             }
             __syncwarp();
             for (int s = lane; s < mi; s += 32) p.cv[mb + s] = from_acc<T, A>(acc[s]);
@@ -592,6 +603,7 @@ __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) 
             __syncwarp();
         }
     }
+    if (lane == 0 && executed) atomicAdd(&p.ctr[GA_CTR_EXECUTED], executed);
 }
 
 static int64_t cta_item_cap(int64_t m, int64_t n, int64_t mask_nnz) {
@@ -605,12 +617,12 @@ static int64_t cta_item_cap(int64_t m, int64_t n, int64_t mask_nnz) {
 // Launch the masked product for one value type and lookup variant.
 template <int LK, bool UB, typename T>
 static void launch_masked(ga_ctx ctx, ga_csr A_, ga_csr B_, ga_csr M_, T* cv, MxmQueue* q, int32_t* warp_rows,
-                          int4* cta_items, int32_t cta_cap) {
+                          int4* cta_items, int32_t cta_cap, const int32_t* mre) {
     using Ac = typename Acc<T>::type;
     MxmArgs<T, Ac> p;
     p.ar = A_->rst; p.ac = A_->col; p.av = static_cast<const T*>(A_->val);
     p.br = B_->rst; p.bc = B_->col; p.bv = static_cast<const T*>(B_->val);
-    p.mr = M_->rst; p.mc = M_->col;
+    p.mr = M_->rst; p.mc = M_->col; p.mre = mre;
     p.cv = cv; p.m = M_->m; p.q = q; p.warp_rows = warp_rows; p.cta_items = cta_items; p.cta_cap = cta_cap;
     p.ctr = ctx->d_counters;
     {
@@ -639,9 +651,10 @@ size_t mxm_scratch_bytes(int64_t m, int64_t n, int64_t mask_nnz) {
 
 // Non-allocating launch (usable inside captured loops): `scratch` holds
 // mxm_scratch_bytes(M->m, M->n, max nnz(M)) bytes; `cap_nnz` is that max.
-// unit_b: B's values are all ones (no value loads).
+// unit_b: B's values are all ones (no value loads). mask_row_end (optional):
+// row i's mask is [M->rst[i], mask_row_end[i]) instead of the whole row.
 void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals, void* scratch,
-                       int64_t cap_nnz, bool unit_b) {
+                       int64_t cap_nnz, bool unit_b, const int32_t* mask_row_end) {
     GA_REQUIRE(algo == GA_MSA || algo == GA_MCA || algo == GA_HEAP, GA_ERR_INVALID_ARG, "mxm: unknown algorithm");
     unsigned char* s = static_cast<unsigned char*>(scratch);
     MxmQueue* q = reinterpret_cast<MxmQueue*>(s);
@@ -657,13 +670,13 @@ void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, v
         T* cv = static_cast<T*>(d_cvals);
         const int32_t c32 = (int32_t)cap;
         if (algo == GA_MSA) {
-            if (unit_b) launch_masked<MD_DENSE, true, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32);
-            else launch_masked<MD_DENSE, false, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32);
+            if (unit_b) launch_masked<MD_DENSE, true, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
+            else launch_masked<MD_DENSE, false, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
         } else if (algo == GA_MCA) {
-            if (unit_b) launch_masked<MD_BSEARCH, true, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32);
-            else launch_masked<MD_BSEARCH, false, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32);
+            if (unit_b) launch_masked<MD_BSEARCH, true, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
+            else launch_masked<MD_BSEARCH, false, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
         } else {
-            launch_masked<MD_MERGE, false, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32);
+            launch_masked<MD_MERGE, false, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
         }
     });
 }

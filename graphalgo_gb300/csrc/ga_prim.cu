@@ -162,6 +162,40 @@ bool csr_unit_values(ga_ctx ctx, ga_csr A) {
     return A->unit == 1;
 }
 
+// Pattern and values symmetric: every (i, j, v) has a (j, i, v).
+template <typename T>
+__global__ void k_check_symmetric(const int32_t* __restrict__ r, const int32_t* __restrict__ c,
+                                  const T* __restrict__ v, int64_t m, int* __restrict__ flag) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < m; i += warps) {
+        bool bad = false;
+        for (int32_t q = r[i] + lane; q < r[i + 1]; q += 32) {
+            const int32_t j = c[q];
+            if ((int64_t)j >= m) { bad = true; continue; }
+            const int32_t jb = r[j], jn = r[j + 1] - jb;
+            const int pos = lower_bound_i32(c + jb, jn, (int32_t)i);
+            if (pos >= jn || c[jb + pos] != (int32_t)i || !(v[jb + pos] == v[q])) bad = true;
+        }
+        if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flag, 1);
+    }
+}
+
+bool csr_is_symmetric(ga_ctx ctx, ga_csr A) {
+    if (A->sym >= 0) return A->sym == 1;
+    if (A->m != A->n) return false;
+    if (A->nnz == 0) return true;
+    DBuf<int> flag(ctx, 1);
+    GA_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), ctx->stream));
+    GA_DISPATCH_DTYPE(A->dtype, T, {
+        k_check_symmetric<T><<<grid_for(A->m * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(
+            A->rst, A->col, static_cast<const T*>(A->val), A->m, flag.p);
+    });
+    post_launch("check_symmetric");
+    A->sym = read_i32(ctx, flag.p) == 0 ? 1 : 0;
+    return A->sym == 1;
+}
+
 template <typename S, typename D>
 __global__ void k_convert(const S* __restrict__ s, D* __restrict__ d, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)

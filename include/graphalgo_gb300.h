@@ -117,11 +117,14 @@ GA_API int ga_mem_info(ga_ctx ctx, int64_t* free_bytes, int64_t* total_bytes);
 
 /* Work counters accumulated on the device by every masked-SpGEMM launch of
  * this context (MSA / MCA / HEAP): Gustavson products P = sum over A entries
- * (i,k) of nnz(B_k), mask entries, launches, A entries and rows. They feed
- * the GFLOP/s (2P) and byte models. out has GA_CTR_COUNT entries; reset != 0
- * zeroes them after reading. Synchronises the stream. */
+ * (i,k) of nnz(B_k) (the work of the reference's C<M> = A*B), mask entries,
+ * launches, A entries, rows, and the products the kernels actually processed
+ * (fewer than P when a k-truss support product only evaluates the upper
+ * triangle of a symmetric matrix and mirrors it). They feed the GFLOP/s (2P)
+ * and byte models. out has GA_CTR_COUNT entries; reset != 0 zeroes them
+ * after reading. Synchronises the stream. */
 enum { GA_CTR_PRODUCTS = 0, GA_CTR_MASK_ENTRIES = 1, GA_CTR_LAUNCHES = 2, GA_CTR_A_ENTRIES = 3,
-       GA_CTR_ROWS = 4, GA_CTR_COUNT = 5 };
+       GA_CTR_ROWS = 4, GA_CTR_EXECUTED = 5, GA_CTR_COUNT = 6 };
 GA_API int ga_ctx_work_counters(ga_ctx ctx, int64_t* out, int reset);
 
 /* Kernel launches issued by this library in this process so far (counted on
