@@ -62,6 +62,12 @@ def parse_args():
                     help="profiling case instead of the benchmark: support product, TC or BC, --reps times")
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--sources", type=int, default=64)
+    ap.add_argument("--workload", choices=["ktruss-sweep", "batch"], default="ktruss-sweep",
+                    help="ktruss-sweep: the R-MAT k-truss sweep; batch: TC + 4-truss of many k-NN graphs")
+    ap.add_argument("--graphs", type=int, default=4096, help="batch workload: number of graphs")
+    ap.add_argument("--plain-graphs", type=int, default=0,
+                    help="batch workload: graphs timed in the per-graph arm (0 = all)")
+    ap.add_argument("--tc-algo", default="msa", choices=["msa", "mca", "heap", "dot"])
     ap.add_argument("--host-loops", action="store_true",
                     help="run the k-truss loop from the host (kernels launched one by one, e.g. for ncu)")
     return ap.parse_args()
@@ -270,6 +276,43 @@ def sweep(ga, ctx, A, algo, kmin, sink=None, per_k=None):
     return out
 
 
+def profile_step(ga, ctx, run, algo, counters, loops):
+    """Runs one step with host-driven loops and per-kernel timing; returns the
+    launch count and the roofline of the masked-SpGEMM kernel.
+
+    achieved = algorithmic bytes of the Gustavson model with int32 values
+    (s = 4): 4(m+1)*2 + nnz(A)*(4+4) + nnz(A)*8 + P*(4+4) + nnz(M)*4 +
+    nnz(C)*4, P being the products the kernel processed (the support of a
+    symmetric C evaluates its upper triangle and mirrors it), divided by the
+    kernel's summed event time."""
+    ctx.set_option(ga.OPT_DEVICE_LOOPS, 0)
+    ctx.set_option(ga.OPT_PROFILE, 1)
+    ctx.reset_kernel_stats()
+    ctx.work_counters(reset=True)
+    l0 = ga.kernel_launches()
+    ctx.flush_l2()
+    run()
+    ctx.sync()
+    launches = ga.kernel_launches() - l0
+    stats = ctx.kernel_stats()
+    ctr = counters()
+    ctx.set_option(ga.OPT_PROFILE, 0)
+    ctx.set_option(ga.OPT_DEVICE_LOOPS, loops)
+    kname = {"msa": "mxm_msa", "mca": "mxm_mca", "heap": "mxm_heap_merge"}[algo]
+    k_launches, k_ms = stats.get(kname, (0, 0.0))
+    bytes_model = 8 * ctr["rows"] + 16 * ctr["a_entries"] + 8 * ctr["executed"] + 8 * ctr["mask_entries"]
+    peak, peak_kind = measured_peak_hbm()
+    achieved = bytes_model / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
+    tpe = profile_traffic()
+    traffic = (tpe * ctr["mask_entries"] / max(1, k_launches)) if tpe is not None else None
+    return {"launches": launches, "kernel_ms": k_ms, "stats": stats, "counters": ctr,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "kernel": kname, "peak_kind": peak_kind,
+                         "bytes_per_launch": bytes_model / max(1, k_launches),
+                         "avg_launch_ms": k_ms / max(1, k_launches)}}
+
+
 def run_gpu(args, dist: Dist):
     import graphalgo_gb300 as ga
     from graphalgo_gb300 import build as gbuild
@@ -312,38 +355,13 @@ def run_gpu(args, dist: Dist):
     value = flops_all / (t_max * 1e-3) / 1e9
 
     # ----------------------------------- per-kernel profile of one step
-    ctx.set_option(ga.OPT_DEVICE_LOOPS, 0)
-    ctx.set_option(ga.OPT_PROFILE, 1)
-    ctx.reset_kernel_stats()
-    ctx.work_counters(reset=True)
-    l0 = ga.kernel_launches()
-    ctx.flush_l2()
     per_k = {}
-    sweep(ga, ctx, A, args.algo, args.kmin, per_k=per_k)
-    ctx.sync()
-    launches_per_step = ga.kernel_launches() - l0
-    stats = ctx.kernel_stats()
-    prof_ctr = {key: sum(v[key] for v in per_k.values()) for key in next(iter(per_k.values()))}
-    ctx.set_option(ga.OPT_PROFILE, 0)
-    ctx.set_option(ga.OPT_DEVICE_LOOPS, loops)
-    kname = {"msa": "mxm_msa", "mca": "mxm_mca", "heap": "mxm_heap_merge"}[args.algo]
-    k_launches, k_ms = stats.get(kname, (0, 0.0))
-    # algorithmic bytes of the Gustavson model, int32 values (s = 4):
-    # 4(m+1)*2 + nnz(A)*(4+4) + nnz(A)*8 + P*(4+4) + nnz(M)*4 + nnz(C)*4,
-    # with P the products the kernel processed (the support of a symmetric C
-    # evaluates its upper triangle and mirrors it)
-    bytes_model = (8 * prof_ctr["rows"] + 16 * prof_ctr["a_entries"] + 8 * prof_ctr["executed"]
-                   + 8 * prof_ctr["mask_entries"])
-    peak, peak_kind = measured_peak_hbm()
-    achieved = bytes_model / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
-    tpe = profile_traffic()
-    traffic = (tpe * prof_ctr["mask_entries"] / max(1, k_launches)) if tpe is not None else None
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                "kernel": kname, "peak_kind": peak_kind,
-                "bytes_per_launch": bytes_model / max(1, k_launches),
-                "avg_launch_ms": k_ms / max(1, k_launches),
-                "kernel_share_of_step": k_ms / (total_ms / args.steps) if total_ms else None}
+    prof = profile_step(ga, ctx, lambda: sweep(ga, ctx, A, args.algo, args.kmin, per_k=per_k), args.algo,
+                        lambda: {key: sum(v[key] for v in per_k.values()) for key in next(iter(per_k.values()))},
+                        loops)
+    launches_per_step = prof["launches"]
+    roofline = prof["roofline"]
+    roofline["kernel_share_of_step"] = prof["kernel_ms"] / (total_ms / args.steps) if total_ms else None
 
     # ---------------------------------------------------------- e2e
     e2e = None
@@ -426,6 +444,173 @@ def run_gpu(args, dist: Dist):
     return line
 
 
+# ----------------------------------------------------------- batch workload
+def knn_batch_sizes(count: int, seed: int):
+    """Graph sizes of the batch workload: n ~ U[32, 4096], dim ~ U[4, 16]."""
+    rng = np.random.default_rng(seed)
+    return rng.integers(32, 4097, count).astype(np.int32), rng.integers(4, 17, count).astype(np.int32)
+
+
+def batch_config(args, n, nnz):
+    return {"workload": f"batched TC + 4-truss of {args.graphs} 30-NN graphs",
+            "graphs": args.graphs, "vertices": int(n.sum()), "stored_entries": int(nnz),
+            "graph": "n ~ U[32,4096], dim ~ U[4,16], points i.i.d. N(0,1), 30 nearest by Euclidean distance, "
+                     f"symmetrised by union, seed {args.seed}",
+            "variant": {"tc": args.tc_algo, "ktruss": args.algo}, "k": 4,
+            "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas only"}
+
+
+def run_batch(args, dist: Dist):
+    """One step = per-graph triangle counts and 4-truss of every graph of the
+    batch, as two batched calls over the block-diagonal union (resident in
+    HBM). Compared with the per-graph form on the same GPU: ga_tc and
+    ga_ktruss called graph by graph on resident per-graph handles."""
+    import graphalgo_gb300 as ga
+    from graphalgo_gb300 import build as gbuild
+    gbuild.build()
+    ctx = ga.Context(dist.local_rank)
+    loops = 0 if args.host_loops else 1
+    ctx.set_option(ga.OPT_DEVICE_LOOPS, loops)
+    n, dim = knn_batch_sizes(args.graphs, args.seed)
+    U, voff = ga.gen_knn_batch(ctx, n, dim, k=30, seed=args.seed + dist.rank)
+    G = args.graphs
+
+    def step():
+        tcs = ga.batch_tc(args.tc_algo, U, voff)
+        C, iters = ga.batch_ktruss(args.algo, U, voff, 4)
+        z = C.nnz
+        C.free()
+        return tcs, iters, z
+
+    for _ in range(max(1, args.warmup)):
+        ref = step()
+    sampler = ClockSampler(dist.local_rank)
+    dist.barrier()
+    ctx.sync()
+    sampler.start()
+    step_ms = []
+    for _ in range(args.steps):
+        ctx.flush_l2()
+        ctx.timer_start()
+        out = step()
+        step_ms.append(ctx.timer_stop())
+    ctx.sync()
+    clocks = sampler.stop()
+    dist.barrier()
+    assert np.array_equal(out[0], ref[0]) and np.array_equal(out[1], ref[1]) and out[2] == ref[2]
+    t_max = dist.max(sum(step_ms))
+    value = dist.sum(G * args.steps) / (t_max * 1e-3)
+
+    prof = profile_step(ga, ctx, step, args.algo, lambda: ctx.work_counters(), loops)
+    prof["roofline"]["kernel_share_of_step"] = prof["kernel_ms"] / (sum(step_ms) / args.steps)
+
+    # ------------------------------------------- per-graph plain launches
+    rst, col, _ = U.download()
+    blocks = ga.split_blocks(rst, col, voff)
+    npl = G if args.plain_graphs <= 0 else min(G, args.plain_graphs)
+    pick = np.sort(np.random.default_rng(args.seed + 1).choice(G, npl, replace=False)) if npl < G else np.arange(G)
+    handles = [ga.Csr.upload(ctx, m_, m_, r, c, np.ones(len(c), np.int32)) for m_, r, c in (blocks[i] for i in pick)]
+    for h in handles[:8]:
+        ga.tc(args.tc_algo, h, per_row=False)
+        ga.ktruss(args.algo, h, 4)[0].free()
+    ctx.sync()
+    ctx.flush_l2()
+    ctx.timer_start()
+    plain_tc = np.zeros(npl, np.int64)
+    plain_it = np.zeros(npl, np.int32)
+    plain_nnz = 0
+    for j, h in enumerate(handles):
+        plain_tc[j] = ga.tc(args.tc_algo, h, per_row=False)[0]
+        C, plain_it[j] = ga.ktruss(args.algo, h, 4)
+        plain_nnz += C.nnz
+        C.free()
+    plain_ms = ctx.timer_stop()
+    same = bool(np.array_equal(plain_tc, ref[0][pick]) and np.array_equal(plain_it, ref[1][pick])
+                and (npl < G or plain_nnz == ref[2]))
+    for h in handles:
+        h.free()
+    plain_value = dist.sum(npl) / (dist.max(plain_ms) * 1e-3)
+
+    # ---------------------------------------------------------- e2e
+    e2e = None
+    if not args.no_e2e:
+        rst_h = np.ascontiguousarray(rst)
+        col_h = np.ascontiguousarray(col)
+        val_h = np.ones(len(col), np.int32)
+        out_rst = np.empty(len(rst), np.int32)
+        out_col = np.empty(len(col) + 1, np.int32)
+        pinned = [rst_h, col_h, val_h, out_rst, out_col]
+        for a in pinned:
+            ga.host_register(a)
+        try:
+            e2e_ms, d2h = [], 0
+            dist.barrier()
+            for _ in range(args.steps):
+                ctx.flush_l2()
+                ctx.timer_start()
+                Ud = ga.Csr.upload(ctx, len(rst) - 1, len(rst) - 1, rst_h, col_h, val_h)
+                tcs = ga.batch_tc(args.tc_algo, Ud, voff)
+                C, iters = ga.batch_ktruss(args.algo, Ud, voff, 4)
+                z = C.nnz
+                ga.lib().ga_csr_download(ctx.handle, C.handle, out_rst.ctypes.data_as(ga._p),
+                                         out_col.ctypes.data_as(ga._p), None)
+                C.free()
+                Ud.free()
+                e2e_ms.append(ctx.timer_stop())
+                d2h = tcs.nbytes + iters.nbytes + out_rst.nbytes + 4 * z
+            e2e_t = dist.max(sum(e2e_ms))
+            e2e = {"value": dist.sum(G * args.steps) / (e2e_t * 1e-3), "unit": "graphs/s",
+                   "h2d_bytes_per_step": int(rst_h.nbytes + col_h.nbytes + val_h.nbytes + voff.nbytes),
+                   "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t / args.steps}
+        finally:
+            for a in pinned:
+                ga.host_unregister(a)
+
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        cpu = batch_cpu_sample(blocks, args.seed)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "graphs/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": batch_config(args, n, len(col)),
+        "roofline": prof["roofline"], "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": int(prof["launches"] * args.steps), "clocks": clocks,
+        "plain": {"value": plain_value, "unit": "graphs/s", "graphs_timed": npl, "ms": plain_ms,
+                  "results_equal": same, "speedup": value / plain_value,
+                  "form": "ga_tc + ga_ktruss per graph, resident per-graph handles"},
+        "work": {"products_per_step": prof["counters"]["products"],
+                 "triangles": int(ref[0].sum()), "truss_entries": int(ref[2]),
+                 "max_iters": int(ref[1].max())},
+    }
+    ctx.close()
+    return line
+
+
+def batch_cpu_sample(blocks, seed, budget_s: float = 15.0):
+    """Oracle port (OpenMP, all host threads): TC + 4-truss graph by graph on
+    a seeded sample of the batch's graphs until the time budget is spent."""
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_num_threads(threads)
+    order = np.random.default_rng(seed + 2).permutation(len(blocks))
+    done, t = 0, 0.0
+    for i in order:
+        m_, r, c = blocks[i]
+        A = oracle.Csr(m_, m_, r, c, np.ones(len(c), np.int32))
+        t0 = time.perf_counter()
+        oracle.tc_sandia(A)
+        oracle.ktruss(A, 4)
+        t += time.perf_counter() - t0
+        done += 1
+        if t >= budget_s:
+            break
+    return {"value": done / t, "unit": "graphs/s", "cores": threads, "kind": "port",
+            "sample": f"{done} of {len(blocks)} graphs (seeded random order), TC + 4-truss each, {t:.1f} s"}
+
+
 # --------------------------------------------------------- reference arm
 def run_reference(args, dist: Dist):
     if dist.rank != 0:
@@ -466,7 +651,12 @@ def main():
         return
     dist = Dist()
     try:
-        line = run_reference(args, dist) if args.impl == "reference" else run_gpu(args, dist)
+        if args.impl == "reference":
+            line = run_reference(args, dist)
+        elif args.workload == "batch":
+            line = run_batch(args, dist)
+        else:
+            line = run_gpu(args, dist)
         if dist.rank == 0 and line is not None:
             print(json.dumps(line), flush=True)
     finally:

@@ -428,3 +428,59 @@ def gen_er(n: int, edges: int, seed: int = 1):
 def gen_knn(n: int, dim: int, k: int = 30, seed: int = 1):
     """Seeded k-NN graph of n Gaussian points in `dim` dimensions, symmetrised."""
     return _gen(lib().ga_gen_knn, int(n), int(dim), int(k), int(seed))
+
+
+# ------------------------------------------------------------- batched graphs
+def _voff_arg(voff) -> np.ndarray:
+    return np.ascontiguousarray(voff, dtype=np.int64)
+
+
+def block_diag(ctx: Context, parts: Sequence[Csr]) -> Tuple[Csr, np.ndarray]:
+    """Block-diagonal union of `parts` and its row offsets (count + 1)."""
+    handles = (_p * max(1, len(parts)))(*[p.handle for p in parts])
+    voff = np.zeros(len(parts) + 1, np.int64)
+    h = _p()
+    _check(lib().ga_csr_block_diag(ctx.handle, _i64(len(parts)), handles, ctypes.byref(h), _ptr(voff)), ctx)
+    return Csr(ctx, h), voff
+
+
+def gen_knn_batch(ctx: Context, n: Sequence[int], dim: Sequence[int], k: int = 30,
+                  seed: int = 1) -> Tuple[Csr, np.ndarray]:
+    """Seeded k-NN graphs built on the device, as one block-diagonal union."""
+    nn = np.ascontiguousarray(n, dtype=np.int32)
+    dd = np.ascontiguousarray(dim, dtype=np.int32)
+    if nn.shape != dd.shape:
+        raise ValueError("n and dim need one entry per graph")
+    voff = np.zeros(len(nn) + 1, np.int64)
+    h = _p()
+    _check(lib().ga_gen_knn_batch(ctx.handle, _i64(len(nn)), _ptr(nn), _ptr(dd), _int(k), ctypes.c_uint64(seed),
+                                  ctypes.byref(h), _ptr(voff)), ctx)
+    return Csr(ctx, h), voff
+
+
+def batch_tc(algo, U: Csr, voff) -> np.ndarray:
+    """Per-graph triangle counts of a block-diagonal union."""
+    v = _voff_arg(voff)
+    out = np.zeros(len(v) - 1, np.int64)
+    _check(lib().ga_batch_tc(U.ctx.handle, _algo(algo), U.handle, _i64(len(v) - 1), _ptr(v), _ptr(out)), U.ctx)
+    return out
+
+
+def batch_ktruss(algo, U: Csr, voff, k: int) -> Tuple[Csr, np.ndarray]:
+    """Per-graph k-truss of a block-diagonal union: (union of results, iterations per graph)."""
+    v = _voff_arg(voff)
+    iters = np.zeros(len(v) - 1, np.int32)
+    h = _p()
+    _check(lib().ga_batch_ktruss(U.ctx.handle, _algo(algo), U.handle, _i64(len(v) - 1), _ptr(v), _int(k),
+                                 ctypes.byref(h), _ptr(iters)), U.ctx)
+    return Csr(U.ctx, h), iters
+
+
+def split_blocks(rst: np.ndarray, col: np.ndarray, voff) -> list:
+    """Host helper: cut a downloaded block-diagonal CSR into per-graph (m, rst, col)."""
+    out = []
+    for g in range(len(voff) - 1):
+        b, e = int(voff[g]), int(voff[g + 1])
+        r = rst[b:e + 1].astype(np.int64)
+        out.append((e - b, (r - r[0]).astype(np.int32), (col[r[0]:r[-1]] - b).astype(np.int32)))
+    return out

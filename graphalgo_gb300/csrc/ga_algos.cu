@@ -227,15 +227,57 @@ struct KtState {
     int32_t first_vals; // C still carries A's values (no swap yet)
 };
 
+// Rows of graphs that have finished (batched k-truss) keep every entry.
+__device__ __forceinline__ bool kt_keep_all(const int32_t* gid, const int32_t* done_g, int64_t i) {
+    return gid != nullptr && done_g[gid[i]] != 0;
+}
+
 __global__ void k_kt_count(const int32_t* __restrict__ cr, const int32_t* __restrict__ sup, int64_t m, int k,
-                           int32_t* __restrict__ cnt) {
+                           int32_t* __restrict__ cnt, const int32_t* __restrict__ gid,
+                           const int32_t* __restrict__ done_g) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < m; i += warps) {
+        if (kt_keep_all(gid, done_g, i)) {
+            if (lane == 0) cnt[i] = cr[i + 1] - cr[i];
+            continue;
+        }
         int c = 0;
         for (int32_t q = cr[i] + lane; q < cr[i + 1]; q += 32) c += sup[q] >= k - 2;
         c = warp_sum<int>(c);
         if (lane == 0) cnt[i] = c;
+    }
+}
+
+// Batched k-truss bookkeeping after iteration t, one block per graph: a graph
+// whose kept count equals its current count has converged (iterations t+1);
+// otherwise it was pruned and stops after n_g iterations (reported as 0),
+// as the reference's loop bound does (src/main.cpp:100).
+__global__ void k_kt_graph_update(const KtState* st, const int32_t* __restrict__ cnt, KtBatch b) {
+    __shared__ int64_t s_part[32];
+    const int64_t g = blockIdx.x;
+    if (g >= b.ngraphs) return;
+    int64_t kept = 0;
+    for (int32_t i = b.voff[g] + threadIdx.x; i < b.voff[g + 1]; i += blockDim.x) kept += cnt[i];
+    kept = warp_sum<int64_t>(kept);
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = kept;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t total = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) total += s_part[w];
+        if (!b.done_g[g]) {
+            const int t = st->t;
+            if (total == b.nnz_g[g]) {
+                b.iters_g[g] = t + 1;
+                b.done_g[g] = 1;
+            } else {
+                b.nnz_g[g] = (int32_t)total;
+                if (t + 1 >= b.nvert[g]) {
+                    b.iters_g[g] = 0;
+                    b.done_g[g] = 1;
+                }
+            }
+        }
     }
 }
 
@@ -244,16 +286,18 @@ __global__ void k_kt_count(const int32_t* __restrict__ cr, const int32_t* __rest
 // the row of each new entry.
 __global__ void k_kt_compact(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
                              const int32_t* __restrict__ sup, const int32_t* __restrict__ tr, int64_t m, int k,
-                             int32_t* __restrict__ tc, int32_t* __restrict__ pos_new, int32_t* __restrict__ trow) {
+                             int32_t* __restrict__ tc, int32_t* __restrict__ pos_new, int32_t* __restrict__ trow,
+                             const int32_t* __restrict__ gid, const int32_t* __restrict__ done_g) {
     const int lane = threadIdx.x & 31;
     const unsigned FULL = 0xffffffffu;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < m; i += warps) {
         int32_t o = tr[i];
         const int32_t b = cr[i], e = cr[i + 1];
+        const bool all = kt_keep_all(gid, done_g, i);
         for (int32_t base = b; base < e; base += 32) {
             int32_t q = base + lane;
-            bool keep = q < e && sup[q] >= k - 2;
+            bool keep = q < e && (all || sup[q] >= k - 2);
             unsigned bal = __ballot_sync(FULL, keep);
             const int32_t dst = o + __popc(bal & ((1u << lane) - 1u));
             if (keep) {
@@ -358,7 +402,7 @@ __global__ void k_kt_copyback_aux(const KtState* st, const int32_t* __restrict__
     }
 }
 
-static ga_csr ktruss(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out) {
+ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, const KtBatch* batch) {
     GA_REQUIRE(A->m == A->n, GA_ERR_SHAPE, "k-truss needs a square matrix");
     GA_REQUIRE(A->dtype == GA_INT32, GA_ERR_DTYPE, "k-truss needs int32 values (spMtx<int>)");
     GA_REQUIRE(algo == GA_MSA || algo == GA_MCA || algo == GA_HEAP || algo == GA_NAIVE, GA_ERR_INVALID_ARG,
@@ -416,11 +460,18 @@ static ga_csr ktruss(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out) 
             } else {
                 mxm_masked_launch(ctx, algo, C, C, C, sup.p, mxm_scr.p, cap, unit);
             }
-            k_kt_count<<<grid_rows, 256, 0, ctx->stream>>>(C->rst, sup.p, m, k, cnt.p);
+            const int32_t* gid = batch ? batch->gid : nullptr;
+            const int32_t* done_g = batch ? batch->done_g : nullptr;
+            k_kt_count<<<grid_rows, 256, 0, ctx->stream>>>(C->rst, sup.p, m, k, cnt.p, gid, done_g);
             post_launch("kt_count");
             scan_exclusive_i32_scratch(ctx, cnt.p, tr.p, m, scan_scr.p);
             k_kt_compact<<<grid_rows, 256, 0, ctx->stream>>>(C->rst, C->col, sup.p, tr.p, m, k, tc.p,
-                                                             upper ? pos_new.p : nullptr, upper ? trow.p : nullptr);
+                                                             upper ? pos_new.p : nullptr, upper ? trow.p : nullptr,
+                                                             gid, done_g);
+            if (batch) {
+                k_kt_graph_update<<<(unsigned)batch->ngraphs, 256, 0, ctx->stream>>>(st.p, cnt.p, *batch);
+                post_launch("kt_graph_update");
+            }
             post_launch("kt_compact");
             if (upper) {
                 k_mirror_update<<<grid_ent, 256, 0, ctx->stream>>>(st.p, pos_new.p, mir.p, mir_new.p);
@@ -526,7 +577,7 @@ int ga_tc_vertex(ga_ctx ctx, ga_algo algo, ga_csr A, int32_t* per_vertex) {
 int ga_ktruss(ga_ctx ctx, ga_algo algo, ga_csr A, int k, ga_csr* C, int* iters) {
     if (!ctx || !A || !C) return GA_ERR_INVALID_ARG;
     *C = nullptr;
-    GA_API_BODY(ctx, *C = ktruss(ctx, algo, A, k, iters));
+    GA_API_BODY(ctx, *C = ktruss_impl(ctx, algo, A, k, iters, nullptr));
 }
 
 }  // extern "C"

@@ -164,6 +164,22 @@ void fill_ones(ga_ctx ctx, void* vals, int64_t count, ga_dtype dt);
 // Validates a device CSR; throws GA_ERR_INVALID_CSR when malformed.
 void validate_csr(ga_ctx ctx, const int32_t* rst, const int32_t* col, int64_t m, int64_t n, int64_t nnz);
 
+// Sorts each CSR row segment by key (payload follows), rows up to 8192 long.
+void sort_rows_by_key(ga_ctx ctx, const int32_t* rst, int64_t m, int32_t* key, int32_t* pay);
+
+// k-truss on a single matrix (batch == nullptr) or on a block-diagonal union
+// of graphs with per-graph convergence (see ga_batch_ktruss).
+struct KtBatch {
+    int64_t ngraphs = 0;
+    const int32_t* voff = nullptr;   // first row of each graph (ngraphs + 1)
+    const int32_t* gid = nullptr;    // graph of each row
+    const int32_t* nvert = nullptr;  // vertices per graph
+    int32_t* nnz_g = nullptr;        // current stored entries per graph
+    int32_t* iters_g = nullptr;      // reported iteration count per graph
+    int32_t* done_g = nullptr;       // graph finished (converged, or stopped after n_g iterations)
+};
+ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, const KtBatch* batch);
+
 // device-side transpose (counting sort; rows of the result sorted)
 ga_csr transpose_csr(ga_ctx ctx, ga_csr A);
 ga_csr extract_tri(ga_ctx ctx, ga_csr A, bool lower);

@@ -299,6 +299,16 @@ __global__ void k_sort_rows(const int32_t* __restrict__ rst, int64_t m, int32_t*
     }
 }
 
+void sort_rows_by_key(ga_ctx ctx, const int32_t* rst, int64_t m, int32_t* key, int32_t* pay) {
+    DBuf<int> flag(ctx, 1);
+    GA_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), ctx->stream));
+    const size_t smem = 2 * kSortCap * sizeof(int32_t);
+    GA_CUDA(cudaFuncSetAttribute(k_sort_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_sort_rows<<<ctx->num_sms * 2, 512, smem, ctx->stream>>>(rst, m, key, pay, flag.p);
+    post_launch("sort_rows");
+    if (read_i32(ctx, flag.p)) fail(GA_ERR_UNSUPPORTED, "row sort: a row holds more than 8192 entries");
+}
+
 template <typename T>
 __global__ void k_gather_vals(const int32_t* __restrict__ src, const T* __restrict__ v, T* __restrict__ out,
                               int64_t n) {

@@ -268,6 +268,32 @@ GA_API int ga_bc(ga_ctx ctx, ga_csr A, const int32_t* sources, int64_t nsrc, dou
 /* Device-result variant (bc: device array of length m, overwritten). */
 GA_API int ga_bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t nsrc, double* d_bc);
 
+/* ------------------------------------------------------ batched graphs */
+/* Many independent graphs as one block-diagonal matrix: rows (and columns)
+ * of graph g are voff[g] .. voff[g+1]-1. The batched calls run each kernel
+ * once over the whole union (the masked-SpGEMM work queue holds the row bins
+ * of every graph) and return per-graph results equal to running each graph
+ * alone. No counterpart in the reference, whose callers take one graph. */
+/* Concatenate `count` CSR handles of one dtype into a block-diagonal U;
+ * voff (host, count+1 entries, may be NULL) receives the row offsets. */
+GA_API int ga_csr_block_diag(ga_ctx ctx, int64_t count, const ga_csr* parts, ga_csr* U, int64_t* voff);
+/* Seeded k-NN graphs built on the device: graph g has n[g] points (1..4096)
+ * i.i.d. N(0,1) in dim[g] dimensions (1..32), each linked to its k nearest
+ * by FP32 Euclidean distance (self excluded, ties to the smaller index),
+ * symmetrised by union; int32 unit values, rows sorted. Returns the union
+ * and its row offsets (voff, host, count+1). */
+GA_API int ga_gen_knn_batch(ga_ctx ctx, int64_t count, const int32_t* n, const int32_t* dim, int k,
+                            uint64_t seed, ga_csr* U, int64_t* voff);
+/* Per-graph triangle counts (totals: host, count entries) of a block-diagonal
+ * union of symmetric adjacency matrices, as ga_tc would give for each graph. */
+GA_API int ga_batch_tc(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, const int64_t* voff, int64_t* totals);
+/* Per-graph k-truss of a block-diagonal union (int32, all values 1): one
+ * device loop prunes every graph, a graph stops changing once it converged,
+ * and iters (host, count entries) receives each graph's iteration count as
+ * ga_ktruss reports it. *C is the union of the per-graph results. */
+GA_API int ga_batch_ktruss(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, const int64_t* voff, int k,
+                           ga_csr* C, int* iters);
+
 /* ------------------------------------------------------ synthetic graphs */
 /* Seeded generators producing sorted, duplicate-free, loop-free symmetric
  * int32 CSR on the host (arrays allocated with malloc; free with

@@ -1,0 +1,152 @@
+"""Batched graphs: a block-diagonal union run by one launch of each kernel
+gives every graph the result it gets alone.
+
+Triangle counts, k-truss edge sets and k-truss iteration counts are compared
+bit-exactly with per-graph single calls and, for a few graphs, with the
+oracle. The device k-NN generator is checked for the structure it promises.
+"""
+import numpy as np
+import pytest
+
+import graphalgo_gb300 as ga
+import oracle
+from graphs import csr_from_arrays, random_graph, to_device
+
+pytestmark = pytest.mark.gpu
+
+
+def _uneven_sizes(count, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    return rng.integers(lo, hi + 1, count).astype(np.int32), rng.integers(4, 17, count).astype(np.int32)
+
+
+def _check_knn_structure(m, rst, col, k):
+    assert rst[0] == 0 and np.all(np.diff(rst) >= 0)
+    for i in range(m):
+        row = col[rst[i]:rst[i + 1]]
+        assert np.all(np.diff(row) > 0), "rows sorted, no duplicates"
+        assert not np.any(row == i), "no self-loops"
+        assert len(row) >= min(k, m - 1)
+    # symmetric pattern
+    rows = np.repeat(np.arange(m), np.diff(rst))
+    a = set(zip(rows.tolist(), col.tolist()))
+    assert all((j, i) in a for i, j in a)
+
+
+def test_knn_batch_structure(ctx):
+    n, dim = _uneven_sizes(12, 1, 300, seed=3)
+    n[0], n[1] = 1, 31  # a single point; fewer points than k + 1
+    U, voff = ga.gen_knn_batch(ctx, n, dim, k=30, seed=9)
+    assert voff[0] == 0 and np.array_equal(np.diff(voff), n)
+    rst, col, val = U.download()
+    assert np.all(val == 1)
+    for g, (m, r, c) in enumerate(ga.split_blocks(rst, col, voff)):
+        assert m == n[g]
+        assert np.all((c >= 0) & (c < m)), "no edge leaves its graph"
+        _check_knn_structure(m, r, c, 30)
+    # same seed, same graphs; another seed, other graphs
+    U2, _ = ga.gen_knn_batch(ctx, n, dim, k=30, seed=9)
+    assert all(np.array_equal(x, y) for x, y in zip(U2.download(), (rst, col, val)))
+    U3, _ = ga.gen_knn_batch(ctx, n, dim, k=30, seed=10)
+    assert not np.array_equal(U3.download()[1], col)
+
+
+def _mixed_parts(ctx):
+    rng = np.random.default_rng(77)
+    host = [
+        csr_from_arrays(*ga.gen_er(200, 1500, seed=2)),
+        random_graph(1, 0.5, rng),
+        csr_from_arrays(*ga.gen_rmat(9, 16, seed=5)),
+        random_graph(40, 0.6, rng),
+        csr_from_arrays(*ga.gen_knn(300, 5, 30, seed=6)),
+        random_graph(3, 0.0, rng),
+        random_graph(120, 0.2, rng),
+    ]
+    return host, [to_device(ctx, G) for G in host]
+
+
+def test_block_diag_round_trip(ctx):
+    host, dev = _mixed_parts(ctx)
+    U, voff = ga.block_diag(ctx, dev)
+    assert np.array_equal(np.diff(voff), [G.m for G in host])
+    rst, col, val = U.download()
+    for G, (m, r, c) in zip(host, ga.split_blocks(rst, col, voff)):
+        assert m == G.m and np.array_equal(r, G.rst) and np.array_equal(c, G.col)
+
+
+@pytest.mark.parametrize("algo", ["dot", "msa", "mca", "heap"])
+def test_batch_tc_matches_single(ctx, algo):
+    host, dev = _mixed_parts(ctx)
+    U, voff = ga.block_diag(ctx, dev)
+    got = ga.batch_tc(algo, U, voff)
+    for g, (G, Gd) in enumerate(zip(host, dev)):
+        assert got[g] == ga.tc(algo, Gd, per_row=False)[0]
+        assert got[g] == oracle.tc_sandia(G)[0]
+
+
+def _solo_ktruss(ctx, algo, blocks, k):
+    out = []
+    for m, r, c in blocks:
+        G = ga.Csr.upload(ctx, m, m, r, c, np.ones(len(c), np.int32))
+        C, it = ga.ktruss(algo, G, k)
+        cr, cc, _ = C.download()
+        out.append((cr, cc, it))
+    return out
+
+
+@pytest.mark.parametrize("algo", ["msa", "mca", "heap"])
+@pytest.mark.parametrize("k", [4, 6])
+def test_batch_ktruss_matches_single(ctx, algo, k):
+    host, dev = _mixed_parts(ctx)
+    U, voff = ga.block_diag(ctx, dev)
+    C, iters = ga.batch_ktruss(algo, U, voff, k)
+    cr, cc, cv = C.download()
+    assert np.all(cv == 1)
+    blocks = [(G.m, G.rst, G.col) for G in host]
+    for g, ((m, r, c), (sr, sc, sit)) in enumerate(zip(ga.split_blocks(cr, cc, voff),
+                                                      _solo_ktruss(ctx, algo, blocks, k))):
+        assert iters[g] == sit, f"graph {g}"
+        assert np.array_equal(r, sr) and np.array_equal(c, sc), f"graph {g}"
+    # two graphs against the oracle as well
+    for g in (0, 4):
+        ref = oracle.ktruss(host[g], k)
+        m, r, c = ga.split_blocks(cr, cc, voff)[g]
+        assert np.array_equal(r, ref[0].rst) and np.array_equal(c, ref[0].col)
+        assert iters[g] == ref[1]
+
+
+@pytest.mark.parametrize("device_loops", [1, 0])
+def test_batch_knn_tc_ktruss(ctx, device_loops):
+    """The batched workload's own graph family: uneven k-NN graphs, TC + 4-truss."""
+    n, dim = _uneven_sizes(40, 32, 700, seed=21)
+    U, voff = ga.gen_knn_batch(ctx, n, dim, k=30, seed=4)
+    ctx.set_option(ga.OPT_DEVICE_LOOPS, device_loops)
+    try:
+        tcs = ga.batch_tc("msa", U, voff)
+        C, iters = ga.batch_ktruss("msa", U, voff, 4)
+    finally:
+        ctx.set_option(ga.OPT_DEVICE_LOOPS, 1)
+    rst, col, _ = U.download()
+    blocks = ga.split_blocks(rst, col, voff)
+    cr, cc, _ = C.download()
+    got = ga.split_blocks(cr, cc, voff)
+    solo = _solo_ktruss(ctx, "msa", blocks, 4)
+    for g, (m, r, c) in enumerate(blocks):
+        G = ga.Csr.upload(ctx, m, m, r, c, np.ones(len(c), np.int32))
+        assert tcs[g] == ga.tc("dot", G, per_row=False)[0]
+        assert iters[g] == solo[g][2]
+        assert np.array_equal(got[g][1], solo[g][0]) and np.array_equal(got[g][2], solo[g][1])
+
+
+def test_batch_rejects_bad_offsets(ctx):
+    host, dev = _mixed_parts(ctx)
+    U, voff = ga.block_diag(ctx, dev)
+    bad = voff.copy()
+    bad[-1] -= 1
+    with pytest.raises(ga.GaError) as e:
+        ga.batch_tc("msa", U, bad)
+    assert e.value.code == ga.ERR_INVALID_ARG
+    bad = voff.copy()
+    bad[2], bad[3] = bad[3], bad[2]
+    with pytest.raises(ga.GaError):
+        ga.batch_ktruss("msa", U, bad, 4)
