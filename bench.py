@@ -62,8 +62,15 @@ def parse_args():
                     help="profiling case instead of the benchmark: support product, TC or BC, --reps times")
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--sources", type=int, default=64)
-    ap.add_argument("--workload", choices=["ktruss-sweep", "batch"], default="ktruss-sweep",
-                    help="ktruss-sweep: the R-MAT k-truss sweep; batch: TC + 4-truss of many k-NN graphs")
+    ap.add_argument("--workload", choices=["ktruss-sweep", "batch", "serve"], default="ktruss-sweep",
+                    help="ktruss-sweep: the R-MAT k-truss sweep; batch: TC + 4-truss of many k-NN graphs; "
+                         "serve: a stream of TC / k-truss / BC requests on a pool of resident graphs")
+    ap.add_argument("--requests", type=int, default=300, help="serve workload: requests per run")
+    ap.add_argument("--workers", type=int, default=4, help="serve workload: server worker threads")
+    ap.add_argument("--rmat-scales", default="10,12,14,16,18,20,22", help="serve workload: R-MAT pool scales")
+    ap.add_argument("--knn-sizes", default="1000,10000,100000,1000000", help="serve workload: k-NN pool sizes")
+    ap.add_argument("--rates", default="0.5,1,2,4",
+                    help="serve workload: Poisson rates as multiples of the plain form's throughput")
     ap.add_argument("--graphs", type=int, default=4096, help="batch workload: number of graphs")
     ap.add_argument("--plain-graphs", type=int, default=0,
                     help="batch workload: graphs timed in the per-graph arm (0 = all)")
@@ -611,6 +618,157 @@ def batch_cpu_sample(blocks, seed, budget_s: float = 15.0):
             "sample": f"{done} of {len(blocks)} graphs (seeded random order), TC + 4-truss each, {t:.1f} s"}
 
 
+# ----------------------------------------------------------- serve workload
+def serve_pool(args, ctx, ga):
+    """Seeded graph pool: R-MAT (edge factor 16) at the given scales and
+    30-NN Gaussian graphs (dim ~ U[4,16]) of the given sizes, host CSR."""
+    pool = []
+    for sc in [int(x) for x in args.rmat_scales.split(",") if x]:
+        m, rst, col = ga.gen_rmat(sc, 16, 0.57, 0.19, 0.19, args.seed + sc)
+        pool.append((f"rmat{sc}", m, rst, col))
+    rng = np.random.default_rng(args.seed)
+    for n in [int(float(x)) for x in args.knn_sizes.split(",") if x]:
+        d = int(rng.integers(4, 17))
+        U, voff = ga.gen_knn_batch(ctx, [n], [d], k=30, seed=args.seed + n)
+        rst, col, _ = U.download()
+        U.free()
+        pool.append((f"knn{n}d{d}", n, rst, col))
+    return pool
+
+
+def serve_requests(args, pool):
+    """Request types uniform over TC / k-truss (k ~ U{3..8}) / BC (32 seeded
+    sources), graphs uniform over the pool."""
+    import graphalgo_gb300 as ga
+    rng = np.random.default_rng(args.seed + 7)
+    out = []
+    for _ in range(args.requests):
+        g = int(rng.integers(len(pool)))
+        t = int(rng.integers(3))
+        m = pool[g][1]
+        if t == ga.REQ_BC:
+            out.append((t, g, 0, rng.choice(m, min(32, m), replace=False).astype(np.int32)))
+        elif t == ga.REQ_KTRUSS:
+            out.append((t, g, int(rng.integers(3, 9)), None))
+        else:
+            out.append((t, g, 0, None))
+    return out
+
+
+def serve_run(ga, pool, reqs, workers, coalesce, arrivals=None):
+    """Runs the requests through a server; arrivals (seconds from the start)
+    or all at once. Returns latencies, makespan and results."""
+    with ga.Server(0, workers=workers, coalesce=coalesce) as srv:
+        for _, m, rst, col in pool:
+            srv.add_graph(m, rst, col)
+        ids = []
+        t0 = time.perf_counter()
+        for i, (t, g, k, src) in enumerate(reqs):
+            if arrivals is not None:
+                dt = t0 + arrivals[i] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+            ids.append(srv.submit(t, g, k=k, sources=src, want_edges=(t == ga.REQ_KTRUSS)))
+        res = [srv.wait(r, timeout=3600) for r in ids]
+        st = srv.stats()
+    bad = [r for r in res if r["status"] != ga.OK]
+    if bad:
+        raise RuntimeError(f"{len(bad)} requests failed: {bad[0]['error']}")
+    lat = np.array([r["t_end"] - r["t_submit"] for r in res])
+    span = max(r["t_end"] for r in res) - min(r["t_submit"] for r in res)
+    d2h = 0
+    for (t, g, _, _), r in zip(reqs, res):
+        d2h += 8 if t == ga.REQ_TC else (8 * pool[g][1] if t == ga.REQ_BC else 4 * (pool[g][1] + 1 + r["nnz"]))
+    return {"req_s": len(reqs) / span, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+            "p99_ms": 1e3 * float(np.percentile(lat, 99)), "makespan_s": span, "stats": st, "results": res,
+            "d2h_bytes": d2h}
+
+
+def serve_digest(ga, reqs, res):
+    """Per-request results reduced to comparable values."""
+    out = []
+    for (t, _, _, _), r in zip(reqs, res):
+        if t == ga.REQ_TC:
+            out.append(("tc", r["tc"]))
+        elif t == ga.REQ_KTRUSS:
+            out.append(("kt", r["iters"], r["nnz"], int(np.sum(r["col"], dtype=np.int64))))
+        else:
+            out.append(("bc", r["bc"]))
+    return out
+
+
+def serve_same(a, b):
+    for x, y in zip(a, b):
+        if x[0] == "bc":
+            if not np.allclose(x[1], y[1], rtol=1e-9, atol=1e-9):
+                return False
+        elif x != y:
+            return False
+    return True
+
+
+def run_serve(args, dist: Dist):
+    """Serving: saturated throughput (every request queued at once) of the
+    server (workers, batching) against the plain sequential form (one worker,
+    no batching) on the same requests, then Poisson arrivals at rates that
+    are multiples of the plain form's throughput, p50/p99 latency of each."""
+    import graphalgo_gb300 as ga
+    from graphalgo_gb300 import build as gbuild
+    gbuild.build()
+    ctx = ga.Context(dist.local_rank)
+    t_pool = time.perf_counter()
+    pool = serve_pool(args, ctx, ga)
+    t_pool = time.perf_counter() - t_pool
+    reqs = serve_requests(args, pool)
+    # warm-up: a few requests of each kind on the smallest graphs
+    warm = [r for r in reqs if pool[r[1]][1] <= 20000][: max(3, 3 * args.warmup)]
+    serve_run(ga, pool, warm, args.workers, True)
+    sampler = ClockSampler(dist.local_rank)
+    sampler.start()
+    plain = serve_run(ga, pool, reqs, 1, False)
+    l0 = ga.kernel_launches()
+    srv = serve_run(ga, pool, reqs, args.workers, True)
+    launches = ga.kernel_launches() - l0
+    clocks = sampler.stop()
+    same = serve_same(serve_digest(ga, reqs, plain["results"]), serve_digest(ga, reqs, srv["results"]))
+    sweep = []
+    rng = np.random.default_rng(args.seed + 11)
+    for f in [float(x) for x in args.rates.split(",") if x]:
+        lam = f * plain["req_s"]
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, len(reqs)))
+        row = {"rate_req_s": lam, "rate_x_plain": f}
+        for name, w, c in (("server", args.workers, True), ("plain", 1, False)):
+            r = serve_run(ga, pool, reqs, w, c, arrivals)
+            row[name] = {k: r[k] for k in ("req_s", "p50_ms", "p99_ms")}
+        sweep.append(row)
+    value = srv["req_s"]
+    h2d = sum(4 * len(src) for (t, _, _, src) in reqs if src is not None)
+    line = {
+        "metric": METRIC, "value": value, "unit": "req/s", "n_gpus": dist.world, "steps": args.requests,
+        "warmup": len(warm), "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic",
+        "config": {"workload": f"serving {args.requests} requests (TC / k-truss k~U{{3..8}} / BC 32 sources) "
+                               f"on {len(pool)} resident graphs",
+                   "graphs": {name: {"vertices": m, "stored_entries": len(col)} for name, m, _, col in pool},
+                   "workers": args.workers, "batching": "coalesced TC / k-truss on graphs <= 2^20 entries",
+                   "hbm_budget": srv["stats"]["budget"], "l2": "inputs resident; not flushed between requests",
+                   "pool_build_s": t_pool, "parallelism": "replicas only"},
+        "roofline": None, "cpu_baseline": None,
+        "e2e": {"value": value, "unit": "req/s", "h2d_bytes_per_step": h2d / len(reqs),
+                "d2h_bytes_per_step": srv["d2h_bytes"] / len(reqs),
+                "note": "requests submitted from the host, results (counts, BC scores, k-truss edge sets) "
+                        "returned to host memory; graphs resident"},
+        "gpu_launches": int(launches), "clocks": clocks,
+        "saturated": {"server": {k: srv[k] for k in ("req_s", "p50_ms", "p99_ms", "makespan_s")},
+                      "plain": {k: plain[k] for k in ("req_s", "p50_ms", "p99_ms", "makespan_s")},
+                      "speedup": value / plain["req_s"], "results_equal": same,
+                      "server_stats": srv["stats"]},
+        "poisson": sweep,
+    }
+    ctx.close()
+    return line
+
+
 # --------------------------------------------------------- reference arm
 def run_reference(args, dist: Dist):
     if dist.rank != 0:
@@ -655,6 +813,8 @@ def main():
             line = run_reference(args, dist)
         elif args.workload == "batch":
             line = run_batch(args, dist)
+        elif args.workload == "serve":
+            line = run_serve(args, dist)
         else:
             line = run_gpu(args, dist)
         if dist.rank == 0 and line is not None:

@@ -30,7 +30,7 @@ INT32, INT64, FP32, FP64, UINT8 = 0, 1, 2, 3, 4
 MSA, MCA, HEAP, NAIVE, DOT = 0, 1, 2, 3, 4
 ALGOS = {"msa": MSA, "mca": MCA, "heap": HEAP, "naive": NAIVE, "dot": DOT}
 # options
-OPT_DEVICE_LOOPS, OPT_PROFILE, OPT_FAIL_ALLOC_AFTER = 1, 2, 3
+OPT_DEVICE_LOOPS, OPT_PROFILE, OPT_FAIL_ALLOC_AFTER, OPT_KNN_TILED = 1, 2, 3, 4
 # status codes
 OK, ERR_INVALID_ARG, ERR_INVALID_CSR, ERR_SHAPE, ERR_DTYPE, ERR_CUDA, ERR_OOM, ERR_NO_DEVICE, \
     ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_ADMISSION = range(11)
@@ -157,6 +157,12 @@ class Context:
         f, t = _i64(), _i64()
         _check(lib().ga_mem_info(self.handle, ctypes.byref(f), ctypes.byref(t)), self)
         return int(f.value), int(t.value)
+
+    def mem_stats(self, reset_peak: bool = False) -> Tuple[int, int]:
+        """(bytes held now, peak since the last reset) by this context's allocations."""
+        u, p = _i64(), _i64()
+        _check(lib().ga_ctx_mem_stats(self.handle, ctypes.byref(u), ctypes.byref(p), _int(int(reset_peak))), self)
+        return int(u.value), int(p.value)
 
     def work_counters(self, reset: bool = False) -> dict:
         """Masked-SpGEMM work since the last reset: Gustavson products P of the
@@ -484,3 +490,111 @@ def split_blocks(rst: np.ndarray, col: np.ndarray, voff) -> list:
         r = rst[b:e + 1].astype(np.int64)
         out.append((e - b, (r - r[0]).astype(np.int32), (col[r[0]:r[-1]] - b).astype(np.int32)))
     return out
+
+
+# ------------------------------------------------------------- request server
+REQ_TC, REQ_KTRUSS, REQ_BC = 0, 1, 2
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("workers", _int), ("coalesce", _int), ("tc_algo", _int), ("ktruss_algo", _int),
+                ("hbm_budget", _i64), ("coalesce_nnz", _i64), ("coalesce_max_nnz", _i64),
+                ("coalesce_max_requests", _i64)]
+
+
+class ServerResult(ctypes.Structure):
+    _fields_ = [("status", _int), ("type", _int), ("graph", _int), ("tc_total", _i64), ("iters", _int),
+                ("truss_nnz", _i64), ("truss_rst", ctypes.POINTER(ctypes.c_int32)),
+                ("truss_col", ctypes.POINTER(ctypes.c_int32)), ("bc", ctypes.POINTER(ctypes.c_double)),
+                ("t_submit", ctypes.c_double), ("t_start", ctypes.c_double), ("t_end", ctypes.c_double),
+                ("batch_size", _int), ("worker", _int), ("bytes_bound", _i64), ("error", ctypes.c_char_p)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, _i64) for n in ("submitted", "completed", "failed", "rejected", "calls", "batched_calls",
+                                    "batched_requests", "max_group", "max_in_flight", "budget", "reserved",
+                                    "peak_reserved", "queued")]
+
+
+def request_bytes_bound(req_type: int, m: int, nnz: int, param: int = 0) -> int:
+    b = _i64()
+    _check(lib().ga_request_bytes_bound(_int(req_type), _i64(m), _i64(nnz), _i64(param), ctypes.byref(b)))
+    return int(b.value)
+
+
+class Server:
+    """Request server over device-resident graphs (ga_server_* in the C ABI)."""
+
+    def __init__(self, device: int = 0, workers: int = 4, coalesce: bool = True, tc_algo="msa",
+                 ktruss_algo="msa", hbm_budget: int = 0, coalesce_nnz: int = 0, coalesce_max_nnz: int = 0,
+                 coalesce_max_requests: int = 0):
+        cfg = ServerConfig(int(workers), int(bool(coalesce)), _algo(tc_algo), _algo(ktruss_algo), int(hbm_budget),
+                           int(coalesce_nnz), int(coalesce_max_nnz), int(coalesce_max_requests))
+        self.handle = _p()
+        self.sizes = []
+        _check(lib().ga_server_create(_int(device), ctypes.byref(cfg), ctypes.byref(self.handle)))
+
+    def add_graph(self, m: int, rst, col) -> int:
+        rst = np.ascontiguousarray(rst, dtype=np.int32)
+        col = np.ascontiguousarray(col, dtype=np.int32)
+        gid = _int()
+        rc = lib().ga_server_add_graph(self.handle, _i64(m), _ptr(rst), _ptr(col), ctypes.byref(gid))
+        if rc != OK:
+            raise GaError(rc, lib().ga_status_string(rc).decode())
+        self.sizes.append(m)
+        return int(gid.value)
+
+    def submit(self, req_type: int, graph: int, k: int = 0, sources=None, want_edges: bool = False) -> int:
+        src = None if sources is None else np.ascontiguousarray(sources, dtype=np.int32)
+        rid = _i64()
+        _check(lib().ga_server_submit(self.handle, _int(req_type), _int(graph), _int(k), _ptr(src),
+                                      _int(0 if src is None else len(src)), _int(int(want_edges)),
+                                      ctypes.byref(rid)))
+        return int(rid.value)
+
+    def wait(self, rid: int, timeout: float = 0.0, release: bool = True) -> dict:
+        r = ServerResult()
+        _check(lib().ga_server_wait(self.handle, _i64(rid), ctypes.c_double(timeout), ctypes.byref(r)))
+        out = {"status": r.status, "type": r.type, "graph": r.graph, "t_submit": r.t_submit, "t_start": r.t_start,
+               "t_end": r.t_end, "batch_size": r.batch_size, "worker": r.worker, "bytes_bound": r.bytes_bound,
+               "error": r.error.decode() if r.error else None}
+        if r.status == OK:
+            if r.type == REQ_TC:
+                out["tc"] = int(r.tc_total)
+            elif r.type == REQ_KTRUSS:
+                out["iters"] = int(r.iters)
+                out["nnz"] = int(r.truss_nnz)
+                if r.truss_rst:
+                    m = self.sizes[r.graph]
+                    out["rst"] = np.ctypeslib.as_array(r.truss_rst, (m + 1,)).copy()
+                    out["col"] = np.ctypeslib.as_array(r.truss_col, (max(1, r.truss_nnz),))[:r.truss_nnz].copy()
+            else:
+                out["bc"] = np.ctypeslib.as_array(r.bc, (self.sizes[r.graph],)).copy()
+        if release:
+            lib().ga_server_release(self.handle, _i64(rid))
+        return out
+
+    def drain(self, timeout: float = 0.0):
+        _check(lib().ga_server_drain(self.handle, ctypes.c_double(timeout)))
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        _check(lib().ga_server_get_stats(self.handle, ctypes.byref(s)))
+        return {n: int(getattr(s, n)) for n, _ in ServerStats._fields_}
+
+    def close(self):
+        if self.handle:
+            lib().ga_server_destroy(self.handle)
+            self.handle = _p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -38,7 +38,7 @@ static ga_csr block_diag(ga_ctx ctx, int64_t count, const ga_csr* parts, int64_t
     std::vector<PartDesc> desc((size_t)count);
     int64_t rows = 0, cols = 0, ents = 0;
     ga_dtype dt = count ? parts[0]->dtype : GA_INT32;
-    bool unit = true;
+    bool unit = true, sym = true;
     for (int64_t g = 0; g < count; ++g) {
         const ga_csr P = parts[g];
         GA_REQUIRE(P != nullptr, GA_ERR_INVALID_ARG, "block_diag: NULL part");
@@ -49,6 +49,7 @@ static ga_csr block_diag(ga_ctx ctx, int64_t count, const ga_csr* parts, int64_t
                                    (int32_t)P->m, (int32_t)P->nnz};
         if (voff) voff[g] = rows;
         unit = unit && P->unit == 1;
+        sym = sym && P->sym == 1;
         rows += P->m;
         cols += P->n;
         ents += P->nnz;
@@ -75,6 +76,7 @@ static ga_csr block_diag(ga_ctx ctx, int64_t count, const ga_csr* parts, int64_t
         throw;
     }
     U->unit = unit ? 1 : -1;
+    U->sym = sym ? 1 : -1;  // known-symmetric blocks make a symmetric union
     return U;
 }
 
@@ -169,6 +171,92 @@ __global__ void __launch_bounds__(kKnnThreads) k_knn_select(const int32_t* __res
     for (int r = kk + threadIdx.x; r < k; r += blockDim.x) nb[p * k + r] = -1;
 }
 
+// Graphs above kKnnMaxN points: one thread per query point, candidates
+// staged in shared memory in tiles of kKnnTile points (coordinates padded
+// to a multiple of 4 with zeros, which leaves every distance unchanged), and
+// a sorted top-k list of (distance, index) keys per thread. The keys and the
+// per-coordinate fmaf order are those of k_knn_select, so both kernels pick
+// the same neighbours.
+constexpr int kKnnTile = 256;
+constexpr int kKnnMaxK = 64;
+
+struct KnnTile {
+    int32_t graph, first;  // graph and its first query point of this tile
+};
+
+__global__ void __launch_bounds__(kKnnThreads) k_knn_tiled(const KnnTile* __restrict__ tiles,
+                                                           const int32_t* __restrict__ voff,
+                                                           const int32_t* __restrict__ dim,
+                                                           const int64_t* __restrict__ poff,
+                                                           const float* __restrict__ X, int k,
+                                                           int32_t* __restrict__ nb) {
+    __shared__ __align__(16) float cand[kKnnTile * kKnnMaxDim];
+    const KnnTile tl = tiles[blockIdx.x];
+    const int32_t base = voff[tl.graph];
+    const int n = voff[tl.graph + 1] - base, d = dim[tl.graph];
+    const int dp = (d + 3) & ~3;
+    const float* Xg = X + poff[tl.graph];
+    const int local = tl.first + (int)threadIdx.x;
+    const bool active = local < n;
+    float q[kKnnMaxDim];
+#pragma unroll
+    for (int c = 0; c < kKnnMaxDim; ++c) q[c] = (active && c < d) ? Xg[(int64_t)local * d + c] : 0.f;
+    const int kk = min(k, n - 1);
+    float bd[kKnnMaxK];
+    int bi[kKnnMaxK];
+    int cnt = 0;
+    float worst = INFINITY;
+    int worst_i = INT32_MAX;
+    for (int j0 = 0; j0 < n; j0 += kKnnTile) {
+        const int tn = min(kKnnTile, n - j0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < tn * dp; t += blockDim.x) {
+            const int j = t / dp, c = t - j * dp;
+            cand[t] = c < d ? Xg[(int64_t)(j0 + j) * d + c] : 0.f;
+        }
+        __syncthreads();
+        if (!active || kk <= 0) continue;
+        for (int j = 0; j < tn; ++j) {
+            const float4* xj = reinterpret_cast<const float4*>(cand + j * dp);
+            float s = 0.f;
+#pragma unroll
+            for (int c4 = 0; c4 < kKnnMaxDim / 4; ++c4) {
+                if (4 * c4 < dp) {
+                    const float4 x = xj[c4];
+                    float df = q[4 * c4] - x.x;
+                    s = fmaf(df, df, s);
+                    df = q[4 * c4 + 1] - x.y;
+                    s = fmaf(df, df, s);
+                    df = q[4 * c4 + 2] - x.z;
+                    s = fmaf(df, df, s);
+                    df = q[4 * c4 + 3] - x.w;
+                    s = fmaf(df, df, s);
+                }
+            }
+            const int idx = j0 + j;
+            if (idx == local) continue;
+            if (cnt == kk && (s > worst || (s == worst && idx > worst_i))) continue;
+            // insert (s, idx) into the sorted list
+            int pos = cnt < kk ? cnt : kk - 1;
+            while (pos > 0 && (bd[pos - 1] > s || (bd[pos - 1] == s && bi[pos - 1] > idx))) {
+                bd[pos] = bd[pos - 1];
+                bi[pos] = bi[pos - 1];
+                --pos;
+            }
+            bd[pos] = s;
+            bi[pos] = idx;
+            if (cnt < kk) ++cnt;
+            if (cnt == kk) {
+                worst = bd[kk - 1];
+                worst_i = bi[kk - 1];
+            }
+        }
+    }
+    if (!active) return;
+    const int64_t p = (int64_t)base + local;
+    for (int r = 0; r < k; ++r) nb[p * k + r] = r < cnt ? base + bi[r] : -1;
+}
+
 // Symmetrise the directed k-NN lists: row counts, fill both directions,
 // sort rows, drop duplicates.
 __global__ void k_knn_count(const int32_t* __restrict__ nb, int64_t npoints, int k, int32_t* __restrict__ cnt) {
@@ -211,12 +299,14 @@ __global__ void k_unique_fill(const int32_t* __restrict__ rst, const int32_t* __
 
 static ga_csr gen_knn_batch(ga_ctx ctx, int64_t count, const int32_t* n, const int32_t* dim, int k, uint64_t seed,
                             int64_t* voff_out) {
-    GA_REQUIRE(count >= 1 && k >= 1, GA_ERR_INVALID_ARG, "knn batch: need count >= 1 and k >= 1");
+    GA_REQUIRE(count >= 1 && k >= 1 && k <= kKnnMaxK, GA_ERR_INVALID_ARG, "knn batch: need count >= 1 and 1 <= k <= 64");
+    bool large = false;
     std::vector<int32_t> voff((size_t)count + 1);
     std::vector<int64_t> poff((size_t)count + 1);
     int64_t np = 0, nc = 0;
     for (int64_t g = 0; g < count; ++g) {
-        GA_REQUIRE(n[g] >= 1 && n[g] <= kKnnMaxN, GA_ERR_INVALID_ARG, "knn batch: graph sizes must be 1..4096");
+        GA_REQUIRE(n[g] >= 1 && n[g] <= (1 << 24), GA_ERR_INVALID_ARG, "knn batch: graph sizes must be 1..2^24");
+        large = large || n[g] > kKnnMaxN;
         GA_REQUIRE(dim[g] >= 1 && dim[g] <= kKnnMaxDim, GA_ERR_INVALID_ARG, "knn batch: dimensions must be 1..32");
         voff[(size_t)g] = (int32_t)np;
         poff[(size_t)g] = nc;
@@ -243,8 +333,22 @@ static ga_csr gen_knn_batch(ga_ctx ctx, int64_t count, const int32_t* n, const i
     }
     {
         ProfScope ps(ctx, "knn_select");
-        k_knn_select<<<(unsigned)np, kKnnThreads, 0, ctx->stream>>>(d_voff.p, d_dim.p, d_poff.p, count, X.p, k, nb.p);
-        post_launch("knn_select");
+        if (!large && !ctx->knn_tiled) {
+            k_knn_select<<<(unsigned)np, kKnnThreads, 0, ctx->stream>>>(d_voff.p, d_dim.p, d_poff.p, count, X.p, k,
+                                                                      nb.p);
+            post_launch("knn_select");
+        } else {
+            std::vector<KnnTile> tl;
+            for (int64_t g = 0; g < count; ++g)
+                for (int32_t f = 0; f < n[g]; f += kKnnThreads) tl.push_back(KnnTile{(int32_t)g, f});
+            DBuf<KnnTile> d_tl(ctx, tl.size());
+            GA_CUDA(cudaMemcpyAsync(d_tl.p, tl.data(), sizeof(KnnTile) * tl.size(), cudaMemcpyHostToDevice,
+                                    ctx->stream));
+            k_knn_tiled<<<(unsigned)tl.size(), kKnnThreads, 0, ctx->stream>>>(d_tl.p, d_voff.p, d_dim.p, d_poff.p,
+                                                                            X.p, k, nb.p);
+            post_launch("knn_tiled");
+            GA_CUDA(cudaStreamSynchronize(ctx->stream));  // the host tile table goes out of scope
+        }
     }
     DBuf<int32_t> cnt(ctx, (size_t)np + 1), rst(ctx, (size_t)np + 1), cursor(ctx, (size_t)np + 1);
     GA_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * (np + 1), ctx->stream));

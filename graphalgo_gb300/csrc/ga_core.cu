@@ -66,11 +66,20 @@ void* dalloc(ga_ctx ctx, size_t bytes) {
         snprintf(buf, sizeof(buf), "device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
         fail(e == cudaErrorMemoryAllocation ? GA_ERR_OOM : GA_ERR_CUDA, buf);
     }
+    ctx->live[p] = bytes;
+    ctx->bytes_in_use += (int64_t)bytes;
+    if (ctx->bytes_in_use > ctx->bytes_peak) ctx->bytes_peak = ctx->bytes_in_use;
     return p;
 }
 
 void dfree(ga_ctx ctx, void* p) {
-    if (p) cudaFreeAsync(p, ctx->stream);
+    if (!p) return;
+    auto it = ctx->live.find(p);
+    if (it != ctx->live.end()) {  // memory of another context is freed without accounting
+        ctx->bytes_in_use -= (int64_t)it->second;
+        ctx->live.erase(it);
+    }
+    cudaFreeAsync(p, ctx->stream);
 }
 
 ga_csr csr_alloc(ga_ctx ctx, int64_t m, int64_t n, int64_t nnz, ga_dtype dt) {
@@ -371,6 +380,7 @@ int ga_ctx_set_option(ga_ctx ctx, int option, int64_t value) {
     case GA_OPT_DEVICE_LOOPS: ctx->device_loops = value != 0; return GA_OK;
     case GA_OPT_PROFILE: ctx->profile = value != 0; return GA_OK;
     case GA_OPT_FAIL_ALLOC_AFTER: ctx->fail_alloc_after = value; return GA_OK;
+    case GA_OPT_KNN_TILED: ctx->knn_tiled = value != 0; return GA_OK;
     }
     ctx->last_error = "unknown option";
     return GA_ERR_INVALID_ARG;
@@ -426,6 +436,14 @@ int ga_mem_info(ga_ctx ctx, int64_t* free_bytes, int64_t* total_bytes) {
         if (free_bytes) *free_bytes = (int64_t)f;
         if (total_bytes) *total_bytes = (int64_t)t;
     });
+}
+
+int ga_ctx_mem_stats(ga_ctx ctx, int64_t* in_use, int64_t* peak, int reset_peak) {
+    if (!ctx) return GA_ERR_INVALID_ARG;
+    if (in_use) *in_use = ctx->bytes_in_use;
+    if (peak) *peak = ctx->bytes_peak;
+    if (reset_peak) ctx->bytes_peak = ctx->bytes_in_use;
+    return GA_OK;
 }
 
 // ---------------------------------------------------------------- CSR handle

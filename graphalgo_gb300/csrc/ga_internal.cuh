@@ -9,6 +9,7 @@
 #include <vector>
 #include <map>
 #include <stdexcept>
+#include <unordered_map>
 
 #include "../../include/graphalgo_gb300.h"
 
@@ -58,6 +59,7 @@ struct ga_ctx_s {
     bool device_loops = true;
     bool profile = false;
     int64_t fail_alloc_after = -1;  // fault injection
+    bool knn_tiled = false;         // k-NN generator: tiled kernel for every graph
     // profiling
     std::vector<ga::PendingTiming> pending;
     std::vector<cudaEvent_t> event_pool;
@@ -71,6 +73,10 @@ struct ga_ctx_s {
     // scratch written to evict the L2 between benchmark steps
     void* l2_flush = nullptr;
     size_t l2_flush_bytes = 0;
+    // device bytes this context holds (requested sizes) and their high-water mark
+    std::unordered_map<void*, size_t> live;
+    int64_t bytes_in_use = 0;
+    int64_t bytes_peak = 0;
 };
 
 struct ga_csr_s {

@@ -92,8 +92,10 @@ GA_API int ga_version(int* major, int* minor);
  * GA_OPT_PROFILE: when 1, each kernel launch is bracketed by CUDA events and
  * ga_ctx_kernel_stats reports per-kernel totals. GA_OPT_FAIL_ALLOC_AFTER:
  * fault injection for tests — the N-th device allocation from now on fails
- * with GA_ERR_OOM (-1 disables). */
-enum { GA_OPT_DEVICE_LOOPS = 1, GA_OPT_PROFILE = 2, GA_OPT_FAIL_ALLOC_AFTER = 3 };
+ * with GA_ERR_OOM (-1 disables). GA_OPT_KNN_TILED: when 1, ga_gen_knn_batch
+ * uses its tiled kernel (the one for graphs above 4,096 points) for every
+ * graph; both kernels give the same graphs. */
+enum { GA_OPT_DEVICE_LOOPS = 1, GA_OPT_PROFILE = 2, GA_OPT_FAIL_ALLOC_AFTER = 3, GA_OPT_KNN_TILED = 4 };
 GA_API int ga_ctx_set_option(ga_ctx ctx, int option, int64_t value);
 
 /* Per-kernel timing collected while GA_OPT_PROFILE is on. Writes up to `cap`
@@ -114,6 +116,9 @@ GA_API int ga_timer_stop(ga_ctx ctx, double* ms);
 
 /* Free / total device memory as the CUDA runtime sees it. */
 GA_API int ga_mem_info(ga_ctx ctx, int64_t* free_bytes, int64_t* total_bytes);
+/* Device bytes the context's allocations hold now and at most since the last
+ * reset (requested sizes; reset_peak != 0 sets the peak to the current use). */
+GA_API int ga_ctx_mem_stats(ga_ctx ctx, int64_t* in_use, int64_t* peak, int reset_peak);
 
 /* Work counters accumulated on the device by every masked-SpGEMM launch of
  * this context (MSA / MCA / HEAP): Gustavson products P = sum over A entries
@@ -293,6 +298,73 @@ GA_API int ga_batch_tc(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, const 
  * ga_ktruss reports it. *C is the union of the per-graph results. */
 GA_API int ga_batch_ktruss(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, const int64_t* voff, int k,
                            ga_csr* C, int* iters);
+
+/* ------------------------------------------------------- request server */
+/* Serves triangle-count, k-truss and BC requests on device-resident graphs
+ * as they arrive. Worker threads each own a context (stream), so calls of
+ * different workers overlap on the device. Every request has an upper bound
+ * on the device bytes its call allocates (ga_request_bytes_bound); a worker
+ * starts the oldest queued request only while the bounds of the calls in
+ * flight plus its own fit in the HBM budget, and a request whose bound alone
+ * exceeds the budget completes with GA_ERR_ADMISSION. With coalesce on, a
+ * worker that takes a TC or k-truss request on a small graph also takes the
+ * queued requests of the same kind (same k) on small graphs and serves them
+ * with one batched call (ga_batch_tc / ga_batch_ktruss); each request gets
+ * the result it gets alone. workers = 1 with coalesce = 0 is the plain
+ * sequential form. No counterpart in the reference (one graph per run). */
+typedef struct ga_server_s* ga_server;
+enum { GA_REQ_TC = 0, GA_REQ_KTRUSS = 1, GA_REQ_BC = 2 };
+typedef struct {
+    int workers;                   /* worker threads (1..64); 0: 4 */
+    int coalesce;                  /* 1: batch queued small TC / k-truss requests */
+    int tc_algo;                   /* ga_algo of TC (GA_MSA, GA_MCA, GA_HEAP, GA_NAIVE, GA_DOT) */
+    int ktruss_algo;               /* ga_algo of k-truss (GA_MSA, GA_MCA, GA_HEAP) */
+    int64_t hbm_budget;            /* bytes the calls in flight may hold; 0: 80% of free memory at creation */
+    int64_t coalesce_nnz;          /* graphs with at most this many stored entries are batched; 0: 2^20 */
+    int64_t coalesce_max_nnz;      /* stored entries of one batched union at most; 0: 2^26 */
+    int64_t coalesce_max_requests; /* requests served by one batched call at most; 0: 4096 */
+} ga_server_config;
+typedef struct {
+    int status;                /* GA_OK, the call's error code, or GA_ERR_ADMISSION */
+    int type, graph;
+    int64_t tc_total;          /* TC: triangles */
+    int iters;                 /* k-truss: iteration count as ga_ktruss reports it */
+    int64_t truss_nnz;         /* k-truss: stored entries of the result */
+    const int32_t* truss_rst;  /* k-truss result (m+1 row starts) when requested, else NULL */
+    const int32_t* truss_col;  /* its columns */
+    const double* bc;          /* BC: scores (length m) */
+    double t_submit, t_start, t_end; /* seconds on the server's clock */
+    int batch_size;            /* requests served by the same call */
+    int worker;
+    int64_t bytes_bound;
+    const char* error;         /* message when status != GA_OK */
+} ga_server_result;
+typedef struct {
+    int64_t submitted, completed, failed, rejected;
+    int64_t calls, batched_calls, batched_requests, max_group, max_in_flight;
+    int64_t budget, reserved, peak_reserved, queued;
+} ga_server_stats;
+/* Upper bound on the device bytes of one request (type GA_REQ_*, graph of m
+ * vertices and nnz stored entries; param = number of BC sources). */
+GA_API int ga_request_bytes_bound(int type, int64_t m, int64_t nnz, int64_t param, int64_t* bytes);
+/* cfg may be NULL (defaults). */
+GA_API int ga_server_create(int device, const ga_server_config* cfg, ga_server* srv);
+/* Waits for every queued request, then stops the workers. */
+GA_API int ga_server_destroy(ga_server srv);
+/* Uploads a symmetric adjacency matrix (host CSR, values 1) once; it stays
+ * resident and its bytes come out of the budget. */
+GA_API int ga_server_add_graph(ga_server srv, int64_t m, const int32_t* rst, const int32_t* col, int* graph_id);
+/* Queues a request: GA_REQ_TC, GA_REQ_KTRUSS (k), or GA_REQ_BC (sources,
+ * copied). want_edges: keep the k-truss edge set for ga_server_wait. */
+GA_API int ga_server_submit(ga_server srv, int type, int graph, int k, const int32_t* sources, int nsrc,
+                            int want_edges, int64_t* req_id);
+/* Blocks until the request is done (timeout_s <= 0: no limit; else
+ * GA_ERR_TIMEOUT). The result's arrays stay valid until ga_server_release. */
+GA_API int ga_server_wait(ga_server srv, int64_t req_id, double timeout_s, ga_server_result* res);
+GA_API int ga_server_release(ga_server srv, int64_t req_id);
+/* Blocks until the queue is empty and no call is in flight. */
+GA_API int ga_server_drain(ga_server srv, double timeout_s);
+GA_API int ga_server_get_stats(ga_server srv, ga_server_stats* stats);
 
 /* ------------------------------------------------------ synthetic graphs */
 /* Seeded generators producing sorted, duplicate-free, loop-free symmetric

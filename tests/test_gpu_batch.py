@@ -150,3 +150,26 @@ def test_batch_rejects_bad_offsets(ctx):
     bad[2], bad[3] = bad[3], bad[2]
     with pytest.raises(ga.GaError):
         ga.batch_ktruss("msa", U, bad, 4)
+
+
+def test_knn_tiled_matches_cta(ctx):
+    """The tiled generator kernel (graphs above 4,096 points) picks the same
+    neighbours as the CTA-per-point kernel."""
+    n, dim = _uneven_sizes(6, 2, 900, seed=8)
+    U1, v1 = ga.gen_knn_batch(ctx, n, dim, k=30, seed=3)
+    ctx.set_option(ga.OPT_KNN_TILED, 1)
+    try:
+        U2, v2 = ga.gen_knn_batch(ctx, n, dim, k=30, seed=3)
+    finally:
+        ctx.set_option(ga.OPT_KNN_TILED, 0)
+    assert np.array_equal(v1, v2)
+    assert all(np.array_equal(a, b) for a, b in zip(U1.download(), U2.download()))
+
+
+def test_knn_large_graph(ctx):
+    n = np.array([6000, 100], np.int32)
+    U, voff = ga.gen_knn_batch(ctx, n, np.array([16, 5], np.int32), k=30, seed=11)
+    rst, col, _ = U.download()
+    for g, (m, r, c) in enumerate(ga.split_blocks(rst, col, voff)):
+        assert m == n[g]
+        _check_knn_structure(m, r, c, 30)
