@@ -53,13 +53,14 @@ def parse_args():
     ap.add_argument("--scale", type=int, default=18)
     ap.add_argument("--edge-factor", type=int, default=16)
     ap.add_argument("--seed", type=int, default=42)
-    ap.add_argument("--algo", default="msa", choices=["msa", "mca", "heap"])
+    ap.add_argument("--algo", default="msa", choices=["msa", "mca", "heap", "dot"])
     ap.add_argument("--kmin", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-reps", type=int, default=2)
-    ap.add_argument("--case", choices=["support", "tc", "bc"], default=None,
-                    help="profiling case instead of the benchmark: support product, TC or BC, --reps times")
+    ap.add_argument("--case", choices=["support", "tc", "bc", "ktruss", "batch"], default=None,
+                    help="profiling case instead of the benchmark, --reps times: support product, TC, BC, "
+                         "4-truss from A, or batched TC + 4-truss of --graphs k-NN graphs")
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--sources", type=int, default=64)
     ap.add_argument("--workload", choices=["ktruss-sweep", "batch", "serve"], default="ktruss-sweep",
@@ -197,15 +198,31 @@ def profile_traffic():
 
 
 def run_case(args):
-    """Small profiling cases on the bench's R-MAT graph, --reps times each
-    (used for ncu captures): `support` = the sweep's first support product
-    C<A> = A*A; `tc` = triangle count with the dot-product kernel; `bc` =
-    batched BC over --sources seeded sources."""
+    """Small profiling cases, --reps times each (used for ncu captures):
+    `support` = the sweep's first support product C<A> = A*A; `tc` =
+    triangle count with the dot-product kernel; `bc` = batched BC over
+    --sources seeded sources; `ktruss` = 4-truss from A (all on the bench's
+    R-MAT graph); `batch` = batched TC + 4-truss of --graphs k-NN graphs."""
     import graphalgo_gb300 as ga
     from graphalgo_gb300 import build as gbuild
     gbuild.build()
     ctx = ga.Context(0)
     ctx.set_option(ga.OPT_DEVICE_LOOPS, 0 if args.host_loops else 1)
+    if args.case == "batch":
+        n, dim = knn_batch_sizes(args.graphs, args.seed)
+        U, voff = ga.gen_knn_batch(ctx, n, dim, k=30, seed=args.seed)
+        for _ in range(args.reps):
+            ctx.work_counters(reset=True)
+            ctx.timer_start()
+            tcs = ga.batch_tc(args.tc_algo, U, voff)
+            C, iters = ga.batch_ktruss(args.algo, U, voff, 4)
+            ms = ctx.timer_stop()
+            print(json.dumps({"batch_ms": ms, "graphs": args.graphs, "triangles": int(tcs.sum()),
+                              "truss_entries": C.nnz, "max_iters": int(iters.max()),
+                              "products": ctx.work_counters()["products"]}), flush=True)
+            C.free()
+        ctx.close()
+        return
     m, rst, col = ga.gen_rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, args.seed)
     A = ga.Csr.upload(ctx, m, m, rst, col, np.ones(len(col), np.int32))
     rng = np.random.default_rng(args.seed)
@@ -224,6 +241,11 @@ def run_case(args):
             total, _ = ga.tc("dot", A, per_row=False)
             ms = ctx.timer_stop()
             rec = {"tc_ms": ms, "triangles": total}
+        elif args.case == "ktruss":
+            C, it = ga.ktruss(args.algo, A, 4)
+            ms = ctx.timer_stop()
+            rec = {"ktruss_ms": ms, "iters": it, "nnz": C.nnz, "products": ctx.work_counters()["products"]}
+            C.free()
         else:
             ga.bc(A, src)
             ms = ctx.timer_stop()
@@ -305,7 +327,7 @@ def profile_step(ga, ctx, run, algo, counters, loops):
     ctr = counters()
     ctx.set_option(ga.OPT_PROFILE, 0)
     ctx.set_option(ga.OPT_DEVICE_LOOPS, loops)
-    kname = {"msa": "mxm_msa", "mca": "mxm_mca", "heap": "mxm_heap_merge"}[algo]
+    kname = {"msa": "mxm_msa", "mca": "mxm_mca", "heap": "mxm_heap_merge", "dot": "mxm_dot"}[algo]
     k_launches, k_ms = stats.get(kname, (0, 0.0))
     bytes_model = 8 * ctr["rows"] + 16 * ctr["a_entries"] + 8 * ctr["executed"] + 8 * ctr["mask_entries"]
     peak, peak_kind = measured_peak_hbm()

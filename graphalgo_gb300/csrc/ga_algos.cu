@@ -405,8 +405,8 @@ __global__ void k_kt_copyback_aux(const KtState* st, const int32_t* __restrict__
 ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, const KtBatch* batch) {
     GA_REQUIRE(A->m == A->n, GA_ERR_SHAPE, "k-truss needs a square matrix");
     GA_REQUIRE(A->dtype == GA_INT32, GA_ERR_DTYPE, "k-truss needs int32 values (spMtx<int>)");
-    GA_REQUIRE(algo == GA_MSA || algo == GA_MCA || algo == GA_HEAP || algo == GA_NAIVE, GA_ERR_INVALID_ARG,
-               "k-truss: unknown algorithm");
+    GA_REQUIRE(algo == GA_MSA || algo == GA_MCA || algo == GA_HEAP || algo == GA_NAIVE || algo == GA_DOT,
+               GA_ERR_INVALID_ARG, "k-truss: unknown algorithm");
     const int64_t m = A->m;
     // C = A (a copy; its pattern shrinks in place)
     ga_csr C = copy_csr(ctx, A, GA_INT32);
@@ -430,6 +430,7 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
         // only the upper triangle (columns >= i) is multiplied, the lower
         // triangle is mirrored. Same values, about half the products.
         const bool upper = algo != GA_NAIVE && csr_is_symmetric(ctx, A);
+        GA_REQUIRE(upper || algo != GA_DOT, GA_ERR_UNSUPPORTED, "k-truss with GA_DOT needs a symmetric matrix");
         const size_t aux = upper ? (size_t)cap : 1;
         DBuf<int32_t> ust(ctx, upper ? (size_t)m + 1 : 1);
         DBuf<int32_t> row_of(ctx, aux), mir(ctx, aux), pos_new(ctx, aux), trow(ctx, aux), mir_new(ctx, aux);
@@ -454,7 +455,8 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
                 post_launch("kt_upper_start");
                 Cu = *C;
                 Cu.rst = ust.p;
-                mxm_masked_launch(ctx, algo, C, C, &Cu, sup.p, mxm_scr.p, cap, unit, C->rst + 1);
+                if (algo == GA_DOT) mxm_dot_launch(ctx, C, C, C, &Cu, sup.p, unit, C->rst + 1);
+                else mxm_masked_launch(ctx, algo, C, C, &Cu, sup.p, mxm_scr.p, cap, unit, C->rst + 1);
                 k_gather_lower<<<grid_ent, 256, 0, ctx->stream>>>(st.p, C->col, row_of.p, mir.p, sup.p);
                 post_launch("kt_gather_lower");
             } else {

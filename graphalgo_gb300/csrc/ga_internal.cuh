@@ -197,6 +197,12 @@ ga_csr mxm_cmask(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M);
 size_t mxm_scratch_bytes(int64_t m, int64_t n, int64_t mask_nnz);
 void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals, void* scratch,
                        int64_t cap_nnz, bool unit_b, const int32_t* mask_row_end = nullptr);
+// Inner-product masked product (GA_DOT): Bt holds B^T (B itself when B is
+// symmetric); unit: A's and B's values are all ones. Allocates nothing.
+// With mask_row_end, M->rst holds row starts of the mask and
+// mask_row_end - 1 the row partition of M's column array.
+void mxm_dot_launch(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr Bt, ga_csr M, void* d_cvals, bool unit,
+                    const int32_t* mask_row_end);
 // True when every stored value of A equals 1 (computed once per handle and
 // cached; synchronises the stream the first time).
 bool csr_unit_values(ga_ctx ctx, ga_csr A);

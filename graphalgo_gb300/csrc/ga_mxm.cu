@@ -643,6 +643,148 @@ static void launch_masked(ga_ctx ctx, ga_csr A_, ga_csr B_, ga_csr M_, T* cv, Mx
     post_launch(name);
 }
 
+// ------------------------------------------------------- inner-product form
+// C<M>(i, j) = sum over k in A_i ∩ (B^T)_j of A(i, k) * B(k, j): one warp per
+// mask entry, the shorter of the two sorted lists walked 32 entries at a
+// time (one per lane), each lane binary-searching the longer one. Warps take
+// kDotChunk consecutive mask entries; a chunk finds its row by a binary
+// search of the row partition `seg`. Row i's mask is [lo[i], hi[i]) within
+// the partition [seg[i], seg[i+1]) (the k-truss support evaluates only the
+// upper part of each row). No shared memory and no atomics: each mask entry
+// is written by one warp.
+constexpr int kDotChunk = 8;
+constexpr int kDotThreads = 256;
+
+template <typename T>
+struct DotArgs {
+    const int32_t* ar; const int32_t* ac; const T* av;
+    const int32_t* tr; const int32_t* tc; const T* tv;  // B^T
+    const int32_t* br;                                  // B row starts (product count)
+    const int32_t* seg; const int32_t* lo; const int32_t* hi;
+    const int32_t* mc;
+    T* cv;
+    int64_t m, total;
+    unsigned long long* ctr;
+};
+
+// Gustavson products of the masked rows (the work every other variant does),
+// mask entries and launch counters, as k_row_bin counts them.
+template <typename T>
+__global__ void k_dot_count(DotArgs<T> p) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    unsigned long long my_flops = 0, my_mask = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(&p.ctr[GA_CTR_LAUNCHES], 1ull);
+        atomicAdd(&p.ctr[GA_CTR_A_ENTRIES], (unsigned long long)(p.ar[p.m] - p.ar[0]));
+        atomicAdd(&p.ctr[GA_CTR_ROWS], (unsigned long long)p.m);
+    }
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < p.m; i += warps) {
+        const int32_t mi = p.hi[i] - p.lo[i];
+        if (mi <= 0) continue;
+        long long f = 0;
+        for (int32_t t = p.ar[i] + lane; t < p.ar[i + 1]; t += 32) {
+            const int32_t k = p.ac[t];
+            f += p.br[k + 1] - p.br[k];
+        }
+        f = warp_sum<long long>(f);
+        if (lane == 0) {
+            my_flops += (unsigned long long)f;
+            my_mask += (unsigned long long)mi;
+        }
+    }
+    if (lane == 0 && my_flops) atomicAdd(&p.ctr[GA_CTR_PRODUCTS], my_flops);
+    if (lane == 0 && my_mask) atomicAdd(&p.ctr[GA_CTR_MASK_ENTRIES], my_mask);
+}
+
+template <typename T, bool UNIT>
+__global__ void __launch_bounds__(kDotThreads) k_mxm_dot(DotArgs<T> p) {
+    using Ac = typename Acc<T>::type;
+    const int lane = threadIdx.x & 31;
+    const unsigned FULL = 0xffffffffu;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    unsigned long long executed = 0;
+    // entries of the partition as the device holds it now (inside a captured
+    // k-truss loop, p.total is only the launch-time upper bound)
+    const int64_t total = p.seg[p.m];
+    for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c * kDotChunk < total; c += warps) {
+        const int32_t q0 = (int32_t)(c * kDotChunk);
+        const int32_t q1 = (int32_t)min((int64_t)q0 + kDotChunk, total);
+        int i = upper_bound_i32(p.seg, (int)p.m + 1, q0) - 1;
+        for (int32_t q = q0; q < q1; ++q) {
+            while (q >= p.seg[i + 1]) ++i;
+            if (q < p.lo[i] || q >= p.hi[i]) continue;
+            const int32_t j = p.mc[q];
+            const int32_t ab = p.ar[i], an = p.ar[i + 1] - ab;
+            const int32_t tb = p.tr[j], tn = p.tr[j + 1] - tb;
+            Ac s = 0;
+            if (an > 0 && tn > 0) {
+                const bool walk_a = an <= tn;  // walk the shorter list, search the longer
+                const int32_t* Wc = walk_a ? p.ac + ab : p.tc + tb;
+                const int32_t* Sc = walk_a ? p.tc + tb : p.ac + ab;
+                const int wn = walk_a ? an : tn, sn = walk_a ? tn : an;
+                if (lane == 0) executed += (unsigned long long)wn;
+                for (int base = 0; base < wn; base += 32) {
+                    const int e = base + lane;
+                    bool hit = false;
+                    int pos = 0;
+                    if (e < wn) {
+                        const int32_t x = __ldg(Wc + e);
+                        pos = lower_bound_i32(Sc, sn, x);
+                        hit = pos < sn && __ldg(Sc + pos) == x;
+                    }
+                    if (UNIT) {
+                        s += (Ac)__popc(__ballot_sync(FULL, hit));
+                    } else if (hit) {
+                        const T va = walk_a ? p.av[ab + e] : p.av[ab + pos];
+                        const T vb = walk_a ? p.tv[tb + pos] : p.tv[tb + e];
+                        s += (Ac)va * (Ac)vb;
+                    }
+                }
+                if (!UNIT) s = warp_sum<Ac>(s);
+            }
+            if (lane == 0) p.cv[q] = (T)s;
+        }
+    }
+    if (lane == 0 && executed) atomicAdd(&p.ctr[GA_CTR_EXECUTED], executed);
+}
+
+template <typename T>
+static void launch_dot_t(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr Bt, ga_csr M, T* cv, bool unit,
+                         const int32_t* mre) {
+    DotArgs<T> p;
+    p.ar = A->rst; p.ac = A->col; p.av = static_cast<const T*>(A->val);
+    p.tr = Bt->rst; p.tc = Bt->col; p.tv = static_cast<const T*>(Bt->val);
+    p.br = B->rst;
+    // with mask row ends, M's columns are those of the CSR whose row starts
+    // are mre - 1 (the partition of the entries); else M's own rows
+    p.seg = mre ? mre - 1 : M->rst;
+    p.lo = M->rst;
+    p.hi = mre ? mre : M->rst + 1;
+    p.mc = M->col;
+    p.cv = cv; p.m = M->m; p.ctr = ctx->d_counters;
+    p.total = M->nnz;
+    {
+        ProfScope ps(ctx, "mxm_dot_count");
+        k_dot_count<T><<<grid_for(p.m * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(p);
+        post_launch("mxm_dot_count");
+    }
+    if (p.total == 0) return;
+    const int grid = grid_for((p.total + kDotChunk - 1) / kDotChunk * 32, kDotThreads, ctx->num_sms * 16);
+    ProfScope ps(ctx, "mxm_dot");
+    if (unit) k_mxm_dot<T, true><<<grid, kDotThreads, 0, ctx->stream>>>(p);
+    else k_mxm_dot<T, false><<<grid, kDotThreads, 0, ctx->stream>>>(p);
+    post_launch("mxm_dot");
+}
+
+// Inner-product launch: Bt holds B^T (B itself when B is symmetric); unit:
+// A's and B's values are all ones. Allocates nothing (capturable). With
+// mask_row_end, M->nnz must be the entry count of the full partition.
+void mxm_dot_launch(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr Bt, ga_csr M, void* d_cvals, bool unit,
+                    const int32_t* mask_row_end) {
+    GA_DISPATCH_DTYPE(A->dtype, T, { launch_dot_t<T>(ctx, A, B, Bt, M, static_cast<T*>(d_cvals), unit, mask_row_end); });
+}
+
 void naive_masked_into(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M, void* d_cvals);
 
 size_t mxm_scratch_bytes(int64_t m, int64_t n, int64_t mask_nnz) {
@@ -688,6 +830,22 @@ void mxm_masked_into(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, voi
     if (M->nnz == 0 || M->m == 0) return;
     if (algo == GA_NAIVE) {
         naive_masked_into(ctx, A, B, M, d_cvals);
+        return;
+    }
+    if (algo == GA_DOT) {
+        const bool unit = csr_unit_values(ctx, A) && csr_unit_values(ctx, B);
+        if (csr_is_symmetric(ctx, B)) {
+            mxm_dot_launch(ctx, A, B, B, M, d_cvals, unit, nullptr);
+        } else {
+            ga_csr Bt = transpose_csr(ctx, B);
+            try {
+                mxm_dot_launch(ctx, A, B, Bt, M, d_cvals, unit, nullptr);
+            } catch (...) {
+                csr_destroy(ctx, Bt);
+                throw;
+            }
+            csr_destroy(ctx, Bt);
+        }
         return;
     }
     const bool unit_b = csr_unit_values(ctx, B);

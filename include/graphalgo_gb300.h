@@ -50,13 +50,15 @@ typedef enum {
 } ga_dtype;
 
 /* masked-SpGEMM variants: the reference's four mxmOp implementations,
- * plus the dot-product (sorted-list intersection) form used by TC */
+ * plus an inner-product (sorted-list intersection) form */
 typedef enum {
     GA_MSA = 0,   /* mxmm_msa,   include/matrix_la.h:700-749 */
     GA_MCA = 1,   /* mxmm_mca,   include/matrix_la.h:586-641 */
     GA_HEAP = 2,  /* mxmm_heap,  include/matrix_la.h:1013-1084 (a warp-cooperative sorted merge here) */
     GA_NAIVE = 3, /* mxmm_naive, include/matrix_la.h:1139-1277 */
-    GA_DOT = 4    /* triangle counting only: warp sorted-list intersections */
+    GA_DOT = 4    /* inner-product form: each mask entry (i,j) is A_i . (B^T)_j by warp
+                     sorted-list intersection (B^T built on the fly unless B is
+                     symmetric); TC's dot kernel; k-truss support (symmetric A) */
 } ga_algo;
 
 /* status codes */
@@ -121,11 +123,12 @@ GA_API int ga_mem_info(ga_ctx ctx, int64_t* free_bytes, int64_t* total_bytes);
 GA_API int ga_ctx_mem_stats(ga_ctx ctx, int64_t* in_use, int64_t* peak, int reset_peak);
 
 /* Work counters accumulated on the device by every masked-SpGEMM launch of
- * this context (MSA / MCA / HEAP): Gustavson products P = sum over A entries
+ * this context (MSA / MCA / HEAP / DOT): Gustavson products P = sum over A entries
  * (i,k) of nnz(B_k) (the work of the reference's C<M> = A*B), mask entries,
  * launches, A entries, rows, and the products the kernels actually processed
  * (fewer than P when a k-truss support product only evaluates the upper
- * triangle of a symmetric matrix and mirrors it). They feed the GFLOP/s (2P)
+ * triangle of a symmetric matrix and mirrors it; for DOT, the list entries
+ * its intersections walked). They feed the GFLOP/s (2P)
  * and byte models. out has GA_CTR_COUNT entries; reset != 0 zeroes them
  * after reading. Synchronises the stream. */
 enum { GA_CTR_PRODUCTS = 0, GA_CTR_MASK_ENTRIES = 1, GA_CTR_LAUNCHES = 2, GA_CTR_A_ENTRIES = 3,

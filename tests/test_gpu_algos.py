@@ -51,7 +51,7 @@ def test_tc_other_forms(ctx):
     assert int(ref.sum()) == 3 * total
 
 
-@pytest.mark.parametrize("algo", ["msa", "mca", "heap"])
+@pytest.mark.parametrize("algo", ["msa", "mca", "heap", "dot"])
 @pytest.mark.parametrize("device_loops", [1, 0])
 def test_ktruss(ctx, algo, device_loops):
     ctx.set_option(ga.OPT_DEVICE_LOOPS, device_loops)
@@ -66,6 +66,16 @@ def test_ktruss(ctx, algo, device_loops):
                 assert np.array_equal(r, R.rst) and np.array_equal(c, R.col) and np.array_equal(v, R.val), (name, k)
     finally:
         ctx.set_option(ga.OPT_DEVICE_LOOPS, 1)
+
+
+def test_ktruss_dot_needs_symmetric(ctx):
+    rng = np.random.default_rng(4)
+    D = np.triu(rng.random((30, 30)) < 0.3, 1)
+    from graphs import dense_to_csr
+    G = dense_to_csr(D)  # upper triangle only: not symmetric
+    with pytest.raises(ga.GaError) as e:
+        ga.ktruss("dot", to_device(ctx, G), 3)
+    assert e.value.code == ga.ERR_UNSUPPORTED
 
 
 def test_ktruss_naive_and_trivial_k(ctx):
