@@ -53,7 +53,8 @@ def parse_args():
     ap.add_argument("--scale", type=int, default=18)
     ap.add_argument("--edge-factor", type=int, default=16)
     ap.add_argument("--seed", type=int, default=42)
-    ap.add_argument("--algo", default="msa", choices=["msa", "mca", "heap", "dot"])
+    ap.add_argument("--algo", default=None, choices=["msa", "mca", "heap", "dot", "auto"],
+                    help="k-truss variant (default: msa; auto for the batch workload)")
     ap.add_argument("--kmin", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -75,10 +76,17 @@ def parse_args():
     ap.add_argument("--graphs", type=int, default=4096, help="batch workload: number of graphs")
     ap.add_argument("--plain-graphs", type=int, default=0,
                     help="batch workload: graphs timed in the per-graph arm (0 = all)")
-    ap.add_argument("--tc-algo", default="msa", choices=["msa", "mca", "heap", "dot"])
+    ap.add_argument("--tc-algo", default=None, choices=["msa", "mca", "heap", "dot", "auto"],
+                    help="TC variant (default: msa; auto for the batch workload)")
     ap.add_argument("--host-loops", action="store_true",
                     help="run the k-truss loop from the host (kernels launched one by one, e.g. for ncu)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    auto = args.workload == "batch" or args.case == "batch"
+    if args.algo is None:
+        args.algo = "auto" if auto else "msa"
+    if args.tc_algo is None:
+        args.tc_algo = "auto" if auto else "msa"
+    return args
 
 
 # ---------------------------------------------------------------- plumbing
@@ -443,7 +451,7 @@ def run_gpu(args, dist: Dist):
 
     # ------------------------------------------------- support variants
     variants = {}
-    for algo in ("msa", "mca", "heap"):
+    for algo in ("msa", "mca", "heap", "dot"):
         ctx.work_counters(reset=True)
         ctx.flush_l2()
         ctx.timer_start()
@@ -451,6 +459,7 @@ def run_gpu(args, dist: Dist):
         ms = ctx.timer_stop()
         C.free()
         variants[algo] = {"ms": ms, "gflops": 2.0 * ctx.work_counters()["products"] / ms / 1e6}
+    variants["autotune_ktruss"] = ga.autotune(ga.TUNE_KTRUSS, A)
 
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
@@ -503,6 +512,15 @@ def run_batch(args, dist: Dist):
     n, dim = knn_batch_sizes(args.graphs, args.seed)
     U, voff = ga.gen_knn_batch(ctx, n, dim, k=30, seed=args.seed + dist.rank)
     G = args.graphs
+    # autotuned schedules for the union (cached; GA_AUTO calls use them)
+    tuning = {}
+    kt_algo, tc_algo = args.algo, args.tc_algo
+    if args.algo == "auto":
+        tuning["ktruss"] = ga.autotune(ga.TUNE_KTRUSS, U)
+        kt_algo = tuning["ktruss"]["algo"]
+    if args.tc_algo == "auto":
+        tuning["tc"] = ga.autotune(ga.TUNE_TC, U)
+        tc_algo = tuning["tc"]["algo"]
 
     def step():
         tcs = ga.batch_tc(args.tc_algo, U, voff)
@@ -530,7 +548,7 @@ def run_batch(args, dist: Dist):
     t_max = dist.max(sum(step_ms))
     value = dist.sum(G * args.steps) / (t_max * 1e-3)
 
-    prof = profile_step(ga, ctx, step, args.algo, lambda: ctx.work_counters(), loops)
+    prof = profile_step(ga, ctx, step, kt_algo, lambda: ctx.work_counters(), loops)
     prof["roofline"]["kernel_share_of_step"] = prof["kernel_ms"] / (sum(step_ms) / args.steps)
 
     # ------------------------------------------- per-graph plain launches
@@ -539,9 +557,10 @@ def run_batch(args, dist: Dist):
     npl = G if args.plain_graphs <= 0 else min(G, args.plain_graphs)
     pick = np.sort(np.random.default_rng(args.seed + 1).choice(G, npl, replace=False)) if npl < G else np.arange(G)
     handles = [ga.Csr.upload(ctx, m_, m_, r, c, np.ones(len(c), np.int32)) for m_, r, c in (blocks[i] for i in pick)]
+    # the plain form runs the variants the tuner chose for the union, default schedule
     for h in handles[:8]:
-        ga.tc(args.tc_algo, h, per_row=False)
-        ga.ktruss(args.algo, h, 4)[0].free()
+        ga.tc(tc_algo, h, per_row=False)
+        ga.ktruss(kt_algo, h, 4)[0].free()
     ctx.sync()
     ctx.flush_l2()
     ctx.timer_start()
@@ -549,8 +568,8 @@ def run_batch(args, dist: Dist):
     plain_it = np.zeros(npl, np.int32)
     plain_nnz = 0
     for j, h in enumerate(handles):
-        plain_tc[j] = ga.tc(args.tc_algo, h, per_row=False)[0]
-        C, plain_it[j] = ga.ktruss(args.algo, h, 4)
+        plain_tc[j] = ga.tc(tc_algo, h, per_row=False)[0]
+        C, plain_it[j] = ga.ktruss(kt_algo, h, 4)
         plain_nnz += C.nnz
         C.free()
     plain_ms = ctx.timer_stop()
@@ -606,9 +625,10 @@ def run_batch(args, dist: Dist):
         "config": batch_config(args, n, len(col)),
         "roofline": prof["roofline"], "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(prof["launches"] * args.steps), "clocks": clocks,
+        "autotune": tuning,
         "plain": {"value": plain_value, "unit": "graphs/s", "graphs_timed": npl, "ms": plain_ms,
                   "results_equal": same, "speedup": value / plain_value,
-                  "form": "ga_tc + ga_ktruss per graph, resident per-graph handles"},
+                  "form": f"ga_tc({tc_algo}) + ga_ktruss({kt_algo}) per graph, resident per-graph handles"},
         "work": {"products_per_step": prof["counters"]["products"],
                  "triangles": int(ref[0].sum()), "truss_entries": int(ref[2]),
                  "max_iters": int(ref[1].max())},

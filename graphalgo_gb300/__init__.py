@@ -27,10 +27,13 @@ LIB_PATH = os.path.join(HERE, "_lib", "libgraphalgo_gb300.so")
 # dtypes
 INT32, INT64, FP32, FP64, UINT8 = 0, 1, 2, 3, 4
 # algorithms
-MSA, MCA, HEAP, NAIVE, DOT = 0, 1, 2, 3, 4
-ALGOS = {"msa": MSA, "mca": MCA, "heap": HEAP, "naive": NAIVE, "dot": DOT}
+MSA, MCA, HEAP, NAIVE, DOT, AUTO = 0, 1, 2, 3, 4, 5
+ALGOS = {"msa": MSA, "mca": MCA, "heap": HEAP, "naive": NAIVE, "dot": DOT, "auto": AUTO}
+ALGO_NAMES = {v: k for k, v in ALGOS.items()}
 # options
 OPT_DEVICE_LOOPS, OPT_PROFILE, OPT_FAIL_ALLOC_AFTER, OPT_KNN_TILED = 1, 2, 3, 4
+OPT_MXM_WARP_FLOPS, OPT_MXM_HEAVY_FLOPS, OPT_MXM_CTAS_PER_SM, OPT_DOT_CHUNK = 5, 6, 7, 8
+TUNE_KTRUSS, TUNE_PRODUCT, TUNE_TC = 0, 1, 2
 # status codes
 OK, ERR_INVALID_ARG, ERR_INVALID_CSR, ERR_SHAPE, ERR_DTYPE, ERR_CUDA, ERR_OOM, ERR_NO_DEVICE, \
     ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_ADMISSION = range(11)
@@ -598,3 +601,21 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------------------------------ autotuner
+class TuneResult(ctypes.Structure):
+    _fields_ = [("algo", _int), ("warp_max_flops", _i64), ("heavy_flops", _i64), ("ctas_per_sm", _int),
+                ("dot_chunk", _int), ("ms", ctypes.c_double), ("default_ms", ctypes.c_double),
+                ("candidates", _int), ("cached", _int)]
+
+
+def autotune(kind: int, A: Csr, B: Optional[Csr] = None, M: Optional[Csr] = None, force: bool = False) -> dict:
+    """Tunes (or looks up) the masked-product schedule for A's problem; GA_AUTO
+    calls on problems of the same signature use the result."""
+    r = TuneResult()
+    _check(lib().ga_autotune(A.ctx.handle, _int(kind), A.handle, B.handle if B else None,
+                             M.handle if M else None, _int(int(force)), ctypes.byref(r)), A.ctx)
+    out = {n: getattr(r, n) for n, _ in TuneResult._fields_}
+    out["algo"] = ALGO_NAMES.get(r.algo, r.algo)
+    return out

@@ -184,6 +184,8 @@ struct CsrGuard {
 
 static void tc_device(ga_ctx ctx, ga_algo algo, ga_csr A, int64_t* d_total, int64_t* d_per_row) {
     GA_REQUIRE(A->m == A->n, GA_ERR_SHAPE, "triangle counting needs a square matrix");
+    TuneScope tscope(ctx);
+    algo = resolve_tc_algo(ctx, algo, A);
     unsigned long long* tot = reinterpret_cast<unsigned long long*>(d_total);
     GA_CUDA(cudaMemsetAsync(tot, 0, sizeof(unsigned long long), ctx->stream));
     if (A->m == 0) return;
@@ -232,20 +234,49 @@ __device__ __forceinline__ bool kt_keep_all(const int32_t* gid, const int32_t* d
     return gid != nullptr && done_g[gid[i]] != 0;
 }
 
-__global__ void k_kt_count(const int32_t* __restrict__ cr, const int32_t* __restrict__ sup, int64_t m, int k,
-                           int32_t* __restrict__ cnt, const int32_t* __restrict__ gid,
-                           const int32_t* __restrict__ done_g) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < m; i += warps) {
-        if (kt_keep_all(gid, done_g, i)) {
-            if (lane == 0) cnt[i] = cr[i + 1] - cr[i];
-            continue;
+// Row of entry q: the maintained row index when there is one, else a binary
+// search of the row starts.
+__device__ __forceinline__ int64_t kt_row(const int32_t* cr, int64_t m, const int32_t* row_of, int64_t q) {
+    return row_of ? row_of[q] : upper_bound_i32(cr, (int)m + 1, (int32_t)q) - 1;
+}
+
+// Prune, step 1 (one thread per entry): keep flag of every entry of C
+// (support >= k-2, or the entry's graph has finished), 0 past C's end up to
+// cap so the exclusive scan over cap entries gives new positions.
+__global__ void k_kt_flags(const int32_t* __restrict__ cr, const int32_t* __restrict__ sup, int64_t m, int k,
+                           int64_t cap, int32_t* __restrict__ flag, const int32_t* __restrict__ gid,
+                           const int32_t* __restrict__ done_g, const int32_t* __restrict__ row_of) {
+    const int64_t cur = cr[m];
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cap; q += (int64_t)gridDim.x * blockDim.x) {
+        int32_t keep = 0;
+        if (q < cur) {
+            keep = sup[q] >= k - 2;
+            if (!keep && gid) keep = kt_keep_all(gid, done_g, kt_row(cr, m, row_of, q));
         }
-        int c = 0;
-        for (int32_t q = cr[i] + lane; q < cr[i + 1]; q += 32) c += sup[q] >= k - 2;
-        c = warp_sum<int>(c);
-        if (lane == 0) cnt[i] = c;
+        flag[q] = keep;
+    }
+}
+
+// Prune, step 2, after the exclusive scan `pos` of the flags: kept entries
+// move to pos[q] (columns, and their rows when tracked), pos_new[q] is the
+// new position or -1, and the new row starts are tr[i] = pos[cr[i]].
+__global__ void k_kt_scatter(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
+                             const int32_t* __restrict__ pos, int64_t m, int32_t* __restrict__ tc,
+                             int32_t* __restrict__ tr, int32_t* __restrict__ pos_new, int32_t* __restrict__ trow,
+                             const int32_t* __restrict__ row_of) {
+    const int64_t cur = cr[m];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cur || q <= m; q += stride) {
+        if (q <= m) tr[q] = pos[cr[q]];
+        if (q < cur) {
+            const int32_t d = pos[q];
+            const bool keep = pos[q + 1] != d;
+            if (keep) {
+                tc[d] = cc[q];
+                if (trow) trow[d] = row_of[q];
+            }
+            if (pos_new) pos_new[q] = keep ? d : -1;
+        }
     }
 }
 
@@ -253,59 +284,20 @@ __global__ void k_kt_count(const int32_t* __restrict__ cr, const int32_t* __rest
 // whose kept count equals its current count has converged (iterations t+1);
 // otherwise it was pruned and stops after n_g iterations (reported as 0),
 // as the reference's loop bound does (src/main.cpp:100).
-__global__ void k_kt_graph_update(const KtState* st, const int32_t* __restrict__ cnt, KtBatch b) {
-    __shared__ int64_t s_part[32];
-    const int64_t g = blockIdx.x;
-    if (g >= b.ngraphs) return;
-    int64_t kept = 0;
-    for (int32_t i = b.voff[g] + threadIdx.x; i < b.voff[g + 1]; i += blockDim.x) kept += cnt[i];
-    kept = warp_sum<int64_t>(kept);
-    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = kept;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int64_t total = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) total += s_part[w];
-        if (!b.done_g[g]) {
-            const int t = st->t;
-            if (total == b.nnz_g[g]) {
-                b.iters_g[g] = t + 1;
+__global__ void k_kt_graph_update(const KtState* st, const int32_t* __restrict__ tr, KtBatch b) {
+    const int t = st->t;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < b.ngraphs; g += (int64_t)gridDim.x * blockDim.x) {
+        if (b.done_g[g]) continue;
+        const int32_t kept = tr[b.voff[g + 1]] - tr[b.voff[g]];
+        if (kept == b.nnz_g[g]) {
+            b.iters_g[g] = t + 1;
+            b.done_g[g] = 1;
+        } else {
+            b.nnz_g[g] = kept;
+            if (t + 1 >= b.nvert[g]) {
+                b.iters_g[g] = 0;
                 b.done_g[g] = 1;
-            } else {
-                b.nnz_g[g] = (int32_t)total;
-                if (t + 1 >= b.nvert[g]) {
-                    b.iters_g[g] = 0;
-                    b.done_g[g] = 1;
-                }
             }
-        }
-    }
-}
-
-// Keep entries with support >= k-2, in order (ballot compaction per row).
-// Optionally records each old entry's new position (-1 when dropped) and
-// the row of each new entry.
-__global__ void k_kt_compact(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
-                             const int32_t* __restrict__ sup, const int32_t* __restrict__ tr, int64_t m, int k,
-                             int32_t* __restrict__ tc, int32_t* __restrict__ pos_new, int32_t* __restrict__ trow,
-                             const int32_t* __restrict__ gid, const int32_t* __restrict__ done_g) {
-    const int lane = threadIdx.x & 31;
-    const unsigned FULL = 0xffffffffu;
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < m; i += warps) {
-        int32_t o = tr[i];
-        const int32_t b = cr[i], e = cr[i + 1];
-        const bool all = kt_keep_all(gid, done_g, i);
-        for (int32_t base = b; base < e; base += 32) {
-            int32_t q = base + lane;
-            bool keep = q < e && (all || sup[q] >= k - 2);
-            unsigned bal = __ballot_sync(FULL, keep);
-            const int32_t dst = o + __popc(bal & ((1u << lane) - 1u));
-            if (keep) {
-                tc[dst] = cc[q];
-                if (trow) trow[dst] = (int32_t)i;
-            }
-            if (pos_new && q < e) pos_new[q] = keep ? dst : -1;
-            o += __popc(bal);
         }
     }
 }
@@ -402,9 +394,16 @@ __global__ void k_kt_copyback_aux(const KtState* st, const int32_t* __restrict__
     }
 }
 
+void upper_starts(ga_ctx ctx, ga_csr A, int32_t* ust) {
+    k_upper_start<<<grid_for(A->m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(A->rst, A->col, A->m, ust);
+    post_launch("kt_upper_start");
+}
+
 ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, const KtBatch* batch) {
     GA_REQUIRE(A->m == A->n, GA_ERR_SHAPE, "k-truss needs a square matrix");
     GA_REQUIRE(A->dtype == GA_INT32, GA_ERR_DTYPE, "k-truss needs int32 values (spMtx<int>)");
+    TuneScope tscope(ctx);
+    algo = resolve_ktruss_algo(ctx, algo, A);
     GA_REQUIRE(algo == GA_MSA || algo == GA_MCA || algo == GA_HEAP || algo == GA_NAIVE || algo == GA_DOT,
                GA_ERR_INVALID_ARG, "k-truss: unknown algorithm");
     const int64_t m = A->m;
@@ -416,8 +415,9 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
             return C;
         }
         const int64_t cap = A->nnz > 0 ? A->nnz : 1;
-        DBuf<int32_t> sup(ctx, (size_t)cap), cnt(ctx, (size_t)m + 1), tr(ctx, (size_t)m + 1), tc(ctx, (size_t)cap);
-        DBuf<unsigned char> scan_scr(ctx, scan_scratch_bytes(m));
+        // eflag: keep flags of the entries, scanned in place into new positions
+        DBuf<int32_t> sup(ctx, (size_t)cap), eflag(ctx, (size_t)cap + 1), tr(ctx, (size_t)m + 1), tc(ctx, (size_t)cap);
+        DBuf<unsigned char> scan_scr(ctx, scan_scratch_bytes(cap));
         DBuf<unsigned char> mxm_scr(ctx, mxm_scratch_bytes(m, m, cap));
         DBuf<KtState> st(ctx, 1);
         KtState h0 = {};
@@ -462,19 +462,22 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
             } else {
                 mxm_masked_launch(ctx, algo, C, C, C, sup.p, mxm_scr.p, cap, unit);
             }
+            // prune: keep flags, their exclusive scan (new positions), scatter
             const int32_t* gid = batch ? batch->gid : nullptr;
             const int32_t* done_g = batch ? batch->done_g : nullptr;
-            k_kt_count<<<grid_rows, 256, 0, ctx->stream>>>(C->rst, sup.p, m, k, cnt.p, gid, done_g);
-            post_launch("kt_count");
-            scan_exclusive_i32_scratch(ctx, cnt.p, tr.p, m, scan_scr.p);
-            k_kt_compact<<<grid_rows, 256, 0, ctx->stream>>>(C->rst, C->col, sup.p, tr.p, m, k, tc.p,
+            k_kt_flags<<<grid_ent, 256, 0, ctx->stream>>>(C->rst, sup.p, m, k, cap, eflag.p, gid, done_g,
+                                                          upper ? row_of.p : nullptr);
+            post_launch("kt_flags");
+            scan_exclusive_i32_scratch(ctx, eflag.p, eflag.p, cap, scan_scr.p);
+            k_kt_scatter<<<grid_copy, 256, 0, ctx->stream>>>(C->rst, C->col, eflag.p, m, tc.p, tr.p,
                                                              upper ? pos_new.p : nullptr, upper ? trow.p : nullptr,
-                                                             gid, done_g);
+                                                             upper ? row_of.p : nullptr);
+            post_launch("kt_scatter");
             if (batch) {
-                k_kt_graph_update<<<(unsigned)batch->ngraphs, 256, 0, ctx->stream>>>(st.p, cnt.p, *batch);
+                k_kt_graph_update<<<grid_for(batch->ngraphs, 128, ctx->num_sms * 4), 128, 0, ctx->stream>>>(
+                    st.p, tr.p, *batch);
                 post_launch("kt_graph_update");
             }
-            post_launch("kt_compact");
             if (upper) {
                 k_mirror_update<<<grid_ent, 256, 0, ctx->stream>>>(st.p, pos_new.p, mir.p, mir_new.p);
                 post_launch("kt_mirror_update");

@@ -381,6 +381,16 @@ int ga_ctx_set_option(ga_ctx ctx, int option, int64_t value) {
     case GA_OPT_PROFILE: ctx->profile = value != 0; return GA_OK;
     case GA_OPT_FAIL_ALLOC_AFTER: ctx->fail_alloc_after = value; return GA_OK;
     case GA_OPT_KNN_TILED: ctx->knn_tiled = value != 0; return GA_OK;
+    case GA_OPT_MXM_WARP_FLOPS: ctx->tune.warp_max_flops = value; return GA_OK;
+    case GA_OPT_MXM_HEAVY_FLOPS: ctx->tune.heavy_flops = value; return GA_OK;
+    case GA_OPT_MXM_CTAS_PER_SM:
+        if (value < 0) break;
+        ctx->tune.ctas_per_sm = (int)value;
+        return GA_OK;
+    case GA_OPT_DOT_CHUNK:
+        if (value < 1 || value > 4096) break;
+        ctx->tune.dot_chunk = (int)value;
+        return GA_OK;
     }
     ctx->last_error = "unknown option";
     return GA_ERR_INVALID_ARG;

@@ -44,6 +44,14 @@ struct KStat {
     double total_ms = 0.0;
 };
 
+// Schedule parameters of the masked products (options or autotuner).
+struct MxmTune {
+    int64_t warp_max_flops = 32768;  // rows with more Gustavson products go to a CTA
+    int64_t heavy_flops = 1 << 20;   // CTA items of rows with at least this many products run first
+    int ctas_per_sm = 0;             // persistent grid: CTAs per SM (0: as many as fit)
+    int dot_chunk = 8;               // inner-product form: mask entries per warp task
+};
+
 }  // namespace ga
 
 struct ga_ctx_s {
@@ -60,6 +68,7 @@ struct ga_ctx_s {
     bool profile = false;
     int64_t fail_alloc_after = -1;  // fault injection
     bool knn_tiled = false;         // k-NN generator: tiled kernel for every graph
+    ga::MxmTune tune;               // masked-product schedule
     // profiling
     std::vector<ga::PendingTiming> pending;
     std::vector<cudaEvent_t> event_pool;
@@ -185,6 +194,21 @@ struct KtBatch {
     int32_t* done_g = nullptr;       // graph finished (converged, or stopped after n_g iterations)
 };
 ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, const KtBatch* batch);
+
+// Autotuned algorithm resolution: GA_AUTO becomes the cached (or freshly
+// tuned) variant, and ctx->tune its schedule; other values pass through.
+// Callers hold a TuneScope so the context's schedule is restored afterwards.
+ga_algo resolve_ktruss_algo(ga_ctx ctx, ga_algo algo, ga_csr A);
+ga_algo resolve_tc_algo(ga_ctx ctx, ga_algo algo, ga_csr A);
+ga_algo resolve_mxm_algo(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M);
+struct TuneScope {
+    ga_ctx ctx;
+    MxmTune saved;
+    explicit TuneScope(ga_ctx c) : ctx(c), saved(c->tune) {}
+    ~TuneScope() { ctx->tune = saved; }
+};
+// Position of the first entry with column >= i in each row (rows sorted).
+void upper_starts(ga_ctx ctx, ga_csr A, int32_t* ust);
 
 // device-side transpose (counting sort; rows of the result sorted)
 ga_csr transpose_csr(ga_ctx ctx, ga_csr A);

@@ -4,7 +4,7 @@
 //  1. k_row_bin: one warp per output row computes the mask length m_i and the
 //     Gustavson product count P_i = sum_{k in A_i} nnz(B_k). Rows with an
 //     empty mask are skipped, rows without products get explicit zeros, short
-//     light rows (m_i <= kWarpSlots, P_i <= kWarpMaxFlops) go to a warp
+//     light rows (m_i <= kWarpSlots, P_i <= warp_max_flops) go to a warp
 //     queue, all others to a CTA queue as windows of at most kCtaSlots mask
 //     slots spanning fewer than kWinCols columns (heavy rows first).
 //  2. k_mxm_masked: a persistent kernel (one wave of CTAs sized by occupancy)
@@ -14,7 +14,9 @@
 //       GA_MSA  : a dense bitmap of the window's mask columns in shared memory
 //                 (the reference MSA keeps a dense state array over the
 //                 columns, matrix_la.h:681-749); a set bit is resolved to its
-//                 slot by binary search. Warp rows use a 4096-bit hashed filter.
+//                 slot as the word's first slot plus a popcount (the
+//                 slot base is kept per 32-column word). Warp rows use a
+//                 4096-bit hashed filter and a 512-entry hash table.
 //       GA_MCA  : binary search of the sorted mask row in shared memory (the
 //                 reference MCA walks the mask row, matrix_la.h:625-632);
 //       GA_HEAP : warp-cooperative sorted merge of each B row against the
@@ -39,8 +41,10 @@ constexpr int kWinWords = kWinCols / 32;   // dense bitmap words
 constexpr int kWarpSlots = 256;            // mask slots per warp row
 constexpr int kWarpTblBits = 9;            // warp-row hash table: 512 entries
 constexpr int kFilterBits = 12;            // warp-row filter: 4096 bits
-constexpr int64_t kWarpMaxFlops = 32768;   // rows above this go to a CTA
-constexpr int64_t kHeavyFlops = 1 << 20;   // CTA items scheduled first
+// Bin thresholds (rows above warp_max_flops products go to a CTA; CTA items
+// of rows with at least heavy_flops products are scheduled first) and the
+// persistent grid size are runtime parameters (ga_ctx tune, set by options
+// or the autotuner).
 constexpr int kLongSeg = 256;              // B rows longer than this are shared by the CTA
 constexpr int kLongCap = 1024;             // long B rows listed per item
 constexpr int kChunk = 1024;               // entries per long-row piece
@@ -68,6 +72,7 @@ struct MxmArgs {
     int4* cta_items;          // (row, first slot, end slot, unused)
     int32_t cta_cap;
     unsigned long long* ctr;  // context work counters (GA_CTR_*)
+    int64_t warp_max_flops, heavy_flops;
 };
 
 __global__ void k_reset_queue(MxmQueue* q) {
@@ -106,12 +111,12 @@ __global__ void k_row_bin(MxmArgs<T, A> p) {
         }
         if (lane == 0) {
             my_flops += (unsigned long long)f;
-            if (mi <= kWarpSlots && f <= kWarpMaxFlops) {
+            if (mi <= kWarpSlots && f <= p.warp_max_flops) {
                 int pos = atomicAdd(&p.q->warp_count, 1);
                 p.warp_rows[pos] = (int32_t)i;
             } else {
                 const int32_t* mcol = p.mc + mb;
-                const bool heavy = f >= kHeavyFlops;
+                const bool heavy = f >= p.heavy_flops;
                 int s0 = 0;
                 while (s0 < mi) {
                     int s1 = min(mi, s0 + kCtaSlots);
@@ -625,6 +630,8 @@ static void launch_masked(ga_ctx ctx, ga_csr A_, ga_csr B_, ga_csr M_, T* cv, Mx
     p.mr = M_->rst; p.mc = M_->col; p.mre = mre;
     p.cv = cv; p.m = M_->m; p.q = q; p.warp_rows = warp_rows; p.cta_items = cta_items; p.cta_cap = cta_cap;
     p.ctr = ctx->d_counters;
+    p.warp_max_flops = ctx->tune.warp_max_flops;
+    p.heavy_flops = ctx->tune.heavy_flops;
     {
         ProfScope ps(ctx, "mxm_row_bin");
         int grid = grid_for(p.m * 32, 256, ctx->num_sms * 16);
@@ -637,6 +644,7 @@ static void launch_masked(ga_ctx ctx, ga_csr A_, ga_csr B_, ga_csr M_, T* cv, Mx
     int per_sm = 0;
     GA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMxmThreads, smem));
     if (per_sm < 1) per_sm = 1;
+    if (ctx->tune.ctas_per_sm > 0 && ctx->tune.ctas_per_sm < per_sm) per_sm = ctx->tune.ctas_per_sm;
     const char* name = LK == MD_DENSE ? "mxm_msa" : LK == MD_BSEARCH ? "mxm_mca" : "mxm_heap_merge";
     ProfScope ps(ctx, name);
     kern<<<ctx->num_sms * per_sm, kMxmThreads, smem, ctx->stream>>>(p);
@@ -647,12 +655,11 @@ static void launch_masked(ga_ctx ctx, ga_csr A_, ga_csr B_, ga_csr M_, T* cv, Mx
 // C<M>(i, j) = sum over k in A_i ∩ (B^T)_j of A(i, k) * B(k, j): one warp per
 // mask entry, the shorter of the two sorted lists walked 32 entries at a
 // time (one per lane), each lane binary-searching the longer one. Warps take
-// kDotChunk consecutive mask entries; a chunk finds its row by a binary
+// `chunk` consecutive mask entries; a chunk finds its row by a binary
 // search of the row partition `seg`. Row i's mask is [lo[i], hi[i]) within
 // the partition [seg[i], seg[i+1]) (the k-truss support evaluates only the
 // upper part of each row). No shared memory and no atomics: each mask entry
 // is written by one warp.
-constexpr int kDotChunk = 8;
 constexpr int kDotThreads = 256;
 
 template <typename T>
@@ -664,6 +671,7 @@ struct DotArgs {
     const int32_t* mc;
     T* cv;
     int64_t m, total;
+    int chunk;  // mask entries per warp task
     unsigned long long* ctr;
 };
 
@@ -707,9 +715,9 @@ __global__ void __launch_bounds__(kDotThreads) k_mxm_dot(DotArgs<T> p) {
     // entries of the partition as the device holds it now (inside a captured
     // k-truss loop, p.total is only the launch-time upper bound)
     const int64_t total = p.seg[p.m];
-    for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c * kDotChunk < total; c += warps) {
-        const int32_t q0 = (int32_t)(c * kDotChunk);
-        const int32_t q1 = (int32_t)min((int64_t)q0 + kDotChunk, total);
+    for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c * p.chunk < total; c += warps) {
+        const int32_t q0 = (int32_t)(c * p.chunk);
+        const int32_t q1 = (int32_t)min((int64_t)q0 + p.chunk, total);
         int i = upper_bound_i32(p.seg, (int)p.m + 1, q0) - 1;
         for (int32_t q = q0; q < q1; ++q) {
             while (q >= p.seg[i + 1]) ++i;
@@ -764,13 +772,14 @@ static void launch_dot_t(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr Bt, ga_csr M, T*
     p.mc = M->col;
     p.cv = cv; p.m = M->m; p.ctr = ctx->d_counters;
     p.total = M->nnz;
+    p.chunk = ctx->tune.dot_chunk > 0 ? ctx->tune.dot_chunk : 8;
     {
         ProfScope ps(ctx, "mxm_dot_count");
         k_dot_count<T><<<grid_for(p.m * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(p);
         post_launch("mxm_dot_count");
     }
     if (p.total == 0) return;
-    const int grid = grid_for((p.total + kDotChunk - 1) / kDotChunk * 32, kDotThreads, ctx->num_sms * 16);
+    const int grid = grid_for((p.total + p.chunk - 1) / p.chunk * 32, kDotThreads, ctx->num_sms * 16);
     ProfScope ps(ctx, "mxm_dot");
     if (unit) k_mxm_dot<T, true><<<grid, kDotThreads, 0, ctx->stream>>>(p);
     else k_mxm_dot<T, false><<<grid, kDotThreads, 0, ctx->stream>>>(p);
@@ -828,6 +837,8 @@ void mxm_masked_into(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, voi
     GA_REQUIRE(M->m == A->m && M->n == B->n, GA_ERR_SHAPE, "mxm: mask shape differs from A*B");
     GA_REQUIRE(A->dtype == B->dtype, GA_ERR_DTYPE, "mxm: A and B dtypes differ");
     if (M->nnz == 0 || M->m == 0) return;
+    TuneScope tscope(ctx);
+    algo = resolve_mxm_algo(ctx, algo, A, B, M);
     if (algo == GA_NAIVE) {
         naive_masked_into(ctx, A, B, M, d_cvals);
         return;

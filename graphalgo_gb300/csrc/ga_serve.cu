@@ -37,7 +37,7 @@ static int64_t bound_tc(int64_t m, int64_t nnz, int64_t sval) {
 
 static int64_t bound_ktruss(int64_t m, int64_t nnz) {
     // copy of C, support, compaction, SpGEMM scratch, mirror index arrays
-    return 32 * (m + 2) + 56 * (nnz + 1) + (1 << 20);
+    return 32 * (m + 2) + 60 * (nnz + 1) + (1 << 20);
 }
 
 static int64_t bound_bc(int64_t m, int64_t nnz, int64_t ns) {

@@ -1,0 +1,235 @@
+// Autotuner for the masked products: times candidate schedules (variant,
+// bin thresholds, persistent grid size, inner-product chunk) on the caller's
+// own problem, with the L2 flushed before each run, and keeps the fastest per
+// problem signature (device, kind, half-octave buckets of the sizes,
+// symmetry) in a process-wide cache. Calls with GA_AUTO resolve to the cached
+// choice, tuning on first use. Every candidate computes the same values, so
+// tuning changes only speed. The context's work counters are restored
+// afterwards: tuning launches are not counted as work.
+#include "ga_internal.cuh"
+
+#include <cmath>
+#include <functional>
+#include <mutex>
+#include <tuple>
+
+namespace ga {
+
+namespace {
+
+struct Cand {
+    ga_algo algo;
+    MxmTune t;
+};
+
+struct TuneEntry {
+    ga_algo algo = GA_MSA;
+    MxmTune t;
+    double ms = 0.0, default_ms = 0.0;
+    int candidates = 0;
+};
+
+using TuneKey = std::tuple<int, int, int, int, int, int, int, int>;
+
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneEntry> g_tune_cache;
+
+int bucket(int64_t x) { return x <= 0 ? 0 : 1 + (int)std::floor(2.0 * std::log2((double)x)); }
+
+MxmTune tune_of(int64_t warp_max, int ctas, int chunk) {
+    MxmTune t;
+    t.warp_max_flops = warp_max;
+    t.ctas_per_sm = ctas;
+    t.dot_chunk = chunk;
+    return t;
+}
+
+std::vector<Cand> product_candidates(bool dot_ok) {
+    std::vector<Cand> c;
+    c.push_back({GA_MSA, MxmTune()});  // the default schedule first
+    c.push_back({GA_MSA, tune_of(8192, 0, 8)});
+    c.push_back({GA_MSA, tune_of(131072, 0, 8)});
+    c.push_back({GA_MSA, tune_of(32768, 1, 8)});
+    c.push_back({GA_MCA, MxmTune()});
+    if (dot_ok)
+        for (int chunk : {4, 8, 16}) c.push_back({GA_DOT, tune_of(32768, 0, chunk)});
+    return c;
+}
+
+// Saves the context's work counters and puts them back on scope exit.
+struct CounterGuard {
+    ga_ctx ctx;
+    unsigned long long saved[GA_CTR_COUNT];
+    explicit CounterGuard(ga_ctx c) : ctx(c) {
+        GA_CUDA(cudaMemcpyAsync(saved, ctx->d_counters, sizeof(saved), cudaMemcpyDeviceToHost, ctx->stream));
+        GA_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    ~CounterGuard() {
+        cudaMemcpyAsync(ctx->d_counters, saved, sizeof(saved), cudaMemcpyHostToDevice, ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+    }
+};
+
+double time_once(ga_ctx ctx, const std::function<void()>& f) {
+    if (ga_ctx_flush_l2(ctx) != GA_OK) fail(GA_ERR_CUDA, ctx->last_error);
+    cudaEvent_t a, b;
+    GA_CUDA(cudaEventCreate(&a));
+    GA_CUDA(cudaEventCreate(&b));
+    float ms = 0.f;
+    try {
+        GA_CUDA(cudaEventRecord(a, ctx->stream));
+        f();
+        GA_CUDA(cudaEventRecord(b, ctx->stream));
+        GA_CUDA(cudaEventSynchronize(b));
+        GA_CUDA(cudaEventElapsedTime(&ms, a, b));
+    } catch (...) {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        throw;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms;
+}
+
+// Runs every candidate once after one untimed warm-up of the first, and
+// returns the fastest.
+TuneEntry pick(ga_ctx ctx, const std::vector<Cand>& cands, const std::function<void(const Cand&)>& run) {
+    CounterGuard cg(ctx);
+    const MxmTune saved = ctx->tune;
+    TuneEntry best;
+    try {
+        ctx->tune = cands[0].t;
+        run(cands[0]);
+        GA_CUDA(cudaStreamSynchronize(ctx->stream));
+        best.ms = INFINITY;
+        for (size_t i = 0; i < cands.size(); ++i) {
+            ctx->tune = cands[i].t;
+            const double ms = time_once(ctx, [&] { run(cands[i]); });
+            if (i == 0) best.default_ms = ms;
+            if (ms < best.ms) {
+                best.ms = ms;
+                best.algo = cands[i].algo;
+                best.t = cands[i].t;
+            }
+        }
+    } catch (...) {
+        ctx->tune = saved;
+        throw;
+    }
+    ctx->tune = saved;
+    best.candidates = (int)cands.size();
+    return best;
+}
+
+TuneEntry tune_support(ga_ctx ctx, ga_csr A) {
+    const int64_t m = A->m, nnz = A->nnz;
+    const bool sym = csr_is_symmetric(ctx, A);
+    const bool unit = csr_unit_values(ctx, A);
+    DBuf<int32_t> sup(ctx, (size_t)nnz + 1), ust(ctx, (size_t)m + 1);
+    DBuf<unsigned char> scr(ctx, mxm_scratch_bytes(m, m, nnz));
+    ga_csr_s Au = *A;
+    if (sym) {
+        upper_starts(ctx, A, ust.p);
+        Au.rst = ust.p;
+    }
+    ga_csr M = sym ? &Au : A;
+    const int32_t* mre = sym ? A->rst + 1 : nullptr;
+    return pick(ctx, product_candidates(sym), [&](const Cand& c) {
+        if (c.algo == GA_DOT) mxm_dot_launch(ctx, A, A, A, M, sup.p, unit, mre);
+        else mxm_masked_launch(ctx, c.algo, A, A, M, sup.p, scr.p, nnz, unit, mre);
+    });
+}
+
+TuneEntry tune_product(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M) {
+    DBuf<unsigned char> cv(ctx, (size_t)(M->nnz + 1) * dtype_size(A->dtype));
+    return pick(ctx, product_candidates(true), [&](const Cand& c) { mxm_masked_into(ctx, c.algo, A, B, M, cv.p); });
+}
+
+TuneEntry tune_tc(ga_ctx ctx, ga_csr A) {
+    DBuf<int64_t> tot(ctx, 1);
+    std::vector<Cand> c = {{GA_MSA, MxmTune()}, {GA_DOT, MxmTune()}, {GA_MCA, MxmTune()},
+                           {GA_MSA, tune_of(8192, 0, 8)}};
+    return pick(ctx, c, [&](const Cand& x) {
+        const int rc = ga_tc_device(ctx, x.algo, A, tot.p, nullptr);
+        if (rc != GA_OK) fail(rc, ctx->last_error);
+    });
+}
+
+TuneEntry lookup_or_tune(ga_ctx ctx, int kind, ga_csr A, ga_csr B, ga_csr M, bool force, bool* cached) {
+    const bool sym = csr_is_symmetric(ctx, A);
+    const TuneKey key{ctx->device, kind, bucket(A->m), bucket(A->n), bucket(A->nnz), bucket(B ? B->nnz : 0),
+                      bucket(M ? M->nnz : 0), sym ? 1 : 0};
+    if (!force) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            if (cached) *cached = true;
+            return it->second;
+        }
+    }
+    TuneEntry e = kind == GA_TUNE_KTRUSS ? tune_support(ctx, A)
+                  : kind == GA_TUNE_TC   ? tune_tc(ctx, A)
+                                         : tune_product(ctx, A, B, M);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = e;
+    }
+    if (cached) *cached = false;
+    return e;
+}
+
+}  // namespace
+
+ga_algo resolve_ktruss_algo(ga_ctx ctx, ga_algo algo, ga_csr A) {
+    if (algo != GA_AUTO) return algo;
+    if (A->m == 0 || A->nnz == 0) return GA_MSA;
+    const TuneEntry e = lookup_or_tune(ctx, GA_TUNE_KTRUSS, A, nullptr, nullptr, false, nullptr);
+    ctx->tune = e.t;
+    return e.algo;
+}
+
+ga_algo resolve_tc_algo(ga_ctx ctx, ga_algo algo, ga_csr A) {
+    if (algo != GA_AUTO) return algo;
+    if (A->m == 0 || A->nnz == 0) return GA_DOT;
+    const TuneEntry e = lookup_or_tune(ctx, GA_TUNE_TC, A, nullptr, nullptr, false, nullptr);
+    ctx->tune = e.t;
+    return e.algo;
+}
+
+ga_algo resolve_mxm_algo(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M) {
+    if (algo != GA_AUTO) return algo;
+    if (M->nnz == 0 || A->nnz == 0 || B->nnz == 0) return GA_MSA;
+    const TuneEntry e = lookup_or_tune(ctx, GA_TUNE_PRODUCT, A, B, M, false, nullptr);
+    ctx->tune = e.t;
+    return e.algo;
+}
+
+}  // namespace ga
+
+using namespace ga;
+
+extern "C" {
+
+int ga_autotune(ga_ctx ctx, int kind, ga_csr A, ga_csr B, ga_csr M, int force, ga_tune_result* out) {
+    if (!ctx || !A || !out) return GA_ERR_INVALID_ARG;
+    if (kind != GA_TUNE_KTRUSS && kind != GA_TUNE_TC && kind != GA_TUNE_PRODUCT) return GA_ERR_INVALID_ARG;
+    if (kind == GA_TUNE_PRODUCT && (!B || !M)) return GA_ERR_INVALID_ARG;
+    GA_API_BODY(ctx, {
+        GA_REQUIRE(kind == GA_TUNE_PRODUCT || A->m == A->n, GA_ERR_SHAPE, "autotune: square matrix expected");
+        GA_REQUIRE(A->nnz > 0, GA_ERR_INVALID_ARG, "autotune: empty matrix");
+        bool cached = false;
+        const TuneEntry e = lookup_or_tune(ctx, kind, A, B, M, force != 0, &cached);
+        out->algo = e.algo;
+        out->warp_max_flops = e.t.warp_max_flops;
+        out->heavy_flops = e.t.heavy_flops;
+        out->ctas_per_sm = e.t.ctas_per_sm;
+        out->dot_chunk = e.t.dot_chunk;
+        out->ms = e.ms;
+        out->default_ms = e.default_ms;
+        out->candidates = e.candidates;
+        out->cached = cached ? 1 : 0;
+    });
+}
+
+}  // extern "C"

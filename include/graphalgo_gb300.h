@@ -56,9 +56,10 @@ typedef enum {
     GA_MCA = 1,   /* mxmm_mca,   include/matrix_la.h:586-641 */
     GA_HEAP = 2,  /* mxmm_heap,  include/matrix_la.h:1013-1084 (a warp-cooperative sorted merge here) */
     GA_NAIVE = 3, /* mxmm_naive, include/matrix_la.h:1139-1277 */
-    GA_DOT = 4    /* inner-product form: each mask entry (i,j) is A_i . (B^T)_j by warp
+    GA_DOT = 4,   /* inner-product form: each mask entry (i,j) is A_i . (B^T)_j by warp
                      sorted-list intersection (B^T built on the fly unless B is
                      symmetric); TC's dot kernel; k-truss support (symmetric A) */
+    GA_AUTO = 5   /* the autotuner's choice of variant and schedule (ga_autotune) */
 } ga_algo;
 
 /* status codes */
@@ -96,8 +97,16 @@ GA_API int ga_version(int* major, int* minor);
  * fault injection for tests — the N-th device allocation from now on fails
  * with GA_ERR_OOM (-1 disables). GA_OPT_KNN_TILED: when 1, ga_gen_knn_batch
  * uses its tiled kernel (the one for graphs above 4,096 points) for every
- * graph; both kernels give the same graphs. */
-enum { GA_OPT_DEVICE_LOOPS = 1, GA_OPT_PROFILE = 2, GA_OPT_FAIL_ALLOC_AFTER = 3, GA_OPT_KNN_TILED = 4 };
+ * graph; both kernels give the same graphs. Masked-product schedule (what
+ * the autotuner chooses; results do not depend on it):
+ * GA_OPT_MXM_WARP_FLOPS (32768): output rows with at most this many
+ * Gustavson products (and at most 256 mask entries) are computed by one
+ * warp, larger rows by CTAs; GA_OPT_MXM_HEAVY_FLOPS (2^20): CTA work of rows
+ * with at least this many products is scheduled first;
+ * GA_OPT_MXM_CTAS_PER_SM (0 = as many as fit): persistent grid size;
+ * GA_OPT_DOT_CHUNK (8): mask entries per warp task of the inner-product form. */
+enum { GA_OPT_DEVICE_LOOPS = 1, GA_OPT_PROFILE = 2, GA_OPT_FAIL_ALLOC_AFTER = 3, GA_OPT_KNN_TILED = 4,
+       GA_OPT_MXM_WARP_FLOPS = 5, GA_OPT_MXM_HEAVY_FLOPS = 6, GA_OPT_MXM_CTAS_PER_SM = 7, GA_OPT_DOT_CHUNK = 8 };
 GA_API int ga_ctx_set_option(ga_ctx ctx, int option, int64_t value);
 
 /* Per-kernel timing collected while GA_OPT_PROFILE is on. Writes up to `cap`
@@ -275,6 +284,28 @@ GA_API int ga_ktruss(ga_ctx ctx, ga_algo algo, ga_csr A, int k, ga_csr* C, int* 
 GA_API int ga_bc(ga_ctx ctx, ga_csr A, const int32_t* sources, int64_t nsrc, double* bc);
 /* Device-result variant (bc: device array of length m, overwritten). */
 GA_API int ga_bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t nsrc, double* d_bc);
+
+/* -------------------------------------------------------------- autotuner */
+/* Times candidate schedules — MSA with three warp/CTA bin thresholds and
+ * two grid sizes, MCA, and the inner-product form with three chunk sizes —
+ * on the caller's problem (L2 flushed before each run) and keeps the fastest
+ * for problems of the same signature (device, kind, half-octave size
+ * buckets, symmetry) in a process-wide cache; GA_AUTO calls use it, tuning
+ * on first use. Kinds: GA_TUNE_KTRUSS (the support product C<A> = A*A of
+ * k-truss), GA_TUNE_PRODUCT (A*B masked by M), GA_TUNE_TC (triangle count
+ * of A). force != 0 re-tunes. Tuning launches are not counted in the work
+ * counters. No counterpart in the reference (its variant is a CLI flag). */
+enum { GA_TUNE_KTRUSS = 0, GA_TUNE_PRODUCT = 1, GA_TUNE_TC = 2 };
+typedef struct {
+    int algo;               /* chosen ga_algo */
+    int64_t warp_max_flops, heavy_flops;
+    int ctas_per_sm, dot_chunk;
+    double ms;              /* its time on the problem */
+    double default_ms;      /* the default schedule (MSA) on the same problem */
+    int candidates;
+    int cached;             /* 1: taken from the cache, no timing run */
+} ga_tune_result;
+GA_API int ga_autotune(ga_ctx ctx, int kind, ga_csr A, ga_csr B, ga_csr M, int force, ga_tune_result* out);
 
 /* ------------------------------------------------------ batched graphs */
 /* Many independent graphs as one block-diagonal matrix: rows (and columns)
