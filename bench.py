@@ -58,6 +58,10 @@ def parse_args():
     ap.add_argument("--kmin", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="k-truss sweep: keep the default bin thresholds instead of the tuned ones")
+    ap.add_argument("--no-other-configs", action="store_true",
+                    help="skip the TC (Erdos-Renyi n=1000) and BC (R-MAT 20) measurements")
     ap.add_argument("--cpu-reps", type=int, default=2)
     ap.add_argument("--case", choices=["support", "tc", "bc", "ktruss", "batch"], default=None,
                     help="profiling case instead of the benchmark, --reps times: support product, TC, BC, "
@@ -69,6 +73,8 @@ def parse_args():
                          "serve: a stream of TC / k-truss / BC requests on a pool of resident graphs")
     ap.add_argument("--requests", type=int, default=300, help="serve workload: requests per run")
     ap.add_argument("--workers", type=int, default=4, help="serve workload: server worker threads")
+    ap.add_argument("--serve-algo", default="auto", choices=["msa", "mca", "heap", "dot", "auto"],
+                    help="serve workload: variant of single TC / k-truss requests (both forms)")
     ap.add_argument("--rmat-scales", default="10,12,14,16,18,20,22", help="serve workload: R-MAT pool scales")
     ap.add_argument("--knn-sizes", default="1000,10000,100000,1000000", help="serve workload: k-NN pool sizes")
     ap.add_argument("--rates", default="0.5,1,2,4",
@@ -262,8 +268,10 @@ def run_case(args):
     ctx.close()
 
 
-def workload_config(args, m, nnz, kmax):
+def workload_config(args, m, nnz, kmax, schedule=None):
     return {"workload": f"k-truss sweep k={args.kmin}..{kmax} (k_max), R-MAT scale {args.scale}",
+            "schedule": None if schedule is None else
+            {k: schedule[k] for k in ("algo", "warp_max_flops", "heavy_flops", "ctas_per_sm", "dot_chunk")},
             "graph": f"R-MAT scale {args.scale}, edge factor {args.edge_factor}, a/b/c/d=0.57/0.19/0.19/0.05, "
                      f"seed {args.seed}, symmetrised, no loops/duplicates",
             "vertices": m, "stored_entries": nnz, "variant": args.algo, "k_range": [args.kmin, kmax],
@@ -350,6 +358,66 @@ def profile_step(ga, ctx, run, algo, counters, loops):
                          "avg_launch_ms": k_ms / max(1, k_launches)}}
 
 
+def other_configs(ga, ctx, args):
+    """The survey's other single-GPU configurations, measured beside the
+    headline: config 1 (triangle count of a seeded Erdos-Renyi graph, n=1000,
+    9,990 edges, uint8 values; latency, bit-exact against the oracle) and
+    config 3 (batched BC on R-MAT scale 20, 64 and 256 seeded sources, FP64;
+    GTEPS = sources * nnz / 2 / t)."""
+    import oracle
+    out = {}
+    # config 1
+    m, rst, col = ga.gen_er(1000, 9990, seed=args.seed)
+    A8 = ga.Csr.upload(ctx, m, m, rst, col, np.ones(len(col), np.uint8))
+    ref_total, ref_rows = oracle.tc_sandia(oracle.Csr(m, m, rst, col, np.ones(len(col), np.int32)))
+    rec = {}
+    tot = ga.Dense.create(ctx, 1, 1, ga.INT64)
+    for algo in ("msa", "dot"):
+        got, rows = ga.tc(algo, A8)
+        assert got == ref_total and np.array_equal(rows, ref_rows)
+        reps = 200
+        ctx.sync()
+        ctx.timer_start()
+        for _ in range(reps):
+            ga.tc_device(algo, A8, tot)
+        rec[algo + "_us"] = 1e3 * ctx.timer_stop() / reps
+    # e2e: upload (host CSR), count, per-row counts back to the host
+    reps = 50
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        X = ga.Csr.upload(ctx, m, m, rst, col, np.ones(len(col), np.uint8))
+        ga.tc("dot", X)
+        X.free()
+    rec["e2e_dot_us"] = 1e6 * (time.perf_counter() - t0) / reps
+    Gh = oracle.Csr(m, m, rst, col, np.ones(len(col), np.int32))
+    oracle.set_num_threads(os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        oracle.tc_sandia(Gh)
+    rec["cpu_port_us"] = 1e6 * (time.perf_counter() - t0) / reps
+    rec["cpu_port_threads"] = os.cpu_count() or 1
+    out["tc_er1000"] = {"triangles": ref_total, "edges": len(col) // 2, "bit_exact": True, **rec,
+                        "note": "device time per call (CUDA events, 200 calls, graph resident); e2e includes "
+                                "upload, validation and the per-row download"}
+    # config 3
+    m, rst, col = ga.gen_rmat(20, 16, 0.57, 0.19, 0.19, args.seed)
+    A = ga.Csr.upload(ctx, m, m, rst, col, np.ones(len(col), np.int32))
+    rng = np.random.default_rng(args.seed)
+    for ns in (64, 256):
+        src = rng.choice(m, ns, replace=False).astype(np.int32)
+        ga.bc(A, src)
+        ms = []
+        for _ in range(3):
+            ctx.flush_l2()
+            ctx.timer_start()
+            ga.bc(A, src)
+            ms.append(ctx.timer_stop())
+        t = min(ms)
+        out[f"bc_rmat20_{ns}src"] = {"ms": t, "gteps": ns * len(col) / 2 / t / 1e6, "runs_ms": ms}
+    return out
+
+
+
 def run_gpu(args, dist: Dist):
     import graphalgo_gb300 as ga
     from graphalgo_gb300 import build as gbuild
@@ -362,6 +430,11 @@ def run_gpu(args, dist: Dist):
     nnz = len(col)
     val = np.ones(nnz, np.int32)
     A = ga.Csr.upload(ctx, m, m, rst, col, val)
+    # the variant's bin thresholds and grid size, tuned on the first support product
+    schedule = None
+    if not args.no_tune and args.algo in ("msa", "mca", "dot"):
+        schedule = ga.autotune(ga.TUNE_KTRUSS, A, only=args.algo)
+        ga.apply_schedule(ctx, schedule)
 
     # warm-up (also fixes k_max)
     shape = None
@@ -451,6 +524,8 @@ def run_gpu(args, dist: Dist):
 
     # ------------------------------------------------- support variants
     variants = {}
+    default = {"warp_max_flops": 32768, "heavy_flops": 1 << 20, "ctas_per_sm": 0, "dot_chunk": 8}
+    ga.apply_schedule(ctx, default)  # each variant with the default schedule
     for algo in ("msa", "mca", "heap", "dot"):
         ctx.work_counters(reset=True)
         ctx.flush_l2()
@@ -461,6 +536,8 @@ def run_gpu(args, dist: Dist):
         variants[algo] = {"ms": ms, "gflops": 2.0 * ctx.work_counters()["products"] / ms / 1e6}
     variants["autotune_ktruss"] = ga.autotune(ga.TUNE_KTRUSS, A)
 
+    others = other_configs(ga, ctx, args) if not args.no_other_configs else None
+
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         import oracle
@@ -470,13 +547,14 @@ def run_gpu(args, dist: Dist):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": workload_config(args, m, nnz, kmax),
+        "config": workload_config(args, m, nnz, kmax, schedule),
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(launches_per_step * args.steps), "clocks": clocks,
         "work": {"products_per_step": wc["products"] / args.steps,
                  "executed_products_per_step": wc["executed"] / args.steps, "k_max": kmax,
                  "support_products_k3": per_k.get(args.kmin, {}).get("products")},
         "support_variants": variants,
+        "other_configs": others,
     }
     ctx.close()
     return line
@@ -592,24 +670,33 @@ def run_batch(args, dist: Dist):
             ga.host_register(a)
         try:
             e2e_ms, d2h = [], 0
+            phases = {"upload": 0.0, "tc": 0.0, "ktruss": 0.0, "download": 0.0}
             dist.barrier()
             for _ in range(args.steps):
                 ctx.flush_l2()
                 ctx.timer_start()
+                t0 = time.perf_counter()
                 Ud = ga.Csr.upload(ctx, len(rst) - 1, len(rst) - 1, rst_h, col_h, val_h)
+                t1 = time.perf_counter()
                 tcs = ga.batch_tc(args.tc_algo, Ud, voff)
+                t2 = time.perf_counter()
                 C, iters = ga.batch_ktruss(args.algo, Ud, voff, 4)
                 z = C.nnz
+                t3 = time.perf_counter()
                 ga.lib().ga_csr_download(ctx.handle, C.handle, out_rst.ctypes.data_as(ga._p),
                                          out_col.ctypes.data_as(ga._p), None)
                 C.free()
                 Ud.free()
                 e2e_ms.append(ctx.timer_stop())
+                t4 = time.perf_counter()
+                for key, a, b in (("upload", t0, t1), ("tc", t1, t2), ("ktruss", t2, t3), ("download", t3, t4)):
+                    phases[key] += 1e3 * (b - a) / args.steps
                 d2h = tcs.nbytes + iters.nbytes + out_rst.nbytes + 4 * z
             e2e_t = dist.max(sum(e2e_ms))
             e2e = {"value": dist.sum(G * args.steps) / (e2e_t * 1e-3), "unit": "graphs/s",
                    "h2d_bytes_per_step": int(rst_h.nbytes + col_h.nbytes + val_h.nbytes + voff.nbytes),
-                   "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t / args.steps}
+                   "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t / args.steps,
+                   "host_phases_ms": {k: round(v, 2) for k, v in phases.items()}}
         finally:
             for a in pinned:
                 ga.host_unregister(a)
@@ -697,10 +784,10 @@ def serve_requests(args, pool):
     return out
 
 
-def serve_run(ga, pool, reqs, workers, coalesce, arrivals=None):
+def serve_run(ga, pool, reqs, workers, coalesce, arrivals=None, algo="msa"):
     """Runs the requests through a server; arrivals (seconds from the start)
     or all at once. Returns latencies, makespan and results."""
-    with ga.Server(0, workers=workers, coalesce=coalesce) as srv:
+    with ga.Server(0, workers=workers, coalesce=coalesce, tc_algo=algo, ktruss_algo=algo) as srv:
         for _, m, rst, col in pool:
             srv.add_graph(m, rst, col)
         ids = []
@@ -762,14 +849,26 @@ def run_serve(args, dist: Dist):
     pool = serve_pool(args, ctx, ga)
     t_pool = time.perf_counter() - t_pool
     reqs = serve_requests(args, pool)
+    # the tuner's choices for every pool graph (process-wide cache), outside the timed runs
+    tuned = {}
+    t_tune = time.perf_counter()
+    if args.serve_algo == "auto":
+        for name, m, rst, col in pool:
+            A = ga.Csr.upload(ctx, m, m, rst, col, np.ones(len(col), np.int32))
+            kt = ga.autotune(ga.TUNE_KTRUSS, A)
+            tc = ga.autotune(ga.TUNE_TC, A)
+            tuned[name] = {"ktruss": kt["algo"], "tc": tc["algo"]}
+            A.free()
+    t_tune = time.perf_counter() - t_tune
     # warm-up: a few requests of each kind on the smallest graphs
     warm = [r for r in reqs if pool[r[1]][1] <= 20000][: max(3, 3 * args.warmup)]
-    serve_run(ga, pool, warm, args.workers, True)
+    al = args.serve_algo
+    serve_run(ga, pool, warm, args.workers, True, algo=al)
     sampler = ClockSampler(dist.local_rank)
     sampler.start()
-    plain = serve_run(ga, pool, reqs, 1, False)
+    plain = serve_run(ga, pool, reqs, 1, False, algo=al)
     l0 = ga.kernel_launches()
-    srv = serve_run(ga, pool, reqs, args.workers, True)
+    srv = serve_run(ga, pool, reqs, args.workers, True, algo=al)
     launches = ga.kernel_launches() - l0
     clocks = sampler.stop()
     same = serve_same(serve_digest(ga, reqs, plain["results"]), serve_digest(ga, reqs, srv["results"]))
@@ -780,7 +879,7 @@ def run_serve(args, dist: Dist):
         arrivals = np.cumsum(rng.exponential(1.0 / lam, len(reqs)))
         row = {"rate_req_s": lam, "rate_x_plain": f}
         for name, w, c in (("server", args.workers, True), ("plain", 1, False)):
-            r = serve_run(ga, pool, reqs, w, c, arrivals)
+            r = serve_run(ga, pool, reqs, w, c, arrivals, algo=al)
             row[name] = {k: r[k] for k in ("req_s", "p50_ms", "p99_ms")}
         sweep.append(row)
     value = srv["req_s"]
@@ -794,7 +893,8 @@ def run_serve(args, dist: Dist):
                    "graphs": {name: {"vertices": m, "stored_entries": len(col)} for name, m, _, col in pool},
                    "workers": args.workers, "batching": "coalesced TC / k-truss on graphs <= 2^20 entries",
                    "hbm_budget": srv["stats"]["budget"], "l2": "inputs resident; not flushed between requests",
-                   "pool_build_s": t_pool, "parallelism": "replicas only"},
+                   "pool_build_s": t_pool, "variant": al, "tuned": tuned, "tuning_s": t_tune,
+                   "parallelism": "replicas only"},
         "roofline": None, "cpu_baseline": None,
         "e2e": {"value": value, "unit": "req/s", "h2d_bytes_per_step": h2d / len(reqs),
                 "d2h_bytes_per_step": srv["d2h_bytes"] / len(reqs),

@@ -380,6 +380,13 @@ def tc(algo, A: Csr, per_row: bool = True):
     return int(total.value), rows
 
 
+def tc_device(algo, A: Csr, total: "Dense"):
+    """Device-result triangle count into a 1x1 INT64 Dense (no synchronisation)."""
+    ptr = _p()
+    _check(lib().ga_dense_device_ptr(total.handle, ctypes.byref(ptr)))
+    _check(lib().ga_tc_device(A.ctx.handle, _algo(algo), A.handle, ptr, None), A.ctx)
+
+
 def tc_lu(algo, A: Csr) -> int:
     total = _i64()
     _check(lib().ga_tc_lu(A.ctx.handle, _algo(algo), A.handle, ctypes.byref(total)), A.ctx)
@@ -610,12 +617,23 @@ class TuneResult(ctypes.Structure):
                 ("candidates", _int), ("cached", _int)]
 
 
-def autotune(kind: int, A: Csr, B: Optional[Csr] = None, M: Optional[Csr] = None, force: bool = False) -> dict:
+def autotune(kind: int, A: Csr, B: Optional[Csr] = None, M: Optional[Csr] = None, force: bool = False,
+             only=None) -> dict:
     """Tunes (or looks up) the masked-product schedule for A's problem; GA_AUTO
-    calls on problems of the same signature use the result."""
+    calls on problems of the same signature use the result. only: restrict to
+    one variant ("msa", "mca", "dot")."""
     r = TuneResult()
-    _check(lib().ga_autotune(A.ctx.handle, _int(kind), A.handle, B.handle if B else None,
-                             M.handle if M else None, _int(int(force)), ctypes.byref(r)), A.ctx)
+    algo = -1 if only is None else _algo(only)
+    _check(lib().ga_autotune_variant(A.ctx.handle, _int(kind), _int(algo), A.handle, B.handle if B else None,
+                                     M.handle if M else None, _int(int(force)), ctypes.byref(r)), A.ctx)
     out = {n: getattr(r, n) for n, _ in TuneResult._fields_}
     out["algo"] = ALGO_NAMES.get(r.algo, r.algo)
     return out
+
+
+def apply_schedule(ctx: Context, tuned: dict) -> None:
+    """Sets a tuning result's schedule as the context's masked-product options."""
+    ctx.set_option(OPT_MXM_WARP_FLOPS, tuned["warp_max_flops"])
+    ctx.set_option(OPT_MXM_HEAVY_FLOPS, tuned["heavy_flops"])
+    ctx.set_option(OPT_MXM_CTAS_PER_SM, tuned["ctas_per_sm"])
+    ctx.set_option(OPT_DOT_CHUNK, tuned["dot_chunk"])

@@ -70,67 +70,84 @@ void run_device_loop(ga_ctx ctx, const std::function<void(const LoopCtl&)>& body
 constexpr int kTcThreads = 256;
 constexpr int kTcChunk = 8;  // edges (i, j) of one L row per work unit
 
-// Work units of the dot-product kernel: (row i, first edge t0) for t0 = 1,
-// 1 + kTcChunk, ... < |L_i| (edge t = 0 has no smaller neighbour to meet).
-__global__ void k_tc_unit_count(const int32_t* __restrict__ lr, int64_t m, int32_t* __restrict__ cnt) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t ln = lr[i + 1] - lr[i];
-        cnt[i] = ln > 1 ? (ln - 1 + kTcChunk - 1) / kTcChunk : 0;
-    }
-}
-
-__global__ void k_tc_unit_fill(const int32_t* __restrict__ cnt, const int32_t* __restrict__ offs, int64_t m,
-                               int2* __restrict__ units) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
-        for (int32_t u = 0; u < cnt[i]; ++u) units[offs[i] + u] = make_int2((int)i, 1 + u * kTcChunk);
-}
-
-// Dot-product form over L (strict lower triangle, rows sorted): for an edge
-// (i, j) = (i, L_i[t]), |L_i[0..t) ∩ L_j| by warp-level sorted-list
-// intersection - only the prefix L_i[0..t) (entries < j) can meet L_j. The
-// shorter list is walked 32 entries at a time, one per lane, each lane
-// binary-searches the longer one, and __ballot_sync/__popc count the hits.
-// Each warp takes work units of kTcChunk edges, so the edges of a hub row
-// spread over many warps. per_row[i] = triangles whose largest vertex is i
-// (the row sums of the reference's C<L> = L*L).
-__global__ void __launch_bounds__(kTcThreads) k_tc_dot(const int32_t* __restrict__ lr, const int32_t* __restrict__ lc,
-                                                       const int2* __restrict__ units, int32_t nunits,
+// Dot-product form of the triangle count, straight from A (rows sorted, no
+// extraction of L): the strictly lower part of row i is L_i = A_i[0, low_i)
+// with low_i = ust[i] - rst[i]. For an edge (i, j) = (i, L_i[t]), the
+// triangles (i, j, k) with k < j are |L_i[0..t) ∩ L_j| (only entries below j
+// can meet L_j). Warps take kTcChunk consecutive entries of A (a chunk finds
+// its row by a binary search of the row starts, upper entries are skipped).
+// The shorter list is walked 32 entries at a time, one per lane; the longer
+// one is held in registers when it has at most 32 entries (searched by
+// shuffles), else, when 32 or more entries are walked, as the last entries
+// of 32 buckets (the shuffle search picks the bucket, a binary search in
+// memory finishes), else searched in memory; __ballot_sync/__popc count the
+// hits. per_row[i] = triangles whose largest vertex is i (the row
+// sums of the reference's C<L> = L*L). No host synchronisation.
+__global__ void __launch_bounds__(kTcThreads) k_tc_dot(const int32_t* __restrict__ ar, const int32_t* __restrict__ ac,
+                                                       const int32_t* __restrict__ ust, int64_t m,
                                                        unsigned long long* __restrict__ total,
                                                        unsigned long long* __restrict__ per_row) {
     const int lane = threadIdx.x & 31;
     const unsigned FULL = 0xffffffffu;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t nnz = ar[m];
     unsigned long long acc_total = 0;
-    for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < nunits; u += warps) {
-        const int2 unit = units[u];
-        const int32_t i = unit.x;
-        const int32_t lb = lr[i], ln = lr[i + 1] - lb;
-        const int32_t* Li = lc + lb;
-        const int t1 = min(ln, unit.y + kTcChunk);
-        unsigned long long cnt = 0;
-        for (int t = unit.y; t < t1; ++t) {
-            const int32_t j = __ldg(Li + t);
-            const int32_t jb = lr[j], jn = lr[j + 1] - jb;
+    for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c * kTcChunk < nnz; c += warps) {
+        const int32_t q0 = (int32_t)(c * kTcChunk);
+        const int32_t q1 = (int32_t)min((int64_t)q0 + kTcChunk, nnz);
+        int i = upper_bound_i32(ar, (int)m + 1, q0) - 1;
+        unsigned long long row_cnt = 0;
+        for (int32_t q = q0; q < q1; ++q) {
+            while (q >= ar[i + 1]) {
+                if (lane == 0 && row_cnt && per_row) atomicAdd(&per_row[i], row_cnt);
+                acc_total += row_cnt;
+                row_cnt = 0;
+                ++i;
+            }
+            const int32_t ib = ar[i];
+            const int t = q - ib;
+            if (t == 0 || q >= ust[i]) continue;  // first lower entry meets nothing; upper part skipped
+            const int32_t j = __ldg(ac + q);
+            const int32_t jb = ar[j], jn = ust[j] - jb;
             if (jn == 0) continue;
             const bool walk_j = jn <= t;  // walk the shorter list
-            const int32_t* W = walk_j ? lc + jb : Li;
-            const int32_t* S = walk_j ? Li : lc + jb;
+            const int32_t* W = walk_j ? ac + jb : ac + ib;
+            const int32_t* S = walk_j ? ac + ib : ac + jb;
             const int wn = walk_j ? jn : t, sn = walk_j ? t : jn;
+            const bool small = sn <= 32, bucketed = !small && wn >= 32;
+            int32_t key = INT32_MAX;
+            if (small) {
+                key = lane < sn ? __ldg(S + lane) : INT32_MAX;
+            } else if (bucketed) {
+                const int hi_b = (int)(((int64_t)(lane + 1) * sn) >> 5);
+                key = __ldg(S + hi_b - 1);
+            }
+            unsigned long long cnt = 0;
             for (int base = 0; base < wn; base += 32) {
-                const int q = base + lane;
+                const int e = base + lane;
+                const int32_t x = e < wn ? __ldg(W + e) : INT32_MAX;
+                const int b = (small || bucketed) ? warp_lower_bound(key, x) : 0;
                 bool hit = false;
-                if (q < wn) {
-                    const int32_t x = __ldg(W + q);
-                    const int p = lower_bound_i32(S, sn, x);
-                    hit = p < sn && __ldg(S + p) == x;
+                if (small) {
+                    const int32_t y = __shfl_sync(FULL, key, b & 31);
+                    hit = e < wn && b < sn && y == x;
+                } else if (bucketed) {
+                    if (e < wn && b < 32) {
+                        const int lo_b = (int)(((int64_t)b * sn) >> 5);
+                        const int hi_b = (int)(((int64_t)(b + 1) * sn) >> 5);
+                        const int pos = lo_b + lower_bound_i32(S + lo_b, hi_b - lo_b, x);
+                        hit = pos < hi_b && __ldg(S + pos) == x;
+                    }
+                } else if (e < wn) {
+                    const int pos = lower_bound_i32(S, sn, x);
+                    hit = pos < sn && __ldg(S + pos) == x;
                 }
                 cnt += __popc(__ballot_sync(FULL, hit));
             }
+            row_cnt += cnt;
         }
-        if (lane == 0 && cnt) {
-            if (per_row) atomicAdd(&per_row[i], cnt);
-            acc_total += cnt;
-        }
+        if (lane == 0 && row_cnt && per_row) atomicAdd(&per_row[i], row_cnt);
+        acc_total += row_cnt;
     }
     if (lane == 0 && acc_total) atomicAdd(total, acc_total);
 }
@@ -189,25 +206,20 @@ static void tc_device(ga_ctx ctx, ga_algo algo, ga_csr A, int64_t* d_total, int6
     unsigned long long* tot = reinterpret_cast<unsigned long long*>(d_total);
     GA_CUDA(cudaMemsetAsync(tot, 0, sizeof(unsigned long long), ctx->stream));
     if (A->m == 0) return;
-    ga_csr L0 = extract_tri(ctx, A, true);
-    CsrGuard g0(ctx, L0);
     if (algo == GA_DOT) {
         const int64_t m = A->m;
-        DBuf<int32_t> ucnt(ctx, (size_t)m + 1), uoff(ctx, (size_t)m + 1);
-        k_tc_unit_count<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(L0->rst, m, ucnt.p);
-        post_launch("tc_unit_count");
-        scan_exclusive_i32(ctx, ucnt.p, uoff.p, m);
-        const int32_t nunits = read_i32(ctx, uoff.p + m);
-        DBuf<int2> units(ctx, (size_t)nunits + 1);
-        k_tc_unit_fill<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(ucnt.p, uoff.p, m, units.p);
-        post_launch("tc_unit_fill");
+        DBuf<int32_t> ust(ctx, (size_t)m + 1);
+        upper_starts(ctx, A, ust.p);
         if (d_per_row) GA_CUDA(cudaMemsetAsync(d_per_row, 0, sizeof(int64_t) * m, ctx->stream));
+        if (A->nnz == 0) return;
         ProfScope ps(ctx, "tc_dot");
-        k_tc_dot<<<grid_for((int64_t)nunits * 32, kTcThreads, ctx->num_sms * 16), kTcThreads, 0, ctx->stream>>>(
-            L0->rst, L0->col, units.p, nunits, tot, reinterpret_cast<unsigned long long*>(d_per_row));
+        k_tc_dot<<<grid_for((A->nnz + kTcChunk - 1) / kTcChunk * 32, kTcThreads, ctx->num_sms * 16), kTcThreads, 0,
+                   ctx->stream>>>(A->rst, A->col, ust.p, m, tot, reinterpret_cast<unsigned long long*>(d_per_row));
         post_launch("tc_dot");
         return;
     }
+    ga_csr L0 = extract_tri(ctx, A, true);
+    CsrGuard g0(ctx, L0);
     // Sandia form with a masked-SpGEMM variant on the unit-valued L
     ga_csr L = adjacency_of(ctx, L0);
     CsrGuard g1(ctx, L);
@@ -456,11 +468,11 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
                 Cu = *C;
                 Cu.rst = ust.p;
                 if (algo == GA_DOT) mxm_dot_launch(ctx, C, C, C, &Cu, sup.p, unit, C->rst + 1);
-                else mxm_masked_launch(ctx, algo, C, C, &Cu, sup.p, mxm_scr.p, cap, unit, C->rst + 1);
+                else mxm_masked_launch(ctx, algo, C, C, &Cu, sup.p, mxm_scr.p, cap, unit, C->rst + 1, unit);
                 k_gather_lower<<<grid_ent, 256, 0, ctx->stream>>>(st.p, C->col, row_of.p, mir.p, sup.p);
                 post_launch("kt_gather_lower");
             } else {
-                mxm_masked_launch(ctx, algo, C, C, C, sup.p, mxm_scr.p, cap, unit);
+                mxm_masked_launch(ctx, algo, C, C, C, sup.p, mxm_scr.p, cap, unit, nullptr, unit);
             }
             // prune: keep flags, their exclusive scan (new positions), scatter
             const int32_t* gid = batch ? batch->gid : nullptr;

@@ -145,6 +145,23 @@ __device__ __forceinline__ int upper_bound_i32(const int32_t* a, int n, int32_t 
     return lo;
 }
 
+// Lower bound of x among 32 ascending values held one per lane (`key`):
+// the first lane whose value is >= x, 32 if none. Six shuffle steps; every
+// lane searches for its own x.
+__device__ __forceinline__ int warp_lower_bound(int32_t key, int32_t x) {
+    int lo = 0, hi = 32;
+#pragma unroll
+    for (int step = 0; step < 6; ++step) {
+        const int mid = (lo + hi) >> 1;
+        const int32_t v = __shfl_sync(0xffffffffu, key, mid & 31);
+        if (lo < hi) {
+            if (v < x) lo = mid + 1;
+            else hi = mid;
+        }
+    }
+    return lo;
+}
+
 }  // namespace ga
 
 // value-type dispatch over a ga_dtype

@@ -219,8 +219,9 @@ ga_csr copy_csr(ga_ctx ctx, ga_csr A, ga_dtype to);
 void mxm_masked_into(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals);
 ga_csr mxm_cmask(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M);
 size_t mxm_scratch_bytes(int64_t m, int64_t n, int64_t mask_nnz);
+// unit_a / unit_b: A's / B's values are all ones (skips value loads).
 void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals, void* scratch,
-                       int64_t cap_nnz, bool unit_b, const int32_t* mask_row_end = nullptr);
+                       int64_t cap_nnz, bool unit_b, const int32_t* mask_row_end = nullptr, bool unit_a = false);
 // Inner-product masked product (GA_DOT): Bt holds B^T (B itself when B is
 // symmetric); unit: A's and B's values are all ones. Allocates nothing.
 // With mask_row_end, M->rst holds row starts of the mask and

@@ -31,12 +31,14 @@
 // are accumulated with shared-memory atomics (order not fixed).
 #include "ga_device.cuh"
 
+#include <type_traits>
+
 namespace ga {
 
 constexpr int kMxmThreads = 512;
 constexpr int kMxmWarps = kMxmThreads / 32;
 constexpr int kCtaSlots = 4096;            // mask slots per CTA work item
-constexpr int kWinCols = 1 << 18;          // column span of a CTA work item
+constexpr int kWinCols = 1 << 17;          // column span of a CTA work item
 constexpr int kWinWords = kWinCols / 32;   // dense bitmap words
 constexpr int kWarpSlots = 256;            // mask slots per warp row
 constexpr int kWarpTblBits = 9;            // warp-row hash table: 512 entries
@@ -187,11 +189,19 @@ __device__ __forceinline__ int slot_of(const SlotView& v, int32_t c) {
     }
 }
 
-// B value of entry j in the accumulator type (1 without a load when B's
-// values are known to be all ones).
-template <bool UB, typename T, typename A>
+// Value modes: VM 0 general, 1 B's values are all ones (no B value loads),
+// 2 A's and B's values are all ones (every product is 1: no value loads or
+// multiplies at all; int32 only).
+// B value of entry j in the accumulator type.
+template <int VM, typename T, typename A>
 __device__ __forceinline__ A bval(const MxmArgs<T, A>& p, int32_t j) {
-    return UB ? (A)1 : to_acc<T, A>(__ldg(p.bv + j));
+    return VM >= 1 ? (A)1 : to_acc<T, A>(__ldg(p.bv + j));
+}
+
+// Product of the A value staged for segment q and a B value.
+template <int VM, typename A>
+__device__ __forceinline__ A seg_product(const A* s_a, int q, A b) {
+    return VM == 2 ? (A)1 : s_a[q] * b;
 }
 
 template <int MD, typename A>
@@ -241,7 +251,7 @@ __device__ __forceinline__ void b_range(const MxmArgs<T, A>& p, int32_t t, bool 
 // reduction), so every lane finds its B row with a popcount - no per-lane
 // search loop. Lanes whose B row is long may hand it to the CTA's long list.
 // Returns the number of products it processed (warp-uniform).
-template <int MD, bool UB, typename T, typename A, bool PUSH>
+template <int MD, int VM, typename T, typename A, bool PUSH>
 __device__ __forceinline__ int group_products(const MxmArgs<T, A>& p, int32_t t_first, int32_t t_end, bool clip,
                                               const SlotView& v, A* acc, int* s_incl, int* s_off, A* s_a,
                                               int* s_nlong, int32_t* s_lbs, int32_t* s_lend, A* s_la) {
@@ -254,7 +264,7 @@ __device__ __forceinline__ int group_products(const MxmArgs<T, A>& p, int32_t t_
     if (t < t_end) {
         int32_t be;
         b_range(p, t, clip, v.lo, v.hi, bs, be);
-        av = to_acc<T, A>(__ldg(p.av + t));
+        av = VM == 2 ? (A)1 : to_acc<T, A>(__ldg(p.av + t));
         len = be - bs;
         if (PUSH && len > kLongSeg) {
             const int slot = atomicAdd(s_nlong, 1);
@@ -275,7 +285,7 @@ __device__ __forceinline__ int group_products(const MxmArgs<T, A>& p, int32_t t_
         const int rank = __popc(nz & ((1u << lane) - 1u));
         s_incl[rank] = incl;
         s_off[rank] = bs - (incl - len);
-        s_a[rank] = av;
+        if (VM != 2) s_a[rank] = av;
     }
     __syncwarp();
     const int my_end = lane < nseg ? s_incl[lane] - 1 : INT32_MAX;  // last product of segment `lane`
@@ -291,16 +301,16 @@ __device__ __forceinline__ int group_products(const MxmArgs<T, A>& p, int32_t t_
         const int x1 = base + 32 + lane;
         const int32_t j0 = base + lane + s_off[q0];
         const int32_t c0 = __ldg(p.bc + j0);
-        const A b0 = bval<UB, T, A>(p, j0);
+        const A b0 = bval<VM, T, A>(p, j0);
         int32_t c1 = 0;
         A b1 = (A)0;
         if (x1 < total) {
             const int32_t j1 = x1 + s_off[q1];
             c1 = __ldg(p.bc + j1);
-            b1 = bval<UB, T, A>(p, j1);
+            b1 = bval<VM, T, A>(p, j1);
         }
-        add_product<MD, A>(v, acc, c0, s_a[q0] * b0);
-        if (x1 < total) add_product<MD, A>(v, acc, c1, s_a[q1] * b1);
+        add_product<MD, A>(v, acc, c0, seg_product<VM, A>(s_a, q0, b0));
+        if (x1 < total) add_product<MD, A>(v, acc, c1, seg_product<VM, A>(s_a, q1, b1));
         q_base += __popc(bm0) + __popc(bm1);
     }
     if (base < total) {
@@ -310,7 +320,7 @@ __device__ __forceinline__ int group_products(const MxmArgs<T, A>& p, int32_t t_
         if (x < total) {
             const int q = q_base + __popc(bm0 & lt);
             const int32_t j = x + s_off[q];
-            add_product<MD, A>(v, acc, __ldg(p.bc + j), s_a[q] * bval<UB, T, A>(p, j));
+            add_product<MD, A>(v, acc, __ldg(p.bc + j), seg_product<VM, A>(s_a, q, bval<VM, T, A>(p, j)));
         }
     }
     __syncwarp();
@@ -319,20 +329,20 @@ __device__ __forceinline__ int group_products(const MxmArgs<T, A>& p, int32_t t_
 
 // Stream B entries [j0, j1) of one row with scalar head/tail and a
 // 16-byte vector body (columns, and values unless they are all ones).
-template <int MD, bool UB, typename T, typename A>
+template <int MD, int VM, typename T, typename A>
 __device__ __forceinline__ void stream_row(const MxmArgs<T, A>& p, const SlotView& v, A* acc, int32_t j0,
                                            int32_t j1, A a) {
     const int lane = threadIdx.x & 31;
     int32_t ja = (j0 + 3) & ~3;
     if (ja > j1) ja = j1;
-    if (j0 + lane < ja) add_product<MD, A>(v, acc, __ldg(p.bc + j0 + lane), a * bval<UB, T, A>(p, j0 + lane));
+    if (j0 + lane < ja) add_product<MD, A>(v, acc, __ldg(p.bc + j0 + lane), a * bval<VM, T, A>(p, j0 + lane));
     const int32_t groups = (j1 - ja) >> 2;
     int32_t g = lane;
     for (; g + 32 < groups; g += 64) {
         const int32_t j = ja + 4 * g, jy = j + 128;
         const Vec4<int32_t> x = load4<int32_t>(p.bc + j);
         const Vec4<int32_t> y = load4<int32_t>(p.bc + jy);
-        if (UB) {
+        if (VM >= 1) {
             add_product<MD, A>(v, acc, x.x, a); add_product<MD, A>(v, acc, x.y, a);
             add_product<MD, A>(v, acc, x.z, a); add_product<MD, A>(v, acc, x.w, a);
             add_product<MD, A>(v, acc, y.x, a); add_product<MD, A>(v, acc, y.y, a);
@@ -353,7 +363,7 @@ __device__ __forceinline__ void stream_row(const MxmArgs<T, A>& p, const SlotVie
     if (g < groups) {
         const int32_t j = ja + 4 * g;
         const Vec4<int32_t> x = load4<int32_t>(p.bc + j);
-        if (UB) {
+        if (VM >= 1) {
             add_product<MD, A>(v, acc, x.x, a); add_product<MD, A>(v, acc, x.y, a);
             add_product<MD, A>(v, acc, x.z, a); add_product<MD, A>(v, acc, x.w, a);
         } else {
@@ -365,7 +375,7 @@ __device__ __forceinline__ void stream_row(const MxmArgs<T, A>& p, const SlotVie
         }
     }
     const int32_t jt = ja + 4 * groups;
-    if (jt + lane < j1) add_product<MD, A>(v, acc, __ldg(p.bc + jt + lane), a * bval<UB, T, A>(p, jt + lane));
+    if (jt + lane < j1) add_product<MD, A>(v, acc, __ldg(p.bc + jt + lane), a * bval<VM, T, A>(p, jt + lane));
 }
 
 // Warp-cooperative sorted merge of B row [bs, be) against the item's sorted
@@ -427,8 +437,8 @@ struct MxmSmem {
     static constexpr size_t total = region + scratch_bytes;
 };
 
-template <int MD, bool UB, typename T, typename A>
-__global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) {
+template <int MD, int VM, typename T, typename A>
+__global__ void __launch_bounds__(kMxmThreads, 3) k_mxm_masked(MxmArgs<T, A> p) {
     extern __shared__ __align__(16) unsigned char smem[];
     using SM = MxmSmem<MD, A>;
     constexpr bool DENSE = MD == MD_DENSE;
@@ -499,7 +509,7 @@ __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) 
             } else {
                 // phase A: short B rows flattened per warp, long ones listed
                 for (int32_t g = ab + wid * 32; g < ae; g += kMxmWarps * 32)
-                    executed += (unsigned long long)group_products<MD, UB, T, A, true>(
+                    executed += (unsigned long long)group_products<MD, VM, T, A, true>(
                         p, g, ae, clip, v, acc, s_incl, s_off, s_a, &s_nlong, lbs, lend, la);
                 __syncthreads();
                 // phase B: long B rows cut into kChunk pieces shared by all warps
@@ -530,7 +540,7 @@ __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) 
                         const int seg = upper_bound_i32(lchunk + 1, nlong, c);
                         const int32_t j0 = lbs[seg] + (c - lchunk[seg]) * kChunk;
                         const int32_t j1 = min(lend[seg], j0 + kChunk);
-                        stream_row<MD, UB, T, A>(p, v, acc, j0, j1, la[seg]);
+                        stream_row<MD, VM, T, A>(p, v, acc, j0, j1, la[seg]);
                         executed += (unsigned long long)(j1 - j0);
                     }
                 }
@@ -596,7 +606,7 @@ __global__ void __launch_bounds__(kMxmThreads, 2) k_mxm_masked(MxmArgs<T, A> p) 
                 }
             } else {
                 for (int32_t g = ab; g < ae; g += 32)
-                    executed += (unsigned long long)group_products<WMD, UB, T, A, false>(
+                    executed += (unsigned long long)group_products<WMD, VM, T, A, false>(
                         p, g, ae, clip, v, acc, s_incl, s_off, s_a, nullptr, nullptr, nullptr, nullptr);
             }
             __syncwarp();
@@ -620,7 +630,7 @@ static int64_t cta_item_cap(int64_t m, int64_t n, int64_t mask_nnz) {
 }
 
 // Launch the masked product for one value type and lookup variant.
-template <int LK, bool UB, typename T>
+template <int LK, int VM, typename T>
 static void launch_masked(ga_ctx ctx, ga_csr A_, ga_csr B_, ga_csr M_, T* cv, MxmQueue* q, int32_t* warp_rows,
                           int4* cta_items, int32_t cta_cap, const int32_t* mre) {
     using Ac = typename Acc<T>::type;
@@ -639,7 +649,7 @@ static void launch_masked(ga_ctx ctx, ga_csr A_, ga_csr B_, ga_csr M_, T* cv, Mx
         post_launch("mxm_row_bin");
     }
     const size_t smem = MxmSmem<LK, Ac>::total;
-    auto kern = k_mxm_masked<LK, UB, T, Ac>;
+    auto kern = k_mxm_masked<LK, VM, T, Ac>;
     GA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     GA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMxmThreads, smem));
@@ -732,12 +742,40 @@ __global__ void __launch_bounds__(kDotThreads) k_mxm_dot(DotArgs<T> p) {
                 const int32_t* Sc = walk_a ? p.tc + tb : p.ac + ab;
                 const int wn = walk_a ? an : tn, sn = walk_a ? tn : an;
                 if (lane == 0) executed += (unsigned long long)wn;
+                // The searched list in registers: up to 32 entries one per
+                // lane (searched by shuffles, no memory access), else, when
+                // 32 or more entries are walked, the last entry of each of 32
+                // equal buckets (the shuffle search picks the bucket, a
+                // binary search in memory finishes); else a plain binary
+                // search.
+                // bucket splitters pay off only when at least 32 entries are walked
+                const bool small = sn <= 32, bucketed = !small && wn >= 32;
+                int32_t key = INT32_MAX;
+                if (small) {
+                    key = lane < sn ? __ldg(Sc + lane) : INT32_MAX;
+                } else if (bucketed) {
+                    const int hi_b = (int)(((int64_t)(lane + 1) * sn) >> 5);
+                    key = __ldg(Sc + hi_b - 1);
+                }
                 for (int base = 0; base < wn; base += 32) {
                     const int e = base + lane;
+                    const int32_t x = e < wn ? __ldg(Wc + e) : INT32_MAX;
+                    // first register entry >= x (32: none)
+                    const int b = (small || bucketed) ? warp_lower_bound(key, x) : 0;
                     bool hit = false;
                     int pos = 0;
-                    if (e < wn) {
-                        const int32_t x = __ldg(Wc + e);
+                    if (small) {
+                        const int32_t y = __shfl_sync(FULL, key, b & 31);
+                        pos = b;
+                        hit = e < wn && b < sn && y == x;
+                    } else if (bucketed) {
+                        if (e < wn && b < 32) {
+                            const int lo_b = (int)(((int64_t)b * sn) >> 5);
+                            const int hi_b = (int)(((int64_t)(b + 1) * sn) >> 5);
+                            pos = lo_b + lower_bound_i32(Sc + lo_b, hi_b - lo_b, x);
+                            hit = pos < hi_b && __ldg(Sc + pos) == x;
+                        }
+                    } else if (e < wn) {
                         pos = lower_bound_i32(Sc, sn, x);
                         hit = pos < sn && __ldg(Sc + pos) == x;
                     }
@@ -805,7 +843,7 @@ size_t mxm_scratch_bytes(int64_t m, int64_t n, int64_t mask_nnz) {
 // unit_b: B's values are all ones (no value loads). mask_row_end (optional):
 // row i's mask is [M->rst[i], mask_row_end[i]) instead of the whole row.
 void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals, void* scratch,
-                       int64_t cap_nnz, bool unit_b, const int32_t* mask_row_end) {
+                       int64_t cap_nnz, bool unit_b, const int32_t* mask_row_end, bool unit_a) {
     GA_REQUIRE(algo == GA_MSA || algo == GA_MCA || algo == GA_HEAP, GA_ERR_INVALID_ARG, "mxm: unknown algorithm");
     unsigned char* s = static_cast<unsigned char*>(scratch);
     MxmQueue* q = reinterpret_cast<MxmQueue*>(s);
@@ -820,14 +858,17 @@ void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, v
     GA_DISPATCH_DTYPE(A->dtype, T, {
         T* cv = static_cast<T*>(d_cvals);
         const int32_t c32 = (int32_t)cap;
+        // value mode 2 (every product is 1) only for int32, the k-truss / TC type
+        const bool ones = unit_a && unit_b && std::is_same<T, int32_t>::value;
         if (algo == GA_MSA) {
-            if (unit_b) launch_masked<MD_DENSE, true, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
-            else launch_masked<MD_DENSE, false, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
+            if (ones) launch_masked<MD_DENSE, 2, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
+            else if (unit_b) launch_masked<MD_DENSE, 1, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
+            else launch_masked<MD_DENSE, 0, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
         } else if (algo == GA_MCA) {
-            if (unit_b) launch_masked<MD_BSEARCH, true, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
-            else launch_masked<MD_BSEARCH, false, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
+            if (unit_b) launch_masked<MD_BSEARCH, 1, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
+            else launch_masked<MD_BSEARCH, 0, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
         } else {
-            launch_masked<MD_MERGE, false, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
+            launch_masked<MD_MERGE, 0, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
         }
     });
 }
@@ -860,8 +901,9 @@ void mxm_masked_into(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, voi
         return;
     }
     const bool unit_b = csr_unit_values(ctx, B);
+    const bool unit_a = unit_b && A->dtype == GA_INT32 && csr_unit_values(ctx, A);
     DBuf<unsigned char> scratch(ctx, mxm_scratch_bytes(M->m, M->n, M->nnz));
-    mxm_masked_launch(ctx, algo, A, B, M, d_cvals, scratch.p, M->nnz, unit_b);
+    mxm_masked_launch(ctx, algo, A, B, M, d_cvals, scratch.p, M->nnz, unit_b, nullptr, unit_a);
 }
 
 }  // namespace ga

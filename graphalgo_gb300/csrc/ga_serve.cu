@@ -189,6 +189,10 @@ static void run_single(Server* s, ga_ctx ctx, SrvReq* r) {
     fill_error(r, rc, ctx);
 }
 
+// Batched calls run on unions whose sizes change from call to call: with
+// GA_AUTO they use MSA rather than tune each new union.
+static ga_algo group_algo(int a) { return a == GA_AUTO ? GA_MSA : (ga_algo)a; }
+
 static void run_group(Server* s, ga_ctx ctx, std::vector<SrvReq*>& group) {
     // distinct graphs of the group, in first-seen order
     std::vector<int> order;
@@ -203,13 +207,13 @@ static void run_group(Server* s, ga_ctx ctx, std::vector<SrvReq*>& group) {
     int rc = ga_csr_block_diag(ctx, count, parts.data(), &U, voff.data());
     if (rc == GA_OK && group[0]->type == GA_REQ_TC) {
         std::vector<int64_t> totals((size_t)count);
-        rc = ga_batch_tc(ctx, (ga_algo)s->cfg.tc_algo, U, count, voff.data(), totals.data());
+        rc = ga_batch_tc(ctx, group_algo(s->cfg.tc_algo), U, count, voff.data(), totals.data());
         if (rc == GA_OK)
             for (SrvReq* r : group) r->res.tc_total = totals[(size_t)slot[r->graph]];
     } else if (rc == GA_OK) {
         ga_csr C = nullptr;
         std::vector<int> iters((size_t)count);
-        rc = ga_batch_ktruss(ctx, (ga_algo)s->cfg.ktruss_algo, U, count, voff.data(), group[0]->k, &C, iters.data());
+        rc = ga_batch_ktruss(ctx, group_algo(s->cfg.ktruss_algo), U, count, voff.data(), group[0]->k, &C, iters.data());
         if (rc == GA_OK) {
             bool edges = false;
             for (SrvReq* r : group) edges = edges || r->want_edges;

@@ -29,7 +29,7 @@ struct TuneEntry {
     int candidates = 0;
 };
 
-using TuneKey = std::tuple<int, int, int, int, int, int, int, int>;
+using TuneKey = std::tuple<int, int, int, int, int, int, int, int, int>;
 
 std::mutex g_tune_mu;
 std::map<TuneKey, TuneEntry> g_tune_cache;
@@ -44,14 +44,22 @@ MxmTune tune_of(int64_t warp_max, int ctas, int chunk) {
     return t;
 }
 
-std::vector<Cand> product_candidates(bool dot_ok) {
+// Candidates, the default MSA schedule first; `only` >= 0 keeps one variant
+// (its schedules only).
+std::vector<Cand> product_candidates(bool dot_ok, int only) {
     std::vector<Cand> c;
-    c.push_back({GA_MSA, MxmTune()});  // the default schedule first
-    c.push_back({GA_MSA, tune_of(8192, 0, 8)});
-    c.push_back({GA_MSA, tune_of(131072, 0, 8)});
-    c.push_back({GA_MSA, tune_of(32768, 1, 8)});
-    c.push_back({GA_MCA, MxmTune()});
-    if (dot_ok)
+    if (only < 0 || only == GA_MSA) {
+        c.push_back({GA_MSA, MxmTune()});
+        c.push_back({GA_MSA, tune_of(8192, 0, 8)});
+        c.push_back({GA_MSA, tune_of(131072, 0, 8)});
+        c.push_back({GA_MSA, tune_of(32768, 1, 8)});
+        c.push_back({GA_MSA, tune_of(131072, 1, 8)});
+    }
+    if (only < 0 || only == GA_MCA) {
+        c.push_back({GA_MCA, MxmTune()});
+        if (only == GA_MCA) c.push_back({GA_MCA, tune_of(131072, 0, 8)});
+    }
+    if (dot_ok && (only < 0 || only == GA_DOT))
         for (int chunk : {4, 8, 16}) c.push_back({GA_DOT, tune_of(32768, 0, chunk)});
     return c;
 }
@@ -122,7 +130,7 @@ TuneEntry pick(ga_ctx ctx, const std::vector<Cand>& cands, const std::function<v
     return best;
 }
 
-TuneEntry tune_support(ga_ctx ctx, ga_csr A) {
+TuneEntry tune_support(ga_ctx ctx, ga_csr A, int only) {
     const int64_t m = A->m, nnz = A->nnz;
     const bool sym = csr_is_symmetric(ctx, A);
     const bool unit = csr_unit_values(ctx, A);
@@ -135,31 +143,36 @@ TuneEntry tune_support(ga_ctx ctx, ga_csr A) {
     }
     ga_csr M = sym ? &Au : A;
     const int32_t* mre = sym ? A->rst + 1 : nullptr;
-    return pick(ctx, product_candidates(sym), [&](const Cand& c) {
+    return pick(ctx, product_candidates(sym, only), [&](const Cand& c) {
         if (c.algo == GA_DOT) mxm_dot_launch(ctx, A, A, A, M, sup.p, unit, mre);
-        else mxm_masked_launch(ctx, c.algo, A, A, M, sup.p, scr.p, nnz, unit, mre);
+        else mxm_masked_launch(ctx, c.algo, A, A, M, sup.p, scr.p, nnz, unit, mre, unit);
     });
 }
 
-TuneEntry tune_product(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M) {
+TuneEntry tune_product(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M, int only) {
     DBuf<unsigned char> cv(ctx, (size_t)(M->nnz + 1) * dtype_size(A->dtype));
-    return pick(ctx, product_candidates(true), [&](const Cand& c) { mxm_masked_into(ctx, c.algo, A, B, M, cv.p); });
+    return pick(ctx, product_candidates(true, only),
+                [&](const Cand& c) { mxm_masked_into(ctx, c.algo, A, B, M, cv.p); });
 }
 
-TuneEntry tune_tc(ga_ctx ctx, ga_csr A) {
+TuneEntry tune_tc(ga_ctx ctx, ga_csr A, int only) {
     DBuf<int64_t> tot(ctx, 1);
-    std::vector<Cand> c = {{GA_MSA, MxmTune()}, {GA_DOT, MxmTune()}, {GA_MCA, MxmTune()},
-                           {GA_MSA, tune_of(8192, 0, 8)}};
+    std::vector<Cand> all = {{GA_MSA, MxmTune()}, {GA_DOT, MxmTune()}, {GA_MCA, MxmTune()},
+                             {GA_MSA, tune_of(8192, 0, 8)}, {GA_MSA, tune_of(131072, 0, 8)}};
+    std::vector<Cand> c;
+    for (const Cand& x : all)
+        if (only < 0 || x.algo == only) c.push_back(x);
     return pick(ctx, c, [&](const Cand& x) {
         const int rc = ga_tc_device(ctx, x.algo, A, tot.p, nullptr);
         if (rc != GA_OK) fail(rc, ctx->last_error);
     });
 }
 
-TuneEntry lookup_or_tune(ga_ctx ctx, int kind, ga_csr A, ga_csr B, ga_csr M, bool force, bool* cached) {
+TuneEntry lookup_or_tune(ga_ctx ctx, int kind, ga_csr A, ga_csr B, ga_csr M, bool force, bool* cached,
+                         int only = -1) {
     const bool sym = csr_is_symmetric(ctx, A);
     const TuneKey key{ctx->device, kind, bucket(A->m), bucket(A->n), bucket(A->nnz), bucket(B ? B->nnz : 0),
-                      bucket(M ? M->nnz : 0), sym ? 1 : 0};
+                      bucket(M ? M->nnz : 0), sym ? 1 : 0, only};
     if (!force) {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune_cache.find(key);
@@ -168,9 +181,9 @@ TuneEntry lookup_or_tune(ga_ctx ctx, int kind, ga_csr A, ga_csr B, ga_csr M, boo
             return it->second;
         }
     }
-    TuneEntry e = kind == GA_TUNE_KTRUSS ? tune_support(ctx, A)
-                  : kind == GA_TUNE_TC   ? tune_tc(ctx, A)
-                                         : tune_product(ctx, A, B, M);
+    TuneEntry e = kind == GA_TUNE_KTRUSS ? tune_support(ctx, A, only)
+                  : kind == GA_TUNE_TC   ? tune_tc(ctx, A, only)
+                                         : tune_product(ctx, A, B, M, only);
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune_cache[key] = e;
@@ -212,14 +225,22 @@ using namespace ga;
 extern "C" {
 
 int ga_autotune(ga_ctx ctx, int kind, ga_csr A, ga_csr B, ga_csr M, int force, ga_tune_result* out) {
+    return ga_autotune_variant(ctx, kind, -1, A, B, M, force, out);
+}
+
+int ga_autotune_variant(ga_ctx ctx, int kind, int algo, ga_csr A, ga_csr B, ga_csr M, int force,
+                        ga_tune_result* out) {
     if (!ctx || !A || !out) return GA_ERR_INVALID_ARG;
+    if (algo != -1 && algo != GA_MSA && algo != GA_MCA && algo != GA_DOT) return GA_ERR_INVALID_ARG;
     if (kind != GA_TUNE_KTRUSS && kind != GA_TUNE_TC && kind != GA_TUNE_PRODUCT) return GA_ERR_INVALID_ARG;
     if (kind == GA_TUNE_PRODUCT && (!B || !M)) return GA_ERR_INVALID_ARG;
     GA_API_BODY(ctx, {
         GA_REQUIRE(kind == GA_TUNE_PRODUCT || A->m == A->n, GA_ERR_SHAPE, "autotune: square matrix expected");
         GA_REQUIRE(A->nnz > 0, GA_ERR_INVALID_ARG, "autotune: empty matrix");
         bool cached = false;
-        const TuneEntry e = lookup_or_tune(ctx, kind, A, B, M, force != 0, &cached);
+        if (algo == GA_DOT && kind == GA_TUNE_KTRUSS)
+            GA_REQUIRE(csr_is_symmetric(ctx, A), GA_ERR_UNSUPPORTED, "autotune: GA_DOT k-truss needs a symmetric matrix");
+        const TuneEntry e = lookup_or_tune(ctx, kind, A, B, M, force != 0, &cached, algo);
         out->algo = e.algo;
         out->warp_max_flops = e.t.warp_max_flops;
         out->heavy_flops = e.t.heavy_flops;

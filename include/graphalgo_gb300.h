@@ -214,8 +214,8 @@ GA_API int ga_mxm_masked_vals(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_c
  * GA_HEAP; b_unit != 0 promises that B's values are all 1 (they are then not
  * read). The work runs on `stream` (NULL: the default stream) and is not
  * synchronised. Returns GA_ERR_INVALID_ARG when the scratch this shape needs
- * - 256 + 4(m+1) + 16 + 16 min(m(1 + ceil(n/2^18)) + mask_nnz/4096 + 1,
- * mask_nnz + 1) bytes - exceeds 16 MiB (about 460k rows when n <= 2^18).
+ * - 256 + 4(m+1) + 16 + 16 min(m(1 + ceil(n/2^17)) + mask_nnz/4096 + 1,
+ * mask_nnz + 1) bytes - exceeds 16 MiB (about 460k rows when n <= 2^17).
  * The first call on a device looks up the array's device address for that
  * device; make that first call before any stream capture. Calls share the
  * array: two calls whose work overlaps on the GPU race with each other, so
@@ -306,6 +306,11 @@ typedef struct {
     int cached;             /* 1: taken from the cache, no timing run */
 } ga_tune_result;
 GA_API int ga_autotune(ga_ctx ctx, int kind, ga_csr A, ga_csr B, ga_csr M, int force, ga_tune_result* out);
+/* The same restricted to one variant (GA_MSA, GA_MCA or GA_DOT; -1: any):
+ * tunes that variant's schedule only. To run it, set the result's schedule
+ * with ga_ctx_set_option and call with that variant. */
+GA_API int ga_autotune_variant(ga_ctx ctx, int kind, int algo, ga_csr A, ga_csr B, ga_csr M, int force,
+                               ga_tune_result* out);
 
 /* ------------------------------------------------------ batched graphs */
 /* Many independent graphs as one block-diagonal matrix: rows (and columns)
@@ -351,8 +356,8 @@ enum { GA_REQ_TC = 0, GA_REQ_KTRUSS = 1, GA_REQ_BC = 2 };
 typedef struct {
     int workers;                   /* worker threads (1..64); 0: 4 */
     int coalesce;                  /* 1: batch queued small TC / k-truss requests */
-    int tc_algo;                   /* ga_algo of TC (GA_MSA, GA_MCA, GA_HEAP, GA_NAIVE, GA_DOT) */
-    int ktruss_algo;               /* ga_algo of k-truss (GA_MSA, GA_MCA, GA_HEAP) */
+    int tc_algo;                   /* ga_algo of TC (any; GA_AUTO: tuned per graph, MSA for batched calls) */
+    int ktruss_algo;               /* ga_algo of k-truss (GA_MSA, GA_MCA, GA_HEAP, GA_DOT, GA_AUTO as for TC) */
     int64_t hbm_budget;            /* bytes the calls in flight may hold; 0: 80% of free memory at creation */
     int64_t coalesce_nnz;          /* graphs with at most this many stored entries are batched; 0: 2^20 */
     int64_t coalesce_max_nnz;      /* stored entries of one batched union at most; 0: 2^26 */
