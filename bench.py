@@ -58,8 +58,9 @@ def parse_args():
     ap.add_argument("--kmin", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-tune", action="store_true",
-                    help="k-truss sweep: keep the default bin thresholds instead of the tuned ones")
+    ap.add_argument("--tune", action="store_true",
+                    help="k-truss sweep: use the bin thresholds tuned on the first support product "
+                         "(slower over the whole sweep, whose later graphs are small)")
     ap.add_argument("--no-other-configs", action="store_true",
                     help="skip the TC (Erdos-Renyi n=1000) and BC (R-MAT 20) measurements")
     ap.add_argument("--cpu-reps", type=int, default=2)
@@ -432,7 +433,7 @@ def run_gpu(args, dist: Dist):
     A = ga.Csr.upload(ctx, m, m, rst, col, val)
     # the variant's bin thresholds and grid size, tuned on the first support product
     schedule = None
-    if not args.no_tune and args.algo in ("msa", "mca", "dot"):
+    if args.tune and args.algo in ("msa", "mca", "dot"):
         schedule = ga.autotune(ga.TUNE_KTRUSS, A, only=args.algo)
         ga.apply_schedule(ctx, schedule)
 

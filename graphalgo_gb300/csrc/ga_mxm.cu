@@ -23,7 +23,8 @@
 //                 mask row (replaces the priority-queue merge,
 //                 matrix_la.h:1030-1084).
 //     Work distribution inside a CTA item: warps take the row's A entries 32
-//     at a time; B rows of up to kLongSeg entries are flattened over the
+//     at a time; B rows of up to kLongSeg entries (32 when the A row is too
+//     short to occupy every warp) are flattened over the
 //     warp's lanes (warp scan of the lengths, lanes walk the flattened index);
 //     longer B rows (hubs) go to a shared list and are cut into kChunk-entry
 //     pieces that all warps of the CTA stream coalesced.
@@ -48,6 +49,8 @@ constexpr int kFilterBits = 12;            // warp-row filter: 4096 bits
 // persistent grid size are runtime parameters (ga_ctx tune, set by options
 // or the autotuner).
 constexpr int kLongSeg = 256;              // B rows longer than this are shared by the CTA
+constexpr int kShortARow = kMxmThreads;    // A rows with fewer entries leave warps idle in phase A:
+constexpr int kLongSegShort = 32;          // their B rows longer than this are shared instead
 constexpr int kLongCap = 1024;             // long B rows listed per item
 constexpr int kChunk = 1024;               // entries per long-row piece
 
@@ -254,7 +257,8 @@ __device__ __forceinline__ void b_range(const MxmArgs<T, A>& p, int32_t t, bool 
 template <int MD, int VM, typename T, typename A, bool PUSH>
 __device__ __forceinline__ int group_products(const MxmArgs<T, A>& p, int32_t t_first, int32_t t_end, bool clip,
                                               const SlotView& v, A* acc, int* s_incl, int* s_off, A* s_a,
-                                              int* s_nlong, int32_t* s_lbs, int32_t* s_lend, A* s_la) {
+                                              int* s_nlong, int32_t* s_lbs, int32_t* s_lend, A* s_la,
+                                              int long_seg = kLongSeg) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int32_t t = t_first + lane;
@@ -266,7 +270,7 @@ __device__ __forceinline__ int group_products(const MxmArgs<T, A>& p, int32_t t_
         b_range(p, t, clip, v.lo, v.hi, bs, be);
         av = VM == 2 ? (A)1 : to_acc<T, A>(__ldg(p.av + t));
         len = be - bs;
-        if (PUSH && len > kLongSeg) {
+        if (PUSH && len > long_seg) {
             const int slot = atomicAdd(s_nlong, 1);
             if (slot < kLongCap) {
                 s_lbs[slot] = bs;
@@ -508,9 +512,12 @@ __global__ void __launch_bounds__(kMxmThreads, 3) k_mxm_masked(MxmArgs<T, A> p) 
                 }
             } else {
                 // phase A: short B rows flattened per warp, long ones listed
+                // (an A row too short to give every warp 32 entries lists
+                // its B rows from 32 entries up, so all warps share them)
+                const int long_seg = ae - ab < kShortARow ? kLongSegShort : kLongSeg;
                 for (int32_t g = ab + wid * 32; g < ae; g += kMxmWarps * 32)
                     executed += (unsigned long long)group_products<MD, VM, T, A, true>(
-                        p, g, ae, clip, v, acc, s_incl, s_off, s_a, &s_nlong, lbs, lend, la);
+                        p, g, ae, clip, v, acc, s_incl, s_off, s_a, &s_nlong, lbs, lend, la, long_seg);
                 __syncthreads();
                 // phase B: long B rows cut into kChunk pieces shared by all warps
                 const int nlong = min(s_nlong, kLongCap);
