@@ -883,6 +883,21 @@ def run_serve(args, dist: Dist):
             r = serve_run(ga, pool, reqs, w, c, arrivals, algo=al)
             row[name] = {k: r[k] for k in ("req_s", "p50_ms", "p99_ms")}
         sweep.append(row)
+    # the same request mix on the pool's small graphs (<= 2^20 stored entries),
+    # where per-request overheads, not one graph's kernels, bound the rate
+    light = [g for g in pool if len(g[3]) <= (1 << 20)]
+    light_mix = None
+    if light:
+        reqs_l = serve_requests(args, light)
+        pl = serve_run(ga, light, reqs_l, 1, False, algo=al)
+        sl = serve_run(ga, light, reqs_l, args.workers, True, algo=al)
+        light_mix = {"graphs": [g[0] for g in light], "requests": len(reqs_l),
+                     "server": {k: sl[k] for k in ("req_s", "p50_ms", "p99_ms", "makespan_s")},
+                     "plain": {k: pl[k] for k in ("req_s", "p50_ms", "p99_ms", "makespan_s")},
+                     "speedup": sl["req_s"] / pl["req_s"],
+                     "results_equal": serve_same(serve_digest(ga, reqs_l, pl["results"]),
+                                                 serve_digest(ga, reqs_l, sl["results"])),
+                     "batched_calls": sl["stats"]["batched_calls"], "max_group": sl["stats"]["max_group"]}
     value = srv["req_s"]
     h2d = sum(4 * len(src) for (t, _, _, src) in reqs if src is not None)
     line = {
@@ -907,6 +922,7 @@ def run_serve(args, dist: Dist):
                       "speedup": value / plain["req_s"], "results_equal": same,
                       "server_stats": srv["stats"]},
         "poisson": sweep,
+        "light_mix": light_mix,
     }
     ctx.close()
     return line

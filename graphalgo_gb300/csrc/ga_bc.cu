@@ -36,6 +36,9 @@ struct BcState {
     int32_t entries;  // entries appended so far (store size)
     int32_t rows;     // frontier rows appended so far
     int32_t overflow;
+    int32_t mode;          // forward direction of the current level: 0 pull, 1 push
+    int32_t ntouched;      // vertices reached by the current push level
+    unsigned long long cur_work, next_work;  // sum over frontier rows of entries x out-degree
 };
 
 struct BcArgs {
@@ -58,7 +61,17 @@ struct BcArgs {
     double* bc;
     const int32_t* heavy_in;  // vertices with more than kBcHeavyDeg in-neighbours
     int nheavy_in;
+    int64_t nnz;            // stored entries of A (direction choice)
+    uint32_t* tbits;        // push levels: m x words, sources that reached each vertex
+    int32_t* tlist;         // push levels: vertices reached, in order of first touch
+    int32_t* tmark;         // push levels: vertex already listed
 };
+
+// A level pushes (frontier rows scatter along their out-edges with global
+// atomics) when its frontier's work, entries x out-degree, is below
+// nnz / kBcPushDiv; otherwise every unvisited vertex pulls (no atomics on
+// global memory, but a pass over all in-edges).
+constexpr unsigned long long kBcPushDiv = 8;
 
 __global__ void k_bc_init(BcArgs p) {
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < p.ns; j += gridDim.x * blockDim.x) {
@@ -70,12 +83,26 @@ __global__ void k_bc_init(BcArgs p) {
         atomicAdd(&p.vcnt[v], 1);
         p.cur_start[0][v] = j;
         p.cur_len[0][v] = 1;
+        atomicAdd(&p.st->next_work, (unsigned long long)(p.ar[v + 1] - p.ar[v]));
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        p.st->d = 0; p.st->depth = 0; p.st->k = 0; p.st->done = 0;
-        p.st->entries = p.ns; p.st->rows = 0; p.st->overflow = 0;
-        p.level_rows[0] = 0;
-    }
+}
+
+__global__ void k_bc_state_init(BcArgs p) {
+    p.st->d = 0; p.st->depth = 0; p.st->k = 0; p.st->done = 0;
+    p.st->entries = p.ns; p.st->rows = 0; p.st->overflow = 0;
+    p.st->mode = 0; p.st->ntouched = 0;
+    p.st->cur_work = 0; p.st->next_work = 0;
+    p.level_rows[0] = 0;
+}
+
+// Level start: the frontier's work decides the direction.
+__global__ void k_bc_level_begin(BcArgs p) {
+    BcState* st = p.st;
+    if (st->done) return;
+    st->cur_work = st->next_work;
+    st->next_work = 0;
+    st->ntouched = 0;
+    st->mode = st->cur_work * kBcPushDiv < (unsigned long long)p.nnz ? 1 : 0;
 }
 
 // Vertices with more than kBcHeavyDeg neighbours are handled by a whole CTA
@@ -159,6 +186,7 @@ __device__ __forceinline__ void bc_emit_row(const BcArgs& p, int64_t v, int32_t*
         } else {
             p.rv[r] = (int32_t)v; p.rs[r] = start; p.rl[r] = count;
             p.vcnt[v] += count;
+            atomicAdd(&p.st->next_work, (unsigned long long)count * (unsigned long long)(p.ar[v + 1] - p.ar[v]));
         }
         nxtS[v] = start;
         nxtL[v] = start < 0 ? 0 : count;
@@ -209,7 +237,7 @@ __global__ void __launch_bounds__(kBcThreads) k_bc_forward(BcArgs p) {
     double* acc0; uint32_t* touched0; uint32_t* vis0; int* i0; int* o0; double* a0;
     region(0, acc0, touched0, vis0, i0, o0, a0);
 
-    if (p.st->done) return;
+    if (p.st->done || p.st->mode != 0) return;
     const int d = p.st->d;
     const int par = d & 1;
     const int32_t* curS = p.cur_start[par];
@@ -252,6 +280,97 @@ __global__ void __launch_bounds__(kBcThreads) k_bc_forward(BcArgs p) {
         for (int32_t g = ab; g < ae; g += 32)
             bc_pull_group<UNIT>(p, curS, curL, g, ae, vis, acc, touched, s_incl, s_off, s_a);
         bc_emit_row(p, v, nxtS, nxtL, vis, acc, touched);
+    }
+}
+
+// Push level, one frontier row (vertex u, entries [e0, e0+len)) and the
+// out-neighbours [t0, t1) of u, lanes over neighbours 32 at a time (group
+// stride `step`): for every entry (source s, sigma) and neighbour w that s has
+// not reached, W[w][s] += A[u][w] * sigma, and w's touched bit for s is set;
+// the first touch of w lists it.
+template <bool UNIT>
+__device__ __forceinline__ void bc_push_row(const BcArgs& p, int32_t e0, int32_t len, int32_t t0, int32_t t1,
+                                            int32_t step) {
+    const int lane = threadIdx.x & 31;
+    for (int32_t g = t0; g < t1; g += step) {
+        const int32_t t = g + lane;
+        if (t >= t1) continue;
+        const int32_t w = __ldg(p.ac + t);
+        const double a = UNIT ? 1.0 : __ldg(p.av + t);
+        const uint32_t* vis = p.vbits + (size_t)w * p.words;
+        for (int e = 0; e < len; ++e) {
+            const int s = p.es[e0 + e];
+            const uint32_t bit = 1u << (s & 31);
+            if (vis[s >> 5] & bit) continue;
+            atomicAdd(&p.W[(size_t)w * p.ns + s], a * p.ev[e0 + e]);
+            const uint32_t old = atomicOr(&p.tbits[(size_t)w * p.words + (s >> 5)], bit);
+            if (old == 0u && atomicExch(&p.tmark[w], 1) == 0) p.tlist[atomicAdd(&p.st->ntouched, 1)] = w;
+        }
+    }
+}
+
+// Frontier items of level d: the sources at level 0, else the rows found
+// while level d-1 ran, [level_rows[d-1], level_rows[d]).
+__device__ __forceinline__ void bc_frontier_item(const BcArgs& p, int d, int64_t it, int32_t& u, int32_t& e0,
+                                                 int32_t& len) {
+    if (d == 0) {
+        u = p.sources[it]; e0 = (int32_t)it; len = 1;
+    } else {
+        const int64_t r = p.level_rows[d - 1] + it;
+        u = p.rv[r]; e0 = p.rs[r]; len = p.rl[r];
+    }
+}
+
+template <bool UNIT>
+__global__ void __launch_bounds__(kBcThreads) k_bc_push(BcArgs p) {
+    const BcState* st = p.st;
+    if (st->done || st->mode != 1) return;
+    const int d = st->d;
+    const int wid = threadIdx.x >> 5;
+    const int64_t items = d == 0 ? p.ns : (int64_t)p.level_rows[d] - p.level_rows[d - 1];
+    // rows of high-degree vertices: the CTA's warps split the neighbours
+    for (int64_t it = blockIdx.x; it < items; it += gridDim.x) {
+        int32_t u, e0, len;
+        bc_frontier_item(p, d, it, u, e0, len);
+        const int32_t ab = p.ar[u], ae = p.ar[u + 1];
+        if (ae - ab <= kBcHeavyDeg) continue;
+        bc_push_row<UNIT>(p, e0, len, ab + wid * 32, ae, kBcWarps * 32);
+    }
+    const int64_t warps = (int64_t)gridDim.x * kBcWarps;
+    for (int64_t it = (int64_t)blockIdx.x * kBcWarps + wid; it < items; it += warps) {
+        int32_t u, e0, len;
+        bc_frontier_item(p, d, it, u, e0, len);
+        const int32_t ab = p.ar[u], ae = p.ar[u + 1];
+        if (ae - ab > kBcHeavyDeg) continue;
+        bc_push_row<UNIT>(p, e0, len, ab, ae, 32);
+    }
+}
+
+// Push level, after the scatter: every vertex's next-frontier length is
+// cleared, then each reached vertex appends its row (one warp each) from its
+// W row and touched bits, which are reset.
+__global__ void k_bc_push_clear(BcArgs p) {
+    const BcState* st = p.st;
+    if (st->done || st->mode != 1) return;
+    int32_t* nxtL = p.cur_len[(st->d & 1) ^ 1];
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < p.m; v += (int64_t)gridDim.x * blockDim.x)
+        nxtL[v] = 0;
+}
+
+__global__ void __launch_bounds__(kBcThreads) k_bc_push_emit(BcArgs p) {
+    const BcState* st = p.st;
+    if (st->done || st->mode != 1) return;
+    const int lane = threadIdx.x & 31;
+    const int par = st->d & 1;
+    int32_t* nxtS = p.cur_start[par ^ 1];
+    int32_t* nxtL = p.cur_len[par ^ 1];
+    const int n = st->ntouched;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+        const int32_t w = p.tlist[i];
+        bc_emit_row(p, w, nxtS, nxtL, p.vbits + (size_t)w * p.words, p.W + (size_t)w * p.ns,
+                    p.tbits + (size_t)w * p.words);
+        if (lane == 0) p.tmark[w] = 0;
     }
 }
 
@@ -422,31 +541,18 @@ __global__ void k_bc_backward_finalize(BcArgs p, LoopCtl ctl) {
     loop_continue(ctl, st->k >= 1);
 }
 
-// checks: self-loops, symmetric pattern and values, unit values
-__global__ void k_bc_checks(const int32_t* __restrict__ r, const int32_t* __restrict__ c,
-                            const double* __restrict__ v, int64_t m, int* __restrict__ flags) {
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    const int lane = threadIdx.x & 31;
-    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < m; i += warps) {
-        int bad_loop = 0, asym = 0, nonunit = 0;
-        for (int32_t q = r[i] + lane; q < r[i + 1]; q += 32) {
-            int32_t j = c[q];
-            if (j == (int32_t)i) bad_loop = 1;
-            if (v[q] != 1.0) nonunit = 1;
-            int32_t jb = r[j], jn = r[j + 1] - jb;
-            int pos = lower_bound_i32(c + jb, jn, (int32_t)i);
-            if (pos >= jn || c[jb + pos] != (int32_t)i || v[jb + pos] != v[q]) asym = 1;
-        }
-        int f = (bad_loop ? 1 : 0) | (asym ? 2 : 0) | (nonunit ? 4 : 0);
-        f = __reduce_or_sync(0xffffffffu, f);
-        if (lane == 0 && f) atomicOr(flags, f);
+// Per vertex (one thread): a self-loop (flags bit 1; rows are sorted, so a
+// binary search finds it) and the list of vertices with more than
+// kBcHeavyDeg in-neighbours (count in flags[1]).
+__global__ void k_bc_scan_vertices(const int32_t* __restrict__ r, const int32_t* __restrict__ c,
+                                   const int32_t* __restrict__ tr, int64_t m, int32_t* __restrict__ heavy,
+                                   int* __restrict__ flags) {
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < m; v += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t b = r[v], n = r[v + 1] - b;
+        const int pos = lower_bound_i32(c + b, n, (int32_t)v);
+        if (pos < n && c[b + pos] == (int32_t)v) atomicOr(flags, 1);
+        if (tr[v + 1] - tr[v] > kBcHeavyDeg) heavy[atomicAdd(flags + 1, 1)] = (int32_t)v;
     }
-}
-
-__global__ void k_bc_heavy(const int32_t* __restrict__ r, int64_t m, int32_t* __restrict__ out,
-                           int* __restrict__ count) {
-    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < m; v += (int64_t)gridDim.x * blockDim.x)
-        if (r[v + 1] - r[v] > kBcHeavyDeg) out[atomicAdd(count, 1)] = (int32_t)v;
 }
 
 __global__ void k_bc_check_sources(const int32_t* __restrict__ src, int ns, int64_t m, int* __restrict__ mark,
@@ -468,32 +574,40 @@ static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t ns
     const int words = (ns + 31) / 32;
     GA_REQUIRE(m * (int64_t)(ns + 1) < INT32_MAX, GA_ERR_UNSUPPORTED, "BC: m x sources exceeds the int32 entry range");
     ProfScope whole(ctx, "bc");
-    // FP64 copy of A (the algebra's values) and checks
-    ga_csr Ad = copy_csr(ctx, A, GA_FP64);
+    // Values enter the algebra as FP64. All-ones values are never read (the
+    // unit kernels), so A's own arrays serve; otherwise an FP64 copy. A
+    // symmetric A is its own transpose. Both properties are cached on the
+    // handle after their first check.
+    const bool unit = csr_unit_values(ctx, A);
+    const bool symmetric = csr_is_symmetric(ctx, A);
+    ga_csr Ad = unit ? nullptr : copy_csr(ctx, A, GA_FP64);
     ga_csr AT = nullptr;
     try {
-        DBuf<int> flags(ctx, 1), mark(ctx, (size_t)m);
-        GA_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int), ctx->stream));
+        ga_csr Av = unit ? A : Ad;
+        if (!symmetric) AT = transpose_csr(ctx, Av);
+        ga_csr ATu = symmetric ? Av : AT;
+        DBuf<int> flags(ctx, 2), mark(ctx, (size_t)m);
+        DBuf<int32_t> heavy(ctx, (size_t)m + 1);
+        GA_CUDA(cudaMemsetAsync(flags.p, 0, 2 * sizeof(int), ctx->stream));
         GA_CUDA(cudaMemsetAsync(mark.p, 0, sizeof(int) * m, ctx->stream));
-        k_bc_checks<<<grid_for(m * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(
-            Ad->rst, Ad->col, static_cast<const double*>(Ad->val), m, flags.p);
-        post_launch("bc_checks");
+        k_bc_scan_vertices<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(Av->rst, Av->col, ATu->rst,
+                                                                                        m, heavy.p, flags.p);
+        post_launch("bc_scan_vertices");
         k_bc_check_sources<<<grid_for(ns, 256, 64), 256, 0, ctx->stream>>>(d_sources, ns, m, mark.p, flags.p);
         post_launch("bc_check_sources");
-        const int f = read_i32(ctx, flags.p);
+        int hf[2];
+        GA_CUDA(cudaMemcpyAsync(hf, flags.p, sizeof(hf), cudaMemcpyDeviceToHost, ctx->stream));
+        GA_CUDA(cudaStreamSynchronize(ctx->stream));
+        const int f = hf[0];
         GA_REQUIRE(!(f & 1), GA_ERR_INVALID_ARG, "BC: the graph has self-loops");
         GA_REQUIRE(!(f & 8), GA_ERR_INVALID_ARG, "BC: source index out of range");
         GA_REQUIRE(!(f & 16), GA_ERR_INVALID_ARG, "BC: sources must be distinct");
-        const bool symmetric = !(f & 2);
-        const bool unit = !(f & 4);
-        if (!symmetric) AT = transpose_csr(ctx, Ad);
-        ga_csr ATu = symmetric ? Ad : AT;
 
         const int64_t cap_entries = m * (int64_t)ns + ns;
         const int64_t cap_rows = cap_entries;
         BcArgs p;
-        p.atr = ATu->rst; p.atc = ATu->col; p.atv = static_cast<const double*>(ATu->val);
-        p.ar = Ad->rst; p.ac = Ad->col; p.av = static_cast<const double*>(Ad->val);
+        p.atr = ATu->rst; p.atc = ATu->col; p.atv = unit ? nullptr : static_cast<const double*>(ATu->val);
+        p.ar = Av->rst; p.ac = Av->col; p.av = unit ? nullptr : static_cast<const double*>(Av->val);
         p.m = m; p.ns = ns; p.words = words; p.sources = d_sources;
         DBuf<BcState> st(ctx, 1);
         DBuf<int32_t> level_rows(ctx, (size_t)m + 2);
@@ -517,14 +631,18 @@ static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t ns
         p.cap_entries = cap_entries; p.cap_rows = cap_rows;
         p.W = W.p; p.inlvl = inlvl.p; p.bc = d_bc;
         // vertices whose in-neighbour lists are split over a CTA
-        DBuf<int32_t> heavy(ctx, (size_t)m + 1);
-        DBuf<int> nheavy(ctx, 1);
-        GA_CUDA(cudaMemsetAsync(nheavy.p, 0, sizeof(int), ctx->stream));
-        k_bc_heavy<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(ATu->rst, m, heavy.p, nheavy.p);
-        post_launch("bc_heavy");
         p.heavy_in = heavy.p;
-        p.nheavy_in = read_i32(ctx, nheavy.p);
+        p.nheavy_in = hf[1];
 
+        // push-level state: touched bits, list of reached vertices, marks
+        DBuf<uint32_t> tbits(ctx, (size_t)m * words);
+        DBuf<int32_t> tlist(ctx, (size_t)m), tmark(ctx, (size_t)m);
+        GA_CUDA(cudaMemsetAsync(tbits.p, 0, sizeof(uint32_t) * m * words, ctx->stream));
+        GA_CUDA(cudaMemsetAsync(tmark.p, 0, sizeof(int32_t) * m, ctx->stream));
+        p.tbits = tbits.p; p.tlist = tlist.p; p.tmark = tmark.p;
+        p.nnz = ATu->nnz;
+        k_bc_state_init<<<1, 1, 0, ctx->stream>>>(p);
+        post_launch("bc_state_init");
         k_bc_init<<<grid_for(ns, 256, 64), 256, 0, ctx->stream>>>(p);
         post_launch("bc_init");
 
@@ -540,9 +658,18 @@ static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t ns
         const int grid_rows = ctx->num_sms * 8;
         {
             ProfScope ps(ctx, "bc_forward_loop");
+            auto push = unit ? k_bc_push<true> : k_bc_push<false>;
             run_device_loop(ctx, [&](const LoopCtl& ctl) {
+                k_bc_level_begin<<<1, 1, 0, ctx->stream>>>(p);
+                post_launch("bc_level_begin");
                 fwd<<<grid_fwd, kBcThreads, smem, ctx->stream>>>(p);
                 post_launch("bc_forward");
+                push<<<grid_rows, kBcThreads, 0, ctx->stream>>>(p);
+                post_launch("bc_push");
+                k_bc_push_clear<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(p);
+                post_launch("bc_push_clear");
+                k_bc_push_emit<<<grid_rows, kBcThreads, 0, ctx->stream>>>(p);
+                post_launch("bc_push_emit");
                 k_bc_forward_finalize<<<1, 32, 0, ctx->stream>>>(p, ctl);
                 post_launch("bc_forward_finalize");
             }, m + 2);
