@@ -496,8 +496,9 @@ def run_gpu(args, dist: Dist):
                     z = C.nnz
                     r = res_rst[state["i"]]
                     c = res_col[state["off"]:state["off"] + z]
-                    ga.lib().ga_csr_download(ctx.handle, C.handle, r.ctypes.data_as(ga._p),
-                                             c.ctypes.data_as(ga._p), None)
+                    # on the copy stream: overlaps with the next k's pruning
+                    ga.lib().ga_csr_download_async(ctx.handle, C.handle, r.ctypes.data_as(ga._p),
+                                                   c.ctypes.data_as(ga._p), None)
                     d2h += (m + 1) * 4 + z * 4
                     state["i"] += 1
                     state["off"] += z
@@ -513,6 +514,7 @@ def run_gpu(args, dist: Dist):
                 Ad = ga.Csr.upload(ctx, m, m, rst_h, col_h, val_h)
                 sweep(ga, ctx, Ad, args.algo, args.kmin, sink=sink_factory())
                 Ad.free()
+                ga.lib().ga_ctx_copy_sync(ctx.handle)
                 e2e_ms.append(ctx.timer_stop())
             wce = ctx.work_counters(reset=True)
             e2e_t = dist.max(sum(e2e_ms))

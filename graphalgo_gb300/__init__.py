@@ -492,6 +492,30 @@ def batch_ktruss(algo, U: Csr, voff, k: int) -> Tuple[Csr, np.ndarray]:
     return Csr(U.ctx, h), iters
 
 
+def batch_ktruss_k(algo, U: Csr, voff, ks) -> Tuple[Csr, np.ndarray]:
+    """Batched k-truss with one k per graph."""
+    v = _voff_arg(voff)
+    kk = np.ascontiguousarray(ks, dtype=np.int32)
+    iters = np.zeros(len(v) - 1, np.int32)
+    h = _p()
+    _check(lib().ga_batch_ktruss_k(U.ctx.handle, _algo(algo), U.handle, _i64(len(v) - 1), _ptr(v), _ptr(kk),
+                                   ctypes.byref(h), _ptr(iters)), U.ctx)
+    return Csr(U.ctx, h), iters
+
+
+def batch_bc(U: Csr, voff, sources_per_graph) -> np.ndarray:
+    """Batched BC: one source list (local vertex indices) per graph of the union."""
+    v = _voff_arg(voff)
+    lists = [np.ascontiguousarray(x, dtype=np.int32) for x in sources_per_graph]
+    soff = np.zeros(len(lists) + 1, np.int64)
+    soff[1:] = np.cumsum([len(x) for x in lists])
+    src = np.concatenate(lists).astype(np.int32) if lists else np.zeros(0, np.int32)
+    out = np.zeros(U.shape[0], np.float64)
+    _check(lib().ga_batch_bc(U.ctx.handle, U.handle, _i64(len(v) - 1), _ptr(v), _ptr(soff), _ptr(src), _ptr(out)),
+           U.ctx)
+    return out
+
+
 def split_blocks(rst: np.ndarray, col: np.ndarray, voff) -> list:
     """Host helper: cut a downloaded block-diagonal CSR into per-graph (m, rst, col)."""
     out = []

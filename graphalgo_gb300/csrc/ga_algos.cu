@@ -257,13 +257,19 @@ __device__ __forceinline__ int64_t kt_row(const int32_t* cr, int64_t m, const in
 // cap so the exclusive scan over cap entries gives new positions.
 __global__ void k_kt_flags(const int32_t* __restrict__ cr, const int32_t* __restrict__ sup, int64_t m, int k,
                            int64_t cap, int32_t* __restrict__ flag, const int32_t* __restrict__ gid,
-                           const int32_t* __restrict__ done_g, const int32_t* __restrict__ row_of) {
+                           const int32_t* __restrict__ done_g, const int32_t* __restrict__ row_of,
+                           const int32_t* __restrict__ kg) {
     const int64_t cur = cr[m];
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cap; q += (int64_t)gridDim.x * blockDim.x) {
         int32_t keep = 0;
         if (q < cur) {
-            keep = sup[q] >= k - 2;
-            if (!keep && gid) keep = kt_keep_all(gid, done_g, kt_row(cr, m, row_of, q));
+            if (kg) {  // per-graph k (batches)
+                const int g = gid[kt_row(cr, m, row_of, q)];
+                keep = done_g[g] != 0 || sup[q] >= kg[g] - 2;
+            } else {
+                keep = sup[q] >= k - 2;
+                if (!keep && gid) keep = kt_keep_all(gid, done_g, kt_row(cr, m, row_of, q));
+            }
         }
         flag[q] = keep;
     }
@@ -478,7 +484,7 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
             const int32_t* gid = batch ? batch->gid : nullptr;
             const int32_t* done_g = batch ? batch->done_g : nullptr;
             k_kt_flags<<<grid_ent, 256, 0, ctx->stream>>>(C->rst, sup.p, m, k, cap, eflag.p, gid, done_g,
-                                                          upper ? row_of.p : nullptr);
+                                                          upper ? row_of.p : nullptr, batch ? batch->kg : nullptr);
             post_launch("kt_flags");
             scan_exclusive_i32_scratch(ctx, eflag.p, eflag.p, cap, scan_scr.p);
             k_kt_scatter<<<grid_copy, 256, 0, ctx->stream>>>(C->rst, C->col, eflag.p, m, tc.p, tr.p,

@@ -467,18 +467,20 @@ int ga_batch_tc(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, const int64_t
     });
 }
 
-int ga_batch_ktruss(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, const int64_t* voff, int k, ga_csr* C,
-                    int* iters) {
+static int batch_ktruss(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, const int64_t* voff, int k,
+                        const int* k_per_graph, ga_csr* C, int* iters) {
     if (!ctx || !U || !C || !iters) return GA_ERR_INVALID_ARG;
     *C = nullptr;
     GA_API_BODY(ctx, {
         check_voff(U, count, voff);
         GA_REQUIRE(U->dtype == GA_INT32, GA_ERR_DTYPE, "batched k-truss needs int32 values");
         GA_REQUIRE(csr_unit_values(ctx, U), GA_ERR_INVALID_ARG, "batched k-truss needs adjacency (all-ones) values");
-        GA_REQUIRE(algo != GA_NAIVE, GA_ERR_UNSUPPORTED, "batched k-truss runs MSA, MCA or HEAP");
+        GA_REQUIRE(algo != GA_NAIVE, GA_ERR_UNSUPPORTED, "batched k-truss runs MSA, MCA, HEAP or DOT");
         DBuf<int32_t> dv = upload_voff(ctx, count, voff);
         DBuf<int32_t> gid(ctx, (size_t)U->m + 1), nvert(ctx, (size_t)count), nnz_g(ctx, (size_t)count),
-            iters_g(ctx, (size_t)count), done_g(ctx, (size_t)count);
+            iters_g(ctx, (size_t)count), done_g(ctx, (size_t)count), kg(ctx, k_per_graph ? (size_t)count : 1);
+        if (k_per_graph)
+            GA_CUDA(cudaMemcpyAsync(kg.p, k_per_graph, sizeof(int32_t) * count, cudaMemcpyHostToDevice, ctx->stream));
         k_batch_setup<<<grid_for(count + U->m, 128, ctx->num_sms * 8), 128, 0, ctx->stream>>>(U->rst, dv.p, count, gid.p,
                                                                                      nvert.p, nnz_g.p, iters_g.p,
                                                                                      done_g.p);
@@ -486,9 +488,51 @@ int ga_batch_ktruss(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, const int
         KtBatch b;
         b.ngraphs = count; b.voff = dv.p; b.gid = gid.p; b.nvert = nvert.p;
         b.nnz_g = nnz_g.p; b.iters_g = iters_g.p; b.done_g = done_g.p;
+        b.kg = k_per_graph ? kg.p : nullptr;
         ProfScope ps(ctx, "batch_ktruss");
         *C = ktruss_impl(ctx, algo, U, k, nullptr, &b);
         GA_CUDA(cudaMemcpyAsync(iters, iters_g.p, sizeof(int32_t) * count, cudaMemcpyDeviceToHost, ctx->stream));
+        GA_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int ga_batch_ktruss(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, const int64_t* voff, int k, ga_csr* C,
+                    int* iters) {
+    return batch_ktruss(ctx, algo, U, count, voff, k, nullptr, C, iters);
+}
+
+int ga_batch_ktruss_k(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, const int64_t* voff, const int* k,
+                      ga_csr* C, int* iters) {
+    if (!k) return GA_ERR_INVALID_ARG;
+    return batch_ktruss(ctx, algo, U, count, voff, 0, k, C, iters);
+}
+
+int ga_batch_bc(ga_ctx ctx, ga_csr U, int64_t count, const int64_t* voff, const int64_t* soff,
+                const int32_t* sources, double* bc) {
+    if (!ctx || !U || !soff || !bc) return GA_ERR_INVALID_ARG;
+    GA_API_BODY(ctx, {
+        check_voff(U, count, voff);
+        GA_REQUIRE(soff[0] == 0, GA_ERR_INVALID_ARG, "batched BC: source offsets must start at 0");
+        const int64_t ns = soff[count];
+        GA_REQUIRE(ns >= 0 && (ns == 0 || sources), GA_ERR_INVALID_ARG, "batched BC: sources missing");
+        // graph g's sources, shifted to its rows of the union
+        std::vector<int32_t> global((size_t)(ns > 0 ? ns : 1));
+        for (int64_t g = 0; g < count; ++g) {
+            GA_REQUIRE(soff[g] <= soff[g + 1], GA_ERR_INVALID_ARG, "batched BC: source offsets must not decrease");
+            const int64_t mg = voff[g + 1] - voff[g];
+            for (int64_t j = soff[g]; j < soff[g + 1]; ++j) {
+                GA_REQUIRE(sources[j] >= 0 && sources[j] < mg, GA_ERR_INVALID_ARG, "batched BC: source out of range");
+                global[(size_t)j] = (int32_t)(sources[j] + voff[g]);
+            }
+        }
+        DBuf<int32_t> d_src(ctx, global.size());
+        DBuf<double> d_bc(ctx, (size_t)(U->m > 0 ? U->m : 1));
+        GA_CUDA(cudaMemcpyAsync(d_src.p, global.data(), sizeof(int32_t) * global.size(), cudaMemcpyHostToDevice,
+                                ctx->stream));
+        const int rc = ga_bc_device(ctx, U, d_src.p, ns, d_bc.p);
+        if (rc != GA_OK) fail(rc, ctx->last_error);
+        if (U->m)
+            GA_CUDA(cudaMemcpyAsync(bc, d_bc.p, sizeof(double) * U->m, cudaMemcpyDeviceToHost, ctx->stream));
         GA_CUDA(cudaStreamSynchronize(ctx->stream));
     });
 }

@@ -312,6 +312,12 @@ int ga_ctx_destroy(ga_ctx ctx) {
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
     if (ctx->l2_flush) cudaFree(ctx->l2_flush);
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
+        cudaEventDestroy(ctx->copy_ready);
+        cudaEventDestroy(ctx->copy_done);
+    }
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return GA_OK;
@@ -532,7 +538,41 @@ int ga_csr_device_ptrs(ga_csr A, void** rst, void** col, void** val) {
 int ga_csr_free(ga_ctx ctx, ga_csr A) {
     if (!ctx) return GA_ERR_INVALID_ARG;
     if (!A) return GA_OK;
-    GA_API_BODY(ctx, csr_destroy(ctx, A));
+    GA_API_BODY(ctx, {
+        // a download still in flight on the copy stream finishes before the
+        // stream-ordered free
+        if (ctx->copy_stream) GA_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->copy_done, 0));
+        csr_destroy(ctx, A);
+    });
+}
+
+int ga_csr_download_async(ga_ctx ctx, ga_csr A, int32_t* rst, int32_t* col, void* val) {
+    if (!ctx || !A) return GA_ERR_INVALID_ARG;
+    GA_API_BODY(ctx, {
+        if (!ctx->copy_stream) {
+            GA_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+            GA_CUDA(cudaEventCreateWithFlags(&ctx->copy_ready, cudaEventDisableTiming));
+            GA_CUDA(cudaEventCreateWithFlags(&ctx->copy_done, cudaEventDisableTiming));
+        }
+        GA_CUDA(cudaEventRecord(ctx->copy_ready, ctx->stream));
+        GA_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ready, 0));
+        if (rst)
+            GA_CUDA(cudaMemcpyAsync(rst, A->rst, sizeof(int32_t) * (A->m + 1), cudaMemcpyDeviceToHost,
+                                    ctx->copy_stream));
+        if (col && A->nnz)
+            GA_CUDA(cudaMemcpyAsync(col, A->col, sizeof(int32_t) * A->nnz, cudaMemcpyDeviceToHost, ctx->copy_stream));
+        if (val && A->nnz)
+            GA_CUDA(cudaMemcpyAsync(val, A->val, dtype_size(A->dtype) * A->nnz, cudaMemcpyDeviceToHost,
+                                    ctx->copy_stream));
+        GA_CUDA(cudaEventRecord(ctx->copy_done, ctx->copy_stream));
+    });
+}
+
+int ga_ctx_copy_sync(ga_ctx ctx) {
+    if (!ctx) return GA_ERR_INVALID_ARG;
+    GA_API_BODY(ctx, {
+        if (ctx->copy_stream) GA_CUDA(cudaStreamSynchronize(ctx->copy_stream));
+    });
 }
 
 int ga_csr_convert(ga_ctx ctx, ga_csr A, ga_dtype dtype, ga_csr* out) {

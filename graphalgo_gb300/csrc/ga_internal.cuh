@@ -83,6 +83,10 @@ struct ga_ctx_s {
     void* l2_flush = nullptr;
     size_t l2_flush_bytes = 0;
     // device bytes this context holds (requested sizes) and their high-water mark
+    // asynchronous downloads: a copy stream, the event its copies wait for and
+    // the event marking the last one done (created on first use)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_ready = nullptr, copy_done = nullptr;
     std::unordered_map<void*, size_t> live;
     int64_t bytes_in_use = 0;
     int64_t bytes_peak = 0;
@@ -192,6 +196,7 @@ struct KtBatch {
     int32_t* nnz_g = nullptr;        // current stored entries per graph
     int32_t* iters_g = nullptr;      // reported iteration count per graph
     int32_t* done_g = nullptr;       // graph finished (converged, or stopped after n_g iterations)
+    const int32_t* kg = nullptr;     // per-graph k (nullptr: the call's k for every graph)
 };
 ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, const KtBatch* batch);
 

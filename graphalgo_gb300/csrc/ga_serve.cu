@@ -46,10 +46,11 @@ static int64_t bound_bc(int64_t m, int64_t nnz, int64_t ns) {
     return 40 * (m + 1) * (ns + 1) + 4 * m * words + 80 * (m + 2) + 32 * nnz + (1 << 20);
 }
 
-static int64_t bound_batch(int type, int64_t m, int64_t nnz, int64_t count) {
+static int64_t bound_batch(int type, int64_t m, int64_t nnz, int64_t count, int64_t ns) {
     // union (int32 values), per-graph arrays, then the call on the union
-    const int64_t u = 4 * (m + 1) + 8 * nnz + 64 * (count + 1) + 16 * (m + 2);
-    return u + (type == GA_REQ_TC ? bound_tc(m, nnz, 4) : bound_ktruss(m, nnz));
+    const int64_t u = 4 * (m + 1) + 8 * nnz + 64 * (count + 1) + 16 * (m + 2) + 4 * ns;
+    return u + (type == GA_REQ_TC ? bound_tc(m, nnz, 4) : type == GA_REQ_KTRUSS ? bound_ktruss(m, nnz)
+                                                                               : bound_bc(m, nnz, ns));
 }
 
 int64_t request_bytes_bound(int type, int64_t m, int64_t nnz, int64_t param) {
@@ -106,13 +107,26 @@ struct Server {
 };
 
 static bool coalescible(const Server* s, const SrvReq* r) {
-    return s->cfg.coalesce && (r->type == GA_REQ_TC || r->type == GA_REQ_KTRUSS) &&
-           s->graphs[(size_t)r->graph].nnz <= s->cfg.coalesce_nnz;
+    return s->cfg.coalesce && s->graphs[(size_t)r->graph].nnz <= s->cfg.coalesce_nnz;
 }
 
+// One slot of a batched call: a graph copy in the union and the requests it
+// serves. TC requests share a slot per graph, k-truss requests per (graph,
+// k); every BC request has its own slot (its own sources).
+static int64_t slot_key(const SrvReq* r) {
+    if (r->type == GA_REQ_TC) return r->graph;
+    if (r->type == GA_REQ_KTRUSS) return ((int64_t)r->graph << 20) | (int64_t)(r->k & 0xfffff);
+    return -r->id;
+}
+
+// Batched BC keeps per (vertex, source) state for the whole union, so its
+// groups stay small: union vertices x sources at most this.
+constexpr int64_t kBcGroupPairs = (int64_t)1 << 22;
+constexpr int64_t kBcMaxSrc = 1024;                   // sources of one BC call
+
 // Picks the calls to run next (under the lock): the queue head and, when it
-// can be batched, the compatible requests behind it. Returns the group and
-// its byte reservation; an empty group means nothing can start now.
+// can be batched, the requests of the same type behind it. Returns the group
+// and its byte reservation; an empty group means nothing can start now.
 static std::vector<SrvReq*> take_group(Server* s, int64_t* reserve) {
     std::vector<SrvReq*> group;
     while (!s->queue.empty()) {
@@ -131,26 +145,28 @@ static std::vector<SrvReq*> take_group(Server* s, int64_t* reserve) {
         *reserve = head->bound;
         s->queue.pop_front();
         if (!coalescible(s, head)) return group;
-        // gather compatible requests, keeping queue order for the rest
-        std::unordered_map<int, int> seen{{head->graph, 0}};  // graphs already in the union
-        int64_t um = s->graphs[(size_t)head->graph].m, unz = s->graphs[(size_t)head->graph].nnz, ng = 1;
+        // gather same-type requests on small graphs, keeping queue order for the rest
+        std::unordered_map<int64_t, int> slots{{slot_key(head), 0}};
+        const SrvGraph& hg = s->graphs[(size_t)head->graph];
+        int64_t um = hg.m, unz = hg.nnz, ns = (int64_t)head->sources.size(), nslots = 1;
         for (auto it = s->queue.begin(); it != s->queue.end() && (int64_t)group.size() < s->cfg.coalesce_max_requests;) {
             SrvReq* r = *it;
-            const bool same_kind = r->type == head->type && (r->type != GA_REQ_KTRUSS || r->k == head->k);
-            if (!same_kind || !coalescible(s, r)) { ++it; continue; }
-            const bool fresh = seen.find(r->graph) == seen.end();
-            const int64_t m2 = um + (fresh ? s->graphs[(size_t)r->graph].m : 0);
-            const int64_t z2 = unz + (fresh ? s->graphs[(size_t)r->graph].nnz : 0);
+            if (r->type != head->type || !coalescible(s, r)) { ++it; continue; }
+            const bool fresh = slots.find(slot_key(r)) == slots.end();
+            const SrvGraph& g = s->graphs[(size_t)r->graph];
+            const int64_t m2 = um + (fresh ? g.m : 0), z2 = unz + (fresh ? g.nnz : 0);
+            const int64_t ns2 = ns + (int64_t)r->sources.size();
             if (z2 > s->cfg.coalesce_max_nnz) { ++it; continue; }
-            const int64_t b2 = bound_batch(head->type, m2, z2, ng + (fresh ? 1 : 0));
+            if (r->type == GA_REQ_BC && (ns2 > kBcMaxSrc || m2 * (ns2 + 1) > kBcGroupPairs)) { ++it; continue; }
+            const int64_t b2 = bound_batch(head->type, m2, z2, nslots + (fresh ? 1 : 0), ns2);
             if (s->reserved + b2 > s->budget) { ++it; continue; }
-            if (fresh) { seen[r->graph] = (int)ng; ++ng; }
-            um = m2; unz = z2;
+            if (fresh) slots[slot_key(r)] = (int)nslots++;
+            um = m2; unz = z2; ns = ns2;
             *reserve = b2;
             group.push_back(r);
             it = s->queue.erase(it);
         }
-        if (group.size() > 1) *reserve = std::max(*reserve, bound_batch(head->type, um, unz, ng));
+        if (group.size() > 1) *reserve = std::max(*reserve, bound_batch(head->type, um, unz, nslots, ns));
         return group;
     }
     return group;
@@ -194,26 +210,33 @@ static void run_single(Server* s, ga_ctx ctx, SrvReq* r) {
 static ga_algo group_algo(int a) { return a == GA_AUTO ? GA_MSA : (ga_algo)a; }
 
 static void run_group(Server* s, ga_ctx ctx, std::vector<SrvReq*>& group) {
-    // distinct graphs of the group, in first-seen order
-    std::vector<int> order;
-    std::unordered_map<int, int> slot;
+    // slots of the union, in first-seen order
+    std::vector<int64_t> order;
+    std::vector<SrvReq*> first;
+    std::unordered_map<int64_t, int> slot;
     for (SrvReq* r : group)
-        if (slot.emplace(r->graph, (int)order.size()).second) order.push_back(r->graph);
+        if (slot.emplace(slot_key(r), (int)order.size()).second) {
+            order.push_back(slot_key(r));
+            first.push_back(r);
+        }
     std::vector<ga_csr> parts;
-    for (int g : order) parts.push_back(s->graphs[(size_t)g].A);
+    for (SrvReq* r : first) parts.push_back(s->graphs[(size_t)r->graph].A);
     const int64_t count = (int64_t)parts.size();
     std::vector<int64_t> voff((size_t)count + 1);
     ga_csr U = nullptr;
     int rc = ga_csr_block_diag(ctx, count, parts.data(), &U, voff.data());
-    if (rc == GA_OK && group[0]->type == GA_REQ_TC) {
+    const int type = group[0]->type;
+    if (rc == GA_OK && type == GA_REQ_TC) {
         std::vector<int64_t> totals((size_t)count);
         rc = ga_batch_tc(ctx, group_algo(s->cfg.tc_algo), U, count, voff.data(), totals.data());
         if (rc == GA_OK)
-            for (SrvReq* r : group) r->res.tc_total = totals[(size_t)slot[r->graph]];
-    } else if (rc == GA_OK) {
+            for (SrvReq* r : group) r->res.tc_total = totals[(size_t)slot[slot_key(r)]];
+    } else if (rc == GA_OK && type == GA_REQ_KTRUSS) {
         ga_csr C = nullptr;
-        std::vector<int> iters((size_t)count);
-        rc = ga_batch_ktruss(ctx, group_algo(s->cfg.ktruss_algo), U, count, voff.data(), group[0]->k, &C, iters.data());
+        std::vector<int> iters((size_t)count), ks((size_t)count);
+        for (int64_t g = 0; g < count; ++g) ks[(size_t)g] = first[(size_t)g]->k;
+        rc = ga_batch_ktruss_k(ctx, group_algo(s->cfg.ktruss_algo), U, count, voff.data(), ks.data(), &C,
+                               iters.data());
         if (rc == GA_OK) {
             bool edges = false;
             for (SrvReq* r : group) edges = edges || r->want_edges;
@@ -222,7 +245,7 @@ static void run_group(Server* s, ga_ctx ctx, std::vector<SrvReq*>& group) {
             rc = ga_csr_download(ctx, C, crst.data(), edges ? ccol.data() : nullptr, nullptr);
             if (rc == GA_OK) {
                 for (SrvReq* r : group) {
-                    const int g = slot[r->graph];
+                    const int g = slot[slot_key(r)];
                     const int64_t b = voff[(size_t)g], e = voff[(size_t)g + 1];
                     r->res.iters = iters[(size_t)g];
                     r->res.truss_nnz = crst[(size_t)e] - crst[(size_t)b];
@@ -237,6 +260,22 @@ static void run_group(Server* s, ga_ctx ctx, std::vector<SrvReq*>& group) {
             }
             ga_csr_free(ctx, C);
         }
+    } else if (rc == GA_OK) {  // BC: every request its own slot and sources
+        std::vector<int64_t> soff((size_t)count + 1, 0);
+        std::vector<int32_t> src;
+        for (int64_t g = 0; g < count; ++g) {
+            const auto& sv = first[(size_t)g]->sources;
+            src.insert(src.end(), sv.begin(), sv.end());
+            soff[(size_t)g + 1] = (int64_t)src.size();
+        }
+        std::vector<double> bc((size_t)std::max<int64_t>(U->m, 1));
+        rc = ga_batch_bc(ctx, U, count, voff.data(), soff.data(), src.data(), bc.data());
+        if (rc == GA_OK)
+            for (SrvReq* r : group) {
+                const int g = slot[slot_key(r)];
+                r->bc.assign(bc.begin() + voff[(size_t)g], bc.begin() + voff[(size_t)g + 1]);
+                if (r->bc.empty()) r->bc.assign(1, 0.0);
+            }
     }
     if (U) ga_csr_free(ctx, U);
     for (SrvReq* r : group) fill_error(r, rc, ctx);
@@ -318,7 +357,7 @@ int ga_server_create(int device, const ga_server_config* cfg, ga_server* out) {
     if (cfg) c = *cfg;
     if (c.workers <= 0) c.workers = 4;
     if (c.coalesce_nnz <= 0) c.coalesce_nnz = 1 << 20;
-    if (c.coalesce_max_nnz <= 0) c.coalesce_max_nnz = 1 << 26;
+    if (c.coalesce_max_nnz <= 0) c.coalesce_max_nnz = 1 << 22;
     if (c.coalesce_max_requests <= 0) c.coalesce_max_requests = 4096;
     if (c.workers > 64) return GA_ERR_INVALID_ARG;
     s->cfg = c;

@@ -173,6 +173,13 @@ GA_API int ga_csr_info(ga_csr A, int64_t* m, int64_t* n, int64_t* nnz, int* dtyp
 /* Copy back into caller-allocated host arrays (rst: m+1, col/val: nnz).
  * Any of the three may be NULL to skip it. */
 GA_API int ga_csr_download(ga_ctx ctx, ga_csr A, int32_t* rst, int32_t* col, void* val);
+/* Asynchronous download on the context's copy stream: it starts once the
+ * work queued so far on the context's stream is done and overlaps with work
+ * queued after it. Host buffers should be page-locked (ga_host_register)
+ * for the copy to be asynchronous. ga_ctx_copy_sync waits for every
+ * download; ga_csr_free on a handle orders its free after them. */
+GA_API int ga_csr_download_async(ga_ctx ctx, ga_csr A, int32_t* rst, int32_t* col, void* val);
+GA_API int ga_ctx_copy_sync(ga_ctx ctx);
 GA_API int ga_csr_device_ptrs(ga_csr A, void** rst, void** col, void** val);
 GA_API int ga_csr_free(ga_ctx ctx, ga_csr A);
 /* Deep copy, optionally converting the value type
@@ -337,6 +344,17 @@ GA_API int ga_batch_tc(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, const 
  * ga_ktruss reports it. *C is the union of the per-graph results. */
 GA_API int ga_batch_ktruss(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, const int64_t* voff, int k,
                            ga_csr* C, int* iters);
+/* The same with one k per graph (k: host, count entries). */
+GA_API int ga_batch_ktruss_k(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, const int64_t* voff, const int* k,
+                             ga_csr* C, int* iters);
+/* Batched BC over a block-diagonal union: graph g's sources are
+ * sources[soff[g] .. soff[g+1]) (vertex indices within graph g; soff: host,
+ * count+1 entries, at most 1,024 sources in all). No path leaves a graph,
+ * so bc (host, length m of the union) holds in graph g's rows the scores
+ * ga_bc gives for graph g and its sources alone (FP64, up to the order of
+ * the sums). */
+GA_API int ga_batch_bc(ga_ctx ctx, ga_csr U, int64_t count, const int64_t* voff, const int64_t* soff,
+                       const int32_t* sources, double* bc);
 
 /* ------------------------------------------------------- request server */
 /* Serves triangle-count, k-truss and BC requests on device-resident graphs
@@ -360,7 +378,8 @@ typedef struct {
     int ktruss_algo;               /* ga_algo of k-truss (GA_MSA, GA_MCA, GA_HEAP, GA_DOT, GA_AUTO as for TC) */
     int64_t hbm_budget;            /* bytes the calls in flight may hold; 0: 80% of free memory at creation */
     int64_t coalesce_nnz;          /* graphs with at most this many stored entries are batched; 0: 2^20 */
-    int64_t coalesce_max_nnz;      /* stored entries of one batched union at most; 0: 2^26 */
+    int64_t coalesce_max_nnz;      /* stored entries of one batched union at most; 0: 2^22 (several groups
+                                      keep several workers busy) */
     int64_t coalesce_max_requests; /* requests served by one batched call at most; 0: 4096 */
 } ga_server_config;
 typedef struct {

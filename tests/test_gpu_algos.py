@@ -126,3 +126,29 @@ def test_bc_rejects_bad_sources(ctx):
         ga.bc(Gd, [1, 1])
     with pytest.raises(ga.GaError):
         ga.bc(Gd, [100])
+
+
+def test_async_download_overlaps_and_orders_free(ctx):
+    """ga_csr_download_async copies on the context's copy stream; a free right
+    after it is ordered behind the copy, and the data equal a plain download."""
+    import ctypes
+    G = csr_from_arrays(*ga.gen_rmat(12, 16, seed=13))
+    A = to_device(ctx, G)
+    C, _ = ga.ktruss("msa", A, 4)
+    ref = C.download()
+    rst = np.empty(G.m + 1, np.int32)
+    col = np.empty(max(1, C.nnz), np.int32)
+    ga.host_register(rst)
+    ga.host_register(col)
+    try:
+        rc = ga.lib().ga_csr_download_async(ctx.handle, C.handle, rst.ctypes.data_as(ctypes.c_void_p),
+                                            col.ctypes.data_as(ctypes.c_void_p), None)
+        assert rc == ga.OK
+        C.free()
+        D, _ = ga.ktruss("msa", A, 5)  # new work (and allocations) queued behind the free
+        assert ga.lib().ga_ctx_copy_sync(ctx.handle) == ga.OK
+        assert np.array_equal(rst, ref[0]) and np.array_equal(col[:len(ref[1])], ref[1])
+        D.free()
+    finally:
+        ga.host_unregister(rst)
+        ga.host_unregister(col)

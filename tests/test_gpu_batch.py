@@ -173,3 +173,31 @@ def test_knn_large_graph(ctx):
     for g, (m, r, c) in enumerate(ga.split_blocks(rst, col, voff)):
         assert m == n[g]
         _check_knn_structure(m, r, c, 30)
+
+
+def test_batch_ktruss_per_graph_k(ctx):
+    host, dev = _mixed_parts(ctx)
+    U, voff = ga.block_diag(ctx, dev)
+    ks = [3, 4, 5, 6, 7, 8, 4][:len(host)]
+    C, iters = ga.batch_ktruss_k("msa", U, voff, ks)
+    cr, cc, _ = C.download()
+    got = ga.split_blocks(cr, cc, voff)
+    for g, (G, k) in enumerate(zip(host, ks)):
+        Cs, it = ga.ktruss("msa", dev[g], k)
+        sr, sc, _ = Cs.download()
+        assert iters[g] == it, g
+        assert np.array_equal(got[g][1], sr) and np.array_equal(got[g][2], sc), g
+
+
+def test_batch_bc_matches_single(ctx):
+    host, dev = _mixed_parts(ctx)
+    U, voff = ga.block_diag(ctx, dev)
+    rng = np.random.default_rng(17)
+    srcs = [rng.choice(G.m, min(G.m, 9), replace=False) for G in host]
+    got = ga.batch_bc(U, voff, srcs)
+    for g, (G, Gd, src) in enumerate(zip(host, dev, srcs)):
+        ref = ga.bc(Gd, src)
+        part = got[voff[g]:voff[g + 1]]
+        assert np.all(np.abs(part - ref) <= 1e-9 * np.maximum(np.abs(ref), 1.0)), g
+        orc = oracle.bc_batch(G, src)
+        assert np.all(np.abs(part - orc) <= 1e-9 * np.maximum(np.abs(orc), 1.0)), g
