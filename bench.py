@@ -638,10 +638,12 @@ def run_batch(args, dist: Dist):
     npl = G if args.plain_graphs <= 0 else min(G, args.plain_graphs)
     pick = np.sort(np.random.default_rng(args.seed + 1).choice(G, npl, replace=False)) if npl < G else np.arange(G)
     handles = [ga.Csr.upload(ctx, m_, m_, r, c, np.ones(len(c), np.int32)) for m_, r, c in (blocks[i] for i in pick)]
-    # the plain form runs the variants the tuner chose for the union, default schedule
+    # the plain form: the reference's default variant (MSA), default schedule
+    plain_tc_algo = args.tc_algo if args.tc_algo != "auto" else "msa"
+    plain_kt_algo = args.algo if args.algo != "auto" else "msa"
     for h in handles[:8]:
-        ga.tc(tc_algo, h, per_row=False)
-        ga.ktruss(kt_algo, h, 4)[0].free()
+        ga.tc(plain_tc_algo, h, per_row=False)
+        ga.ktruss(plain_kt_algo, h, 4)[0].free()
     ctx.sync()
     ctx.flush_l2()
     ctx.timer_start()
@@ -649,8 +651,8 @@ def run_batch(args, dist: Dist):
     plain_it = np.zeros(npl, np.int32)
     plain_nnz = 0
     for j, h in enumerate(handles):
-        plain_tc[j] = ga.tc(tc_algo, h, per_row=False)[0]
-        C, plain_it[j] = ga.ktruss(kt_algo, h, 4)
+        plain_tc[j] = ga.tc(plain_tc_algo, h, per_row=False)[0]
+        C, plain_it[j] = ga.ktruss(plain_kt_algo, h, 4)
         plain_nnz += C.nnz
         C.free()
     plain_ms = ctx.timer_stop()
@@ -718,7 +720,7 @@ def run_batch(args, dist: Dist):
         "autotune": tuning,
         "plain": {"value": plain_value, "unit": "graphs/s", "graphs_timed": npl, "ms": plain_ms,
                   "results_equal": same, "speedup": value / plain_value,
-                  "form": f"ga_tc({tc_algo}) + ga_ktruss({kt_algo}) per graph, resident per-graph handles"},
+                  "form": f"ga_tc({plain_tc_algo}) + ga_ktruss({plain_kt_algo}) per graph, resident per-graph handles"},
         "work": {"products_per_step": prof["counters"]["products"],
                  "triangles": int(ref[0].sum()), "truss_entries": int(ref[2]),
                  "max_iters": int(ref[1].max())},

@@ -25,6 +25,7 @@ void run_device_loop(ga_ctx ctx, const std::function<void(const LoopCtl&)>& body
     }
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    bool capture_failed = false;
     GA_CUDA(cudaGraphCreate(&graph, 0));
     try {
         GA_CUDA(cudaGraphConditionalHandleCreate(&ctl.handle, graph, 1, cudaGraphCondAssignDefault));
@@ -43,6 +44,7 @@ void run_device_loop(ga_ctx ctx, const std::function<void(const LoopCtl&)>& body
             body(ctl);
         } catch (...) {
             ctx->capturing = false;
+            capture_failed = true;
             cudaGraph_t dummy;
             cudaStreamEndCapture(ctx->stream, &dummy);
             cudaGetLastError();
@@ -59,7 +61,10 @@ void run_device_loop(ga_ctx ctx, const std::function<void(const LoopCtl&)>& body
         GA_CUDA(cudaStreamSynchronize(ctx->stream));
     } catch (...) {
         if (exec) cudaGraphExecDestroy(exec);
-        cudaGraphDestroy(graph);
+        // A graph whose conditional body was left by a failed capture is not
+        // destroyed (destroying it crashed the driver); it leaks on this
+        // error path only.
+        if (!capture_failed) cudaGraphDestroy(graph);
         throw;
     }
     cudaGraphExecDestroy(exec);

@@ -650,7 +650,14 @@ static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t ns
                                 32 * (2 * sizeof(int) + sizeof(double));
         const size_t smem = kBcWarps * ((per_warp + 15) & ~(size_t)15);
         auto fwd = unit ? k_bc_forward<true> : k_bc_forward<false>;
-        GA_CUDA(cudaFuncSetAttribute(fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        // The attribute is per kernel, not per call: calls with other source
+        // counts may run concurrently (other contexts, other threads), so it
+        // is always set to the largest size any call launches with.
+        constexpr size_t kMaxWords = (kBcMaxSources + 31) / 32;
+        constexpr size_t max_per_warp = (size_t)kBcMaxSources * sizeof(double) + 2 * kMaxWords * sizeof(uint32_t) +
+                                        32 * (2 * sizeof(int) + sizeof(double));
+        constexpr size_t max_smem = kBcWarps * ((max_per_warp + 15) & ~(size_t)15);
+        GA_CUDA(cudaFuncSetAttribute(fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem));
         int per_sm = 1;
         GA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd, kBcThreads, smem));
         if (per_sm < 1) per_sm = 1;

@@ -8,6 +8,7 @@
 // afterwards: tuning launches are not counted as work.
 #include "ga_internal.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <functional>
 #include <mutex>
@@ -100,8 +101,9 @@ double time_once(ga_ctx ctx, const std::function<void()>& f) {
     return ms;
 }
 
-// Runs every candidate once after one untimed warm-up of the first, and
-// returns the fastest.
+// Runs every candidate once after one untimed warm-up of the first, times
+// the three fastest and the default once more (each keeps its better run),
+// and returns the fastest.
 TuneEntry pick(ga_ctx ctx, const std::vector<Cand>& cands, const std::function<void(const Cand&)>& run) {
     CounterGuard cg(ctx);
     const MxmTune saved = ctx->tune;
@@ -110,17 +112,28 @@ TuneEntry pick(ga_ctx ctx, const std::vector<Cand>& cands, const std::function<v
         ctx->tune = cands[0].t;
         run(cands[0]);
         GA_CUDA(cudaStreamSynchronize(ctx->stream));
-        best.ms = INFINITY;
+        std::vector<double> ms(cands.size());
         for (size_t i = 0; i < cands.size(); ++i) {
             ctx->tune = cands[i].t;
-            const double ms = time_once(ctx, [&] { run(cands[i]); });
-            if (i == 0) best.default_ms = ms;
-            if (ms < best.ms) {
-                best.ms = ms;
+            ms[i] = time_once(ctx, [&] { run(cands[i]); });
+        }
+        std::vector<size_t> order(cands.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+        std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return ms[a] < ms[b]; });
+        std::vector<size_t> again(order.begin(), order.begin() + std::min<size_t>(3, order.size()));
+        if (std::find(again.begin(), again.end(), (size_t)0) == again.end()) again.push_back(0);
+        for (size_t i : again) {
+            ctx->tune = cands[i].t;
+            ms[i] = std::min(ms[i], time_once(ctx, [&] { run(cands[i]); }));
+        }
+        best.ms = INFINITY;
+        for (size_t i = 0; i < cands.size(); ++i)
+            if (ms[i] < best.ms) {
+                best.ms = ms[i];
                 best.algo = cands[i].algo;
                 best.t = cands[i].t;
             }
-        }
+        best.default_ms = ms[0];
     } catch (...) {
         ctx->tune = saved;
         throw;

@@ -146,3 +146,32 @@ def test_bounds_cover_allocations(ctx, gid):
         _, peak = ctx.mem_stats()
         bound = ga.request_bytes_bound(t, m, nnz, len(src))
         assert peak - base <= bound, (t, peak - base, bound)
+
+
+def test_concurrent_bc_with_different_source_counts(built):
+    """Two host threads, each with its own context, run BC with 8 and with
+    300 sources at the same time: the forward kernel's shared-memory size
+    differs per call, and no call may fail because of the other."""
+    from concurrent.futures import ThreadPoolExecutor
+    m, rst, col = ga.gen_rmat(11, 16, seed=91)
+    rng = np.random.default_rng(3)
+    sets = [rng.choice(m, 8, replace=False).astype(np.int32), rng.choice(m, 300, replace=False).astype(np.int32)]
+    refs = []
+    with ga.Context(0) as c0:
+        A0 = ga.Csr.upload(c0, m, m, rst, col)
+        refs = [ga.bc(A0, s) for s in sets]
+        A0.free()
+
+    def run(which):
+        with ga.Context(0) as c:
+            A = ga.Csr.upload(c, m, m, rst, col)
+            out = [ga.bc(A, sets[which]) for _ in range(12)]
+            A.free()
+            return out
+
+    with ThreadPoolExecutor(2) as ex:
+        futs = [ex.submit(run, w) for w in (0, 1)]
+        results = [f.result() for f in futs]
+    for w in (0, 1):
+        for got in results[w]:
+            np.testing.assert_allclose(got, refs[w], rtol=BC_RTOL, atol=1e-9)
