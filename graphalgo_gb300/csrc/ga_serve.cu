@@ -8,11 +8,12 @@
 // the server's HBM budget; a request whose bound alone exceeds the budget
 // is refused with GA_ERR_ADMISSION.
 //
-// Continuous batching. When a worker takes a TC or k-truss request on a
-// small graph, it also takes the other queued requests of the same kind
-// (same k) on small graphs and runs them as one batched call over the
-// block-diagonal union of their graphs; identical requests share one slot.
-// The batched calls give every graph the result it gets alone.
+// Continuous batching. When a worker takes a request on a small graph, it
+// also takes the other queued requests of the same type on small graphs and
+// runs them as one batched call over the block-diagonal union of their
+// graphs: TC requests share a slot per graph, k-truss requests per (graph,
+// k) with one k per graph, and every BC request has its own slot and
+// sources. The batched calls give every request the result it gets alone.
 #include "ga_internal.cuh"
 
 #include <algorithm>

@@ -364,16 +364,17 @@ GA_API int ga_batch_bc(ga_ctx ctx, ga_csr U, int64_t count, const int64_t* voff,
  * starts the oldest queued request only while the bounds of the calls in
  * flight plus its own fit in the HBM budget, and a request whose bound alone
  * exceeds the budget completes with GA_ERR_ADMISSION. With coalesce on, a
- * worker that takes a TC or k-truss request on a small graph also takes the
- * queued requests of the same kind (same k) on small graphs and serves them
- * with one batched call (ga_batch_tc / ga_batch_ktruss); each request gets
- * the result it gets alone. workers = 1 with coalesce = 0 is the plain
- * sequential form. No counterpart in the reference (one graph per run). */
+ * worker that takes a request on a small graph also takes the queued
+ * requests of the same type on small graphs and serves them with one
+ * batched call (ga_batch_tc, ga_batch_ktruss_k with one k per graph,
+ * ga_batch_bc); each request gets the result it gets alone. workers = 1
+ * with coalesce = 0 is the plain sequential form. No counterpart in the
+ * reference (one graph per run). */
 typedef struct ga_server_s* ga_server;
 enum { GA_REQ_TC = 0, GA_REQ_KTRUSS = 1, GA_REQ_BC = 2 };
 typedef struct {
     int workers;                   /* worker threads (1..64); 0: 4 */
-    int coalesce;                  /* 1: batch queued small TC / k-truss requests */
+    int coalesce;                  /* 1: batch queued requests on small graphs */
     int tc_algo;                   /* ga_algo of TC (any; GA_AUTO: tuned per graph, MSA for batched calls) */
     int ktruss_algo;               /* ga_algo of k-truss (GA_MSA, GA_MCA, GA_HEAP, GA_DOT, GA_AUTO as for TC) */
     int64_t hbm_budget;            /* bytes the calls in flight may hold; 0: 80% of free memory at creation */
