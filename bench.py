@@ -53,11 +53,13 @@ def parse_args():
     ap.add_argument("--scale", type=int, default=18)
     ap.add_argument("--edge-factor", type=int, default=16)
     ap.add_argument("--seed", type=int, default=42)
-    ap.add_argument("--algo", default=None, choices=["msa", "mca", "heap", "dot", "auto"],
+    ap.add_argument("--algo", default=None, choices=["msa", "mca", "heap", "dot", "hybrid", "auto"],
                     help="k-truss variant (default: msa; auto for the batch workload)")
     ap.add_argument("--kmin", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--hybrid-ratio", type=int, default=None,
+                    help="hybrid variant: work ratio above which a row goes to the inner-product form")
     ap.add_argument("--tune", action="store_true",
                     help="k-truss sweep: use the bin thresholds tuned on the first support product "
                          "(slower over the whole sweep, whose later graphs are small)")
@@ -223,6 +225,8 @@ def run_case(args):
     gbuild.build()
     ctx = ga.Context(0)
     ctx.set_option(ga.OPT_DEVICE_LOOPS, 0 if args.host_loops else 1)
+    if args.hybrid_ratio is not None:
+        ctx.set_option(ga.OPT_HYBRID_RATIO, args.hybrid_ratio)
     if args.case == "batch":
         n, dim = knn_batch_sizes(args.graphs, args.seed)
         U, voff = ga.gen_knn_batch(ctx, n, dim, k=30, seed=args.seed)
@@ -344,7 +348,8 @@ def profile_step(ga, ctx, run, algo, counters, loops):
     ctr = counters()
     ctx.set_option(ga.OPT_PROFILE, 0)
     ctx.set_option(ga.OPT_DEVICE_LOOPS, loops)
-    kname = {"msa": "mxm_msa", "mca": "mxm_mca", "heap": "mxm_heap_merge", "dot": "mxm_dot"}[algo]
+    kname = {"msa": "mxm_msa", "mca": "mxm_mca", "heap": "mxm_heap_merge", "dot": "mxm_dot",
+             "hybrid": "mxm_msa"}[algo]
     k_launches, k_ms = stats.get(kname, (0, 0.0))
     bytes_model = 8 * ctr["rows"] + 16 * ctr["a_entries"] + 8 * ctr["executed"] + 8 * ctr["mask_entries"]
     peak, peak_kind = measured_peak_hbm()
@@ -426,6 +431,8 @@ def run_gpu(args, dist: Dist):
     ctx = ga.Context(dist.local_rank)
     loops = 0 if args.host_loops else 1
     ctx.set_option(ga.OPT_DEVICE_LOOPS, loops)
+    if args.hybrid_ratio is not None:
+        ctx.set_option(ga.OPT_HYBRID_RATIO, args.hybrid_ratio)
 
     m, rst, col = ga.gen_rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, args.seed)
     nnz = len(col)
@@ -529,7 +536,7 @@ def run_gpu(args, dist: Dist):
     variants = {}
     default = {"warp_max_flops": 32768, "heavy_flops": 1 << 20, "ctas_per_sm": 0, "dot_chunk": 8}
     ga.apply_schedule(ctx, default)  # each variant with the default schedule
-    for algo in ("msa", "mca", "heap", "dot"):
+    for algo in ("msa", "mca", "heap", "dot", "hybrid"):
         ctx.work_counters(reset=True)
         ctx.flush_l2()
         ctx.timer_start()

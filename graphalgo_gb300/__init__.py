@@ -27,12 +27,12 @@ LIB_PATH = os.path.join(HERE, "_lib", "libgraphalgo_gb300.so")
 # dtypes
 INT32, INT64, FP32, FP64, UINT8 = 0, 1, 2, 3, 4
 # algorithms
-MSA, MCA, HEAP, NAIVE, DOT, AUTO = 0, 1, 2, 3, 4, 5
-ALGOS = {"msa": MSA, "mca": MCA, "heap": HEAP, "naive": NAIVE, "dot": DOT, "auto": AUTO}
+MSA, MCA, HEAP, NAIVE, DOT, AUTO, HYBRID = 0, 1, 2, 3, 4, 5, 6
+ALGOS = {"msa": MSA, "mca": MCA, "heap": HEAP, "naive": NAIVE, "dot": DOT, "auto": AUTO, "hybrid": HYBRID}
 ALGO_NAMES = {v: k for k, v in ALGOS.items()}
 # options
 OPT_DEVICE_LOOPS, OPT_PROFILE, OPT_FAIL_ALLOC_AFTER, OPT_KNN_TILED = 1, 2, 3, 4
-OPT_MXM_WARP_FLOPS, OPT_MXM_HEAVY_FLOPS, OPT_MXM_CTAS_PER_SM, OPT_DOT_CHUNK = 5, 6, 7, 8
+OPT_MXM_WARP_FLOPS, OPT_MXM_HEAVY_FLOPS, OPT_MXM_CTAS_PER_SM, OPT_DOT_CHUNK, OPT_HYBRID_RATIO = 5, 6, 7, 8, 9
 TUNE_KTRUSS, TUNE_PRODUCT, TUNE_TC = 0, 1, 2
 # status codes
 OK, ERR_INVALID_ARG, ERR_INVALID_CSR, ERR_SHAPE, ERR_DTYPE, ERR_CUDA, ERR_OOM, ERR_NO_DEVICE, \
@@ -637,7 +637,7 @@ class Server:
 # ------------------------------------------------------------------ autotuner
 class TuneResult(ctypes.Structure):
     _fields_ = [("algo", _int), ("warp_max_flops", _i64), ("heavy_flops", _i64), ("ctas_per_sm", _int),
-                ("dot_chunk", _int), ("ms", ctypes.c_double), ("default_ms", ctypes.c_double),
+                ("dot_chunk", _int), ("hybrid_ratio", _i64), ("ms", ctypes.c_double), ("default_ms", ctypes.c_double),
                 ("candidates", _int), ("cached", _int)]
 
 
@@ -661,3 +661,4 @@ def apply_schedule(ctx: Context, tuned: dict) -> None:
     ctx.set_option(OPT_MXM_HEAVY_FLOPS, tuned["heavy_flops"])
     ctx.set_option(OPT_MXM_CTAS_PER_SM, tuned["ctas_per_sm"])
     ctx.set_option(OPT_DOT_CHUNK, tuned["dot_chunk"])
+    ctx.set_option(OPT_HYBRID_RATIO, tuned.get("hybrid_ratio", 16))

@@ -427,7 +427,8 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
     GA_REQUIRE(A->dtype == GA_INT32, GA_ERR_DTYPE, "k-truss needs int32 values (spMtx<int>)");
     TuneScope tscope(ctx);
     algo = resolve_ktruss_algo(ctx, algo, A);
-    GA_REQUIRE(algo == GA_MSA || algo == GA_MCA || algo == GA_HEAP || algo == GA_NAIVE || algo == GA_DOT,
+    GA_REQUIRE(algo == GA_MSA || algo == GA_MCA || algo == GA_HEAP || algo == GA_NAIVE || algo == GA_DOT ||
+                   algo == GA_HYBRID,
                GA_ERR_INVALID_ARG, "k-truss: unknown algorithm");
     const int64_t m = A->m;
     // C = A (a copy; its pattern shrinks in place)
@@ -453,7 +454,8 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
         // only the upper triangle (columns >= i) is multiplied, the lower
         // triangle is mirrored. Same values, about half the products.
         const bool upper = algo != GA_NAIVE && csr_is_symmetric(ctx, A);
-        GA_REQUIRE(upper || algo != GA_DOT, GA_ERR_UNSUPPORTED, "k-truss with GA_DOT needs a symmetric matrix");
+        GA_REQUIRE(upper || (algo != GA_DOT && algo != GA_HYBRID), GA_ERR_UNSUPPORTED,
+                   "k-truss with GA_DOT or GA_HYBRID needs a symmetric matrix");
         const size_t aux = upper ? (size_t)cap : 1;
         DBuf<int32_t> ust(ctx, upper ? (size_t)m + 1 : 1);
         DBuf<int32_t> row_of(ctx, aux), mir(ctx, aux), pos_new(ctx, aux), trow(ctx, aux), mir_new(ctx, aux);
@@ -479,7 +481,8 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
                 Cu = *C;
                 Cu.rst = ust.p;
                 if (algo == GA_DOT) mxm_dot_launch(ctx, C, C, C, &Cu, sup.p, unit, C->rst + 1);
-                else mxm_masked_launch(ctx, algo, C, C, &Cu, sup.p, mxm_scr.p, cap, unit, C->rst + 1, unit);
+                else mxm_masked_launch(ctx, algo, C, C, &Cu, sup.p, mxm_scr.p, cap, unit, C->rst + 1, unit,
+                                       algo == GA_HYBRID ? C : nullptr);
                 k_gather_lower<<<grid_ent, 256, 0, ctx->stream>>>(st.p, C->col, row_of.p, mir.p, sup.p);
                 post_launch("kt_gather_lower");
             } else {

@@ -397,6 +397,10 @@ int ga_ctx_set_option(ga_ctx ctx, int option, int64_t value) {
         if (value < 1 || value > 4096) break;
         ctx->tune.dot_chunk = (int)value;
         return GA_OK;
+    case GA_OPT_HYBRID_RATIO:
+        if (value < 0 || value > (1 << 20)) break;
+        ctx->tune.hybrid_ratio = value;
+        return GA_OK;
     }
     ctx->last_error = "unknown option";
     return GA_ERR_INVALID_ARG;

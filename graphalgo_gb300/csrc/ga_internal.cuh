@@ -50,6 +50,8 @@ struct MxmTune {
     int64_t heavy_flops = 1 << 20;   // CTA items of rows with at least this many products run first
     int ctas_per_sm = 0;             // persistent grid: CTAs per SM (0: as many as fit)
     int dot_chunk = 8;               // inner-product form: mask entries per warp task
+    int64_t hybrid_ratio = 16;       // hybrid form: a row goes to the inner product when its
+                                     // inner-product work x this is below its Gustavson work
 };
 
 }  // namespace ga
@@ -223,10 +225,13 @@ ga_csr copy_csr(ga_ctx ctx, ga_csr A, ga_dtype to);
 // Masked SpGEMM into caller-provided value storage aligned with M.
 void mxm_masked_into(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals);
 ga_csr mxm_cmask(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M);
-size_t mxm_scratch_bytes(int64_t m, int64_t n, int64_t mask_nnz);
+// hybrid: room for the hybrid form's inner-product tasks too.
+size_t mxm_scratch_bytes(int64_t m, int64_t n, int64_t mask_nnz, bool hybrid = true);
 // unit_a / unit_b: A's / B's values are all ones (skips value loads).
+// GA_HYBRID: Bt holds B^T (B itself when B is symmetric).
 void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals, void* scratch,
-                       int64_t cap_nnz, bool unit_b, const int32_t* mask_row_end = nullptr, bool unit_a = false);
+                       int64_t cap_nnz, bool unit_b, const int32_t* mask_row_end = nullptr, bool unit_a = false,
+                       ga_csr Bt = nullptr);
 // Inner-product masked product (GA_DOT): Bt holds B^T (B itself when B is
 // symmetric); unit: A's and B's values are all ones. Allocates nothing.
 // With mask_row_end, M->rst holds row starts of the mask and

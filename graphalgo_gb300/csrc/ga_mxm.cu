@@ -44,6 +44,7 @@ constexpr int kWinWords = kWinCols / 32;   // dense bitmap words
 constexpr int kWarpSlots = 256;            // mask slots per warp row
 constexpr int kWarpTblBits = 9;            // warp-row hash table: 512 entries
 constexpr int kFilterBits = 12;            // warp-row filter: 4096 bits
+constexpr int kDotTask = 8;                // hybrid form: mask entries per inner-product task
 // Bin thresholds (rows above warp_max_flops products go to a CTA; CTA items
 // of rows with at least heavy_flops products are scheduled first) and the
 // persistent grid size are runtime parameters (ga_ctx tune, set by options
@@ -60,7 +61,7 @@ struct MxmQueue {
     int32_t normal_count;  // CTA items at the back
     int32_t warp_next;
     int32_t cta_next;
-    int32_t pad;
+    int32_t dot_count;     // hybrid form: inner-product tasks listed
     unsigned long long flops;
 };
 
@@ -78,12 +79,19 @@ struct MxmArgs {
     int32_t cta_cap;
     unsigned long long* ctr;  // context work counters (GA_CTR_*)
     int64_t warp_max_flops, heavy_flops;
+    // hybrid form: rows whose inner-product work (sum over mask entries of
+    // min(|A_i|, |B^T_j|)) times hybrid_ratio is below their Gustavson work
+    // are listed in dot_tasks (row, first mask entry; count in the queue),
+    // kDotTask mask entries per task, for the inner-product kernel
+    const int32_t* btr;  // B^T row starts (nullptr: no hybrid)
+    int2* dot_tasks;
+    int64_t hybrid_ratio;
 };
 
 __global__ void k_reset_queue(MxmQueue* q) {
     if (threadIdx.x == 0) {
         q->warp_count = 0; q->heavy_count = 0; q->normal_count = 0;
-        q->warp_next = 0; q->cta_next = 0; q->flops = 0ull;
+        q->warp_next = 0; q->cta_next = 0; q->dot_count = 0; q->flops = 0ull;
     }
 }
 
@@ -113,6 +121,28 @@ __global__ void k_row_bin(MxmArgs<T, A> p) {
         if (f == 0) {
             for (int32_t q = mb + lane; q < me; q += 32) p.cv[q] = (T)0;
             continue;
+        }
+        if (p.btr) {
+            // inner-product work of the row; the cheaper form takes it
+            const int32_t an = ae - ab;
+            long long dsum = 0;
+            for (int32_t q = mb + lane; q < me; q += 32) {
+                const int32_t j = p.mc[q];
+                const int32_t bn = p.btr[j + 1] - p.btr[j];
+                dsum += an < bn ? an : bn;
+            }
+            dsum = warp_sum<long long>(dsum);
+            if (dsum * p.hybrid_ratio < f) {
+                const int ntask = (mi + kDotTask - 1) / kDotTask;
+                int first = 0;
+                if (lane == 0) {
+                    my_flops += (unsigned long long)f;
+                    first = atomicAdd(&p.q->dot_count, ntask);
+                }
+                first = __shfl_sync(0xffffffffu, first, 0);
+                for (int t = lane; t < ntask; t += 32) p.dot_tasks[first + t] = make_int2((int)i, mb + t * kDotTask);
+                continue;
+            }
         }
         if (lane == 0) {
             my_flops += (unsigned long long)f;
@@ -639,7 +669,8 @@ static int64_t cta_item_cap(int64_t m, int64_t n, int64_t mask_nnz) {
 // Launch the masked product for one value type and lookup variant.
 template <int LK, int VM, typename T>
 static void launch_masked(ga_ctx ctx, ga_csr A_, ga_csr B_, ga_csr M_, T* cv, MxmQueue* q, int32_t* warp_rows,
-                          int4* cta_items, int32_t cta_cap, const int32_t* mre) {
+                          int4* cta_items, int32_t cta_cap, const int32_t* mre, const int32_t* btr = nullptr,
+                          int2* dot_tasks = nullptr) {
     using Ac = typename Acc<T>::type;
     MxmArgs<T, Ac> p;
     p.ar = A_->rst; p.ac = A_->col; p.av = static_cast<const T*>(A_->val);
@@ -649,6 +680,9 @@ static void launch_masked(ga_ctx ctx, ga_csr A_, ga_csr B_, ga_csr M_, T* cv, Mx
     p.ctr = ctx->d_counters;
     p.warp_max_flops = ctx->tune.warp_max_flops;
     p.heavy_flops = ctx->tune.heavy_flops;
+    p.btr = btr;
+    p.dot_tasks = dot_tasks;
+    p.hybrid_ratio = ctx->tune.hybrid_ratio;
     {
         ProfScope ps(ctx, "mxm_row_bin");
         int grid = grid_for(p.m * 32, 256, ctx->num_sms * 16);
@@ -802,9 +836,80 @@ __global__ void __launch_bounds__(kDotThreads) k_mxm_dot(DotArgs<T> p) {
     if (lane == 0 && executed) atomicAdd(&p.ctr[GA_CTR_EXECUTED], executed);
 }
 
+// Hybrid form, inner-product rows: one warp per listed task (a row and up
+// to kDotTask of its mask entries), each entry an intersection as in k_mxm_dot.
+template <typename T, bool UNIT>
+__global__ void __launch_bounds__(kDotThreads) k_mxm_dot_rows(DotArgs<T> p, const int2* __restrict__ tasks,
+                                                              const MxmQueue* __restrict__ q) {
+    using Ac = typename Acc<T>::type;
+    const int lane = threadIdx.x & 31;
+    const unsigned FULL = 0xffffffffu;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int n = q->dot_count;
+    unsigned long long executed = 0;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+        const int2 task = tasks[r];
+        const int32_t i = task.x;
+        const int32_t ab = p.ar[i], an = p.ar[i + 1] - ab;
+        const int32_t q_end = min(p.hi[i], task.y + kDotTask);
+        for (int32_t qq = task.y; qq < q_end; ++qq) {
+            const int32_t j = p.mc[qq];
+            const int32_t tb = p.tr[j], tn = p.tr[j + 1] - tb;
+            Ac s = 0;
+            if (an > 0 && tn > 0) {
+                const bool walk_a = an <= tn;
+                const int32_t* Wc = walk_a ? p.ac + ab : p.tc + tb;
+                const int32_t* Sc = walk_a ? p.tc + tb : p.ac + ab;
+                const int wn = walk_a ? an : tn, sn = walk_a ? tn : an;
+                if (lane == 0) executed += (unsigned long long)wn;
+                const bool small = sn <= 32, bucketed = !small && wn >= 32;
+                int32_t key = INT32_MAX;
+                if (small) {
+                    key = lane < sn ? __ldg(Sc + lane) : INT32_MAX;
+                } else if (bucketed) {
+                    const int hi_b = (int)(((int64_t)(lane + 1) * sn) >> 5);
+                    key = __ldg(Sc + hi_b - 1);
+                }
+                for (int base = 0; base < wn; base += 32) {
+                    const int e = base + lane;
+                    const int32_t x = e < wn ? __ldg(Wc + e) : INT32_MAX;
+                    const int b = (small || bucketed) ? warp_lower_bound(key, x) : 0;
+                    bool hit = false;
+                    int pos = 0;
+                    if (small) {
+                        const int32_t y = __shfl_sync(FULL, key, b & 31);
+                        pos = b;
+                        hit = e < wn && b < sn && y == x;
+                    } else if (bucketed) {
+                        if (e < wn && b < 32) {
+                            const int lo_b = (int)(((int64_t)b * sn) >> 5);
+                            const int hi_b = (int)(((int64_t)(b + 1) * sn) >> 5);
+                            pos = lo_b + lower_bound_i32(Sc + lo_b, hi_b - lo_b, x);
+                            hit = pos < hi_b && __ldg(Sc + pos) == x;
+                        }
+                    } else if (e < wn) {
+                        pos = lower_bound_i32(Sc, sn, x);
+                        hit = pos < sn && __ldg(Sc + pos) == x;
+                    }
+                    if (UNIT) {
+                        s += (Ac)__popc(__ballot_sync(FULL, hit));
+                    } else if (hit) {
+                        const T va = walk_a ? p.av[ab + e] : p.av[ab + pos];
+                        const T vb = walk_a ? p.tv[tb + pos] : p.tv[tb + e];
+                        s += (Ac)va * (Ac)vb;
+                    }
+                }
+                if (!UNIT) s = warp_sum<Ac>(s);
+            }
+            if (lane == 0) p.cv[qq] = (T)s;
+        }
+    }
+    if (lane == 0 && executed) atomicAdd(&p.ctr[GA_CTR_EXECUTED], executed);
+}
+
 template <typename T>
 static void launch_dot_t(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr Bt, ga_csr M, T* cv, bool unit,
-                         const int32_t* mre) {
+                         const int32_t* mre, const int2* dot_tasks = nullptr, const MxmQueue* q = nullptr) {
     DotArgs<T> p;
     p.ar = A->rst; p.ac = A->col; p.av = static_cast<const T*>(A->val);
     p.tr = Bt->rst; p.tc = Bt->col; p.tv = static_cast<const T*>(Bt->val);
@@ -818,6 +923,14 @@ static void launch_dot_t(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr Bt, ga_csr M, T*
     p.cv = cv; p.m = M->m; p.ctr = ctx->d_counters;
     p.total = M->nnz;
     p.chunk = ctx->tune.dot_chunk > 0 ? ctx->tune.dot_chunk : 8;
+    if (dot_tasks) {  // hybrid form: the tasks binning listed (it also counted the work)
+        ProfScope ps(ctx, "mxm_dot_rows");
+        const int grid = ctx->num_sms * (2048 / kDotThreads);
+        if (unit) k_mxm_dot_rows<T, true><<<grid, kDotThreads, 0, ctx->stream>>>(p, dot_tasks, q);
+        else k_mxm_dot_rows<T, false><<<grid, kDotThreads, 0, ctx->stream>>>(p, dot_tasks, q);
+        post_launch("mxm_dot_rows");
+        return;
+    }
     {
         ProfScope ps(ctx, "mxm_dot_count");
         k_dot_count<T><<<grid_for(p.m * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(p);
@@ -841,8 +954,13 @@ void mxm_dot_launch(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr Bt, ga_csr M, void* d
 
 void naive_masked_into(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M, void* d_cvals);
 
-size_t mxm_scratch_bytes(int64_t m, int64_t n, int64_t mask_nnz) {
-    return 256 + sizeof(int32_t) * (size_t)(m + 1) + 16 + sizeof(int4) * (size_t)cta_item_cap(m, n, mask_nnz);
+// Hybrid form: inner-product tasks, at most one per kDotTask mask entries of a row.
+static int64_t dot_task_cap(int64_t m, int64_t mask_nnz) { return mask_nnz / kDotTask + m + 1; }
+
+size_t mxm_scratch_bytes(int64_t m, int64_t n, int64_t mask_nnz, bool hybrid) {
+    // queue header, warp rows, CTA items, hybrid inner-product tasks
+    return 256 + sizeof(int32_t) * (size_t)(m + 1) + 16 + sizeof(int4) * (size_t)cta_item_cap(m, n, mask_nnz) +
+           (hybrid ? sizeof(int2) * (size_t)dot_task_cap(m, mask_nnz) : 0);
 }
 
 // Non-allocating launch (usable inside captured loops): `scratch` holds
@@ -850,8 +968,10 @@ size_t mxm_scratch_bytes(int64_t m, int64_t n, int64_t mask_nnz) {
 // unit_b: B's values are all ones (no value loads). mask_row_end (optional):
 // row i's mask is [M->rst[i], mask_row_end[i]) instead of the whole row.
 void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals, void* scratch,
-                       int64_t cap_nnz, bool unit_b, const int32_t* mask_row_end, bool unit_a) {
-    GA_REQUIRE(algo == GA_MSA || algo == GA_MCA || algo == GA_HEAP, GA_ERR_INVALID_ARG, "mxm: unknown algorithm");
+                       int64_t cap_nnz, bool unit_b, const int32_t* mask_row_end, bool unit_a, ga_csr Bt) {
+    GA_REQUIRE(algo == GA_MSA || algo == GA_MCA || algo == GA_HEAP || algo == GA_HYBRID, GA_ERR_INVALID_ARG,
+               "mxm: unknown algorithm");
+    GA_REQUIRE(algo != GA_HYBRID || Bt != nullptr, GA_ERR_INVALID_ARG, "mxm: the hybrid form needs B^T");
     unsigned char* s = static_cast<unsigned char*>(scratch);
     MxmQueue* q = reinterpret_cast<MxmQueue*>(s);
     int32_t* warp_rows = reinterpret_cast<int32_t*>(s + 256);
@@ -859,6 +979,7 @@ void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, v
     off = (off + 15) & ~(size_t)15;
     int4* cta_items = reinterpret_cast<int4*>(s + off);
     const int64_t cap = cta_item_cap(M->m, M->n, cap_nnz);
+    int2* dot_tasks = algo == GA_HYBRID ? reinterpret_cast<int2*>(s + off + sizeof(int4) * (size_t)cap) : nullptr;
     GA_REQUIRE(cap < INT32_MAX, GA_ERR_UNSUPPORTED, "mxm: too many work items");
     k_reset_queue<<<1, 32, 0, ctx->stream>>>(q);
     post_launch("mxm_reset_queue");
@@ -867,7 +988,20 @@ void mxm_masked_launch(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, v
         const int32_t c32 = (int32_t)cap;
         // value mode 2 (every product is 1) only for int32, the k-truss / TC type
         const bool ones = unit_a && unit_b && std::is_same<T, int32_t>::value;
-        if (algo == GA_MSA) {
+        if (algo == GA_HYBRID) {
+            // Gustavson (MSA) rows, then the inner-product rows flagged while binning
+            const int32_t* btr = Bt->rst;
+            if (ones)
+                launch_masked<MD_DENSE, 2, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end, btr,
+                                              dot_tasks);
+            else if (unit_b)
+                launch_masked<MD_DENSE, 1, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end, btr,
+                                              dot_tasks);
+            else
+                launch_masked<MD_DENSE, 0, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end, btr,
+                                              dot_tasks);
+            launch_dot_t<T>(ctx, A, B, Bt, M, cv, unit_a && unit_b, mask_row_end, dot_tasks, q);
+        } else if (algo == GA_MSA) {
             if (ones) launch_masked<MD_DENSE, 2, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
             else if (unit_b) launch_masked<MD_DENSE, 1, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
             else launch_masked<MD_DENSE, 0, T>(ctx, A, B, M, cv, q, warp_rows, cta_items, c32, mask_row_end);
@@ -891,20 +1025,24 @@ void mxm_masked_into(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, voi
         naive_masked_into(ctx, A, B, M, d_cvals);
         return;
     }
-    if (algo == GA_DOT) {
-        const bool unit = csr_unit_values(ctx, A) && csr_unit_values(ctx, B);
-        if (csr_is_symmetric(ctx, B)) {
-            mxm_dot_launch(ctx, A, B, B, M, d_cvals, unit, nullptr);
-        } else {
-            ga_csr Bt = transpose_csr(ctx, B);
-            try {
-                mxm_dot_launch(ctx, A, B, Bt, M, d_cvals, unit, nullptr);
-            } catch (...) {
-                csr_destroy(ctx, Bt);
-                throw;
+    if (algo == GA_DOT || algo == GA_HYBRID) {
+        const bool unit_b = csr_unit_values(ctx, B);
+        const bool unit_a = csr_unit_values(ctx, A);
+        const bool sym = csr_is_symmetric(ctx, B);
+        ga_csr Bt = sym ? B : transpose_csr(ctx, B);
+        try {
+            if (algo == GA_DOT) {
+                mxm_dot_launch(ctx, A, B, Bt, M, d_cvals, unit_a && unit_b, nullptr);
+            } else {
+                DBuf<unsigned char> scratch(ctx, mxm_scratch_bytes(M->m, M->n, M->nnz));
+                mxm_masked_launch(ctx, GA_HYBRID, A, B, M, d_cvals, scratch.p, M->nnz, unit_b, nullptr,
+                                  unit_a && A->dtype == GA_INT32, Bt);
             }
-            csr_destroy(ctx, Bt);
+        } catch (...) {
+            if (!sym) csr_destroy(ctx, Bt);
+            throw;
         }
+        if (!sym) csr_destroy(ctx, Bt);
         return;
     }
     const bool unit_b = csr_unit_values(ctx, B);

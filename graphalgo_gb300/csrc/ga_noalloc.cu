@@ -73,7 +73,7 @@ extern "C" int ga_mxm_masked_noalloc(void* stream, ga_algo algo, int64_t m, int6
     if (!a_rst || !a_val || !b_rst || !m_rst || !m_col || !c_val) return GA_ERR_INVALID_ARG;
     if (!b_unit && !b_val) return GA_ERR_INVALID_ARG;
     // the scratch needed for this shape must fit the fixed array
-    if (mxm_scratch_bytes(m, n, mask_nnz) > kNoAllocScratchBytes) return GA_ERR_INVALID_ARG;
+    if (mxm_scratch_bytes(m, n, mask_nnz, false) > kNoAllocScratchBytes) return GA_ERR_INVALID_ARG;
     try {
         const NoAllocDevice& d = noalloc_setup();
         ga_ctx_s ctx;  // stack-only view: stream and device facts, no allocations

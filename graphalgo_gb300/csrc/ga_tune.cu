@@ -37,11 +37,12 @@ std::map<TuneKey, TuneEntry> g_tune_cache;
 
 int bucket(int64_t x) { return x <= 0 ? 0 : 1 + (int)std::floor(2.0 * std::log2((double)x)); }
 
-MxmTune tune_of(int64_t warp_max, int ctas, int chunk) {
+MxmTune tune_of(int64_t warp_max, int ctas, int chunk, int64_t ratio = 16) {
     MxmTune t;
     t.warp_max_flops = warp_max;
     t.ctas_per_sm = ctas;
     t.dot_chunk = chunk;
+    t.hybrid_ratio = ratio;
     return t;
 }
 
@@ -62,6 +63,8 @@ std::vector<Cand> product_candidates(bool dot_ok, int only) {
     }
     if (dot_ok && (only < 0 || only == GA_DOT))
         for (int chunk : {4, 8, 16}) c.push_back({GA_DOT, tune_of(32768, 0, chunk)});
+    if (dot_ok && (only < 0 || only == GA_HYBRID))
+        for (int64_t ratio : {4, 16, 64}) c.push_back({GA_HYBRID, tune_of(32768, 0, 8, ratio)});
     return c;
 }
 
@@ -158,7 +161,8 @@ TuneEntry tune_support(ga_ctx ctx, ga_csr A, int only) {
     const int32_t* mre = sym ? A->rst + 1 : nullptr;
     return pick(ctx, product_candidates(sym, only), [&](const Cand& c) {
         if (c.algo == GA_DOT) mxm_dot_launch(ctx, A, A, A, M, sup.p, unit, mre);
-        else mxm_masked_launch(ctx, c.algo, A, A, M, sup.p, scr.p, nnz, unit, mre, unit);
+        else mxm_masked_launch(ctx, c.algo, A, A, M, sup.p, scr.p, nnz, unit, mre, unit,
+                               c.algo == GA_HYBRID ? A : nullptr);
     });
 }
 
@@ -244,21 +248,24 @@ int ga_autotune(ga_ctx ctx, int kind, ga_csr A, ga_csr B, ga_csr M, int force, g
 int ga_autotune_variant(ga_ctx ctx, int kind, int algo, ga_csr A, ga_csr B, ga_csr M, int force,
                         ga_tune_result* out) {
     if (!ctx || !A || !out) return GA_ERR_INVALID_ARG;
-    if (algo != -1 && algo != GA_MSA && algo != GA_MCA && algo != GA_DOT) return GA_ERR_INVALID_ARG;
+    if (algo != -1 && algo != GA_MSA && algo != GA_MCA && algo != GA_DOT && algo != GA_HYBRID)
+        return GA_ERR_INVALID_ARG;
     if (kind != GA_TUNE_KTRUSS && kind != GA_TUNE_TC && kind != GA_TUNE_PRODUCT) return GA_ERR_INVALID_ARG;
     if (kind == GA_TUNE_PRODUCT && (!B || !M)) return GA_ERR_INVALID_ARG;
     GA_API_BODY(ctx, {
         GA_REQUIRE(kind == GA_TUNE_PRODUCT || A->m == A->n, GA_ERR_SHAPE, "autotune: square matrix expected");
         GA_REQUIRE(A->nnz > 0, GA_ERR_INVALID_ARG, "autotune: empty matrix");
         bool cached = false;
-        if (algo == GA_DOT && kind == GA_TUNE_KTRUSS)
-            GA_REQUIRE(csr_is_symmetric(ctx, A), GA_ERR_UNSUPPORTED, "autotune: GA_DOT k-truss needs a symmetric matrix");
+        if ((algo == GA_DOT || algo == GA_HYBRID) && kind == GA_TUNE_KTRUSS)
+            GA_REQUIRE(csr_is_symmetric(ctx, A), GA_ERR_UNSUPPORTED,
+                       "autotune: GA_DOT / GA_HYBRID k-truss needs a symmetric matrix");
         const TuneEntry e = lookup_or_tune(ctx, kind, A, B, M, force != 0, &cached, algo);
         out->algo = e.algo;
         out->warp_max_flops = e.t.warp_max_flops;
         out->heavy_flops = e.t.heavy_flops;
         out->ctas_per_sm = e.t.ctas_per_sm;
         out->dot_chunk = e.t.dot_chunk;
+        out->hybrid_ratio = e.t.hybrid_ratio;
         out->ms = e.ms;
         out->default_ms = e.default_ms;
         out->candidates = e.candidates;

@@ -59,7 +59,10 @@ typedef enum {
     GA_DOT = 4,   /* inner-product form: each mask entry (i,j) is A_i . (B^T)_j by warp
                      sorted-list intersection (B^T built on the fly unless B is
                      symmetric); TC's dot kernel; k-truss support (symmetric A) */
-    GA_AUTO = 5   /* the autotuner's choice of variant and schedule (ga_autotune) */
+    GA_AUTO = 5,  /* the autotuner's choice of variant and schedule (ga_autotune) */
+    GA_HYBRID = 6 /* per output row, the cheaper of MSA (Gustavson work: the row's
+                     products) and the inner-product form (work: sum over its mask
+                     entries of min(|A_i|, |B^T_j|)), decided while binning */
 } ga_algo;
 
 /* status codes */
@@ -104,9 +107,12 @@ GA_API int ga_version(int* major, int* minor);
  * warp, larger rows by CTAs; GA_OPT_MXM_HEAVY_FLOPS (2^20): CTA work of rows
  * with at least this many products is scheduled first;
  * GA_OPT_MXM_CTAS_PER_SM (0 = as many as fit): persistent grid size;
- * GA_OPT_DOT_CHUNK (8): mask entries per warp task of the inner-product form. */
+ * GA_OPT_DOT_CHUNK (8): mask entries per warp task of the inner-product form;
+ * GA_OPT_HYBRID_RATIO (16): GA_HYBRID sends a row to the inner-product form
+ * when its inner-product work times this is below its Gustavson work. */
 enum { GA_OPT_DEVICE_LOOPS = 1, GA_OPT_PROFILE = 2, GA_OPT_FAIL_ALLOC_AFTER = 3, GA_OPT_KNN_TILED = 4,
-       GA_OPT_MXM_WARP_FLOPS = 5, GA_OPT_MXM_HEAVY_FLOPS = 6, GA_OPT_MXM_CTAS_PER_SM = 7, GA_OPT_DOT_CHUNK = 8 };
+       GA_OPT_MXM_WARP_FLOPS = 5, GA_OPT_MXM_HEAVY_FLOPS = 6, GA_OPT_MXM_CTAS_PER_SM = 7, GA_OPT_DOT_CHUNK = 8,
+       GA_OPT_HYBRID_RATIO = 9 };
 GA_API int ga_ctx_set_option(ga_ctx ctx, int option, int64_t value);
 
 /* Per-kernel timing collected while GA_OPT_PROFILE is on. Writes up to `cap`
@@ -307,6 +313,7 @@ typedef struct {
     int algo;               /* chosen ga_algo */
     int64_t warp_max_flops, heavy_flops;
     int ctas_per_sm, dot_chunk;
+    int64_t hybrid_ratio;
     double ms;              /* its time on the problem */
     double default_ms;      /* the default schedule (MSA) on the same problem */
     int candidates;

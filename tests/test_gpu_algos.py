@@ -51,7 +51,7 @@ def test_tc_other_forms(ctx):
     assert int(ref.sum()) == 3 * total
 
 
-@pytest.mark.parametrize("algo", ["msa", "mca", "heap", "dot"])
+@pytest.mark.parametrize("algo", ["msa", "mca", "heap", "dot", "hybrid"])
 @pytest.mark.parametrize("device_loops", [1, 0])
 def test_ktruss(ctx, algo, device_loops):
     ctx.set_option(ga.OPT_DEVICE_LOOPS, device_loops)

@@ -13,7 +13,7 @@ from graphs import random_csr, random_graph, to_device
 
 pytestmark = pytest.mark.gpu
 
-ALGOS = ["msa", "mca", "heap", "naive", "dot"]
+ALGOS = ["msa", "mca", "heap", "naive", "dot", "hybrid"]
 
 
 def _abs_product(A, B, M):
@@ -49,7 +49,7 @@ def test_masked_random(ctx, algo, dtype):
         _check_vals(val, ref, A, B, M, dtype)
 
 
-@pytest.mark.parametrize("algo", ["msa", "mca", "heap", "dot"])
+@pytest.mark.parametrize("algo", ["msa", "mca", "heap", "dot", "hybrid"])
 def test_masked_uint8_wraps_like_reference(ctx, algo):
     rng = np.random.default_rng(3)
     A = random_csr(70, 70, 0.5, rng, np.uint8)
@@ -61,7 +61,7 @@ def test_masked_uint8_wraps_like_reference(ctx, algo):
     assert np.array_equal(C.download()[2], ref)
 
 
-@pytest.mark.parametrize("algo", ["msa", "mca", "heap", "dot"])
+@pytest.mark.parametrize("algo", ["msa", "mca", "heap", "dot", "hybrid"])
 def test_masked_long_rows_and_hubs(ctx, algo):
     """Mask rows longer than one CTA item (4096 slots) and hub rows of B."""
     rng = np.random.default_rng(5)

@@ -21,7 +21,7 @@ def test_autotune_ktruss_cached_and_exact(ctx, rmat):
     G, A = rmat
     before = ctx.work_counters()
     r1 = ga.autotune(ga.TUNE_KTRUSS, A, force=True)
-    assert r1["algo"] in ("msa", "mca", "dot") and r1["cached"] == 0 and r1["candidates"] >= 5
+    assert r1["algo"] in ("msa", "mca", "dot", "hybrid") and r1["cached"] == 0 and r1["candidates"] >= 5
     assert 0 < r1["ms"] <= r1["default_ms"] + 1e-9
     r2 = ga.autotune(ga.TUNE_KTRUSS, A)
     assert r2["cached"] == 1 and r2["algo"] == r1["algo"]
@@ -51,15 +51,16 @@ def test_autotune_tc_and_product(ctx, rmat):
 
 @pytest.mark.parametrize("opt,val", [(ga.OPT_MXM_WARP_FLOPS, 0), (ga.OPT_MXM_WARP_FLOPS, 1 << 40),
                                      (ga.OPT_MXM_HEAVY_FLOPS, 1), (ga.OPT_MXM_CTAS_PER_SM, 1),
-                                     (ga.OPT_DOT_CHUNK, 1), (ga.OPT_DOT_CHUNK, 64)])
+                                     (ga.OPT_DOT_CHUNK, 1), (ga.OPT_DOT_CHUNK, 64),
+                                     (ga.OPT_HYBRID_RATIO, 0), (ga.OPT_HYBRID_RATIO, 1 << 20)])
 def test_schedule_options_do_not_change_results(ctx, rmat, opt, val):
     G, A = rmat
     ref = oracle.mxm_masked(G, G, G)
     defaults = {ga.OPT_MXM_WARP_FLOPS: 32768, ga.OPT_MXM_HEAVY_FLOPS: 1 << 20, ga.OPT_MXM_CTAS_PER_SM: 0,
-                ga.OPT_DOT_CHUNK: 8}
+                ga.OPT_DOT_CHUNK: 8, ga.OPT_HYBRID_RATIO: 16}
     ctx.set_option(opt, val)
     try:
-        for algo in ("msa", "mca", "heap", "dot"):
+        for algo in ("msa", "mca", "heap", "dot", "hybrid"):
             assert np.array_equal(ga.mxm_masked(algo, A, A, A).download()[2], ref), algo
         C, it = ga.ktruss("msa", A, 4)
         R, rit = oracle.ktruss(G, 4)
