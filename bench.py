@@ -5,11 +5,14 @@ Workload (one step): the k-truss sweep k = 3, 4, ... up to the largest k with
 a non-empty truss, on a seeded R-MAT graph (scale 18, edge factor 16,
 a/b/c/d = 0.57/0.19/0.19/0.05, symmetrised, loops and duplicates removed,
 int32 CSR, 262,144 vertices, 7.6M stored entries). Each k runs the
-reference's k_truss (src/main.cpp:90-146: Tmp<C> = C*C with the MSA masked
-SpGEMM, prune below k-2, repeat until nnz is unchanged) through the C ABI;
+reference's k_truss (src/main.cpp:90-146: Tmp<C> = C*C masked by C, prune
+below k-2, repeat until nnz is unchanged) through the C ABI, the support
+product with the hybrid masked SpGEMM by default (per output row the cheaper
+of MSA and the inner-product form; --algo msa|mca|heap|dot runs one form);
 k starts from the (k-1)-truss, which contains it (same edge sets as starting
-from A). value = 2 * (Gustavson products of every support product) / time,
-inputs resident in HBM, L2 flushed (256 MiB write) between steps.
+from A). value = 2 * (Gustavson products of every support product, the work
+of the reference's C<M> = A*B whatever form computes it) / time, inputs
+resident in HBM, L2 flushed (256 MiB write) between steps.
 
 e2e: the same sweep through the public API from pinned host buffers: upload
 A, run the sweep, download every k-truss (row starts and columns).
@@ -92,7 +95,7 @@ def parse_args():
     args = ap.parse_args()
     auto = args.workload == "batch" or args.case == "batch"
     if args.algo is None:
-        args.algo = "auto" if auto else "msa"
+        args.algo = "auto" if auto else ("hybrid" if args.workload == "ktruss-sweep" and not args.case else "msa")
     if args.tc_algo is None:
         args.tc_algo = "auto" if auto else "msa"
     return args
@@ -351,7 +354,9 @@ def profile_step(ga, ctx, run, algo, counters, loops):
     kname = {"msa": "mxm_msa", "mca": "mxm_mca", "heap": "mxm_heap_merge", "dot": "mxm_dot",
              "hybrid": "mxm_msa"}[algo]
     k_launches, k_ms = stats.get(kname, (0, 0.0))
-    bytes_model = 8 * ctr["rows"] + 16 * ctr["a_entries"] + 8 * ctr["executed"] + 8 * ctr["mask_entries"]
+    # products of the Gustavson kernels; list entries walked for the inner-product one
+    ex = ctr["executed_dot"] if algo == "dot" else ctr["executed"]
+    bytes_model = 8 * ctr["rows"] + 16 * ctr["a_entries"] + 8 * ex + 8 * ctr["mask_entries"]
     peak, peak_kind = measured_peak_hbm()
     achieved = bytes_model / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
     tpe = profile_traffic()

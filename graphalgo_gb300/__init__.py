@@ -169,11 +169,12 @@ class Context:
 
     def work_counters(self, reset: bool = False) -> dict:
         """Masked-SpGEMM work since the last reset: Gustavson products P of the
-        requested products, mask entries, launches, A entries, rows, and the
-        products the kernels actually processed (device counters)."""
-        out = (ctypes.c_int64 * 6)()
+        requested products, mask entries, launches, A entries, rows, the
+        products the Gustavson kernels processed, and the list entries the
+        inner-product kernels walked (device counters)."""
+        out = (ctypes.c_int64 * 7)()
         _check(lib().ga_ctx_work_counters(self.handle, out, int(bool(reset))), self)
-        return dict(zip(("products", "mask_entries", "launches", "a_entries", "rows", "executed"),
+        return dict(zip(("products", "mask_entries", "launches", "a_entries", "rows", "executed", "executed_dot"),
                         (int(x) for x in out)))
 
     def flush_l2(self):

@@ -833,7 +833,7 @@ __global__ void __launch_bounds__(kDotThreads) k_mxm_dot(DotArgs<T> p) {
             if (lane == 0) p.cv[q] = (T)s;
         }
     }
-    if (lane == 0 && executed) atomicAdd(&p.ctr[GA_CTR_EXECUTED], executed);
+    if (lane == 0 && executed) atomicAdd(&p.ctr[GA_CTR_EXECUTED_DOT], executed);
 }
 
 // Hybrid form, inner-product rows: one warp per listed task (a row and up
@@ -904,7 +904,7 @@ __global__ void __launch_bounds__(kDotThreads) k_mxm_dot_rows(DotArgs<T> p, cons
             if (lane == 0) p.cv[qq] = (T)s;
         }
     }
-    if (lane == 0 && executed) atomicAdd(&p.ctr[GA_CTR_EXECUTED], executed);
+    if (lane == 0 && executed) atomicAdd(&p.ctr[GA_CTR_EXECUTED_DOT], executed);
 }
 
 template <typename T>

@@ -142,12 +142,13 @@ GA_API int ga_ctx_mem_stats(ga_ctx ctx, int64_t* in_use, int64_t* peak, int rese
  * (i,k) of nnz(B_k) (the work of the reference's C<M> = A*B), mask entries,
  * launches, A entries, rows, and the products the kernels actually processed
  * (fewer than P when a k-truss support product only evaluates the upper
- * triangle of a symmetric matrix and mirrors it; for DOT, the list entries
- * its intersections walked). They feed the GFLOP/s (2P)
+ * triangle of a symmetric matrix and mirrors it), and the list entries the
+ * inner-product intersections walked (DOT, and the hybrid form's
+ * inner-product rows). They feed the GFLOP/s (2P)
  * and byte models. out has GA_CTR_COUNT entries; reset != 0 zeroes them
  * after reading. Synchronises the stream. */
 enum { GA_CTR_PRODUCTS = 0, GA_CTR_MASK_ENTRIES = 1, GA_CTR_LAUNCHES = 2, GA_CTR_A_ENTRIES = 3,
-       GA_CTR_ROWS = 4, GA_CTR_EXECUTED = 5, GA_CTR_COUNT = 6 };
+       GA_CTR_ROWS = 4, GA_CTR_EXECUTED = 5, GA_CTR_EXECUTED_DOT = 6, GA_CTR_COUNT = 7 };
 GA_API int ga_ctx_work_counters(ga_ctx ctx, int64_t* out, int reset);
 
 /* Kernel launches issued by this library in this process so far (counted on
