@@ -34,6 +34,8 @@ ALGO_NAMES = {v: k for k, v in ALGOS.items()}
 OPT_DEVICE_LOOPS, OPT_PROFILE, OPT_FAIL_ALLOC_AFTER, OPT_KNN_TILED = 1, 2, 3, 4
 OPT_MXM_WARP_FLOPS, OPT_MXM_HEAVY_FLOPS, OPT_MXM_CTAS_PER_SM, OPT_DOT_CHUNK, OPT_HYBRID_RATIO = 5, 6, 7, 8, 9
 TUNE_KTRUSS, TUNE_PRODUCT, TUNE_TC = 0, 1, 2
+# edge-list / file ingestion flags
+EDGES_MIRROR, EDGES_DROP_LOOPS, EDGES_LOWER_SYMM, EDGES_UNIT = 1, 2, 4, 8
 # status codes
 OK, ERR_INVALID_ARG, ERR_INVALID_CSR, ERR_SHAPE, ERR_DTYPE, ERR_CUDA, ERR_OOM, ERR_NO_DEVICE, \
     ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_ADMISSION = range(11)
@@ -365,6 +367,48 @@ def symm_from_lower(L: Csr) -> Csr:
 
 def adjacency(A: Csr) -> Csr:
     return _new(A.ctx, lib().ga_adjacency, A.handle)
+
+
+# ------------------------------------------------------------- ingestion
+def csr_from_edges(ctx: Context, m: int, n: int, src, dst, val=None, flags: int = 0,
+                   dtype: Optional[int] = None) -> Csr:
+    """Edge list to a device CSR (rows sorted, duplicates merged onto the
+    earliest edge's value); `flags` from EDGES_*."""
+    src = np.ascontiguousarray(src, dtype=np.int32)
+    dst = np.ascontiguousarray(dst, dtype=np.int32)
+    if val is not None:
+        val = np.ascontiguousarray(val)
+        if dtype is None:
+            dtype = _DT[val.dtype]
+        val = np.ascontiguousarray(val, dtype=_NP[dtype])
+    elif dtype is None:
+        dtype = INT32
+    h = _p()
+    _check(lib().ga_csr_from_edges(ctx.handle, _i64(m), _i64(n), _i64(len(src)), _ptr(src), _ptr(dst), _ptr(val),
+                                   int(dtype), int(flags), ctypes.byref(h)), ctx)
+    return Csr(ctx, h)
+
+
+def read_mtx(ctx: Context, path: str, flags: int = 0) -> Tuple[Csr, bytes]:
+    """Matrix Market coordinate file parsed on the device, with the
+    reference's reader semantics; returns (matrix, 4-byte type code)."""
+    h = _p()
+    code = ctypes.create_string_buffer(4)
+    _check(lib().ga_read_mtx(ctx.handle, os.fsencode(path), int(flags), code, ctypes.byref(h)), ctx)
+    return Csr(ctx, h), code.raw
+
+
+def read_bin(ctx: Context, path: str, flags: int = 0) -> Tuple[Csr, bytes]:
+    """Binary CSR file in the reference's layout; returns (matrix, matcode)."""
+    h = _p()
+    code = ctypes.create_string_buffer(4)
+    _check(lib().ga_read_bin(ctx.handle, os.fsencode(path), int(flags), code, ctypes.byref(h)), ctx)
+    return Csr(ctx, h), code.raw
+
+
+def write_bin(A: Csr, path: str, matcode: Optional[bytes] = None) -> None:
+    code = None if matcode is None else ctypes.create_string_buffer(bytes(matcode[:4]), 4)
+    _check(lib().ga_write_bin(A.ctx.handle, A.handle, code, os.fsencode(path)), A.ctx)
 
 
 def convert(A: Csr, dtype: int) -> Csr:

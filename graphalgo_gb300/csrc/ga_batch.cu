@@ -360,7 +360,7 @@ static ga_csr gen_knn_batch(ga_ctx ctx, int64_t count, const int32_t* n, const i
     GA_CUDA(cudaMemcpyAsync(cursor.p, rst.p, sizeof(int32_t) * (np + 1), cudaMemcpyDeviceToDevice, ctx->stream));
     k_knn_fill<<<grid_for(np * k, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(nb.p, np, k, cursor.p, col.p);
     post_launch("knn_fill");
-    sort_rows_by_key(ctx, rst.p, np, col.p, pay.p);
+    sort_rows_by_key(ctx, rst.p, np, col.p, pay.p, total);
     k_unique_count<<<grid_for(np, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(rst.p, col.p, np, cnt.p);
     post_launch("unique_count");
     DBuf<int32_t> orst(ctx, (size_t)np + 1);

@@ -195,14 +195,18 @@ __global__ void k_validate_csr(const int32_t* __restrict__ rst, const int32_t* _
     }
 }
 
-void validate_csr(ga_ctx ctx, const int32_t* rst, const int32_t* col, int64_t m, int64_t n, int64_t nnz) {
+int csr_check_bits(ga_ctx ctx, const int32_t* rst, const int32_t* col, int64_t m, int64_t n, int64_t nnz) {
     DBuf<int> err(ctx, 1);
     GA_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), ctx->stream));
     int block = 256;
     int grid = grid_for(m * 32, block, ctx->num_sms * 16);
     k_validate_csr<<<grid, block, 0, ctx->stream>>>(rst, col, m, n, nnz, err.p);
     post_launch("validate_csr");
-    int e = read_i32(ctx, err.p);
+    return read_i32(ctx, err.p);
+}
+
+void validate_csr(ga_ctx ctx, const int32_t* rst, const int32_t* col, int64_t m, int64_t n, int64_t nnz) {
+    const int e = csr_check_bits(ctx, rst, col, m, n, nnz);
     if (e & 1) fail(GA_ERR_INVALID_CSR, "invalid CSR: row starts are not a monotone 0..nnz sequence");
     if (e & 2) fail(GA_ERR_INVALID_CSR, "invalid CSR: column index out of range");
     if (e & 4) fail(GA_ERR_INVALID_CSR, "invalid CSR: columns not strictly ascending within a row");

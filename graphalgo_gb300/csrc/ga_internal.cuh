@@ -184,9 +184,14 @@ void fill_ones(ga_ctx ctx, void* vals, int64_t count, ga_dtype dt);
 
 // Validates a device CSR; throws GA_ERR_INVALID_CSR when malformed.
 void validate_csr(ga_ctx ctx, const int32_t* rst, const int32_t* col, int64_t m, int64_t n, int64_t nnz);
+// The same checks as bits: 1 row starts not a monotone 0..nnz sequence,
+// 2 a column out of range, 4 columns not strictly ascending in some row.
+int csr_check_bits(ga_ctx ctx, const int32_t* rst, const int32_t* col, int64_t m, int64_t n, int64_t nnz);
 
-// Sorts each CSR row segment by key (payload follows), rows up to 8192 long.
-void sort_rows_by_key(ga_ctx ctx, const int32_t* rst, int64_t m, int32_t* key, int32_t* pay);
+// Sorts each CSR row segment by key (payload follows): rows of up to 8,192
+// entries by a bitonic sort in shared memory, longer ones by one CTA each
+// (sorted pieces, then merge-path merges). nnz: entries of the whole matrix.
+void sort_rows_by_key(ga_ctx ctx, const int32_t* rst, int64_t m, int32_t* key, int32_t* pay, int64_t nnz);
 
 // k-truss on a single matrix (batch == nullptr) or on a block-diagonal union
 // of graphs with per-graph convergence (see ga_batch_ktruss).

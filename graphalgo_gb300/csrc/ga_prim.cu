@@ -253,60 +253,176 @@ __global__ void k_transpose_scatter(const int32_t* __restrict__ rst, const int32
     }
 }
 
-// Sort every row segment by key (distinct keys) with a block-wide bitonic
-// sort in shared memory; payload follows its key. Rows longer than cap are
-// skipped (flagged in *too_long).
+// Sort every row segment by key with a block-wide bitonic sort in shared
+// memory; the payload follows its key. Rows longer than kSortCap are listed
+// in long_rows (count in *nlong) for k_sort_long_rows.
 constexpr int kSortCap = 8192;
 
-__global__ void k_sort_rows(const int32_t* __restrict__ rst, int64_t m, int32_t* __restrict__ key,
-                            int32_t* __restrict__ pay, int* __restrict__ too_long) {
-    extern __shared__ int32_t sm[];
-    int32_t* sk = sm;
-    int32_t* sp = sm + kSortCap;
-    for (int64_t i = blockIdx.x; i < m; i += gridDim.x) {
-        int32_t b = rst[i], e = rst[i + 1];
-        int len = e - b;
-        if (len <= 1) continue;
-        if (len > kSortCap) {
-            if (threadIdx.x == 0) atomicOr(too_long, 1);
-            continue;
-        }
-        int p2 = 1;
-        while (p2 < len) p2 <<= 1;
-        for (int t = threadIdx.x; t < p2; t += blockDim.x) {
-            if (t < len) { sk[t] = key[b + t]; sp[t] = pay[b + t]; }
-            else { sk[t] = INT32_MAX; sp[t] = 0; }
-        }
-        __syncthreads();
-        for (int k = 2; k <= p2; k <<= 1) {
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                for (int t = threadIdx.x; t < p2; t += blockDim.x) {
-                    int x = t ^ j;
-                    if (x > t) {
-                        bool up = (t & k) == 0;
-                        int32_t a = sk[t], c = sk[x];
-                        if ((a > c) == up) {
-                            sk[t] = c; sk[x] = a;
-                            int32_t pa = sp[t]; sp[t] = sp[x]; sp[x] = pa;
-                        }
+// Block-wide bitonic sort of len <= kSortCap (key, payload) pairs at gk/gp,
+// staged in sk/sp (shared, kSortCap entries each). All threads call it.
+__device__ void block_sort_pairs(int32_t* gk, int32_t* gp, int len, int32_t* sk, int32_t* sp) {
+    int p2 = 1;
+    while (p2 < len) p2 <<= 1;
+    for (int t = threadIdx.x; t < p2; t += blockDim.x) {
+        if (t < len) { sk[t] = gk[t]; sp[t] = gp[t]; }
+        else { sk[t] = INT32_MAX; sp[t] = 0; }
+    }
+    __syncthreads();
+    for (int k = 2; k <= p2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int t = threadIdx.x; t < p2; t += blockDim.x) {
+                int x = t ^ j;
+                if (x > t) {
+                    bool up = (t & k) == 0;
+                    int32_t a = sk[t], c = sk[x];
+                    if ((a > c) == up) {
+                        sk[t] = c; sk[x] = a;
+                        int32_t pa = sp[t]; sp[t] = sp[x]; sp[x] = pa;
                     }
                 }
-                __syncthreads();
+            }
+            __syncthreads();
+        }
+    }
+    for (int t = threadIdx.x; t < len; t += blockDim.x) { gk[t] = sk[t]; gp[t] = sp[t]; }
+    __syncthreads();
+}
+
+// Rows of at most 32 entries: one warp, one entry per lane, bitonic network
+// over shuffles (lanes past the row hold INT32_MAX). Longer rows are listed
+// for a CTA: up to kSortCap entries in `mid_rows` (k_sort_mid_rows), beyond
+// that in `long_rows` (k_sort_long_rows).
+__global__ void k_sort_rows(const int32_t* __restrict__ rst, int64_t m, int32_t* __restrict__ key,
+                            int32_t* __restrict__ pay, int32_t* __restrict__ mid_rows, int* __restrict__ nmid,
+                            int32_t* __restrict__ long_rows, int* __restrict__ nlong) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < m; i += warps) {
+        const int32_t b = rst[i], len = rst[i + 1] - b;
+        if (len <= 1) continue;
+        if (len > 32) {
+            if (lane == 0) {
+                if (len > kSortCap) long_rows[atomicAdd(nlong, 1)] = (int32_t)i;
+                else mid_rows[atomicAdd(nmid, 1)] = (int32_t)i;
+            }
+            continue;
+        }
+        int32_t k = lane < len ? key[b + lane] : INT32_MAX;
+        int32_t v = lane < len ? pay[b + lane] : 0;
+        for (int w = 2; w <= 32; w <<= 1) {
+            for (int j = w >> 1; j > 0; j >>= 1) {
+                const int32_t ok = __shfl_xor_sync(0xffffffffu, k, j);
+                const int32_t ov = __shfl_xor_sync(0xffffffffu, v, j);
+                const bool up = (lane & w) == 0, low = (lane & j) == 0;
+                // the lower lane of an ascending pair keeps the smaller key
+                if (low == up ? ok < k : ok > k) {
+                    k = ok;
+                    v = ov;
+                }
             }
         }
-        for (int t = threadIdx.x; t < len; t += blockDim.x) { key[b + t] = sk[t]; pay[b + t] = sp[t]; }
-        __syncthreads();
+        if (lane < len) {
+            key[b + lane] = k;
+            pay[b + lane] = v;
+        }
     }
 }
 
-void sort_rows_by_key(ga_ctx ctx, const int32_t* rst, int64_t m, int32_t* key, int32_t* pay) {
-    DBuf<int> flag(ctx, 1);
-    GA_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), ctx->stream));
-    const size_t smem = 2 * kSortCap * sizeof(int32_t);
-    GA_CUDA(cudaFuncSetAttribute(k_sort_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_sort_rows<<<ctx->num_sms * 2, 512, smem, ctx->stream>>>(rst, m, key, pay, flag.p);
+__global__ void k_sort_mid_rows(const int32_t* __restrict__ rst, const int32_t* __restrict__ rows,
+                                const int* __restrict__ nrows, int32_t* __restrict__ key,
+                                int32_t* __restrict__ pay) {
+    extern __shared__ int32_t sm[];
+    const int n = *nrows;
+    for (int r = blockIdx.x; r < n; r += gridDim.x) {
+        const int32_t i = rows[r];
+        const int32_t b = rst[i];
+        block_sort_pairs(key + b, pay + b, rst[i + 1] - b, sm, sm + kSortCap);
+    }
+}
+
+// First i (A entries among the first d outputs) of the stable merge of
+// sorted A[0, na) and B[0, nb): ties take A first.
+__device__ __forceinline__ int32_t merge_split(const int32_t* A, int32_t na, const int32_t* B, int32_t nb,
+                                               int32_t d) {
+    int32_t lo = d > nb ? d - nb : 0, hi = d < na ? d : na;
+    while (lo < hi) {
+        const int32_t mid = (lo + hi) >> 1;
+        if (A[mid] <= B[d - 1 - mid]) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// One CTA per long row: kSortCap-entry pieces sorted in shared memory, then
+// pairs of sorted runs merged (merge path: each thread finds its split of
+// the output by a binary search and merges its share) between the row's
+// place in key/pay and the same place in tkey/tpay, doubling the run length
+// each pass.
+__global__ void __launch_bounds__(512) k_sort_long_rows(const int32_t* __restrict__ rst,
+                                                        const int32_t* __restrict__ rows, int32_t* key,
+                                                        int32_t* pay, int32_t* tkey, int32_t* tpay) {
+    extern __shared__ int32_t sm[];
+    const int32_t i = rows[blockIdx.x];
+    const int32_t b = rst[i], L = rst[i + 1] - b;
+    int32_t* k0 = key + b;
+    int32_t* p0 = pay + b;
+    int32_t* k1 = tkey + b;
+    int32_t* p1 = tpay + b;
+    for (int32_t c0 = 0; c0 < L; c0 += kSortCap)
+        block_sort_pairs(k0 + c0, p0 + c0, min(kSortCap, L - c0), sm, sm + kSortCap);
+    for (int64_t w = kSortCap; w < L; w <<= 1) {
+        for (int64_t s0 = 0; s0 < L; s0 += 2 * w) {
+            const int32_t na = (int32_t)min(w, (int64_t)L - s0);
+            const int32_t nb = (int32_t)min(w, (int64_t)L - s0 - na);
+            const int32_t total = na + nb;
+            const int32_t* A = k0 + s0;
+            const int32_t* Ap = p0 + s0;
+            const int32_t* B = A + na;
+            const int32_t* Bp = Ap + na;
+            const int32_t per = (total + (int32_t)blockDim.x - 1) / (int32_t)blockDim.x;
+            const int32_t d0 = min(total, (int32_t)threadIdx.x * per), d1 = min(total, d0 + per);
+            if (d0 >= d1) continue;
+            int32_t ia = merge_split(A, na, B, nb, d0), ib = d0 - ia;
+            for (int32_t o = d0; o < d1; ++o) {
+                const bool take_a = ib >= nb || (ia < na && A[ia] <= B[ib]);
+                k1[s0 + o] = take_a ? A[ia] : B[ib];
+                p1[s0 + o] = take_a ? Ap[ia] : Bp[ib];
+                if (take_a) ++ia; else ++ib;
+            }
+        }
+        __syncthreads();
+        int32_t* t = k0; k0 = k1; k1 = t;
+        t = p0; p0 = p1; p1 = t;
+    }
+    if (k0 != key + b)
+        for (int32_t t = threadIdx.x; t < L; t += blockDim.x) {
+            key[b + t] = k0[t];
+            pay[b + t] = p0[t];
+        }
+}
+
+void sort_rows_by_key(ga_ctx ctx, const int32_t* rst, int64_t m, int32_t* key, int32_t* pay, int64_t nnz) {
+    if (m <= 0 || nnz <= 1) return;
+    DBuf<int> counts(ctx, 2);  // [0] medium rows, [1] long rows
+    DBuf<int32_t> mid_rows(ctx, (size_t)m + 1), long_rows(ctx, (size_t)m + 1);
+    GA_CUDA(cudaMemsetAsync(counts.p, 0, 2 * sizeof(int), ctx->stream));
+    k_sort_rows<<<grid_for(m * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(
+        rst, m, key, pay, mid_rows.p, counts.p, long_rows.p, counts.p + 1);
     post_launch("sort_rows");
-    if (read_i32(ctx, flag.p)) fail(GA_ERR_UNSUPPORTED, "row sort: a row holds more than 8192 entries");
+    const size_t smem = 2 * kSortCap * sizeof(int32_t);
+    GA_CUDA(cudaFuncSetAttribute(k_sort_mid_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // 64 KB of shared memory per CTA: three CTAs per SM
+    k_sort_mid_rows<<<ctx->num_sms * 3, 512, smem, ctx->stream>>>(rst, mid_rows.p, counts.p, key, pay);
+    post_launch("sort_mid_rows");
+    int h[2];
+    GA_CUDA(cudaMemcpyAsync(h, counts.p, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    GA_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (h[1] == 0) return;
+    DBuf<int32_t> tkey(ctx, (size_t)nnz), tpay(ctx, (size_t)nnz);
+    GA_CUDA(cudaFuncSetAttribute(k_sort_long_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_sort_long_rows<<<h[1], 512, smem, ctx->stream>>>(rst, long_rows.p, key, pay, tkey.p, tpay.p);
+    post_launch("sort_long_rows");
+    GA_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
 template <typename T>
@@ -330,19 +446,12 @@ ga_csr transpose_csr(ga_ctx ctx, ga_csr A) {
         if (A->nnz) {
             DBuf<int32_t> cursor(ctx, (size_t)A->n + 1);
             DBuf<int32_t> src(ctx, (size_t)A->nnz);
-            DBuf<int> flag(ctx, 1);
-            GA_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), ctx->stream));
             GA_CUDA(cudaMemcpyAsync(cursor.p, T->rst, sizeof(int32_t) * (A->n + 1), cudaMemcpyDeviceToDevice,
                                     ctx->stream));
             k_transpose_scatter<<<grid_for(A->m * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(
                 A->rst, A->col, A->m, cursor.p, T->col, src.p);
             post_launch("transpose_scatter");
-            size_t smem = 2 * kSortCap * sizeof(int32_t);
-            GA_CUDA(cudaFuncSetAttribute(k_sort_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_sort_rows<<<ctx->num_sms * 2, 512, smem, ctx->stream>>>(T->rst, T->m, T->col, src.p, flag.p);
-            post_launch("sort_rows");
-            if (read_i32(ctx, flag.p))
-                fail(GA_ERR_UNSUPPORTED, "transpose: a column holds more than 8192 entries");
+            sort_rows_by_key(ctx, T->rst, T->m, T->col, src.p, A->nnz);
             GA_DISPATCH_DTYPE(A->dtype, V, {
                 k_gather_vals<V><<<grid_for(A->nnz, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
                     src.p, static_cast<const V*>(A->val), static_cast<V*>(T->val), A->nnz);

@@ -265,6 +265,48 @@ GA_API int ga_symm_from_lower(ga_ctx ctx, ga_csr L, ga_csr* S);     /* matrix.h:
 /* All values set to 1 as int32 (build_adjacency_matrix, matrix.h:679-698). */
 GA_API int ga_adjacency(ga_ctx ctx, ga_csr A, ga_csr* adj);
 
+/* ------------------------------------------------- edge lists and files
+ * Ingestion builds the CSR on the device: entries are counted and placed
+ * per row, each row is sorted by column, and duplicate (i, j) entries merge
+ * onto the value of the earliest one in input order (the product's kernels
+ * need strictly ascending columns; the reference keeps duplicates, which
+ * files that follow the Matrix Market rules never hold).
+ * The flags select the reference CLI's preparation steps. */
+enum {
+    GA_EDGES_MIRROR = 1,     /* each kept edge (i, j) also stored as (j, i), right after it
+                                (symmetric Matrix Market files, matrix.h:339-346) */
+    GA_EDGES_DROP_LOOPS = 2, /* drop (i, i) (the Matrix Market reader, matrix.h:355-358) */
+    GA_EDGES_LOWER_SYMM = 4, /* keep i > j only and mirror: build_symm_from_lower(
+                                extract_lower_triangle(.)), src/main.cpp:221-222 */
+    GA_EDGES_UNIT = 8        /* int32 values, all 1: build_adjacency_matrix, matrix.h:679-698 */
+};
+/* Edge list (src[e], dst[e], val[e] of `dtype`; val NULL: all 1) to an
+ * m x n CSR. Host arrays; ga_csr_from_device_edges takes device arrays.
+ * An endpoint outside the matrix gives GA_ERR_INVALID_ARG. */
+GA_API int ga_csr_from_edges(ga_ctx ctx, int64_t m, int64_t n, int64_t ne, const int32_t* src,
+                             const int32_t* dst, const void* val, ga_dtype dtype, int flags, ga_csr* out);
+GA_API int ga_csr_from_device_edges(ga_ctx ctx, int64_t m, int64_t n, int64_t ne, const int32_t* src,
+                                    const int32_t* dst, const void* val, ga_dtype dtype, int flags,
+                                    ga_csr* out);
+/* Matrix Market coordinate file, as spMtx(filename, "mtx") reads it
+ * (matrix.h:280-417): the body is parsed on the device; self-loops are
+ * dropped, symmetric files mirrored; real files give GA_FP64 values,
+ * integer files GA_INT32, pattern files GA_INT32 ones (src/main.cpp:279-310).
+ * `flags` may add GA_EDGES_LOWER_SYMM and GA_EDGES_UNIT (the CLI's
+ * preparation). Complex or array files and non-square matrices are refused
+ * (matrix.h:301-309). `matcode` (4 bytes, may be NULL) receives the file's
+ * Matrix Market type code. Real values are correctly rounded (equal to
+ * strtod's). */
+GA_API int ga_read_mtx(ga_ctx ctx, const char* path, int flags, char* matcode, ga_csr* out);
+/* Binary CSR file of write_crs_to_bin (matrix.h:259-277, 441-482): matcode,
+ * m, n, nz as 8-byte integers, Rst, Col, Val; values are doubles when
+ * matcode[2] is 'R', int32 otherwise. Rows are sorted and duplicates merged
+ * as above; `flags` as for ga_read_mtx. */
+GA_API int ga_read_bin(ga_ctx ctx, const char* path, int flags, char* matcode, ga_csr* out);
+/* Writes A (GA_INT32 or GA_FP64) in that layout; `matcode` NULL writes
+ * "MCIG" / "MCRG". */
+GA_API int ga_write_bin(ga_ctx ctx, ga_csr A, const char* matcode, const char* path);
+
 /* ------------------------------------------------------------ algorithms */
 /* Triangle count of an undirected graph given as symmetric adjacency A.
  * algo GA_MSA/MCA/HEAP/NAIVE: C<L> = L*L with that variant, L = strict lower

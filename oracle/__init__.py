@@ -284,6 +284,43 @@ def ref_read_mtx(path: str, symmetrise: bool = True) -> Csr:
                _take(cv, z.value, np.int32, free))
 
 
+def ref_read_raw(path: str, fmt: str):
+    """The reference's reader on `path` (format "mtx", "bin", ...), before
+    build_adjacency_matrix: (Csr with float64 values, matcode bytes)."""
+    m, n, z = _i64(), _i64(), _i64()
+    cr, cc, cv = _p(), _p(), _p()
+    code = ctypes.create_string_buffer(4)
+    rc = ref().ref_read_raw(path.encode(), fmt.encode(), ctypes.byref(m), ctypes.byref(n), ctypes.byref(z),
+                            ctypes.byref(cr), ctypes.byref(cc), ctypes.byref(cv), code)
+    if rc != 0:
+        raise RuntimeError(f"reference could not read {path}")
+    free = ref().ref_free
+    rst = _take(cr, m.value + 1, np.int32, free)
+    return (Csr(int(m.value), int(n.value), rst, _take(cc, z.value, np.int32, free),
+                _take(cv, z.value, np.float64, free)), code.raw)
+
+
+def ref_read_cli(path: str, fmt: str, symmetrise: bool) -> Csr:
+    """The reference CLI's graph preparation (read, adjacency, and the
+    lower-triangle symmetrisation when `symmetrise`)."""
+    m, n, z = _i64(), _i64(), _i64()
+    cr, cc, cv = _p(), _p(), _p()
+    rc = ref().ref_read_cli(path.encode(), fmt.encode(), int(symmetrise), ctypes.byref(m), ctypes.byref(n),
+                            ctypes.byref(z), ctypes.byref(cr), ctypes.byref(cc), ctypes.byref(cv))
+    if rc != 0:
+        raise RuntimeError(f"reference could not read {path}")
+    free = ref().ref_free
+    rst = _take(cr, m.value + 1, np.int32, free)
+    return Csr(int(m.value), int(n.value), rst, _take(cc, z.value, np.int32, free),
+               _take(cv, z.value, np.int32, free))
+
+
+def ref_tobinary(path: str, fmt: str, out_path: str) -> None:
+    """The reference CLI's "tobinary" action on `path`, written to `out_path`."""
+    if ref().ref_tobinary(path.encode(), fmt.encode(), out_path.encode()) != 0:
+        raise RuntimeError(f"reference could not convert {path}")
+
+
 def ref_mxm(algo: int, A: Csr, B: Csr, M: Csr) -> Csr:
     """Reference C<M> = A*B; algo 0 msa, 1 mca, 2 heap (zero-filled C), 3 naive."""
     dt = np.dtype(A.val.dtype)

@@ -143,6 +143,75 @@ int ref_read_mtx(const char* path, int symmetrise, int64_t* m, int64_t* n,
     }
 }
 
+// Reads a graph file of `format` ("mtx", "bin", "graph", "rmat") with the
+// value type the CLI picks for it (main.cpp:279-310) and returns the matrix
+// exactly as read - before build_adjacency_matrix - with values widened to
+// double and the four matcode bytes.
+int ref_read_raw(const char* path, const char* format, int64_t* m, int64_t* n, int64_t* nnz,
+                 int** rst, int** col, double** val, char* matcode) {
+    try {
+        GraphInfo info{"g", path, "", format};
+        const std::string t = get_graph_val_type(path, info);
+        spMtx<double> g;
+        if (t == "real") {
+            spMtx<double> r(path, format);
+            g = r;
+        } else {
+            spMtx<int> r(path, format);
+            g = spMtx<double>(r.m, r.n, r.nz);
+            std::memcpy(g.Rst, r.Rst, sizeof(int) * (r.m + 1));
+            for (size_t i = 0; i < r.nz; ++i) { g.Col[i] = r.Col[i]; g.Val[i] = r.Val[i]; }
+            std::memcpy(g.matcode, r.matcode, 4);
+        }
+        std::memcpy(matcode, g.matcode, 4);
+        export_csr(g, m, n, nnz, rst, col, val);
+        return 0;
+    } catch (...) {
+        return 1;
+    }
+}
+
+// The CLI's preparation of a graph file of any format: read, adjacency
+// (matrix.h:679-698) and, when `symmetrise`, the lower-triangle
+// symmetrisation every action but BC applies (main.cpp:221-222).
+int ref_read_cli(const char* path, const char* format, int symmetrise, int64_t* m, int64_t* n,
+                 int64_t* nnz, int** rst, int** col, int** val) {
+    try {
+        GraphInfo info{"g", path, "", format};
+        const std::string t = get_graph_val_type(path, info);
+        spMtx<int> adj;
+        if (t == "real") {
+            spMtx<double> g(path, format);
+            adj = build_adjacency_matrix(g);
+        } else {
+            spMtx<int> g(path, format);
+            adj = build_adjacency_matrix(g);
+        }
+        if (symmetrise) adj = build_symm_from_lower(extract_lower_triangle(adj));
+        export_csr(adj, m, n, nnz, rst, col, val);
+        return 0;
+    } catch (...) {
+        return 1;
+    }
+}
+
+// The CLI's "tobinary" action (main.cpp:325-331): read `path` with the value
+// type the CLI picks and write it with write_crs_to_bin (matrix.h:259-277).
+int ref_tobinary(const char* path, const char* format, const char* out_path) {
+    try {
+        GraphInfo info{"g", path, "", format};
+        const std::string t = get_graph_val_type(path, info);
+        if (t == "real") {
+            spMtx<double> g(path, format);
+            return g.write_crs_to_bin(out_path) ? 1 : 0;
+        }
+        spMtx<int> g(path, format);
+        return g.write_crs_to_bin(out_path) ? 1 : 0;
+    } catch (...) {
+        return 1;
+    }
+}
+
 // C<M> = A*B with the reference's mxm entry points; algo 0 msa, 1 mca,
 // 2 heap, 3 naive (matrix_la.h:700-749, 586-641, 1013-1084, 1139-1277).
 int ref_mxm_i32(int algo, int64_t am, int64_t an, int64_t anz, const int* ar, const int* ac, const int* av,

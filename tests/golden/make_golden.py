@@ -13,8 +13,12 @@ product's generators). Outputs come from the reference's own functions:
 For the four Matrix-Market graphs shipped with the reference only the
 known answers (triangles, k-truss edge counts and iterations) are stored;
 the graphs themselves are not copied.
+File formats: seeded Matrix Market files written here (formats/*.mtx), the
+reference's raw reading and CLI preparation of each (formats.npz) and the
+binary files its "tobinary" action writes for them (formats/*.bin).
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # everything
+    python tests/golden/make_golden.py formats    # the file-format fixtures only
 """
 from __future__ import annotations
 
@@ -79,6 +83,114 @@ def pack(prefix, C, out):
     out[prefix + "_rst"] = C.rst
     out[prefix + "_col"] = C.col
     out[prefix + "_val"] = C.val
+
+
+FORMATS = os.path.join(HERE, "formats")
+
+
+def _fmt_real(x: float, style: int) -> str:
+    """Real values in the spellings Matrix Market writers use, including the
+    leading-dot form of the reference's own kNN graphs."""
+    if style == 0:
+        return repr(float(x))
+    if style == 1:
+        t = "%.16f" % x
+        return t.replace("0.", ".", 1) if t.startswith("0.") else t.replace("-0.", "-.", 1)
+    if style == 2:
+        return "%.6e" % x
+    if style == 3:
+        return "%.17g" % x
+    return "%.24f" % x  # more significant digits than the device's fast path takes
+
+
+def write_formats(rng) -> dict:
+    """Seeded Matrix Market files (this script's own content) and what the
+    reference makes of them: its raw reader, its CLI preparation with and
+    without the lower-triangle symmetrisation, and its tobinary output."""
+    os.makedirs(FORMATS, exist_ok=True)
+    files = {}
+
+    def lower_pairs(n, p):
+        U = np.tril(rng.random((n, n)) < p, -1)
+        j, i = np.nonzero(U.T)  # column-major order: by column, then row
+        return i + 1, j + 1
+
+    # pattern symmetric, column-major lower triangle with a few diagonal
+    # entries and comment lines (no blank line before the size line: the
+    # reference's second pass, matrix.h:330-332, would take it for the size
+    # line and read every entry one token off)
+    i, j = lower_pairs(120, 0.06)
+    diag = rng.choice(120, 5, replace=False) + 1
+    lines = ["%%MatrixMarket matrix coordinate pattern symmetric", "% seeded test graph", "%"]
+    body = [f"{a} {b}" for a, b in zip(i, j)] + [f"{d} {d}" for d in diag]
+    lines.append(f"120 120 {len(body)}")
+    files["pat_sym"] = "\n".join(lines + body) + "\n"
+
+    # real symmetric in column-major order, values in mixed spellings
+    i, j = lower_pairs(150, 0.08)
+    v = rng.random(len(i)) * 0.2
+    body = [f"{a} {b} {_fmt_real(x, k % 4)}" for k, (a, b, x) in enumerate(zip(i, j, v))]
+    files["real_sym"] = "\n".join(["%%MatrixMarket matrix coordinate real symmetric",
+                                   f"150 150 {len(body)}"] + body) + "\n"
+
+    # real general, entries in random order (rows unsorted), CRLF line ends,
+    # tabs, long and exponent-heavy values that leave the fast path
+    n = 90
+    D = rng.random((n, n)) < 0.07
+    r, c = np.nonzero(D)
+    order = rng.permutation(len(r))
+    r, c = r[order] + 1, c[order] + 1
+    vals = rng.standard_normal(len(r)) * 10.0 ** rng.integers(-30, 30, len(r))
+    specials = ["-0", "2", "1E+2", "-1.5e-3", "3.0000000000000004", "1e-30", "0.000123456789012345678901",
+                "+.5", "7.", "123456789012345678901234"]
+    body = []
+    for k, (a, b, x) in enumerate(zip(r, c, vals)):
+        t = specials[k] if k < len(specials) else _fmt_real(x, k % 5)
+        sep = "\t" if k % 7 == 0 else " "
+        body.append(f"{a}{sep}{b} {t}")
+    files["real_gen"] = "\r\n".join(["%%MatrixMarket matrix coordinate real general", f"{n} {n} {len(body)}"]
+                                     + body) + "\r\n"
+
+    # integer general with repeated (i, j) entries and negative values
+    n = 60
+    D = rng.random((n, n)) < 0.1
+    r, c = np.nonzero(D)
+    dup = rng.choice(len(r), 15, replace=False)
+    r = np.concatenate([r, r[dup]]) + 1
+    c = np.concatenate([c, c[dup]]) + 1
+    iv = rng.integers(-1000, 1000, len(r))
+    body = [f"{a} {b} {x}" for a, b, x in zip(r, c, iv)]
+    files["int_gen_dup"] = "\n".join(["%%MatrixMarket matrix coordinate integer general",
+                                      f"{n} {n} {len(body)}"] + body) + "\n"
+
+    # integer symmetric with entries in random order
+    i, j = lower_pairs(80, 0.1)
+    order = rng.permutation(len(i))
+    i, j = i[order], j[order]
+    iv = rng.integers(1, 50, len(i))
+    body = [f"{a} {b} {x}" for a, b, x in zip(i, j, iv)]
+    files["int_sym_shuffled"] = "\n".join(["%%MatrixMarket matrix coordinate integer symmetric",
+                                           f"80 80 {len(body)}"] + body) + "\n"
+
+    out = {}
+    meta = {}
+    for name, text in files.items():
+        path = os.path.join(FORMATS, name + ".mtx")
+        with open(path, "w", newline="") as f:
+            f.write(text)
+        R, code = oracle.ref_read_raw(path, "mtx")
+        pack(f"{name}_raw", R, out)
+        for sym in (0, 1):
+            pack(f"{name}_cli{sym}", oracle.ref_read_cli(path, "mtx", bool(sym)), out)
+        binp = os.path.join(FORMATS, name + ".bin")
+        oracle.ref_tobinary(path, "mtx", binp)
+        B, bcode = oracle.ref_read_raw(binp, "bin")
+        pack(f"{name}_bin", B, out)
+        meta[name] = {"matcode": code.decode(), "bin_matcode": bcode.decode(), "m": R.m, "nnz": int(R.nnz)}
+    np.savez_compressed(os.path.join(HERE, "formats.npz"), **out)
+    with open(os.path.join(HERE, "formats.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    return meta
 
 
 def main():
@@ -154,8 +266,14 @@ def main():
             known[g[:-4]] = {"m": G.m, "nnz": int(G.nnz), "triangles": total, "ktruss": kt}
         with open(os.path.join(HERE, "reference_graphs.json"), "w") as f:
             json.dump(known, f, indent=1)
+    write_formats(np.random.default_rng(20261204))
     print("wrote", sorted(os.listdir(HERE)))
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["formats"]:
+        if oracle.build_ref() is None:
+            raise SystemExit("reference sources not available; cannot regenerate fixtures")
+        print(write_formats(np.random.default_rng(20261204)))
+    else:
+        main()
