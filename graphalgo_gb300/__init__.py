@@ -369,6 +369,29 @@ def adjacency(A: Csr) -> Csr:
     return _new(A.ctx, lib().ga_adjacency, A.handle)
 
 
+def ewise_add(A: Csr, B: Csr, M: Optional[Csr] = None) -> Csr:
+    return _new(A.ctx, lib().ga_ewise_add, A.handle, B.handle, M.handle if M is not None else None)
+
+
+def ewise_mult(A: Csr, B: Csr, M: Optional[Csr] = None) -> Csr:
+    return _new(A.ctx, lib().ga_ewise_mult, A.handle, B.handle, M.handle if M is not None else None)
+
+
+def mult_scalar(A: Csr, alpha: float) -> None:
+    """A's values times alpha, in place."""
+    _check(lib().ga_mult_scalar(A.ctx.handle, A.handle, ctypes.c_double(alpha)), A.ctx)
+
+
+def mxv(A: Csr, x: Dense, y: Dense) -> None:
+    """y += A x on the device."""
+    _check(lib().ga_mxv(A.ctx.handle, A.handle, x.handle, y.handle), A.ctx)
+
+
+def vxm(A: Csr, x: Dense, y: Dense) -> None:
+    """y += x^T A on the device."""
+    _check(lib().ga_vxm(A.ctx.handle, A.handle, x.handle, y.handle), A.ctx)
+
+
 # ------------------------------------------------------------- ingestion
 def csr_from_edges(ctx: Context, m: int, n: int, src, dst, val=None, flags: int = 0,
                    dtype: Optional[int] = None) -> Csr:

@@ -133,6 +133,7 @@ static ga_csr edges_to_csr(ga_ctx ctx, int64_t m, int64_t n, int64_t ne, const i
         val = nullptr;
         dt = GA_INT32;
     }
+    ProfScope ps(ctx, "edges_to_csr");
     const int grid_e = grid_for(ne, 256, ctx->num_sms * 8);
     if (ne) {
         DBuf<int> flag(ctx, 1);
@@ -146,20 +147,25 @@ static ga_csr edges_to_csr(ga_ctx ctx, int64_t m, int64_t n, int64_t ne, const i
                "edges: the expanded entry count is beyond the int32 index range");
     DBuf<int32_t> rst(ctx, (size_t)m + 1);
     GA_CUDA(cudaMemsetAsync(rst.p, 0, sizeof(int32_t) * (m + 1), ctx->stream));
+    int prof = prof_begin(ctx, "edges_count");
     if (ne) {
         k_edges_count<<<grid_e, 256, 0, ctx->stream>>>(src, dst, ne, r, rst.p);
         post_launch("edges_count");
     }
+    prof_end(ctx, prof);
     scan_exclusive_i32(ctx, rst.p, rst.p, m);
     const int64_t kept = m ? read_i32(ctx, rst.p + m) : 0;
     DBuf<int32_t> col(ctx, (size_t)kept + 1), pay(ctx, (size_t)kept + 1);
     if (kept) {
         DBuf<int32_t> cursor(ctx, (size_t)m + 1);
         GA_CUDA(cudaMemcpyAsync(cursor.p, rst.p, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToDevice, ctx->stream));
+        prof = prof_begin(ctx, "edges_fill");
         k_edges_fill<<<grid_e, 256, 0, ctx->stream>>>(src, dst, ne, r, cursor.p, col.p, pay.p);
         post_launch("edges_fill");
+        prof_end(ctx, prof);
         sort_rows_by_key(ctx, rst.p, m, col.p, pay.p, kept);
     }
+    prof = prof_begin(ctx, "edges_runs");
     DBuf<int32_t> head(ctx, (size_t)kept + 1), hs(ctx, (size_t)kept + 1);
     const int grid_q = grid_for(kept, 256, ctx->num_sms * 8);
     if (kept) {
@@ -182,6 +188,7 @@ static ga_csr edges_to_csr(ga_ctx ctx, int64_t m, int64_t n, int64_t ne, const i
             });
             post_launch("runs_compact");
         }
+        prof_end(ctx, prof);
         GA_CUDA(cudaStreamSynchronize(ctx->stream));
     } catch (...) {
         csr_destroy(ctx, A);
@@ -625,6 +632,7 @@ static ga_csr read_mtx(ga_ctx ctx, const char* path, int flags, char* matcode) {
     GA_CUDA(cudaMemsetAsync(text.p + body, ' ', (size_t)(nblk * kTokBlockBytes - body), ctx->stream));
     file_to_device(ctx, file.f, text.p, body, "mtx");
     DBuf<int64_t> bcount(ctx, (size_t)nblk + 1);
+    int prof = prof_begin(ctx, "mtx_tokenize");
     k_tok_count<<<(unsigned)nblk, kTokThreads, 0, ctx->stream>>>(text.p, bcount.p);
     post_launch("mtx_tok_count");
     scan_exclusive_i64(ctx, bcount.p, bcount.p, nblk);
@@ -633,6 +641,7 @@ static ga_csr read_mtx(ga_ctx ctx, const char* path, int flags, char* matcode) {
     DBuf<int64_t> tokpos(ctx, (size_t)need + 1);
     k_tok_emit<<<(unsigned)nblk, kTokThreads, 0, ctx->stream>>>(text.p, bcount.p, need, tokpos.p);
     post_launch("mtx_tok_emit");
+    prof_end(ctx, prof);
 
     const bool want_vals = per == 3 && !(flags & GA_EDGES_UNIT);
     const int value_kind = want_vals ? (h.code[2] == 'R' ? 2 : 1) : 0;
@@ -643,11 +652,13 @@ static ga_csr read_mtx(ga_ctx ctx, const char* path, int flags, char* matcode) {
     DBuf<int> err(ctx, 1);
     GA_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), ctx->stream));
     GA_CUDA(cudaMemsetAsync(nslow.p, 0, sizeof(int64_t), ctx->stream));
+    prof = prof_begin(ctx, "mtx_parse");
     if (h.nz) {
         k_mtx_entries<<<grid_for(h.nz, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
             text.p, tokpos.p, h.nz, per, value_kind, h.m, h.n, src.p, dst.p, val.p, err.p, slow.p, nslow.p);
         post_launch("mtx_entries");
     }
+    prof_end(ctx, prof);
     const int e = read_i32(ctx, err.p);
     if (e & kBadIndex) fail(GA_ERR_INVALID_ARG, "mtx: a row or column index is not an integer");
     if (e & kIndexRange) fail(GA_ERR_INVALID_ARG, "mtx: an entry lies outside the matrix");

@@ -188,9 +188,10 @@ void validate_csr(ga_ctx ctx, const int32_t* rst, const int32_t* col, int64_t m,
 // 2 a column out of range, 4 columns not strictly ascending in some row.
 int csr_check_bits(ga_ctx ctx, const int32_t* rst, const int32_t* col, int64_t m, int64_t n, int64_t nnz);
 
-// Sorts each CSR row segment by key (payload follows): rows of up to 8,192
-// entries by a bitonic sort in shared memory, longer ones by one CTA each
-// (sorted pieces, then merge-path merges). nnz: entries of the whole matrix.
+// Sorts each CSR row segment by key (payload follows): rows of up to 256
+// entries by one warp in registers, up to 8,192 by a CTA's bitonic sort in
+// shared memory, longer ones by one CTA each (sorted pieces, then
+// merge-path merges). nnz: entries of the whole matrix.
 void sort_rows_by_key(ga_ctx ctx, const int32_t* rst, int64_t m, int32_t* key, int32_t* pay, int64_t nnz);
 
 // k-truss on a single matrix (batch == nullptr) or on a block-diagonal union

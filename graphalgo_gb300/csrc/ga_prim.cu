@@ -288,10 +288,71 @@ __device__ void block_sort_pairs(int32_t* gk, int32_t* gp, int len, int32_t* sk,
     __syncthreads();
 }
 
-// Rows of at most 32 entries: one warp, one entry per lane, bitonic network
-// over shuffles (lanes past the row hold INT32_MAX). Longer rows are listed
-// for a CTA: up to kSortCap entries in `mid_rows` (k_sort_mid_rows), beyond
-// that in `long_rows` (k_sort_long_rows).
+// Warp-wide bitonic sort of up to 32*K (key, payload) pairs held in
+// registers, element e = r*32 + lane in register r of lane `lane` (a striped
+// layout: loads and stores are coalesced). Pairs at distance j < 32 meet
+// across lanes by shuffles, pairs at distance j >= 32 inside one thread.
+// Padding elements hold INT32_MAX.
+template <int K>
+__device__ __forceinline__ void warp_bitonic(int32_t (&k)[K], int32_t (&v)[K]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int w = 2; w <= 32 * K; w <<= 1) {
+#pragma unroll
+        for (int j = w >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+#pragma unroll
+                for (int r = 0; r < K; ++r) {
+                    const int r2 = r ^ (j >> 5);
+                    if (r2 > r) {
+                        const bool up = ((r * 32 + lane) & w) == 0;
+                        if (up ? k[r] > k[r2] : k[r] < k[r2]) {
+                            const int32_t tk = k[r]; k[r] = k[r2]; k[r2] = tk;
+                            const int32_t tv = v[r]; v[r] = v[r2]; v[r2] = tv;
+                        }
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < K; ++r) {
+                    const int32_t ok = __shfl_xor_sync(0xffffffffu, k[r], j);
+                    const int32_t ov = __shfl_xor_sync(0xffffffffu, v[r], j);
+                    const bool up = ((r * 32 + lane) & w) == 0, low = (lane & j) == 0;
+                    // the lower element of an ascending pair keeps the smaller key
+                    if (low == up ? ok < k[r] : ok > k[r]) {
+                        k[r] = ok;
+                        v[r] = ov;
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void warp_sort_row(int32_t* key, int32_t* pay, int len) {
+    const int lane = threadIdx.x & 31;
+    int32_t k[K], v[K];
+#pragma unroll
+    for (int r = 0; r < K; ++r) {
+        const int e = r * 32 + lane;
+        k[r] = e < len ? key[e] : INT32_MAX;
+        v[r] = e < len ? pay[e] : 0;
+    }
+    warp_bitonic<K>(k, v);
+#pragma unroll
+    for (int r = 0; r < K; ++r) {
+        const int e = r * 32 + lane;
+        if (e < len) {
+            key[e] = k[r];
+            pay[e] = v[r];
+        }
+    }
+}
+
+// Rows of at most 256 entries: one warp each, in registers. Longer rows are
+// listed for a CTA: up to kSortCap entries in `mid_rows` (k_sort_mid_rows),
+// beyond that in `long_rows` (k_sort_long_rows).
 __global__ void k_sort_rows(const int32_t* __restrict__ rst, int64_t m, int32_t* __restrict__ key,
                             int32_t* __restrict__ pay, int32_t* __restrict__ mid_rows, int* __restrict__ nmid,
                             int32_t* __restrict__ long_rows, int* __restrict__ nlong) {
@@ -300,30 +361,16 @@ __global__ void k_sort_rows(const int32_t* __restrict__ rst, int64_t m, int32_t*
     for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < m; i += warps) {
         const int32_t b = rst[i], len = rst[i + 1] - b;
         if (len <= 1) continue;
-        if (len > 32) {
-            if (lane == 0) {
-                if (len > kSortCap) long_rows[atomicAdd(nlong, 1)] = (int32_t)i;
-                else mid_rows[atomicAdd(nmid, 1)] = (int32_t)i;
+        if (len <= 32) warp_sort_row<1>(key + b, pay + b, len);
+        else if (len <= 64) warp_sort_row<2>(key + b, pay + b, len);
+        else if (len <= 256) warp_sort_row<8>(key + b, pay + b, len);
+        else if (lane == 0) {
+            if (len > kSortCap) {
+                long_rows[atomicAdd(nlong, 1)] = (int32_t)i;
+                atomicMax(nlong + 1, len);
+            } else {
+                mid_rows[atomicAdd(nmid, 1)] = (int32_t)i;
             }
-            continue;
-        }
-        int32_t k = lane < len ? key[b + lane] : INT32_MAX;
-        int32_t v = lane < len ? pay[b + lane] : 0;
-        for (int w = 2; w <= 32; w <<= 1) {
-            for (int j = w >> 1; j > 0; j >>= 1) {
-                const int32_t ok = __shfl_xor_sync(0xffffffffu, k, j);
-                const int32_t ov = __shfl_xor_sync(0xffffffffu, v, j);
-                const bool up = (lane & w) == 0, low = (lane & j) == 0;
-                // the lower lane of an ascending pair keeps the smaller key
-                if (low == up ? ok < k : ok > k) {
-                    k = ok;
-                    v = ov;
-                }
-            }
-        }
-        if (lane < len) {
-            key[b + lane] = k;
-            pay[b + lane] = v;
         }
     }
 }
@@ -353,23 +400,32 @@ __device__ __forceinline__ int32_t merge_split(const int32_t* A, int32_t na, con
     return lo;
 }
 
-// One CTA per long row: kSortCap-entry pieces sorted in shared memory, then
-// pairs of sorted runs merged (merge path: each thread finds its split of
-// the output by a binary search and merges its share) between the row's
-// place in key/pay and the same place in tkey/tpay, doubling the run length
-// each pass.
+// Long rows, first step: CTA (r, c) sorts piece c (kSortCap entries) of
+// listed row r in shared memory; pieces past the row's end exit.
+__global__ void __launch_bounds__(512) k_sort_long_pieces(const int32_t* __restrict__ rst,
+                                                          const int32_t* __restrict__ rows, int32_t* key,
+                                                          int32_t* pay) {
+    extern __shared__ int32_t sm[];
+    const int32_t i = rows[blockIdx.x];
+    const int32_t b = rst[i], L = rst[i + 1] - b;
+    const int32_t c0 = (int32_t)blockIdx.y * kSortCap;
+    if (c0 >= L) return;
+    block_sort_pairs(key + b + c0, pay + b + c0, min(kSortCap, L - c0), sm, sm + kSortCap);
+}
+
+// Long rows, second step, one CTA per row: pairs of sorted runs merged
+// (merge path: each thread finds its split of the output by a binary search
+// and merges its share) between the row's place in key/pay and the same
+// place in tkey/tpay, doubling the run length each pass.
 __global__ void __launch_bounds__(512) k_sort_long_rows(const int32_t* __restrict__ rst,
                                                         const int32_t* __restrict__ rows, int32_t* key,
                                                         int32_t* pay, int32_t* tkey, int32_t* tpay) {
-    extern __shared__ int32_t sm[];
     const int32_t i = rows[blockIdx.x];
     const int32_t b = rst[i], L = rst[i + 1] - b;
     int32_t* k0 = key + b;
     int32_t* p0 = pay + b;
     int32_t* k1 = tkey + b;
     int32_t* p1 = tpay + b;
-    for (int32_t c0 = 0; c0 < L; c0 += kSortCap)
-        block_sort_pairs(k0 + c0, p0 + c0, min(kSortCap, L - c0), sm, sm + kSortCap);
     for (int64_t w = kSortCap; w < L; w <<= 1) {
         for (int64_t s0 = 0; s0 < L; s0 += 2 * w) {
             const int32_t na = (int32_t)min(w, (int64_t)L - s0);
@@ -403,9 +459,10 @@ __global__ void __launch_bounds__(512) k_sort_long_rows(const int32_t* __restric
 
 void sort_rows_by_key(ga_ctx ctx, const int32_t* rst, int64_t m, int32_t* key, int32_t* pay, int64_t nnz) {
     if (m <= 0 || nnz <= 1) return;
-    DBuf<int> counts(ctx, 2);  // [0] medium rows, [1] long rows
+    ProfScope ps(ctx, "sort_rows");
+    DBuf<int> counts(ctx, 3);  // medium rows, long rows, longest long row
     DBuf<int32_t> mid_rows(ctx, (size_t)m + 1), long_rows(ctx, (size_t)m + 1);
-    GA_CUDA(cudaMemsetAsync(counts.p, 0, 2 * sizeof(int), ctx->stream));
+    GA_CUDA(cudaMemsetAsync(counts.p, 0, 3 * sizeof(int), ctx->stream));
     k_sort_rows<<<grid_for(m * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(
         rst, m, key, pay, mid_rows.p, counts.p, long_rows.p, counts.p + 1);
     post_launch("sort_rows");
@@ -414,13 +471,17 @@ void sort_rows_by_key(ga_ctx ctx, const int32_t* rst, int64_t m, int32_t* key, i
     // 64 KB of shared memory per CTA: three CTAs per SM
     k_sort_mid_rows<<<ctx->num_sms * 3, 512, smem, ctx->stream>>>(rst, mid_rows.p, counts.p, key, pay);
     post_launch("sort_mid_rows");
-    int h[2];
+    int h[3];
     GA_CUDA(cudaMemcpyAsync(h, counts.p, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
     GA_CUDA(cudaStreamSynchronize(ctx->stream));
     if (h[1] == 0) return;
     DBuf<int32_t> tkey(ctx, (size_t)nnz), tpay(ctx, (size_t)nnz);
-    GA_CUDA(cudaFuncSetAttribute(k_sort_long_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_sort_long_rows<<<h[1], 512, smem, ctx->stream>>>(rst, long_rows.p, key, pay, tkey.p, tpay.p);
+    GA_CUDA(cudaFuncSetAttribute(k_sort_long_pieces, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    GA_REQUIRE((h[2] + kSortCap - 1) / kSortCap <= 65535, GA_ERR_INVALID_ARG, "sort: a row of over 536M entries");
+    const dim3 pieces((unsigned)h[1], (unsigned)((h[2] + kSortCap - 1) / kSortCap));
+    k_sort_long_pieces<<<pieces, 512, smem, ctx->stream>>>(rst, long_rows.p, key, pay);
+    post_launch("sort_long_pieces");
+    k_sort_long_rows<<<h[1], 512, 0, ctx->stream>>>(rst, long_rows.p, key, pay, tkey.p, tpay.p);
     post_launch("sort_long_rows");
     GA_CUDA(cudaStreamSynchronize(ctx->stream));
 }

@@ -257,6 +257,28 @@ GA_API int ga_ewise_mult_masked(ga_ctx ctx, ga_dense A, ga_dense B, ga_csr M, ga
 /* Dense C += A .* B (include/matrix_la.h:192-198). */
 GA_API int ga_fuse_ewise_mult_add(ga_ctx ctx, ga_dense A, ga_dense B, ga_dense C);
 
+/* --------------------------------- sparse element-wise and matrix-vector
+ * The GraphBLAS-style operations the reference declares but its callers
+ * never use (include/matrix_la.h:272-541, 1279-1291), with the intended
+ * semantics where its code slips (named in the oracle's restatement).
+ * A, B (and M) have equal shapes; A and B equal dtypes; M is a pattern. */
+/* M NULL: eWiseAdd(A, B), matrix_la.h:375-435: the union of the rows, A + B
+ * where both hold a column. M given: eWiseAdd(A, B, M), 272-335: at every
+ * mask entry (0 + A(i,j)) + B(i,j), kept when nonzero. */
+GA_API int ga_ewise_add(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M, ga_csr* C);
+/* eWiseMult(A, B [, M]), matrix_la.h:438-533: the columns every operand
+ * holds, value A * B. */
+GA_API int ga_ewise_mult(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M, ga_csr* C);
+/* multScalar, matrix_la.h:535-541: A's values times alpha in place (formed
+ * in double, converted back to A's type). */
+GA_API int ga_mult_scalar(ga_ctx ctx, ga_csr A, double alpha);
+/* MxV, matrix_la.h:1279-1284: y += A x (x: A.n values, y: A.m values, any
+ * dense shape of that size, A's dtype); each row's terms summed in order. */
+GA_API int ga_mxv(ga_ctx ctx, ga_csr A, ga_dense x, ga_dense y);
+/* VxM, matrix_la.h:1286-1291: y += x^T A (x: A.m values, y: A.n values),
+ * each column's terms summed in row order. */
+GA_API int ga_vxm(ga_ctx ctx, ga_csr A, ga_dense x, ga_dense y);
+
 /* ------------------------------------------------------------ graph prep */
 GA_API int ga_transpose(ga_ctx ctx, ga_csr A, ga_csr* AT);          /* matrix_la.h:166-190 */
 GA_API int ga_extract_lower(ga_ctx ctx, ga_csr A, ga_csr* L);       /* matrix.h:736-763 */

@@ -183,6 +183,56 @@ def fuse_ewise_mult_add(Ad: np.ndarray, Bd: np.ndarray, Cd: np.ndarray) -> np.nd
     return C
 
 
+def _maybe(X: Optional[Csr], field: str):
+    return _ptr(_c(getattr(X, field), np.int32)) if X is not None else None
+
+
+def ewise_add(A: Csr, B: Csr, M: Optional[Csr] = None) -> Csr:
+    """eWiseAdd (matrix_la.h:375-435), or its masked form (272-335) when M is given."""
+    dt = np.dtype(A.val.dtype)
+    fn = getattr(lib(), f"or_ewise_add_{_SUFFIX[dt]}")
+    return _new_csr(fn, A.m, A.n, dt, _i64(A.m),
+                    _ptr(_c(A.rst, np.int32)), _ptr(_c(A.col, np.int32)), _ptr(_c(A.val, dt)),
+                    _ptr(_c(B.rst, np.int32)), _ptr(_c(B.col, np.int32)), _ptr(_c(B.val, dt)),
+                    _maybe(M, "rst"), _maybe(M, "col"))
+
+
+def ewise_mult(A: Csr, B: Csr, M: Optional[Csr] = None) -> Csr:
+    """eWiseMult on sparse operands (matrix_la.h:438-533)."""
+    dt = np.dtype(A.val.dtype)
+    fn = getattr(lib(), f"or_ewise_mult_{_SUFFIX[dt]}")
+    return _new_csr(fn, A.m, A.n, dt, _i64(A.m),
+                    _ptr(_c(A.rst, np.int32)), _ptr(_c(A.col, np.int32)), _ptr(_c(A.val, dt)),
+                    _ptr(_c(B.rst, np.int32)), _ptr(_c(B.col, np.int32)), _ptr(_c(B.val, dt)),
+                    _maybe(M, "rst"), _maybe(M, "col"))
+
+
+def mult_scalar(A: Csr, alpha: float) -> Csr:
+    """multScalar (matrix_la.h:535-541) on a copy of A."""
+    dt = np.dtype(A.val.dtype)
+    v = np.array(A.val[: A.nnz], dtype=dt, copy=True)
+    getattr(lib(), f"or_mult_scalar_{_SUFFIX[dt]}")(_i64(len(v)), _ptr(v), ctypes.c_double(alpha))
+    return Csr(A.m, A.n, A.rst.copy(), A.col.copy(), v)
+
+
+def mxv(A: Csr, x: np.ndarray, y: np.ndarray) -> np.ndarray:
+    """y + A x in row order (MxV, matrix_la.h:1279-1284)."""
+    dt = np.dtype(A.val.dtype)
+    out = np.array(y, dtype=dt, copy=True)
+    getattr(lib(), f"or_mxv_{_SUFFIX[dt]}")(_i64(A.m), _ptr(_c(A.rst, np.int32)), _ptr(_c(A.col, np.int32)),
+                                            _ptr(_c(A.val, dt)), _ptr(_c(x, dt)), _ptr(out))
+    return out
+
+
+def vxm(A: Csr, x: np.ndarray, y: np.ndarray) -> np.ndarray:
+    """y + x^T A with rows taken in ascending order (VxM, matrix_la.h:1286-1291)."""
+    dt = np.dtype(A.val.dtype)
+    out = np.array(y, dtype=dt, copy=True)
+    getattr(lib(), f"or_vxm_{_SUFFIX[dt]}")(_i64(A.m), _ptr(_c(A.rst, np.int32)), _ptr(_c(A.col, np.int32)),
+                                            _ptr(_c(A.val, dt)), _ptr(_c(x, dt)), _ptr(out))
+    return out
+
+
 def transpose(A: Csr) -> Csr:
     dt = np.dtype(A.val.dtype)
     cr, cc, cv = _p(), _p(), _p()
@@ -284,6 +334,19 @@ def ref_read_mtx(path: str, symmetrise: bool = True) -> Csr:
                _take(cv, z.value, np.int32, free))
 
 
+def read_mtx_cli(path: str, symmetrise: bool = True) -> Csr:
+    """The C port of the reference CLI's Matrix Market reading and graph
+    preparation (or_read_mtx_cli); values 1."""
+    m, z = _i64(), _i64()
+    cr, cc = _p(), _p()
+    if lib().or_read_mtx_cli(path.encode(), int(symmetrise), ctypes.byref(m), ctypes.byref(z), ctypes.byref(cr),
+                             ctypes.byref(cc)) != 0:
+        raise RuntimeError(f"cannot read {path}")
+    free = lib().or_free
+    rst = _take(cr, m.value + 1, np.int32, free)
+    return Csr(int(m.value), int(m.value), rst, _take(cc, z.value, np.int32, free), np.ones(z.value, np.int32))
+
+
 def ref_read_raw(path: str, fmt: str):
     """The reference's reader on `path` (format "mtx", "bin", ...), before
     build_adjacency_matrix: (Csr with float64 values, matcode bytes)."""
@@ -319,6 +382,27 @@ def ref_tobinary(path: str, fmt: str, out_path: str) -> None:
     """The reference CLI's "tobinary" action on `path`, written to `out_path`."""
     if ref().ref_tobinary(path.encode(), fmt.encode(), out_path.encode()) != 0:
         raise RuntimeError(f"reference could not convert {path}")
+
+
+def ref_ewise_add(A: Csr, B: Csr, M: Optional[Csr] = None) -> Csr:
+    """The reference's eWiseAdd (masked when M is given); int32 or float64."""
+    dt = np.dtype(A.val.dtype)
+    fn = ref().ref_ewise_add_i32 if dt == np.int32 else ref().ref_ewise_add_f64
+    Mx = M if M is not None else A
+    return _ref_new(fn, dt, ctypes.c_int(M is not None), _i64(A.m), _i64(A.n), _i64(A.nnz),
+                    _ptr(_c(A.rst, np.int32)), _ptr(_c(A.col, np.int32)), _ptr(_c(A.val, dt)),
+                    _i64(B.nnz), _ptr(_c(B.rst, np.int32)), _ptr(_c(B.col, np.int32)), _ptr(_c(B.val, dt)),
+                    _i64(Mx.nnz), _ptr(_c(Mx.rst, np.int32)), _ptr(_c(Mx.col, np.int32)))
+
+
+def ref_vxm(A: Csr, x: np.ndarray, y: np.ndarray) -> np.ndarray:
+    dt = np.dtype(A.val.dtype)
+    out = np.array(y, dtype=dt, copy=True)
+    xx = np.array(x, dtype=dt, copy=True)
+    fn = ref().ref_vxm_i32 if dt == np.int32 else ref().ref_vxm_f64
+    if fn(*_ref_args(A, dt), _ptr(xx), _ptr(out)) != 0:
+        raise RuntimeError("reference call failed")
+    return out
 
 
 def ref_mxm(algo: int, A: Csr, B: Csr, M: Csr) -> Csr:

@@ -14,6 +14,7 @@
 #include "oracle.h"
 
 #include <stdlib.h>
+#include <stdio.h>
 #include <string.h>
 #ifdef _OPENMP
 #include <omp.h>
@@ -318,6 +319,129 @@ OR_DEFINE(double, f64)
 #undef OR_DEFINE
 
 /* -------------------------------------------------------------------------
+ * Element-wise operations and matrix-vector products that the reference
+ * declares but its callers never use (include/matrix_la.h:272-541,
+ * 1279-1291). Where the reference's code has slips, the intended operation
+ * is restated and the slip named.
+ * ------------------------------------------------------------------------- */
+static int find_col(const int* c, int b, int e, int j) {
+    while (b < e) {
+        int mid = (b + e) >> 1;
+        if (c[mid] < j) b = mid + 1; else e = mid;
+    }
+    return b;
+}
+
+#define OR_DEFINE_EWISE(T, S)                                                             \
+/* Without a mask: eWiseAdd(A, B), include/matrix_la.h:375-435, the union of the rows     \
+ * with A + B where both hold a column. With a mask: eWiseAdd(A, B, M), 272-335: for     \
+ * every mask entry v = (0 + A(i,j)) + B(i,j), absent entries skipped, kept when v != 0  \
+ * (the reference indexes B's values by A.Col at 291 and 316; B.Col is meant). */        \
+int or_ewise_add_##S(int64_t m, const int* ar, const int* ac, const T* av,                \
+                     const int* br, const int* bc, const T* bv, const int* mr,            \
+                     const int* mc, int** cr_out, int** cc_out, T** cv_out,               \
+                     int64_t* cnz_out) {                                                  \
+    int* cr = (int*)xmalloc(sizeof(int) * ((size_t)m + 1));                               \
+    size_t cap = 0;                                                                       \
+    for (int64_t i = 0; i < m; ++i)                                                       \
+        cap += mr ? (size_t)(mr[i + 1] - mr[i])                                           \
+                  : (size_t)(ar[i + 1] - ar[i] + br[i + 1] - br[i]);                      \
+    int* cc = (int*)xmalloc(sizeof(int) * cap);                                           \
+    T* cv = (T*)xmalloc(sizeof(T) * cap);                                                 \
+    int64_t p = 0;                                                                        \
+    cr[0] = 0;                                                                            \
+    for (int64_t i = 0; i < m; ++i) {                                                     \
+        if (mr) {                                                                         \
+            for (int q = mr[i]; q < mr[i + 1]; ++q) {                                     \
+                int j = mc[q];                                                            \
+                int x = find_col(ac, ar[i], ar[i + 1], j);                                \
+                int y = find_col(bc, br[i], br[i + 1], j);                                \
+                T v = (T)0;                                                               \
+                if (x < ar[i + 1] && ac[x] == j) v = v + av[x];                           \
+                if (y < br[i + 1] && bc[y] == j) v = v + bv[y];                           \
+                if (v != (T)0) { cc[p] = j; cv[p] = v; ++p; }                             \
+            }                                                                             \
+        } else {                                                                          \
+            int x = ar[i], y = br[i];                                                     \
+            while (x < ar[i + 1] || y < br[i + 1]) {                                      \
+                if (y >= br[i + 1] || (x < ar[i + 1] && ac[x] < bc[y])) {                 \
+                    cc[p] = ac[x]; cv[p] = av[x]; ++x;                                    \
+                } else if (x >= ar[i + 1] || bc[y] < ac[x]) {                             \
+                    cc[p] = bc[y]; cv[p] = bv[y]; ++y;                                    \
+                } else {                                                                  \
+                    cc[p] = ac[x]; cv[p] = av[x] + bv[y]; ++x; ++y;                       \
+                }                                                                         \
+                ++p;                                                                      \
+            }                                                                             \
+        }                                                                                 \
+        cr[i + 1] = (int)p;                                                               \
+    }                                                                                     \
+    *cr_out = cr; *cc_out = cc; *cv_out = cv; *cnz_out = p;                               \
+    return 0;                                                                             \
+}                                                                                         \
+                                                                                          \
+/* eWiseMult(A, B), include/matrix_la.h:438-483, and eWiseMult(A, B, M), 486-533: the     \
+ * columns every operand holds, value A * B. (The reference's unmasked fill loop          \
+ * advances i instead of its output index, 470, and its masked count loop steps the      \
+ * mask twice per match, 497-504.) */                                                    \
+int or_ewise_mult_##S(int64_t m, const int* ar, const int* ac, const T* av,               \
+                      const int* br, const int* bc, const T* bv, const int* mr,           \
+                      const int* mc, int** cr_out, int** cc_out, T** cv_out,              \
+                      int64_t* cnz_out) {                                                 \
+    int* cr = (int*)xmalloc(sizeof(int) * ((size_t)m + 1));                               \
+    int* cc = (int*)xmalloc(sizeof(int) * (size_t)ar[m]);                                 \
+    T* cv = (T*)xmalloc(sizeof(T) * (size_t)ar[m]);                                       \
+    int64_t p = 0;                                                                        \
+    cr[0] = 0;                                                                            \
+    for (int64_t i = 0; i < m; ++i) {                                                     \
+        for (int x = ar[i]; x < ar[i + 1]; ++x) {                                         \
+            int j = ac[x];                                                                \
+            int y = find_col(bc, br[i], br[i + 1], j);                                    \
+            if (y >= br[i + 1] || bc[y] != j) continue;                                   \
+            if (mr) {                                                                     \
+                int z = find_col(mc, mr[i], mr[i + 1], j);                                \
+                if (z >= mr[i + 1] || mc[z] != j) continue;                               \
+            }                                                                             \
+            cc[p] = j; cv[p] = av[x] * bv[y]; ++p;                                        \
+        }                                                                                 \
+        cr[i + 1] = (int)p;                                                               \
+    }                                                                                     \
+    *cr_out = cr; *cc_out = cc; *cv_out = cv; *cnz_out = p;                               \
+    return 0;                                                                             \
+}                                                                                         \
+                                                                                          \
+/* multScalar, include/matrix_la.h:535-541: every value times alpha, in place, the       \
+ * product formed in double and converted back to T as `T *= double` does. */            \
+void or_mult_scalar_##S(int64_t nnz, T* v, double alpha) {                                \
+    for (int64_t q = 0; q < nnz; ++q) v[q] = (T)((double)v[q] * alpha);                   \
+}                                                                                         \
+                                                                                          \
+/* MxV, include/matrix_la.h:1279-1284: y[i] += A(i,j) * x[j] over each row in order      \
+ * (the reference reads a G.Xadj member that spMtx does not have; Rst is meant). */       \
+void or_mxv_##S(int64_t m, const int* ar, const int* ac, const T* av, const T* x, T* y) { \
+    for (int64_t i = 0; i < m; ++i)                                                       \
+        for (int q = ar[i]; q < ar[i + 1]; ++q) {                                         \
+            T prod = av[q] * x[ac[q]];                                                    \
+            y[i] = y[i] + prod;                                                           \
+        }                                                                                 \
+}                                                                                         \
+                                                                                          \
+/* VxM, include/matrix_la.h:1286-1291: y[j] += A(i,j) * x[i], rows in ascending order. */ \
+void or_vxm_##S(int64_t m, const int* ar, const int* ac, const T* av, const T* x, T* y) { \
+    for (int64_t i = 0; i < m; ++i)                                                       \
+        for (int q = ar[i]; q < ar[i + 1]; ++q) {                                         \
+            T prod = av[q] * x[i];                                                        \
+            y[ac[q]] = y[ac[q]] + prod;                                                   \
+        }                                                                                 \
+}
+
+OR_DEFINE_EWISE(int32_t, i32)
+OR_DEFINE_EWISE(int64_t, i64)
+OR_DEFINE_EWISE(float, f32)
+OR_DEFINE_EWISE(double, f64)
+#undef OR_DEFINE_EWISE
+
+/* -------------------------------------------------------------------------
  * Callers of the masked SpGEMM.
  * ------------------------------------------------------------------------- */
 
@@ -351,6 +475,61 @@ static int64_t products_of(int64_t m, const int* cr, const int* cc) {
     for (int64_t i = 0; i < m; ++i)
         for (int q = cr[i]; q < cr[i + 1]; ++q) p += cr[cc[q] + 1] - cr[cc[q]];
     return p;
+}
+
+/* The reference CLI's reading of a Matrix Market graph (src/main.cpp:279-331
+ * with read_mtx_to_crs, include/matrix.h:280-417): entries read one token at
+ * a time with stdio (the reference extracts them with iostream >>),
+ * self-loops dropped, symmetric files mirrored, rows placed by a counting
+ * pass; then build_adjacency_matrix (all values 1) and, when `symmetrise`,
+ * build_symm_from_lower(extract_lower_triangle(.)). Serial, as the
+ * reference's reader is. Returns 0, or 1 when the file cannot be read. */
+int or_read_mtx_cli(const char* path, int symmetrise, int64_t* m_out, int64_t* nnz_out, int** rst_out,
+                    int** col_out) {
+    FILE* f = fopen(path, "r");
+    if (!f) return 1;
+    char line[1024];
+    if (!fgets(line, sizeof line, f)) { fclose(f); return 1; }
+    int pattern = strstr(line, "pattern") != NULL, sym = strstr(line, "symmetric") != NULL;
+    long long m = 0, n = 0, nz = 0;
+    for (;;) {
+        if (!fgets(line, sizeof line, f)) { fclose(f); return 1; }
+        if (line[0] == '%') continue;
+        if (sscanf(line, "%lld %lld %lld", &m, &n, &nz) == 3) break;
+    }
+    if (m != n) { fclose(f); return 1; }
+    size_t cap = (size_t)(sym ? 2 * nz : nz);
+    int* ra = (int*)xmalloc(sizeof(int) * cap);
+    int* ca = (int*)xmalloc(sizeof(int) * cap);
+    int* deg = (int*)xcalloc((size_t)m + 1, sizeof(int));
+    size_t cur = 0;
+    for (long long e = 0; e < nz; ++e) {
+        long long r, c;
+        double v;
+        int got = pattern ? fscanf(f, "%lld %lld", &r, &c) : fscanf(f, "%lld %lld %lf", &r, &c, &v);
+        if (got != (pattern ? 2 : 3)) break;
+        if (r == c) continue;
+        ra[cur] = (int)(r - 1); ca[cur++] = (int)(c - 1); ++deg[r];
+        if (sym) { ra[cur] = (int)(c - 1); ca[cur++] = (int)(r - 1); ++deg[c]; }
+    }
+    fclose(f);
+    int* rst = (int*)xmalloc(sizeof(int) * ((size_t)m + 1));
+    int* fill = (int*)xmalloc(sizeof(int) * ((size_t)m + 1));
+    rst[0] = 0;
+    for (long long i = 0; i < m; ++i) rst[i + 1] = rst[i] + deg[i + 1];
+    memcpy(fill, rst, sizeof(int) * ((size_t)m + 1));
+    int* col = (int*)xmalloc(sizeof(int) * (cur ? cur : 1));
+    for (size_t q = 0; q < cur; ++q) col[fill[ra[q]]++] = ca[q];
+    free(ra); free(ca); free(deg); free(fill);
+    if (symmetrise) {
+        int *lr, *lc, *sr, *sc; int32_t *lv, *sv; int64_t lnz, snz;
+        or_extract_lower_i32(m, rst, col, NULL, &lr, &lc, &lv, &lnz);
+        or_symm_from_lower_i32(m, lr, lc, lv, &sr, &sc, &sv, &snz);
+        free(lr); free(lc); free(lv); free(sv); free(rst); free(col);
+        rst = sr; col = sc;
+    }
+    *m_out = m; *nnz_out = rst[m]; *rst_out = rst; *col_out = col;
+    return 0;
 }
 
 int or_ktruss(int64_t m, const int* rst, const int* col, const int* val, int k,

@@ -57,6 +57,24 @@ void or_set_num_threads(int n);
                                const T* av, int** cr, int** cc, T** cv,            \
                                int64_t* cnz);
 
+#define OR_DECL_EWISE(T, S)                                                            \
+    int or_ewise_add_##S(int64_t m, const int* ar, const int* ac, const T* av,           \
+                         const int* br, const int* bc, const T* bv, const int* mr,       \
+                         const int* mc, int** cr, int** cc, T** cv, int64_t* cnz);       \
+    int or_ewise_mult_##S(int64_t m, const int* ar, const int* ac, const T* av,          \
+                          const int* br, const int* bc, const T* bv, const int* mr,      \
+                          const int* mc, int** cr, int** cc, T** cv, int64_t* cnz);      \
+    void or_mult_scalar_##S(int64_t nnz, T* v, double alpha);                            \
+    void or_mxv_##S(int64_t m, const int* ar, const int* ac, const T* av, const T* x,    \
+                    T* y);                                                               \
+    void or_vxm_##S(int64_t m, const int* ar, const int* ac, const T* av, const T* x,    \
+                    T* y);
+OR_DECL_EWISE(int32_t, i32)
+OR_DECL_EWISE(int64_t, i64)
+OR_DECL_EWISE(float, f32)
+OR_DECL_EWISE(double, f64)
+#undef OR_DECL_EWISE
+
 OR_DECL(int32_t, i32)
 OR_DECL(int64_t, i64)
 OR_DECL(float, f32)
@@ -66,6 +84,11 @@ OR_DECL(double, f64)
 /* Triangle count, Sandia form C<L> = L*L with L = strict lower triangle of A;
  * rows (optional, length m) receives the row sums of C. */
 int64_t or_tc_sandia(int64_t m, const int* rst, const int* col, int64_t* rows);
+
+/* The reference CLI's reading of a Matrix Market graph file: read_mtx_to_crs,
+ * build_adjacency_matrix and, when `symmetrise`, the lower-triangle
+ * symmetrisation (pattern in *rst / *col, free with or_free). */
+int or_read_mtx_cli(const char* path, int symmetrise, int64_t* m, int64_t* nnz, int** rst, int** col);
 
 /* k-truss by iterated support Tmp<C> = C*C and pruning below k-2.
  * val may be NULL (all ones). Returns 0 on success; *iters is the count the

@@ -110,6 +110,25 @@ op_t<int> ktruss_op(int algo) {
     }
 }
 
+// eWiseAdd(A, B) (include/matrix_la.h:375-435) or, when `masked`,
+// eWiseAdd(A, B, M) (272-335), on the reference's own code.
+template <typename T>
+int ewise_add_t(int masked, int64_t am, int64_t an, int64_t anz, const int* ar, const int* ac, const T* av,
+                int64_t bnz, const int* br, const int* bc, const T* bv, int64_t mnz, const int* mr,
+                const int* mc, int64_t* cm, int64_t* cn, int64_t* cnz, int** cr, int** cc, T** cv) {
+    spMtx<T> A = make_csr<T>(am, an, anz, ar, ac, av);
+    spMtx<T> B = make_csr<T>(am, an, bnz, br, bc, bv);
+    spMtx<T> C;
+    if (masked) {
+        spMtx<T> M = make_csr<T>(am, an, mnz, mr, mc, nullptr);
+        C = eWiseAdd<T, T>(A, B, M);
+    } else {
+        C = eWiseAdd<T>(A, B);
+    }
+    export_csr(C, cm, cn, cnz, cr, cc, cv);
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -210,6 +229,36 @@ int ref_tobinary(const char* path, const char* format, const char* out_path) {
     } catch (...) {
         return 1;
     }
+}
+
+int ref_ewise_add_i32(int masked, int64_t am, int64_t an, int64_t anz, const int* ar, const int* ac,
+                      const int* av, int64_t bnz, const int* br, const int* bc, const int* bv, int64_t mnz,
+                      const int* mr, const int* mc, int64_t* cm, int64_t* cn, int64_t* cnz, int** cr, int** cc,
+                      int** cv) {
+    return ewise_add_t<int>(masked, am, an, anz, ar, ac, av, bnz, br, bc, bv, mnz, mr, mc, cm, cn, cnz, cr, cc, cv);
+}
+
+int ref_ewise_add_f64(int masked, int64_t am, int64_t an, int64_t anz, const int* ar, const int* ac,
+                      const double* av, int64_t bnz, const int* br, const int* bc, const double* bv, int64_t mnz,
+                      const int* mr, const int* mc, int64_t* cm, int64_t* cn, int64_t* cnz, int** cr, int** cc,
+                      double** cv) {
+    return ewise_add_t<double>(masked, am, an, anz, ar, ac, av, bnz, br, bc, bv, mnz, mr, mc, cm, cn, cnz, cr, cc,
+                               cv);
+}
+
+// VxM (include/matrix_la.h:1286-1291): y[j] += A(i,j) * x[i].
+int ref_vxm_f64(int64_t m, int64_t n, int64_t nnz, const int* rst, const int* col, const double* val,
+                double* x, double* y) {
+    spMtx<double> A = make_csr<double>(m, n, nnz, rst, col, val);
+    VxM<double>(A, x, y);
+    return 0;
+}
+
+int ref_vxm_i32(int64_t m, int64_t n, int64_t nnz, const int* rst, const int* col, const int* val, int* x,
+                int* y) {
+    spMtx<int> A = make_csr<int>(m, n, nnz, rst, col, val);
+    VxM<int>(A, x, y);
+    return 0;
 }
 
 // C<M> = A*B with the reference's mxm entry points; algo 0 msa, 1 mca,

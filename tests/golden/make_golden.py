@@ -16,9 +16,11 @@ the graphs themselves are not copied.
 File formats: seeded Matrix Market files written here (formats/*.mtx), the
 reference's raw reading and CLI preparation of each (formats.npz) and the
 binary files its "tobinary" action writes for them (formats/*.bin).
+Element-wise: the reference's eWiseAdd and VxM on seeded operands (ewise.npz).
 
     python tests/golden/make_golden.py            # everything
     python tests/golden/make_golden.py formats    # the file-format fixtures only
+    python tests/golden/make_golden.py ewise      # eWiseAdd / VxM fixtures only
 """
 from __future__ import annotations
 
@@ -193,6 +195,36 @@ def write_formats(rng) -> dict:
     return meta
 
 
+def write_ewise(rng) -> list:
+    """The reference's eWiseAdd (unmasked; masked on operands that share a
+    pattern, where its B-indexing slip is invisible) and VxM on seeded
+    operands."""
+    out = {}
+    keys = []
+    for t in range(3):
+        m, n = int(rng.integers(20, 60)), int(rng.integers(20, 60))
+        for dt, tag in ((np.int32, "i32"), (np.float64, "f64")):
+            def mat(dens):
+                D = rng.random((m, n)) < dens
+                V = rng.integers(-3, 4, (m, n)) if dt == np.int32 else rng.standard_normal((m, n))
+                return csr_from_dense(D, V, dt)
+            A, B, M = mat(0.2), mat(0.2), mat(0.3)
+            B2 = oracle.Csr(A.m, A.n, A.rst, A.col,
+                            (rng.integers(-3, 4, A.nnz) if dt == np.int32 else rng.standard_normal(A.nnz)).astype(dt))
+            key = f"ew{t}_{tag}"
+            for nm, X in (("A", A), ("B", B), ("M", M), ("B2", B2)):
+                pack(f"{key}_{nm}", X, out)
+            pack(f"{key}_add", oracle.ref_ewise_add(A, B), out)
+            pack(f"{key}_madd", oracle.ref_ewise_add(A, B2, M), out)
+            x = (rng.integers(-5, 5, m) if dt == np.int32 else rng.standard_normal(m)).astype(dt)
+            y = (rng.integers(-5, 5, n) if dt == np.int32 else rng.standard_normal(n)).astype(dt)
+            out[f"{key}_x"], out[f"{key}_y"] = x, y
+            out[f"{key}_vxm"] = oracle.ref_vxm(A, x, y)
+            keys.append(key)
+    np.savez_compressed(os.path.join(HERE, "ewise.npz"), **out)
+    return keys
+
+
 def main():
     if oracle.build_ref() is None:
         raise SystemExit("reference sources not available; cannot regenerate fixtures")
@@ -267,13 +299,17 @@ def main():
         with open(os.path.join(HERE, "reference_graphs.json"), "w") as f:
             json.dump(known, f, indent=1)
     write_formats(np.random.default_rng(20261204))
+    write_ewise(np.random.default_rng(20261205))
     print("wrote", sorted(os.listdir(HERE)))
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] == ["formats"]:
+    if sys.argv[1:] in (["formats"], ["ewise"]):
         if oracle.build_ref() is None:
             raise SystemExit("reference sources not available; cannot regenerate fixtures")
-        print(write_formats(np.random.default_rng(20261204)))
+        if sys.argv[1] == "formats":
+            print(write_formats(np.random.default_rng(20261204)))
+        else:
+            print(write_ewise(np.random.default_rng(20261205)))
     else:
         main()

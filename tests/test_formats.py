@@ -118,3 +118,13 @@ def test_ingest_entry_points_reject_bad_arguments(built):
                                0, 0, ctypes.byref(h)) == ga.ERR_INVALID_ARG
     assert L.ga_csr_from_device_edges(None, ctypes.c_int64(1), ctypes.c_int64(1), ctypes.c_int64(1), None, None,
                                       None, 0, 0, ctypes.byref(h)) == ga.ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("name", sorted(META))
+def test_c_port_of_cli_reading_matches_reference(built, name):
+    """oracle.read_mtx_cli (the CPU baseline of the ingestion benchmark)
+    reproduces the reference CLI's reading, rows in the reference's order."""
+    for sym in (0, 1):
+        A = oracle.read_mtx_cli(os.path.join(FMT, name + ".mtx"), bool(sym))
+        R = golden(name, f"cli{sym}")
+        assert np.array_equal(A.rst, R.rst) and np.array_equal(A.col, R.col)
