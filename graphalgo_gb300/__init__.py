@@ -82,6 +82,8 @@ def lib() -> ctypes.CDLL:
     L.ga_gen_knn.argtypes = [_i64, _int, _int, ctypes.c_uint64, ctypes.POINTER(_i64), ctypes.POINTER(_i64),
                              ctypes.POINTER(_p), ctypes.POINTER(_p)]
     L.ga_ctx_set_option.argtypes = [_p, _int, _i64]
+    L.ga_gen_rmat_device.argtypes = [_p, _int, _int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_uint64, ctypes.POINTER(_p)]
     _lib = L
     return L
 
@@ -504,6 +506,15 @@ def gen_rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19
     return _gen(lib().ga_gen_rmat, int(scale), int(edge_factor), float(a), float(b), float(c), int(seed))
 
 
+def gen_rmat_device(ctx: Context, scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19,
+                    c: float = 0.19, seed: int = 1) -> Csr:
+    """The R-MAT graph of gen_rmat (bit for bit), built on the device."""
+    h = _p()
+    _check(lib().ga_gen_rmat_device(ctx.handle, int(scale), int(edge_factor), float(a), float(b), float(c),
+                                    int(seed), ctypes.byref(h)), ctx)
+    return Csr(ctx, h)
+
+
 def gen_er(n: int, edges: int, seed: int = 1):
     """Seeded Erdos-Renyi G(n, m) graph with `edges` undirected edges."""
     return _gen(lib().ga_gen_er, int(n), int(edges), int(seed))
@@ -645,6 +656,25 @@ class Server:
             raise GaError(rc, lib().ga_status_string(rc).decode())
         self.sizes.append(m)
         return int(gid.value)
+
+    def _added(self, rc: int, gid) -> int:
+        if rc != OK:
+            raise GaError(rc, lib().ga_status_string(rc).decode())
+        m = _i64()
+        _check(lib().ga_server_graph_info(self.handle, gid, ctypes.byref(m), None))
+        self.sizes.append(int(m.value))
+        return int(gid.value)
+
+    def add_graph_device(self, A: Csr) -> int:
+        """Copies a symmetric int32 device CSR of the same device into the pool."""
+        gid = _int()
+        return self._added(lib().ga_server_add_graph_device(self.handle, A.ctx.handle, A.handle, ctypes.byref(gid)),
+                           gid)
+
+    def add_graph_file(self, path: str) -> int:
+        """Reads a ".mtx" or ".bin" graph file on the device into the pool."""
+        gid = _int()
+        return self._added(lib().ga_server_add_graph_file(self.handle, os.fsencode(path), ctypes.byref(gid)), gid)
 
     def submit(self, req_type: int, graph: int, k: int = 0, sources=None, want_edges: bool = False) -> int:
         src = None if sources is None else np.ascontiguousarray(sources, dtype=np.int32)

@@ -198,6 +198,78 @@ static ga_csr edges_to_csr(ga_ctx ctx, int64_t m, int64_t n, int64_t ne, const i
     return A;
 }
 
+// ================================================================ R-MAT
+// The host generator's random streams (ga_gen.cpp): xoshiro256** seeded by
+// splitmix64 per chunk of 2^16 edges; one thread walks one chunk, so every
+// edge gets the same bits as on the host.
+__device__ __forceinline__ uint64_t dev_splitmix64(uint64_t& x) {
+    uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+struct DevXoshiro {
+    uint64_t s0, s1, s2, s3;
+    __device__ explicit DevXoshiro(uint64_t seed) {
+        uint64_t x = seed;
+        s0 = dev_splitmix64(x);
+        s1 = dev_splitmix64(x);
+        s2 = dev_splitmix64(x);
+        s3 = dev_splitmix64(x);
+    }
+    __device__ static uint64_t rotl(uint64_t v, int k) { return (v << k) | (v >> (64 - k)); }
+    __device__ uint64_t next() {
+        const uint64_t r = rotl(s1 * 5, 7) * 9;
+        const uint64_t t = s1 << 17;
+        s2 ^= s0; s3 ^= s1; s1 ^= s2; s0 ^= s3;
+        s2 ^= t;
+        s3 = rotl(s3, 45);
+        return r;
+    }
+    __device__ double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+};
+
+constexpr int64_t kRmatChunk = 1 << 16;
+
+__global__ void k_rmat_edges(int scale, int64_t edges, double a, double ab, double abc, uint64_t seed,
+                             int32_t* __restrict__ src, int32_t* __restrict__ dst) {
+    const int64_t ch = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t e0 = ch * kRmatChunk;
+    if (e0 >= edges) return;
+    const int64_t e1 = min(edges, e0 + kRmatChunk);
+    uint64_t x = seed ^ (0xD1B54A32D192ED03ull * ((uint64_t)ch + 1));
+    DevXoshiro rng(dev_splitmix64(x));
+    for (int64_t e = e0; e < e1; ++e) {
+        uint32_t u = 0, v = 0;
+        for (int l = 0; l < scale; ++l) {
+            const double r = rng.uniform();
+            const uint32_t bu = r >= ab, bv = (r >= a && r < ab) || r >= abc;
+            u = (u << 1) | bu;
+            v = (v << 1) | bv;
+        }
+        src[e] = (int32_t)u;
+        dst[e] = (int32_t)v;
+    }
+}
+
+static ga_csr gen_rmat_device(ga_ctx ctx, int scale, int edge_factor, double a, double b, double c, uint64_t seed) {
+    GA_REQUIRE(scale >= 1 && scale <= 26 && edge_factor >= 1, GA_ERR_INVALID_ARG, "rmat: scale or edge factor");
+    GA_REQUIRE(a >= 0 && b >= 0 && c >= 0 && a + b + c <= 1.0, GA_ERR_INVALID_ARG, "rmat: quadrant probabilities");
+    const int64_t n = 1ll << scale, edges = n * edge_factor;
+    GA_REQUIRE(edges < INT32_MAX / 2, GA_ERR_INVALID_ARG, "rmat: too many edges for int32 entries");
+    DBuf<int32_t> src(ctx, (size_t)edges), dst(ctx, (size_t)edges);
+    const int64_t nch = (edges + kRmatChunk - 1) / kRmatChunk;
+    {
+        ProfScope ps(ctx, "rmat_edges");
+        k_rmat_edges<<<(unsigned)((nch + 63) / 64), 64, 0, ctx->stream>>>(scale, edges, a, a + b, a + b + c, seed,
+                                                                          src.p, dst.p);
+        post_launch("rmat_edges");
+    }
+    return edges_to_csr(ctx, n, n, edges, src.p, dst.p, nullptr, GA_INT32,
+                        GA_EDGES_MIRROR | GA_EDGES_DROP_LOOPS | GA_EDGES_UNIT);
+}
+
 // ============================================================ file staging
 struct File {
     FILE* f = nullptr;
@@ -789,6 +861,16 @@ int ga_csr_from_device_edges(ga_ctx ctx, int64_t m, int64_t n, int64_t ne, const
         return GA_ERR_INVALID_ARG;
     *out = nullptr;
     GA_API_BODY(ctx, *out = edges_to_csr(ctx, m, n, ne, src, dst, val, dtype, flags));
+}
+
+int ga_gen_rmat_device(ga_ctx ctx, int scale, int edge_factor, double a, double b, double c, uint64_t seed,
+                       ga_csr* out) {
+    if (!ctx || !out) return GA_ERR_INVALID_ARG;
+    *out = nullptr;
+    GA_API_BODY(ctx, {
+        *out = gen_rmat_device(ctx, scale, edge_factor, a, b, c, seed);
+        (*out)->sym = 1;
+    });
 }
 
 int ga_read_mtx(ga_ctx ctx, const char* path, int flags, char* matcode, ga_csr* out) {

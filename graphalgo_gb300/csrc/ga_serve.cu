@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstring>
 #include <deque>
 #include <memory>
 #include <mutex>
@@ -386,15 +387,13 @@ int ga_server_create(int device, const ga_server_config* cfg, ga_server* out) {
     return GA_OK;
 }
 
-int ga_server_add_graph(ga_server srv, int64_t m, const int32_t* rst, const int32_t* col, int* graph_id) {
-    if (!srv || !graph_id || m < 0 || !rst) return GA_ERR_INVALID_ARG;
-    std::lock_guard<std::mutex> lk(srv->mu);
-    if (srv->graphs.size() >= kMaxGraphs) return GA_ERR_UNSUPPORTED;
-    const int64_t nnz = rst[m];
-    ga_csr A = nullptr;
-    int rc = ga_csr_upload(srv->home, m, m, nnz, rst, col, nullptr, GA_INT32, &A);
-    if (rc != GA_OK) return rc;
+// Registers A (owned by the home context from now on); the caller holds
+// srv->mu. Frees A when it is refused.
+static int add_resident(ga_server srv, ga_csr A, int* graph_id) {
+    const int64_t m = A->m, nnz = A->nnz;
     try {
+        GA_REQUIRE(A->dtype == GA_INT32 && A->m == A->n, GA_ERR_INVALID_ARG,
+                   "server graphs must be square int32 adjacency matrices");
         // settle the cached flags now: workers only read them afterwards
         csr_unit_values(srv->home, A);
         csr_is_symmetric(srv->home, A);
@@ -412,6 +411,54 @@ int ga_server_add_graph(ga_server srv, int64_t m, const int32_t* rst, const int3
     srv->budget -= 4 * (m + 1) + 8 * nnz;  // the resident graph comes out of the budget
     srv->st.budget = srv->budget;
     *graph_id = (int)srv->graphs.size() - 1;
+    return GA_OK;
+}
+
+int ga_server_add_graph(ga_server srv, int64_t m, const int32_t* rst, const int32_t* col, int* graph_id) {
+    if (!srv || !graph_id || m < 0 || !rst) return GA_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    if (srv->graphs.size() >= kMaxGraphs) return GA_ERR_UNSUPPORTED;
+    ga_csr A = nullptr;
+    int rc = ga_csr_upload(srv->home, m, m, rst[m], rst, col, nullptr, GA_INT32, &A);
+    if (rc != GA_OK) return rc;
+    return add_resident(srv, A, graph_id);
+}
+
+int ga_server_add_graph_device(ga_server srv, ga_ctx ctx, ga_csr A, int* graph_id) {
+    if (!srv || !ctx || !A || !graph_id || ctx->device != srv->device) return GA_ERR_INVALID_ARG;
+    int rc = ga_ctx_sync(ctx);  // A complete before the home stream copies it
+    if (rc != GA_OK) return rc;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    if (srv->graphs.size() >= kMaxGraphs) return GA_ERR_UNSUPPORTED;
+    ga_csr C = nullptr;
+    rc = ga_csr_from_device(srv->home, A->m, A->n, A->nnz, A->rst, A->col, A->val, A->dtype, &C);
+    if (rc != GA_OK) return rc;
+    return add_resident(srv, C, graph_id);
+}
+
+int ga_server_add_graph_file(ga_server srv, const char* path, int* graph_id) {
+    if (!srv || !path || !graph_id) return GA_ERR_INVALID_ARG;
+    const size_t len = strlen(path);
+    const bool mtx = len > 4 && strcmp(path + len - 4, ".mtx") == 0;
+    const bool bin = len > 4 && strcmp(path + len - 4, ".bin") == 0;
+    if (!mtx && !bin) return GA_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    if (srv->graphs.size() >= kMaxGraphs) return GA_ERR_UNSUPPORTED;
+    ga_csr A = nullptr;
+    // the reference CLI's preparation for TC and k-truss: adjacency, lower-triangle symmetrisation
+    const int flags = GA_EDGES_LOWER_SYMM | GA_EDGES_UNIT;
+    int rc = mtx ? ga_read_mtx(srv->home, path, flags, nullptr, &A) : ga_read_bin(srv->home, path, flags, nullptr, &A);
+    if (rc != GA_OK) return rc;
+    return add_resident(srv, A, graph_id);
+}
+
+int ga_server_graph_info(ga_server srv, int graph, int64_t* m, int64_t* nnz) {
+    if (!srv) return GA_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    if (graph < 0 || graph >= (int)srv->graphs.size()) return GA_ERR_INVALID_ARG;
+    const SrvGraph& g = srv->graphs[(size_t)graph];
+    if (m) *m = g.m;
+    if (nnz) *nnz = g.nnz;
     return GA_OK;
 }
 

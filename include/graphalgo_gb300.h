@@ -485,6 +485,15 @@ GA_API int ga_server_destroy(ga_server srv);
 /* Uploads a symmetric adjacency matrix (host CSR, values 1) once; it stays
  * resident and its bytes come out of the budget. */
 GA_API int ga_server_add_graph(ga_server srv, int64_t m, const int32_t* rst, const int32_t* col, int* graph_id);
+/* The same from a device CSR of context ctx (same device; copied on the
+ * device, ctx's stream synchronised first; A stays the caller's), or from a
+ * graph file (".mtx" / ".bin" by extension, read on the device with the
+ * reference CLI's preparation: adjacency and lower-triangle symmetrisation,
+ * src/main.cpp:221-222), so a pool loads without host CSR builds. */
+GA_API int ga_server_add_graph_device(ga_server srv, ga_ctx ctx, ga_csr A, int* graph_id);
+GA_API int ga_server_add_graph_file(ga_server srv, const char* path, int* graph_id);
+/* Vertex count and stored entries of a resident graph (either may be NULL). */
+GA_API int ga_server_graph_info(ga_server srv, int graph, int64_t* m, int64_t* nnz);
 /* Queues a request: GA_REQ_TC, GA_REQ_KTRUSS (k), or GA_REQ_BC (sources,
  * copied). want_edges: keep the k-truss edge set for ga_server_wait. */
 GA_API int ga_server_submit(ga_server srv, int type, int graph, int k, const int32_t* sources, int nsrc,
@@ -508,6 +517,11 @@ GA_API int ga_server_get_stats(ga_server srv, ga_server_stats* stats);
  *  Euclidean distance (self excluded), symmetrised by union. */
 GA_API int ga_gen_rmat(int scale, int edge_factor, double a, double b, double c, uint64_t seed,
                        int64_t* m, int64_t* nnz, int32_t** rst, int32_t** col);
+/* The same R-MAT graph as ga_gen_rmat (bit for bit), generated and built on
+ * the device: edges from the same random streams, then mirrored, loops
+ * dropped, rows sorted and duplicates merged by the ingestion kernels. */
+GA_API int ga_gen_rmat_device(ga_ctx ctx, int scale, int edge_factor, double a, double b, double c, uint64_t seed,
+                              ga_csr* out);
 GA_API int ga_gen_er(int64_t n, int64_t edges, uint64_t seed, int64_t* m, int64_t* nnz, int32_t** rst,
                      int32_t** col);
 GA_API int ga_gen_knn(int64_t n, int dim, int k, uint64_t seed, int64_t* m, int64_t* nnz, int32_t** rst,

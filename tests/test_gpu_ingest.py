@@ -228,3 +228,23 @@ def test_transpose_with_long_columns(ctx):
     T = ga.transpose(A)
     E = oracle.transpose(F.from_edges(m, n, src, dst, val))
     assert_csr(T, E)
+
+
+@pytest.mark.parametrize("scale,ef,seed", [(6, 4, 3), (12, 16, 7), (17, 16, 11)])
+def test_rmat_device_equals_host(ctx, scale, ef, seed):
+    """The device R-MAT builder gives the host generator's graph bit for bit
+    (same random streams; chunks of 2^16 edges cross thread boundaries at
+    scale 17)."""
+    m, rst, col = ga.gen_rmat(scale, ef, seed=seed)
+    A = ga.gen_rmat_device(ctx, scale, ef, seed=seed)
+    assert A.shape == (m, m) and A.dtype == ga.INT32
+    dr, dc, dv = A.download()
+    assert np.array_equal(dr, rst) and np.array_equal(dc, col)
+    assert np.all(dv == 1)
+
+
+def test_rmat_device_errors(ctx):
+    with pytest.raises(ga.GaError):
+        ga.gen_rmat_device(ctx, 0, 16)
+    with pytest.raises(ga.GaError):
+        ga.gen_rmat_device(ctx, 10, 16, a=0.6, b=0.3, c=0.3)

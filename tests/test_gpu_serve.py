@@ -175,3 +175,36 @@ def test_concurrent_bc_with_different_source_counts(built):
     for w in (0, 1):
         for got in results[w]:
             np.testing.assert_allclose(got, refs[w], rtol=BC_RTOL, atol=1e-9)
+
+
+def test_pool_from_device_and_files(ctx, tmp_path):
+    """Graphs added from a device CSR or from a graph file serve the same
+    results as the same graph uploaded from the host."""
+    scale = 9
+    m, rst, col = ga.gen_rmat(scale, 16, seed=77)
+    D = ga.gen_rmat_device(ctx, scale, 16, seed=77)
+    # a Matrix Market file holding the lower triangle, as the reference's graphs do
+    lo = [(i, j) for i in range(m) for j in col[rst[i]:rst[i + 1]] if j < i]
+    mtx = tmp_path / "g.mtx"
+    with open(mtx, "w") as f:
+        f.write("%%MatrixMarket matrix coordinate pattern symmetric\n")
+        f.write(f"{m} {m} {len(lo)}\n")
+        f.writelines(f"{i + 1} {j + 1}\n" for i, j in lo)
+    binp = tmp_path / "g.bin"
+    ga.write_bin(D, str(binp))
+    with ga.Server(0, workers=2, coalesce=True) as srv:
+        g_host = srv.add_graph(m, rst, col)
+        g_dev = srv.add_graph_device(D)
+        g_mtx = srv.add_graph_file(str(mtx))
+        g_bin = srv.add_graph_file(str(binp))
+        assert srv.sizes == [m] * 4
+        with pytest.raises(ga.GaError):
+            srv.add_graph_file(str(tmp_path / "g.txt"))
+        src = np.arange(0, m, m // 16, dtype=np.int32)[:16]
+        reqs = [(t, g, k, s) for g in (g_host, g_dev, g_mtx, g_bin)
+                for t, k, s in ((ga.REQ_TC, 0, None), (ga.REQ_KTRUSS, 4, None), (ga.REQ_BC, 0, src))]
+        got = _serve(srv, reqs)
+    for i in range(3):
+        for j in (1, 2, 3):
+            _same(got[i], got[3 * j + i], reqs[i][0])
+    assert got[0]["tc"] > 0
