@@ -56,7 +56,7 @@ def parse_args():
     ap.add_argument("--scale", type=int, default=18)
     ap.add_argument("--edge-factor", type=int, default=16)
     ap.add_argument("--seed", type=int, default=42)
-    ap.add_argument("--algo", default=None, choices=["msa", "mca", "heap", "dot", "hybrid", "auto"],
+    ap.add_argument("--algo", default=None, choices=["msa", "mca", "heap", "dot", "hybrid", "tri", "auto"],
                     help="k-truss variant (default: msa; auto for the batch workload)")
     ap.add_argument("--kmin", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -204,10 +204,10 @@ def measured_peak_hbm():
     return HBM_FALLBACK_GBS, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per mask entry of the MSA kernel from the committed ncu
-    summary (profiles/mxm_msa_rmat18_support.md), or None."""
-    p = os.path.join(ROOT, "profiles", "mxm_msa_rmat18_support.md")
+def profile_traffic(summary: str = "mxm_msa_rmat18_support.md"):
+    """DRAM bytes per mask entry of the dominant kernel from its committed ncu
+    summary under profiles/ (MSA, or the triangle-listing kernel), or None."""
+    p = os.path.join(ROOT, "profiles", summary)
     try:
         with open(p) as f:
             for line in f:
@@ -353,14 +353,24 @@ def profile_step(ga, ctx, run, algo, counters, loops):
     ctx.set_option(ga.OPT_PROFILE, 0)
     ctx.set_option(ga.OPT_DEVICE_LOOPS, loops)
     kname = {"msa": "mxm_msa", "mca": "mxm_mca", "heap": "mxm_heap_merge", "dot": "mxm_dot",
-             "hybrid": "mxm_msa"}[algo]
+             "hybrid": "mxm_msa", "tri": "tri_support"}[algo]
     k_launches, k_ms = stats.get(kname, (0, 0.0))
-    # products of the Gustavson kernels; list entries walked for the inner-product one
-    ex = ctr["executed_dot"] if algo == "dot" else ctr["executed"]
-    bytes_model = 8 * ctr["rows"] + 16 * ctr["a_entries"] + 8 * ex + 8 * ctr["mask_entries"]
+    if algo == "tri":
+        # triangle listing: oriented row starts and task starts (4 bytes each
+        # per row), per oriented entry (half the stored entries of a graph
+        # without loops) its column, its list bounds and one 4-byte count
+        # read-modify-write, per wedge its column, per triangle two 4-byte
+        # read-modify-writes
+        eo = ctr["a_entries"] / 2
+        bytes_model = 8 * ctr["rows"] + 20 * eo + 4 * ctr["wedges"] + 16 * ctr["triangles"]
+        tpe = profile_traffic("tri_support_rmat18.md")
+    else:
+        # products of the Gustavson kernels; list entries walked for the inner-product one
+        ex = ctr["executed_dot"] if algo == "dot" else ctr["executed"]
+        bytes_model = 8 * ctr["rows"] + 16 * ctr["a_entries"] + 8 * ex + 8 * ctr["mask_entries"]
+        tpe = profile_traffic()
     peak, peak_kind = measured_peak_hbm()
     achieved = bytes_model / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
-    tpe = profile_traffic()
     traffic = (tpe * ctr["mask_entries"] / max(1, k_launches)) if tpe is not None else None
     return {"launches": launches, "kernel_ms": k_ms, "stats": stats, "counters": ctr,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -27,8 +27,9 @@ LIB_PATH = os.path.join(HERE, "_lib", "libgraphalgo_gb300.so")
 # dtypes
 INT32, INT64, FP32, FP64, UINT8 = 0, 1, 2, 3, 4
 # algorithms
-MSA, MCA, HEAP, NAIVE, DOT, AUTO, HYBRID = 0, 1, 2, 3, 4, 5, 6
-ALGOS = {"msa": MSA, "mca": MCA, "heap": HEAP, "naive": NAIVE, "dot": DOT, "auto": AUTO, "hybrid": HYBRID}
+MSA, MCA, HEAP, NAIVE, DOT, AUTO, HYBRID, TRI = 0, 1, 2, 3, 4, 5, 6, 7
+ALGOS = {"msa": MSA, "mca": MCA, "heap": HEAP, "naive": NAIVE, "dot": DOT, "auto": AUTO, "hybrid": HYBRID,
+         "tri": TRI}
 ALGO_NAMES = {v: k for k, v in ALGOS.items()}
 # options
 OPT_DEVICE_LOOPS, OPT_PROFILE, OPT_FAIL_ALLOC_AFTER, OPT_KNN_TILED = 1, 2, 3, 4
@@ -175,11 +176,12 @@ class Context:
         """Masked-SpGEMM work since the last reset: Gustavson products P of the
         requested products, mask entries, launches, A entries, rows, the
         products the Gustavson kernels processed, and the list entries the
-        inner-product kernels walked (device counters)."""
-        out = (ctypes.c_int64 * 7)()
+        inner-product kernels walked, and the wedges and triangles of the
+        triangle-listing form (device counters)."""
+        out = (ctypes.c_int64 * 9)()
         _check(lib().ga_ctx_work_counters(self.handle, out, int(bool(reset))), self)
-        return dict(zip(("products", "mask_entries", "launches", "a_entries", "rows", "executed", "executed_dot"),
-                        (int(x) for x in out)))
+        return dict(zip(("products", "mask_entries", "launches", "a_entries", "rows", "executed", "executed_dot",
+                         "wedges", "triangles"), (int(x) for x in out)))
 
     def flush_l2(self):
         _check(lib().ga_ctx_flush_l2(self.handle), self)

@@ -417,6 +417,18 @@ __global__ void k_kt_copyback_aux(const KtState* st, const int32_t* __restrict__
     }
 }
 
+void expand_rows(ga_ctx ctx, ga_csr A, int32_t* row_of) {
+    k_expand_rows<<<grid_for(A->m * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(A->rst, A->m, row_of);
+    post_launch("expand_rows");
+}
+
+void mirror_index(ga_ctx ctx, ga_csr A, const int32_t* row_of, int32_t* mir) {
+    if (A->nnz == 0) return;
+    k_mirror_index<<<grid_for(A->nnz, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(A->rst, A->col, row_of,
+                                                                                     A->nnz, mir);
+    post_launch("mirror_index");
+}
+
 void upper_starts(ga_ctx ctx, ga_csr A, int32_t* ust) {
     k_upper_start<<<grid_for(A->m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(A->rst, A->col, A->m, ust);
     post_launch("kt_upper_start");
@@ -428,7 +440,7 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
     TuneScope tscope(ctx);
     algo = resolve_ktruss_algo(ctx, algo, A);
     GA_REQUIRE(algo == GA_MSA || algo == GA_MCA || algo == GA_HEAP || algo == GA_NAIVE || algo == GA_DOT ||
-                   algo == GA_HYBRID,
+                   algo == GA_HYBRID || algo == GA_TRI,
                GA_ERR_INVALID_ARG, "k-truss: unknown algorithm");
     const int64_t m = A->m;
     // C = A (a copy; its pattern shrinks in place)
@@ -442,7 +454,6 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
         // eflag: keep flags of the entries, scanned in place into new positions
         DBuf<int32_t> sup(ctx, (size_t)cap), eflag(ctx, (size_t)cap + 1), tr(ctx, (size_t)m + 1), tc(ctx, (size_t)cap);
         DBuf<unsigned char> scan_scr(ctx, scan_scratch_bytes(cap));
-        DBuf<unsigned char> mxm_scr(ctx, mxm_scratch_bytes(m, m, cap));
         DBuf<KtState> st(ctx, 1);
         KtState h0 = {};
         h0.nnz = (int32_t)A->nnz;
@@ -454,10 +465,15 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
         // only the upper triangle (columns >= i) is multiplied, the lower
         // triangle is mirrored. Same values, about half the products.
         const bool upper = algo != GA_NAIVE && csr_is_symmetric(ctx, A);
+        // Triangle listing when C is symmetric with unit values; else the
+        // hybrid form (symmetric) or MSA.
+        const bool tri = algo == GA_TRI && upper && unit;
+        if (algo == GA_TRI && !tri) algo = upper ? GA_HYBRID : GA_MSA;
         GA_REQUIRE(upper || (algo != GA_DOT && algo != GA_HYBRID), GA_ERR_UNSUPPORTED,
                    "k-truss with GA_DOT or GA_HYBRID needs a symmetric matrix");
+        DBuf<unsigned char> mxm_scr(ctx, tri ? tri_scratch_bytes(m, cap) : mxm_scratch_bytes(m, m, cap));
         const size_t aux = upper ? (size_t)cap : 1;
-        DBuf<int32_t> ust(ctx, upper ? (size_t)m + 1 : 1);
+        DBuf<int32_t> ust(ctx, upper && !tri ? (size_t)m + 1 : 1);
         DBuf<int32_t> row_of(ctx, aux), mir(ctx, aux), pos_new(ctx, aux), trow(ctx, aux), mir_new(ctx, aux);
         ga_csr_s Cu;  // C with row starts moved to the upper part
         const int grid_rows = grid_for(m * 32, 256, ctx->num_sms * 16);
@@ -471,10 +487,14 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
             k_mirror_index<<<grid_ent, 256, 0, ctx->stream>>>(C->rst, C->col, row_of.p, C->nnz, mir.p);
             post_launch("kt_mirror_index");
         }
+        if (tri) tri_prepare(ctx, C, mxm_scr.p, cap);
         auto body = [&](const LoopCtl& ctl) {
             // Tmp<C> = C*C, values aligned with C's pattern
             if (algo == GA_NAIVE) {
                 mxm_masked_into(ctx, algo, C, C, C, sup.p);
+            } else if (tri) {
+                // eflag holds the orientation positions until the prune reuses it
+                tri_support_launch(ctx, C, row_of.p, mir.p, eflag.p, sup.p, mxm_scr.p, cap, true);
             } else if (upper) {
                 k_upper_start<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(C->rst, C->col, m, ust.p);
                 post_launch("kt_upper_start");

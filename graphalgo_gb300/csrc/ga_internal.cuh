@@ -222,6 +222,27 @@ struct TuneScope {
 };
 // Position of the first entry with column >= i in each row (rows sorted).
 void upper_starts(ga_ctx ctx, ga_csr A, int32_t* ust);
+// Row index of every entry; position of every entry's mirror (j, i) in a
+// symmetric pattern.
+void expand_rows(ga_ctx ctx, ga_csr A, int32_t* row_of);
+void mirror_index(ga_ctx ctx, ga_csr A, const int32_t* row_of, int32_t* mir);
+
+// Triangle-listing support product (GA_TRI) of a symmetric int32 matrix
+// whose values are all 1. tri_support_launch allocates nothing (capturable):
+// C's entry count is read on the device (at most cap), row_of / mir are the
+// row and mirror position of every entry, pos has cap + 1 entries, scratch
+// tri_scratch_bytes(C->m, cap) bytes; sup receives C·C at C's entries.
+// upper_counts: work counters as for an upper-triangle support product.
+// tri_prepare ranks the vertices by C's degrees into the scratch; it runs
+// once before the evaluations (any ranking gives the same counts).
+size_t tri_scratch_bytes(int64_t m, int64_t cap);
+void tri_prepare(ga_ctx ctx, ga_csr C, void* scratch, int64_t cap);
+void tri_support_launch(ga_ctx ctx, ga_csr C, const int32_t* row_of, const int32_t* mir, int32_t* pos,
+                        int32_t* sup, void* scratch, int64_t cap, bool upper_counts);
+// A, B and M one symmetric int32 matrix with unit values (synchronises the
+// stream the first time a handle is checked).
+bool tri_applies(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M);
+void tri_masked_into(ga_ctx ctx, ga_csr A, int32_t* sup);
 
 // device-side transpose (counting sort; rows of the result sorted)
 ga_csr transpose_csr(ga_ctx ctx, ga_csr A);

@@ -1021,6 +1021,13 @@ void mxm_masked_into(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, voi
     if (M->nnz == 0 || M->m == 0) return;
     TuneScope tscope(ctx);
     algo = resolve_mxm_algo(ctx, algo, A, B, M);
+    if (algo == GA_TRI) {
+        if (tri_applies(ctx, A, B, M)) {
+            tri_masked_into(ctx, A, static_cast<int32_t*>(d_cvals));
+            return;
+        }
+        algo = GA_HYBRID;
+    }
     if (algo == GA_NAIVE) {
         naive_masked_into(ctx, A, B, M, d_cvals);
         return;

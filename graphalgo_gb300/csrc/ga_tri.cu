@@ -1,0 +1,402 @@
+// Triangle-listing form of the support product (GA_TRI): C<A> = A·A for a
+// symmetric matrix A whose stored values are all 1 — the product the
+// reference's k_truss evaluates every iteration (src/main.cpp:103,
+// Tmp<C> = C·C) and whose row sums its triangle counts take.
+//
+// For such an A, C(i, j) = |N(i) ∩ N(j)| over vertices other than i and j
+// (the triangles through edge {i, j}), plus 1 for each of i and j that holds
+// a diagonal entry; C(i, i) = |N(i)| (the row's length, diagonal included).
+// Every triangle is listed once: vertices get ranks 0..m-1 in order of
+// degree (a counting sort, once per call), each undirected edge is kept in
+// the direction of increasing rank (the oriented list O_u of u holds the
+// neighbours ranked above u, in column order), and a triangle u < v < w (by
+// rank) is found as the wedge u -> v -> w with w in O_u. Its three edges'
+// counts are raised: (u, v) by the entry's ballot total, (u, w) in shared
+// memory, (v, w) by a global atomic. The counts go back to both mirror
+// entries of every edge. Integer counts: the result is exact whatever the
+// order, and whatever order ties of degree get.
+//
+// Lookups: after ranking by degree almost every wedge ends at a vertex of
+// the top kTriWin ranks (the hubs), so each warp keeps a bitmap of O_u's
+// members in that rank window, with per-word popcount prefixes giving a
+// member's index in O(1); the rare w below the window is binary-searched in
+// O_u.
+//
+// Per evaluation (all launches read the current entry count on the device, so
+// a captured loop whose matrix shrinks can replay them):
+//   orient     rank flags per entry, diagonal flags, work counters
+//   scan       flags -> positions in the oriented lists
+//   scatter    oriented columns and their ranks, zeroed counts, oriented row
+//              starts, tasks per row (kTriTask oriented entries each)
+//   scan       tasks per row -> task starts; task list
+//   support    one warp per task
+//   writeback  counts (+ diagonal terms) to both mirror entries; C(i, i)
+#include "ga_device.cuh"
+
+namespace ga {
+
+constexpr int kTriThreads = 128;
+constexpr int kTriTask = 32;                  // oriented entries per warp task (at most 32)
+constexpr int kTriWin = 1 << 14;              // rank window of the member bitmaps
+constexpr int kTriWinWords = kTriWin / 32;    // 512 bitmap words per warp
+constexpr int kTriCntMax = 1024;              // longest O_u counted in shared memory
+constexpr int kTriCntWords = kTriCntMax / 4;  // byte counters, four per word
+
+// ------------------------------------------------------------------ ranks
+__global__ void k_tri_deg_count(const int32_t* __restrict__ cr, int64_t m, int32_t* __restrict__ hist) {
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < m; v += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(hist + (cr[v + 1] - cr[v]), 1);
+}
+
+// After the scan of the degree histogram: rank = next free place of the
+// vertex's degree bucket.
+__global__ void k_tri_rank(const int32_t* __restrict__ cr, int64_t m, int32_t* __restrict__ next,
+                           int32_t* __restrict__ rank) {
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < m; v += (int64_t)gridDim.x * blockDim.x)
+        rank[v] = atomicAdd(next + (cr[v + 1] - cr[v]), 1);
+}
+
+// Rank flag of every entry (column ranked above the row: kept in O_row),
+// diagonal flags, and the Gustavson work counters the other forms report:
+// with `upper`, as for a k-truss support that evaluates the upper triangle
+// (products of the rows whose upper part is not empty, upper entries), else
+// as for the whole mask.
+__global__ void k_tri_orient(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
+                             const int32_t* __restrict__ row_of, const int32_t* __restrict__ rank, int64_t m,
+                             int64_t cap, int32_t* __restrict__ flag, int32_t* __restrict__ diag,
+                             unsigned long long* __restrict__ ctr, bool upper) {
+    const int64_t cur = cr[m];
+    unsigned long long prod = 0, mask = 0;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cap; q += (int64_t)gridDim.x * blockDim.x) {
+        int32_t f = 0;
+        if (q < cur) {
+            const int32_t i = row_of[q], j = cc[q];
+            if (i == j) diag[i] = 1;
+            else f = rank[j] > rank[i];
+            if (!upper || j >= i) ++mask;
+            if (!upper || cc[cr[i + 1] - 1] >= i) prod += (unsigned long long)(cr[j + 1] - cr[j]);
+        }
+        flag[q] = f;
+    }
+    prod = warp_sum<unsigned long long>(prod);
+    mask = warp_sum<unsigned long long>(mask);
+    if ((threadIdx.x & 31) == 0) {
+        if (prod) atomicAdd(&ctr[GA_CTR_PRODUCTS], prod);
+        if (mask) atomicAdd(&ctr[GA_CTR_MASK_ENTRIES], mask);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(&ctr[GA_CTR_LAUNCHES], 1ull);
+        atomicAdd(&ctr[GA_CTR_A_ENTRIES], (unsigned long long)cur);
+        atomicAdd(&ctr[GA_CTR_ROWS], (unsigned long long)m);
+    }
+}
+
+// After the scan `pos` of the flags: oriented columns, their ranks and
+// zeroed counts at their positions, oriented row starts ost[i] = pos[cr[i]],
+// and the number of warp tasks of each row.
+__global__ void k_tri_scatter(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
+                              const int32_t* __restrict__ pos, const int32_t* __restrict__ rank, int64_t m,
+                              int32_t* __restrict__ ocol, int32_t* __restrict__ orank, int32_t* __restrict__ sup_o,
+                              int32_t* __restrict__ ost, int32_t* __restrict__ ntask) {
+    const int64_t cur = cr[m];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cur || q <= m; q += stride) {
+        if (q <= m) {
+            const int32_t s = pos[cr[q]];
+            ost[q] = s;
+            if (q < m) ntask[q] = (pos[cr[q + 1]] - s + kTriTask - 1) / kTriTask;
+        }
+        if (q < cur) {
+            const int32_t d = pos[q];
+            if (pos[q + 1] != d) {
+                const int32_t j = cc[q];
+                ocol[d] = j;
+                orank[d] = rank[j];
+                sup_o[d] = 0;
+            }
+        }
+    }
+}
+
+// Row of every task (tasks of row u: tstart[u] .. tstart[u+1]-1).
+__global__ void k_tri_tasklist(const int32_t* __restrict__ tstart, int64_t m, int32_t* __restrict__ task_row) {
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < m; u += (int64_t)gridDim.x * blockDim.x)
+        for (int32_t t = tstart[u]; t < tstart[u + 1]; ++t) task_row[t] = (int32_t)u;
+}
+
+// One warp per task: up to kTriTask consecutive entries (u, v) of O_u. The
+// warp marks O_u's members of the rank window [win0, win0 + kTriWin) in its
+// bitmap (an O_u longer than kTriCntMax uses 32 bucket splitters in
+// registers and a short binary search instead). For each entry v in turn,
+// the lanes take 32 entries w of O_v at a time: a member is the triangle
+// (u, v, w). Its (u, v) count is the entry's ballot total (one atomic per
+// entry), (u, w) a byte counter per member in shared memory (added to the
+// oriented counts when the task ends; a task adds at most kTriTask to one
+// member), (v, w) a global atomic.
+__global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __restrict__ ost,
+                                                             const int32_t* __restrict__ ocol,
+                                                             const int32_t* __restrict__ orank,
+                                                             const int32_t* __restrict__ tstart,
+                                                             const int32_t* __restrict__ task_row, int64_t m,
+                                                             int32_t win0, int32_t* __restrict__ sup_o,
+                                                             unsigned long long* __restrict__ ctr) {
+    __shared__ uint32_t bits_s[kTriThreads / 32][kTriWinWords];
+    __shared__ uint16_t wbase_s[kTriThreads / 32][kTriWinWords];
+    __shared__ uint32_t cnt_s[kTriThreads / 32][kTriCntWords];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    uint32_t* bits = bits_s[threadIdx.x >> 5];
+    uint16_t* wbase = wbase_s[threadIdx.x >> 5];
+    uint32_t* cnt = cnt_s[threadIdx.x >> 5];
+    for (int s = lane; s < kTriWinWords; s += 32) bits[s] = 0;
+    for (int s = lane; s < kTriCntWords; s += 32) cnt[s] = 0;
+    __syncwarp();
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t ntask = tstart[m];
+    unsigned long long wedges = 0, tris = 0;
+    for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ntask; c += warps) {
+        const int u = task_row[c];
+        const int32_t ub = ost[u], un = ost[u + 1] - ub;
+        const int32_t p0 = ub + (int32_t)(c - tstart[u]) * kTriTask;
+        const int ne = min(kTriTask, ub + un - p0);
+        const int32_t* Ou = ocol + ub;
+        const bool counted = un <= kTriCntMax;
+        int32_t key = 0;
+        int n_in = 0;
+        if (counted) {
+            for (int t = lane; t < un; t += 32) {
+                const int32_t b = __ldg(orank + ub + t) - win0;
+                if (b >= 0) atomicOr(bits + (b >> 5), 1u << (b & 31));
+            }
+            __syncwarp();
+            // member index of the first member of every bitmap word
+            int run = 0;
+#pragma unroll 4
+            for (int k = 0; k < kTriWinWords / 32; ++k) {
+                const int c1 = __popc(bits[k * 32 + lane]);
+                const int incl = warp_incl_scan(c1);
+                wbase[k * 32 + lane] = (uint16_t)(run + incl - c1);
+                run += __shfl_sync(FULL, incl, 31);
+            }
+            n_in = run;
+            __syncwarp();
+        } else {
+            key = __ldg(Ou + (int)(((int64_t)(lane + 1) * un) >> 5) - 1);
+        }
+        int32_t vs = 0, vn = 0;
+        if (lane < ne) {
+            const int32_t v = __ldg(ocol + p0 + lane);
+            vs = __ldg(ost + v);
+            vn = __ldg(ost + v + 1) - vs;
+        }
+        for (int e = 0; e < ne; ++e) {
+            const int32_t evs = __shfl_sync(FULL, vs, e);
+            const int32_t evn = __shfl_sync(FULL, vn, e);
+            int32_t found = 0;
+            for (int32_t base = 0; base < evn; base += 32) {
+                const int32_t x = base + lane;
+                const bool valid = x < evn;
+                const int32_t wp = evs + x;
+                bool hit = false;
+                if (counted) {
+                    const int32_t b = valid ? __ldg(orank + wp) - win0 : -1;
+                    if (b >= 0) {
+                        const uint32_t wd = bits[b >> 5];
+                        if ((wd >> (b & 31)) & 1u) {
+                            hit = true;
+                            const int idx = wbase[b >> 5] + __popc(wd & ((1u << (b & 31)) - 1u));
+                            atomicAdd(cnt + (idx >> 2), 1u << ((idx & 3) * 8));  // (u, w)
+                        }
+                    } else if (valid) {
+                        // below the window: binary search of O_u by column
+                        const int32_t w = __ldg(ocol + wp);
+                        const int t = lower_bound_i32(Ou, un, w);
+                        if (t < un && __ldg(Ou + t) == w) {
+                            hit = true;
+                            atomicAdd(sup_o + ub + t, 1);  // (u, w)
+                        }
+                    }
+                } else {
+                    const int32_t w = valid ? __ldg(ocol + wp) : INT32_MAX;
+                    const int bb = warp_lower_bound(key, w);
+                    if (valid && bb < 32) {
+                        const int lo_b = (int)(((int64_t)bb * un) >> 5);
+                        const int hi_b = (int)(((int64_t)(bb + 1) * un) >> 5);
+                        const int t = lo_b + lower_bound_i32(Ou + lo_b, hi_b - lo_b, w);
+                        if (t < hi_b && __ldg(Ou + t) == w) {
+                            hit = true;
+                            atomicAdd(sup_o + ub + t, 1);  // (u, w)
+                        }
+                    }
+                }
+                if (hit) atomicAdd(sup_o + wp, 1);  // (v, w)
+                found += __popc(__ballot_sync(FULL, hit));
+            }
+            if (lane == 0) {
+                wedges += (unsigned long long)evn;
+                tris += (unsigned long long)found;
+                if (found) atomicAdd(sup_o + p0 + e, found);  // (u, v)
+            }
+        }
+        if (counted) {
+            __syncwarp();
+            for (int t = lane; t < un; t += 32) {
+                const int32_t b = __ldg(orank + ub + t) - win0;
+                if (b >= 0) {
+                    const uint32_t wd = bits[b >> 5];
+                    const int idx = wbase[b >> 5] + __popc(wd & ((1u << (b & 31)) - 1u));
+                    const uint32_t n = (cnt[idx >> 2] >> ((idx & 3) * 8)) & 0xffu;
+                    if (n) atomicAdd(sup_o + ub + t, (int32_t)n);
+                }
+            }
+            __syncwarp();
+            for (int s = lane; s < kTriWinWords; s += 32) bits[s] = 0;
+            for (int s = lane; s < ((n_in + 3) >> 2); s += 32) cnt[s] = 0;
+            __syncwarp();
+        }
+    }
+    if (lane == 0) {
+        if (wedges) atomicAdd(&ctr[GA_CTR_WEDGES], wedges);
+        if (tris) atomicAdd(&ctr[GA_CTR_TRIANGLES], tris);
+    }
+}
+
+// Support of every entry of C: an oriented entry's count plus the diagonal
+// terms goes to it and to its mirror; a diagonal entry gets its row length.
+__global__ void k_tri_writeback(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
+                                const int32_t* __restrict__ row_of, const int32_t* __restrict__ mir,
+                                const int32_t* __restrict__ pos, const int32_t* __restrict__ sup_o,
+                                const int32_t* __restrict__ diag, int64_t m, int32_t* __restrict__ sup) {
+    const int64_t cur = cr[m];
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cur; q += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t i = row_of[q], j = cc[q];
+        if (i == j) {
+            sup[q] = cr[i + 1] - cr[i];
+            continue;
+        }
+        const int32_t d = pos[q];
+        if (pos[q + 1] != d) {
+            const int32_t s = sup_o[d] + diag[i] + diag[j];
+            sup[q] = s;
+            sup[mir[q]] = s;
+        }
+    }
+}
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+namespace {
+struct TriScratch {
+    int32_t *ocol, *orank, *sup_o, *task_row, *ost, *tstart, *diag, *rank;
+    void* scan_scr;
+};
+
+size_t task_cap(int64_t m, int64_t cap) { return (size_t)(cap / kTriTask + m + 1); }
+
+// Carves the buffers out of `scratch` (nullptr: only sizes them); returns
+// the bytes used.
+size_t carve(void* scratch, int64_t m, int64_t cap, TriScratch* t) {
+    const size_t c = (size_t)(cap > 0 ? cap : 1), r = (size_t)m + 2;
+    unsigned char* base = static_cast<unsigned char*>(scratch);
+    size_t off = 0;
+    auto take = [&](size_t count) {
+        int32_t* p = base ? reinterpret_cast<int32_t*>(base + off) : nullptr;
+        off += align256(sizeof(int32_t) * count);
+        return p;
+    };
+    TriScratch s;
+    s.ocol = take(c);
+    s.orank = take(c);
+    s.sup_o = take(c);
+    s.task_row = take(task_cap(m, cap));
+    s.ost = take(r);
+    s.tstart = take(r);
+    s.diag = take(r);
+    s.rank = take(r);
+    s.scan_scr = base ? base + off : nullptr;
+    off += align256(scan_scratch_bytes((cap > m ? cap : m) + 2));
+    if (t) *t = s;
+    return off;
+}
+}  // namespace
+
+size_t tri_scratch_bytes(int64_t m, int64_t cap) { return carve(nullptr, m, cap, nullptr); }
+
+void tri_prepare(ga_ctx ctx, ga_csr C, void* scratch, int64_t cap) {
+    const int64_t m = C->m;
+    if (m == 0) return;
+    TriScratch t;
+    carve(scratch, m, cap, &t);
+    // ranks by degree: histogram of the degrees (0..m), its scan, then each
+    // vertex takes the next place of its degree's bucket
+    int32_t* hist = t.tstart;
+    GA_CUDA(cudaMemsetAsync(hist, 0, sizeof(int32_t) * (size_t)(m + 2), ctx->stream));
+    const int grid = grid_for(m, 256, ctx->num_sms * 8);
+    k_tri_deg_count<<<grid, 256, 0, ctx->stream>>>(C->rst, m, hist);
+    post_launch("tri_deg_count");
+    scan_exclusive_i32_scratch(ctx, hist, hist, m + 1, t.scan_scr);
+    k_tri_rank<<<grid, 256, 0, ctx->stream>>>(C->rst, m, hist, t.rank);
+    post_launch("tri_rank");
+}
+
+void tri_support_launch(ga_ctx ctx, ga_csr C, const int32_t* row_of, const int32_t* mir, int32_t* pos,
+                        int32_t* sup, void* scratch, int64_t cap, bool upper_counts) {
+    const int64_t m = C->m;
+    if (m == 0) return;
+    TriScratch t;
+    carve(scratch, m, cap, &t);
+    const int grid_ent = grid_for(cap, 256, ctx->num_sms * 16);
+    const int grid_copy = grid_for(m + cap, 256, ctx->num_sms * 8);
+    const int grid_rows = grid_for(m, 256, ctx->num_sms * 8);
+    {
+        ProfScope ps(ctx, "tri_orient");
+        GA_CUDA(cudaMemsetAsync(t.diag, 0, sizeof(int32_t) * (size_t)m, ctx->stream));
+        k_tri_orient<<<grid_ent, 256, 0, ctx->stream>>>(C->rst, C->col, row_of, t.rank, m, cap, pos, t.diag,
+                                                        ctx->d_counters, upper_counts);
+        post_launch("tri_orient");
+        scan_exclusive_i32_scratch(ctx, pos, pos, cap, t.scan_scr);
+        k_tri_scatter<<<grid_copy, 256, 0, ctx->stream>>>(C->rst, C->col, pos, t.rank, m, t.ocol, t.orank, t.sup_o,
+                                                          t.ost, t.tstart);
+        post_launch("tri_scatter");
+        scan_exclusive_i32_scratch(ctx, t.tstart, t.tstart, m, t.scan_scr);
+        k_tri_tasklist<<<grid_rows, 256, 0, ctx->stream>>>(t.tstart, m, t.task_row);
+        post_launch("tri_tasklist");
+    }
+    // persistent grid: as many blocks as are resident at once
+    static const int per_sm = [] {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_tri_support, kTriThreads, 0) != cudaSuccess || b < 1)
+            b = 1;
+        return b;
+    }();
+    const int32_t win0 = (int32_t)(m > kTriWin ? m - kTriWin : 0);
+    {
+        ProfScope ps(ctx, "tri_support");
+        k_tri_support<<<ctx->num_sms * per_sm, kTriThreads, 0, ctx->stream>>>(
+            t.ost, t.ocol, t.orank, t.tstart, t.task_row, m, win0, t.sup_o, ctx->d_counters);
+        post_launch("tri_support");
+    }
+    ProfScope ps(ctx, "tri_writeback");
+    k_tri_writeback<<<grid_ent, 256, 0, ctx->stream>>>(C->rst, C->col, row_of, mir, pos, t.sup_o, t.diag, m, sup);
+    post_launch("tri_writeback");
+}
+
+bool tri_applies(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M) {
+    const bool same = (A == B || (A->rst == B->rst && A->col == B->col && A->val == B->val)) &&
+                      (A == M || (A->rst == M->rst && A->col == M->col));
+    return same && A->dtype == GA_INT32 && csr_is_symmetric(ctx, A) && csr_unit_values(ctx, A);
+}
+
+// C<A> = A·A by triangle listing into values aligned with A's pattern.
+void tri_masked_into(ga_ctx ctx, ga_csr A, int32_t* sup) {
+    const int64_t m = A->m, cap = A->nnz;
+    if (m == 0 || cap == 0) return;
+    DBuf<int32_t> row_of(ctx, (size_t)cap), mir(ctx, (size_t)cap), pos(ctx, (size_t)cap + 1);
+    DBuf<unsigned char> scr(ctx, tri_scratch_bytes(m, cap));
+    expand_rows(ctx, A, row_of.p);
+    mirror_index(ctx, A, row_of.p, mir.p);
+    tri_prepare(ctx, A, scr.p, cap);
+    tri_support_launch(ctx, A, row_of.p, mir.p, pos.p, sup, scr.p, cap, false);
+}
+
+}  // namespace ga

@@ -60,9 +60,14 @@ typedef enum {
                      sorted-list intersection (B^T built on the fly unless B is
                      symmetric); TC's dot kernel; k-truss support (symmetric A) */
     GA_AUTO = 5,  /* the autotuner's choice of variant and schedule (ga_autotune) */
-    GA_HYBRID = 6 /* per output row, the cheaper of MSA (Gustavson work: the row's
+    GA_HYBRID = 6, /* per output row, the cheaper of MSA (Gustavson work: the row's
                      products) and the inner-product form (work: sum over its mask
                      entries of min(|A_i|, |B^T_j|)), decided while binning */
+    GA_TRI = 7     /* triangle listing, for C<A> = A*A with A one symmetric int32
+                     matrix of unit values (the k-truss support): vertices ranked
+                     by (degree, index), each triangle found once as a wedge of
+                     increasing rank and counted on its three edges; any other
+                     operands (and k-truss from non-unit values) run GA_HYBRID */
 } ga_algo;
 
 /* status codes */
@@ -144,11 +149,13 @@ GA_API int ga_ctx_mem_stats(ga_ctx ctx, int64_t* in_use, int64_t* peak, int rese
  * (fewer than P when a k-truss support product only evaluates the upper
  * triangle of a symmetric matrix and mirrors it), and the list entries the
  * inner-product intersections walked (DOT, and the hybrid form's
- * inner-product rows). They feed the GFLOP/s (2P)
+ * inner-product rows), and for GA_TRI the wedges it looked up and the
+ * triangles it found. They feed the GFLOP/s (2P)
  * and byte models. out has GA_CTR_COUNT entries; reset != 0 zeroes them
  * after reading. Synchronises the stream. */
 enum { GA_CTR_PRODUCTS = 0, GA_CTR_MASK_ENTRIES = 1, GA_CTR_LAUNCHES = 2, GA_CTR_A_ENTRIES = 3,
-       GA_CTR_ROWS = 4, GA_CTR_EXECUTED = 5, GA_CTR_EXECUTED_DOT = 6, GA_CTR_COUNT = 7 };
+       GA_CTR_ROWS = 4, GA_CTR_EXECUTED = 5, GA_CTR_EXECUTED_DOT = 6, GA_CTR_WEDGES = 7,
+       GA_CTR_TRIANGLES = 8, GA_CTR_COUNT = 9 };
 GA_API int ga_ctx_work_counters(ga_ctx ctx, int64_t* out, int reset);
 
 /* Kernel launches issued by this library in this process so far (counted on

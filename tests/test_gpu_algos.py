@@ -51,7 +51,7 @@ def test_tc_other_forms(ctx):
     assert int(ref.sum()) == 3 * total
 
 
-@pytest.mark.parametrize("algo", ["msa", "mca", "heap", "dot", "hybrid"])
+@pytest.mark.parametrize("algo", ["msa", "mca", "heap", "dot", "hybrid", "tri"])
 @pytest.mark.parametrize("device_loops", [1, 0])
 def test_ktruss(ctx, algo, device_loops):
     ctx.set_option(ga.OPT_DEVICE_LOOPS, device_loops)
@@ -152,3 +152,92 @@ def test_async_download_overlaps_and_orders_free(ctx):
     finally:
         ga.host_unregister(rst)
         ga.host_unregister(col)
+
+
+def _with_loops(G, rows):
+    """G plus diagonal entries (i, i) for the given rows (values 1)."""
+    D = np.zeros((G.m, G.m), bool)
+    for i in range(G.m):
+        D[i, G.col[G.rst[i]:G.rst[i + 1]]] = True
+    D[rows, rows] = True
+    from graphs import dense_to_csr
+    return dense_to_csr(D)
+
+
+def _tri_graphs():
+    rng = np.random.default_rng(99)
+    yield from GRAPHS
+    # oriented lists longer than 32 (bucket search) and hubs next to leaves
+    yield "dense300", random_graph(300, 0.5, rng)
+    star = random_graph(400, 0.02, rng)
+    D = np.zeros((400, 400), bool)
+    for i in range(400):
+        D[i, star.col[star.rst[i]:star.rst[i + 1]]] = True
+    D[0, 1:] = D[1:, 0] = True
+    D[1, 2:200] = D[2:200, 1] = True
+    from graphs import dense_to_csr
+    yield "hubs400", dense_to_csr(D)
+    yield "loops", _with_loops(random_graph(80, 0.2, rng), rng.choice(80, 25, replace=False))
+
+
+TRI_GRAPHS = list(_tri_graphs())
+
+
+@pytest.mark.parametrize("name,G", TRI_GRAPHS, ids=[g[0] for g in TRI_GRAPHS])
+def test_tri_support_product(ctx, name, G):
+    """C<A> = A*A by triangle listing equals the Gustavson product bit for bit
+    (diagonal entries included), and the wedge / triangle counters agree with
+    a count of the triangles."""
+    ref = oracle.mxm_masked(G, G, G)
+    Gd = to_device(ctx, G)
+    ctx.work_counters(reset=True)
+    C = ga.mxm_masked("tri", Gd, Gd, Gd)
+    wt = ctx.work_counters(reset=True)
+    _, c, v = C.download()
+    assert np.array_equal(c, G.col) and np.array_equal(v, np.asarray(ref, np.int32))
+    # the same Gustavson work figures as the MSA form reports
+    ga.mxm_masked("msa", Gd, Gd, Gd)
+    wm = ctx.work_counters(reset=True)
+    assert wt["products"] == wm["products"] and wt["mask_entries"] == wm["mask_entries"]
+    loops = any(i in G.col[G.rst[i]:G.rst[i + 1]] for i in range(G.m))
+    if not loops:
+        assert wt["triangles"] == oracle.tc_sandia(G)[0]
+
+
+@pytest.mark.parametrize("device_loops", [1, 0])
+def test_tri_ktruss_with_loops_and_hubs(ctx, device_loops):
+    ctx.set_option(ga.OPT_DEVICE_LOOPS, device_loops)
+    try:
+        for name, G in TRI_GRAPHS[-3:]:
+            Gd = to_device(ctx, G)
+            for k in (3, 4, 6, 9):
+                R, it = oracle.ktruss(G, k)
+                C, git = ga.ktruss("tri", Gd, k)
+                r, c, v = C.download()
+                assert git == it, (name, k)
+                assert np.array_equal(r, R.rst) and np.array_equal(c, R.col) and np.array_equal(v, R.val), (name, k)
+    finally:
+        ctx.set_option(ga.OPT_DEVICE_LOOPS, 1)
+
+
+def test_tri_falls_back_for_other_operands(ctx):
+    """Operands GA_TRI does not cover (different matrices, non-unit values,
+    a non-symmetric matrix) get the hybrid form's results."""
+    rng = np.random.default_rng(5)
+    from graphs import random_csr
+    A = random_csr(50, 60, 0.2, rng)
+    B = random_csr(60, 40, 0.2, rng)
+    M = random_csr(50, 40, 0.3, rng)
+    ref = oracle.mxm_masked(A, B, M)
+    _, _, v = ga.mxm_masked("tri", to_device(ctx, A), to_device(ctx, B), to_device(ctx, M)).download()
+    assert np.array_equal(v, np.asarray(ref, np.int32))
+    G = random_graph(70, 0.2, rng)
+    W = oracle.Csr(G.m, G.n, G.rst, G.col, np.full(G.nnz, 2, np.int32))  # symmetric, values 2
+    Wd = to_device(ctx, W)
+    _, _, v = ga.mxm_masked("tri", Wd, Wd, Wd).download()
+    assert np.array_equal(v, np.asarray(oracle.mxm_masked(W, W, W), np.int32))
+    for k in (3, 5):
+        R, it = oracle.ktruss(W, k)
+        C, git = ga.ktruss("tri", Wd, k)
+        r, c, vv = C.download()
+        assert git == it and np.array_equal(c, R.col) and np.array_equal(vv, R.val)

@@ -94,7 +94,7 @@ def _solo_ktruss(ctx, algo, blocks, k):
     return out
 
 
-@pytest.mark.parametrize("algo", ["msa", "mca", "heap", "dot", "hybrid"])
+@pytest.mark.parametrize("algo", ["msa", "mca", "heap", "dot", "hybrid", "tri"])
 @pytest.mark.parametrize("k", [4, 6])
 def test_batch_ktruss_matches_single(ctx, algo, k):
     host, dev = _mixed_parts(ctx)
