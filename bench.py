@@ -7,8 +7,9 @@ a/b/c/d = 0.57/0.19/0.19/0.05, symmetrised, loops and duplicates removed,
 int32 CSR, 262,144 vertices, 7.6M stored entries). Each k runs the
 reference's k_truss (src/main.cpp:90-146: Tmp<C> = C*C masked by C, prune
 below k-2, repeat until nnz is unchanged) through the C ABI, the support
-product with the hybrid masked SpGEMM by default (per output row the cheaper
-of MSA and the inner-product form; --algo msa|mca|heap|dot runs one form);
+product by triangle listing by default (GA_TRI: each triangle found once
+over a degree orientation and counted on its three edges; --algo
+msa|mca|heap|dot|hybrid runs one of the other forms);
 k starts from the (k-1)-truss, which contains it (same edge sets as starting
 from A). value = 2 * (Gustavson products of every support product, the work
 of the reference's C<M> = A*B whatever form computes it) / time, inputs
@@ -57,7 +58,8 @@ def parse_args():
     ap.add_argument("--edge-factor", type=int, default=16)
     ap.add_argument("--seed", type=int, default=42)
     ap.add_argument("--algo", default=None, choices=["msa", "mca", "heap", "dot", "hybrid", "tri", "auto"],
-                    help="k-truss variant (default: msa; auto for the batch workload)")
+                    help="k-truss variant (default: tri for the sweep, msa for --case, auto for the batch "
+                         "workload)")
     ap.add_argument("--kmin", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -89,14 +91,14 @@ def parse_args():
     ap.add_argument("--graphs", type=int, default=4096, help="batch workload: number of graphs")
     ap.add_argument("--plain-graphs", type=int, default=0,
                     help="batch workload: graphs timed in the per-graph arm (0 = all)")
-    ap.add_argument("--tc-algo", default=None, choices=["msa", "mca", "heap", "dot", "auto"],
+    ap.add_argument("--tc-algo", default=None, choices=["msa", "mca", "heap", "dot", "tri", "auto"],
                     help="TC variant (default: msa; auto for the batch workload)")
     ap.add_argument("--host-loops", action="store_true",
                     help="run the k-truss loop from the host (kernels launched one by one, e.g. for ncu)")
     args = ap.parse_args()
     auto = args.workload == "batch" or args.case == "batch"
     if args.algo is None:
-        args.algo = "auto" if auto else ("hybrid" if args.workload == "ktruss-sweep" and not args.case else "msa")
+        args.algo = "auto" if auto else ("tri" if args.workload == "ktruss-sweep" and not args.case else "msa")
     if args.tc_algo is None:
         args.tc_algo = "auto" if auto else "msa"
     return args
@@ -263,7 +265,10 @@ def run_case(args):
         elif args.case == "tc":
             total, _ = ga.tc("dot", A, per_row=False)
             ms = ctx.timer_stop()
-            rec = {"tc_ms": ms, "triangles": total}
+            ctx.timer_start()
+            total_tri, _ = ga.tc("tri", A, per_row=False)
+            ms_tri = ctx.timer_stop()
+            rec = {"tc_ms": ms, "tc_tri_ms": ms_tri, "triangles": total, "triangles_tri": total_tri}
         elif args.case == "ktruss":
             C, it = ga.ktruss(args.algo, A, 4)
             ms = ctx.timer_stop()
@@ -552,7 +557,7 @@ def run_gpu(args, dist: Dist):
     variants = {}
     default = {"warp_max_flops": 32768, "heavy_flops": 1 << 20, "ctas_per_sm": 0, "dot_chunk": 8}
     ga.apply_schedule(ctx, default)  # each variant with the default schedule
-    for algo in ("msa", "mca", "heap", "dot", "hybrid"):
+    for algo in ("msa", "mca", "heap", "dot", "hybrid", "tri"):
         ctx.work_counters(reset=True)
         ctx.flush_l2()
         ctx.timer_start()

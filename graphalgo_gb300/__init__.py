@@ -34,6 +34,7 @@ ALGO_NAMES = {v: k for k, v in ALGOS.items()}
 # options
 OPT_DEVICE_LOOPS, OPT_PROFILE, OPT_FAIL_ALLOC_AFTER, OPT_KNN_TILED = 1, 2, 3, 4
 OPT_MXM_WARP_FLOPS, OPT_MXM_HEAVY_FLOPS, OPT_MXM_CTAS_PER_SM, OPT_DOT_CHUNK, OPT_HYBRID_RATIO = 5, 6, 7, 8, 9
+OPT_TRI_ORDER = 10
 TUNE_KTRUSS, TUNE_PRODUCT, TUNE_TC = 0, 1, 2
 # edge-list / file ingestion flags
 EDGES_MIRROR, EDGES_DROP_LOOPS, EDGES_LOWER_SYMM, EDGES_UNIT = 1, 2, 4, 8
@@ -738,7 +739,7 @@ class Server:
 class TuneResult(ctypes.Structure):
     _fields_ = [("algo", _int), ("warp_max_flops", _i64), ("heavy_flops", _i64), ("ctas_per_sm", _int),
                 ("dot_chunk", _int), ("hybrid_ratio", _i64), ("ms", ctypes.c_double), ("default_ms", ctypes.c_double),
-                ("candidates", _int), ("cached", _int)]
+                ("candidates", _int), ("cached", _int), ("tri_order", _int)]
 
 
 def autotune(kind: int, A: Csr, B: Optional[Csr] = None, M: Optional[Csr] = None, force: bool = False,
@@ -762,3 +763,4 @@ def apply_schedule(ctx: Context, tuned: dict) -> None:
     ctx.set_option(OPT_MXM_CTAS_PER_SM, tuned["ctas_per_sm"])
     ctx.set_option(OPT_DOT_CHUNK, tuned["dot_chunk"])
     ctx.set_option(OPT_HYBRID_RATIO, tuned.get("hybrid_ratio", 16))
+    ctx.set_option(OPT_TRI_ORDER, tuned.get("tri_order", 0))

@@ -211,6 +211,15 @@ static void tc_device(ga_ctx ctx, ga_algo algo, ga_csr A, int64_t* d_total, int6
     unsigned long long* tot = reinterpret_cast<unsigned long long*>(d_total);
     GA_CUDA(cudaMemsetAsync(tot, 0, sizeof(unsigned long long), ctx->stream));
     if (A->m == 0) return;
+    if (algo == GA_TRI) {
+        // triangle listing on a symmetric pattern; other matrices take the
+        // Sandia form with the hybrid product
+        if (csr_is_symmetric(ctx, A)) {
+            tri_count(ctx, A, tot, reinterpret_cast<unsigned long long*>(d_per_row));
+            return;
+        }
+        algo = GA_HYBRID;
+    }
     if (algo == GA_DOT) {
         const int64_t m = A->m;
         DBuf<int32_t> ust(ctx, (size_t)m + 1);

@@ -405,6 +405,10 @@ int ga_ctx_set_option(ga_ctx ctx, int option, int64_t value) {
         if (value < 0 || value > (1 << 20)) break;
         ctx->tune.hybrid_ratio = value;
         return GA_OK;
+    case GA_OPT_TRI_ORDER:
+        if (value != 0 && value != 1) break;
+        ctx->tune.tri_order = (int)value;
+        return GA_OK;
     }
     ctx->last_error = "unknown option";
     return GA_ERR_INVALID_ARG;

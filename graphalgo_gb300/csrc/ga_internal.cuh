@@ -52,6 +52,7 @@ struct MxmTune {
     int dot_chunk = 8;               // inner-product form: mask entries per warp task
     int64_t hybrid_ratio = 16;       // hybrid form: a row goes to the inner product when its
                                      // inner-product work x this is below its Gustavson work
+    int tri_order = 0;               // triangle listing: vertex ranks by degree (0) or index (1)
 };
 
 }  // namespace ga
@@ -243,6 +244,10 @@ void tri_support_launch(ga_ctx ctx, ga_csr C, const int32_t* row_of, const int32
 // stream the first time a handle is checked).
 bool tri_applies(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M);
 void tri_masked_into(ga_ctx ctx, ga_csr A, int32_t* sup);
+// Triangle count of a symmetric pattern (diagonal ignored) into *d_total
+// (added to) and, when given, per row the triangles whose largest vertex
+// index is the row (zeroed first): the row sums of C<L> = L·L.
+void tri_count(ga_ctx ctx, ga_csr A, unsigned long long* d_total, unsigned long long* d_per_row);
 
 // device-side transpose (counting sort; rows of the result sorted)
 ga_csr transpose_csr(ga_ctx ctx, ga_csr A);

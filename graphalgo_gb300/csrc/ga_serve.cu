@@ -209,7 +209,9 @@ static void run_single(Server* s, ga_ctx ctx, SrvReq* r) {
 
 // Batched calls run on unions whose sizes change from call to call: with
 // GA_AUTO they use MSA rather than tune each new union.
-static ga_algo group_algo(int a) { return a == GA_AUTO ? GA_MSA : (ga_algo)a; }
+// Batched calls under GA_AUTO use triangle listing (unions of symmetric 0/1
+// graphs; other matrices fall back inside the call).
+static ga_algo group_algo(int a) { return a == GA_AUTO ? GA_TRI : (ga_algo)a; }
 
 static void run_group(Server* s, ga_ctx ctx, std::vector<SrvReq*>& group) {
     // slots of the union, in first-seen order

@@ -7,7 +7,7 @@
 // (the triangles through edge {i, j}), plus 1 for each of i and j that holds
 // a diagonal entry; C(i, i) = |N(i)| (the row's length, diagonal included).
 // Every triangle is listed once: vertices get ranks 0..m-1 in order of
-// degree (a counting sort, once per call), each undirected edge is kept in
+// degree (a counting sort, once per call; or their indices), each undirected edge is kept in
 // the direction of increasing rank (the oriented list O_u of u holds the
 // neighbours ranked above u, in column order), and a triangle u < v < w (by
 // rank) is found as the wedge u -> v -> w with w in O_u. Its three edges'
@@ -16,11 +16,13 @@
 // entries of every edge. Integer counts: the result is exact whatever the
 // order, and whatever order ties of degree get.
 //
-// Lookups: after ranking by degree almost every wedge ends at a vertex of
-// the top kTriWin ranks (the hubs), so each warp keeps a bitmap of O_u's
-// members in that rank window, with per-word popcount prefixes giving a
-// member's index in O(1); the rare w below the window is binary-searched in
-// O_u.
+// Lookups: each warp keeps a bitmap of O_u's members in a window of kTriWin
+// ranks ending at O_u's highest rank, with per-word popcount prefixes giving
+// a member's index in O(1); a w ranked below the window is binary-searched
+// in O_u. Ranked by degree, almost every wedge of a power-law graph ends at
+// a vertex of the top ranks (the hubs), inside the window. The ranks may
+// also be the vertex indices (GA_OPT_TRI_ORDER): then the lists of a union
+// of small graphs span fewer ranks than the window and no search is needed.
 //
 // Per evaluation (all launches read the current entry count on the device, so
 // a captured loop whose matrix shrinks can replay them):
@@ -56,15 +58,21 @@ __global__ void k_tri_rank(const int32_t* __restrict__ cr, int64_t m, int32_t* _
         rank[v] = atomicAdd(next + (cr[v + 1] - cr[v]), 1);
 }
 
+__global__ void k_tri_iota(int64_t m, int32_t* __restrict__ rank) {
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < m; v += (int64_t)gridDim.x * blockDim.x)
+        rank[v] = (int32_t)v;
+}
+
 // Rank flag of every entry (column ranked above the row: kept in O_row),
 // diagonal flags, and the Gustavson work counters the other forms report:
-// with `upper`, as for a k-truss support that evaluates the upper triangle
-// (products of the rows whose upper part is not empty, upper entries), else
-// as for the whole mask.
+// counts 1, as for a k-truss support that evaluates the upper triangle
+// (products of the rows whose upper part is not empty, upper entries); 2, as
+// for the whole mask; 0, none (triangle counting).
 __global__ void k_tri_orient(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
                              const int32_t* __restrict__ row_of, const int32_t* __restrict__ rank, int64_t m,
                              int64_t cap, int32_t* __restrict__ flag, int32_t* __restrict__ diag,
-                             unsigned long long* __restrict__ ctr, bool upper) {
+                             unsigned long long* __restrict__ ctr, int counts) {
+    const bool upper = counts == 1;
     const int64_t cur = cr[m];
     unsigned long long prod = 0, mask = 0;
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cap; q += (int64_t)gridDim.x * blockDim.x) {
@@ -73,8 +81,8 @@ __global__ void k_tri_orient(const int32_t* __restrict__ cr, const int32_t* __re
             const int32_t i = row_of[q], j = cc[q];
             if (i == j) diag[i] = 1;
             else f = rank[j] > rank[i];
-            if (!upper || j >= i) ++mask;
-            if (!upper || cc[cr[i + 1] - 1] >= i) prod += (unsigned long long)(cr[j + 1] - cr[j]);
+            if (counts && (!upper || j >= i)) ++mask;
+            if (counts && (!upper || cc[cr[i + 1] - 1] >= i)) prod += (unsigned long long)(cr[j + 1] - cr[j]);
         }
         flag[q] = f;
     }
@@ -133,13 +141,20 @@ __global__ void k_tri_tasklist(const int32_t* __restrict__ tstart, int64_t m, in
 // entry), (u, w) a byte counter per member in shared memory (added to the
 // oriented counts when the task ends; a task adds at most kTriTask to one
 // member), (v, w) a global atomic.
+//
+// COUNT: triangle counting instead: no edge counts; each triangle adds 1 to
+// the total and, with per_row, to the row of its largest vertex index (the
+// row sums of C<L> = L·L over the strictly lower triangle L).
+template <bool COUNT>
 __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __restrict__ ost,
                                                              const int32_t* __restrict__ ocol,
                                                              const int32_t* __restrict__ orank,
                                                              const int32_t* __restrict__ tstart,
                                                              const int32_t* __restrict__ task_row, int64_t m,
-                                                             int32_t win0, int32_t* __restrict__ sup_o,
-                                                             unsigned long long* __restrict__ ctr) {
+                                                             int32_t* __restrict__ sup_o,
+                                                             unsigned long long* __restrict__ ctr,
+                                                             unsigned long long* __restrict__ total,
+                                                             unsigned long long* __restrict__ per_row) {
     __shared__ uint32_t bits_s[kTriThreads / 32][kTriWinWords];
     __shared__ uint16_t wbase_s[kTriThreads / 32][kTriWinWords];
     __shared__ uint32_t cnt_s[kTriThreads / 32][kTriCntWords];
@@ -163,35 +178,53 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __re
         const bool counted = un <= kTriCntMax;
         int32_t key = 0;
         int n_in = 0;
+        // window: the kTriWin ranks up to O_u's highest (all of O_u when its
+        // ranks span fewer); members below it are binary-searched
+        int32_t win0 = 0;
+        int nwords = 0;  // bitmap words the members span
+        bool below = false;
         if (counted) {
+            int32_t lo = INT32_MAX, hi = -1;
+            for (int t = lane; t < un; t += 32) {
+                const int32_t r = __ldg(orank + ub + t);
+                lo = min(lo, r);
+                hi = max(hi, r);
+            }
+            lo = __reduce_min_sync(FULL, lo);
+            hi = __reduce_max_sync(FULL, hi);
+            win0 = max(lo, hi - kTriWin + 1);
+            below = lo < win0;
+            nwords = ((hi - win0) >> 5) + 1;
             for (int t = lane; t < un; t += 32) {
                 const int32_t b = __ldg(orank + ub + t) - win0;
                 if (b >= 0) atomicOr(bits + (b >> 5), 1u << (b & 31));
             }
             __syncwarp();
+        }
+        if (counted && !COUNT) {
             // member index of the first member of every bitmap word
             int run = 0;
-#pragma unroll 4
-            for (int k = 0; k < kTriWinWords / 32; ++k) {
-                const int c1 = __popc(bits[k * 32 + lane]);
+            for (int k = 0; k < nwords; k += 32) {
+                const int c1 = __popc(bits[k + lane]);
                 const int incl = warp_incl_scan(c1);
-                wbase[k * 32 + lane] = (uint16_t)(run + incl - c1);
+                wbase[k + lane] = (uint16_t)(run + incl - c1);
                 run += __shfl_sync(FULL, incl, 31);
             }
             n_in = run;
             __syncwarp();
-        } else {
+        } else if (!counted) {
             key = __ldg(Ou + (int)(((int64_t)(lane + 1) * un) >> 5) - 1);
         }
-        int32_t vs = 0, vn = 0;
+        int32_t v = 0, vs = 0, vn = 0;
         if (lane < ne) {
-            const int32_t v = __ldg(ocol + p0 + lane);
+            v = __ldg(ocol + p0 + lane);
             vs = __ldg(ost + v);
             vn = __ldg(ost + v + 1) - vs;
         }
         for (int e = 0; e < ne; ++e) {
             const int32_t evs = __shfl_sync(FULL, vs, e);
             const int32_t evn = __shfl_sync(FULL, vn, e);
+            const int32_t ev = __shfl_sync(FULL, v, e);
             int32_t found = 0;
             for (int32_t base = 0; base < evn; base += 32) {
                 const int32_t x = base + lane;
@@ -199,21 +232,24 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __re
                 const int32_t wp = evs + x;
                 bool hit = false;
                 if (counted) {
-                    const int32_t b = valid ? __ldg(orank + wp) - win0 : -1;
-                    if (b >= 0) {
+                    // ranks above the window are above every member
+                    const int32_t b = valid ? __ldg(orank + wp) - win0 : kTriWin;
+                    if (b >= 0 && b < kTriWin) {
                         const uint32_t wd = bits[b >> 5];
                         if ((wd >> (b & 31)) & 1u) {
                             hit = true;
-                            const int idx = wbase[b >> 5] + __popc(wd & ((1u << (b & 31)) - 1u));
-                            atomicAdd(cnt + (idx >> 2), 1u << ((idx & 3) * 8));  // (u, w)
+                            if (!COUNT) {
+                                const int idx = wbase[b >> 5] + __popc(wd & ((1u << (b & 31)) - 1u));
+                                atomicAdd(cnt + (idx >> 2), 1u << ((idx & 3) * 8));  // (u, w)
+                            }
                         }
-                    } else if (valid) {
+                    } else if (b < 0 && below) {
                         // below the window: binary search of O_u by column
                         const int32_t w = __ldg(ocol + wp);
                         const int t = lower_bound_i32(Ou, un, w);
                         if (t < un && __ldg(Ou + t) == w) {
                             hit = true;
-                            atomicAdd(sup_o + ub + t, 1);  // (u, w)
+                            if (!COUNT) atomicAdd(sup_o + ub + t, 1);  // (u, w)
                         }
                     }
                 } else {
@@ -225,20 +261,28 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __re
                         const int t = lo_b + lower_bound_i32(Ou + lo_b, hi_b - lo_b, w);
                         if (t < hi_b && __ldg(Ou + t) == w) {
                             hit = true;
-                            atomicAdd(sup_o + ub + t, 1);  // (u, w)
+                            if (!COUNT) atomicAdd(sup_o + ub + t, 1);  // (u, w)
                         }
                     }
                 }
-                if (hit) atomicAdd(sup_o + wp, 1);  // (v, w)
+                if (!COUNT && hit) atomicAdd(sup_o + wp, 1);  // (v, w)
+                if (COUNT && hit && per_row) {
+                    const int32_t w = __ldg(ocol + wp);
+                    atomicAdd(per_row + max(max(u, ev), w), 1ull);
+                }
                 found += __popc(__ballot_sync(FULL, hit));
             }
             if (lane == 0) {
                 wedges += (unsigned long long)evn;
                 tris += (unsigned long long)found;
-                if (found) atomicAdd(sup_o + p0 + e, found);  // (u, v)
+                if (!COUNT && found) atomicAdd(sup_o + p0 + e, found);  // (u, v)
             }
         }
-        if (counted) {
+        if (counted && COUNT) {
+            __syncwarp();
+            for (int s = lane; s < nwords; s += 32) bits[s] = 0;
+            __syncwarp();
+        } else if (counted) {
             __syncwarp();
             for (int t = lane; t < un; t += 32) {
                 const int32_t b = __ldg(orank + ub + t) - win0;
@@ -250,7 +294,7 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __re
                 }
             }
             __syncwarp();
-            for (int s = lane; s < kTriWinWords; s += 32) bits[s] = 0;
+            for (int s = lane; s < nwords; s += 32) bits[s] = 0;
             for (int s = lane; s < ((n_in + 3) >> 2); s += 32) cnt[s] = 0;
             __syncwarp();
         }
@@ -258,6 +302,7 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __re
     if (lane == 0) {
         if (wedges) atomicAdd(&ctr[GA_CTR_WEDGES], wedges);
         if (tris) atomicAdd(&ctr[GA_CTR_TRIANGLES], tris);
+        if (COUNT && tris) atomicAdd(total, tris);
     }
 }
 
@@ -327,16 +372,55 @@ void tri_prepare(ga_ctx ctx, ga_csr C, void* scratch, int64_t cap) {
     if (m == 0) return;
     TriScratch t;
     carve(scratch, m, cap, &t);
+    const int grid = grid_for(m, 256, ctx->num_sms * 8);
+    if (ctx->tune.tri_order == 1) {  // index order
+        k_tri_iota<<<grid, 256, 0, ctx->stream>>>(m, t.rank);
+        post_launch("tri_iota");
+        return;
+    }
     // ranks by degree: histogram of the degrees (0..m), its scan, then each
     // vertex takes the next place of its degree's bucket
     int32_t* hist = t.tstart;
     GA_CUDA(cudaMemsetAsync(hist, 0, sizeof(int32_t) * (size_t)(m + 2), ctx->stream));
-    const int grid = grid_for(m, 256, ctx->num_sms * 8);
     k_tri_deg_count<<<grid, 256, 0, ctx->stream>>>(C->rst, m, hist);
     post_launch("tri_deg_count");
     scan_exclusive_i32_scratch(ctx, hist, hist, m + 1, t.scan_scr);
     k_tri_rank<<<grid, 256, 0, ctx->stream>>>(C->rst, m, hist, t.rank);
     post_launch("tri_rank");
+}
+
+// Orientation, oriented lists and the task list of C's current pattern.
+static void tri_lists(ga_ctx ctx, ga_csr C, const int32_t* row_of, int32_t* pos, const TriScratch& t, int64_t cap,
+                      int counts) {
+    const int64_t m = C->m;
+    const int grid_ent = grid_for(cap, 256, ctx->num_sms * 16);
+    const int grid_copy = grid_for(m + cap, 256, ctx->num_sms * 8);
+    const int grid_rows = grid_for(m, 256, ctx->num_sms * 8);
+    ProfScope ps(ctx, "tri_orient");
+    GA_CUDA(cudaMemsetAsync(t.diag, 0, sizeof(int32_t) * (size_t)m, ctx->stream));
+    k_tri_orient<<<grid_ent, 256, 0, ctx->stream>>>(C->rst, C->col, row_of, t.rank, m, cap, pos, t.diag,
+                                                    ctx->d_counters, counts);
+    post_launch("tri_orient");
+    scan_exclusive_i32_scratch(ctx, pos, pos, cap, t.scan_scr);
+    k_tri_scatter<<<grid_copy, 256, 0, ctx->stream>>>(C->rst, C->col, pos, t.rank, m, t.ocol, t.orank, t.sup_o,
+                                                      t.ost, t.tstart);
+    post_launch("tri_scatter");
+    scan_exclusive_i32_scratch(ctx, t.tstart, t.tstart, m, t.scan_scr);
+    k_tri_tasklist<<<grid_rows, 256, 0, ctx->stream>>>(t.tstart, m, t.task_row);
+    post_launch("tri_tasklist");
+}
+
+// Persistent grid: as many blocks as are resident at once.
+template <bool COUNT>
+static int tri_blocks_per_sm() {
+    static const int per_sm = [] {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_tri_support<COUNT>, kTriThreads, 0) != cudaSuccess ||
+            b < 1)
+            b = 1;
+        return b;
+    }();
+    return per_sm;
 }
 
 void tri_support_launch(ga_ctx ctx, ga_csr C, const int32_t* row_of, const int32_t* mir, int32_t* pos,
@@ -345,40 +429,34 @@ void tri_support_launch(ga_ctx ctx, ga_csr C, const int32_t* row_of, const int32
     if (m == 0) return;
     TriScratch t;
     carve(scratch, m, cap, &t);
-    const int grid_ent = grid_for(cap, 256, ctx->num_sms * 16);
-    const int grid_copy = grid_for(m + cap, 256, ctx->num_sms * 8);
-    const int grid_rows = grid_for(m, 256, ctx->num_sms * 8);
-    {
-        ProfScope ps(ctx, "tri_orient");
-        GA_CUDA(cudaMemsetAsync(t.diag, 0, sizeof(int32_t) * (size_t)m, ctx->stream));
-        k_tri_orient<<<grid_ent, 256, 0, ctx->stream>>>(C->rst, C->col, row_of, t.rank, m, cap, pos, t.diag,
-                                                        ctx->d_counters, upper_counts);
-        post_launch("tri_orient");
-        scan_exclusive_i32_scratch(ctx, pos, pos, cap, t.scan_scr);
-        k_tri_scatter<<<grid_copy, 256, 0, ctx->stream>>>(C->rst, C->col, pos, t.rank, m, t.ocol, t.orank, t.sup_o,
-                                                          t.ost, t.tstart);
-        post_launch("tri_scatter");
-        scan_exclusive_i32_scratch(ctx, t.tstart, t.tstart, m, t.scan_scr);
-        k_tri_tasklist<<<grid_rows, 256, 0, ctx->stream>>>(t.tstart, m, t.task_row);
-        post_launch("tri_tasklist");
-    }
-    // persistent grid: as many blocks as are resident at once
-    static const int per_sm = [] {
-        int b = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_tri_support, kTriThreads, 0) != cudaSuccess || b < 1)
-            b = 1;
-        return b;
-    }();
-    const int32_t win0 = (int32_t)(m > kTriWin ? m - kTriWin : 0);
+    tri_lists(ctx, C, row_of, pos, t, cap, upper_counts ? 1 : 2);
     {
         ProfScope ps(ctx, "tri_support");
-        k_tri_support<<<ctx->num_sms * per_sm, kTriThreads, 0, ctx->stream>>>(
-            t.ost, t.ocol, t.orank, t.tstart, t.task_row, m, win0, t.sup_o, ctx->d_counters);
+        k_tri_support<false><<<ctx->num_sms * tri_blocks_per_sm<false>(), kTriThreads, 0, ctx->stream>>>(
+            t.ost, t.ocol, t.orank, t.tstart, t.task_row, m, t.sup_o, ctx->d_counters, nullptr, nullptr);
         post_launch("tri_support");
     }
     ProfScope ps(ctx, "tri_writeback");
-    k_tri_writeback<<<grid_ent, 256, 0, ctx->stream>>>(C->rst, C->col, row_of, mir, pos, t.sup_o, t.diag, m, sup);
+    k_tri_writeback<<<grid_for(cap, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(C->rst, C->col, row_of, mir,
+                                                                                   pos, t.sup_o, t.diag, m, sup);
     post_launch("tri_writeback");
+}
+
+void tri_count(ga_ctx ctx, ga_csr A, unsigned long long* d_total, unsigned long long* d_per_row) {
+    const int64_t m = A->m, cap = A->nnz;
+    if (d_per_row) GA_CUDA(cudaMemsetAsync(d_per_row, 0, sizeof(int64_t) * (size_t)m, ctx->stream));
+    if (m == 0 || cap == 0) return;
+    DBuf<int32_t> row_of(ctx, (size_t)cap), pos(ctx, (size_t)cap + 1);
+    DBuf<unsigned char> scr(ctx, tri_scratch_bytes(m, cap));
+    TriScratch t;
+    carve(scr.p, m, cap, &t);
+    expand_rows(ctx, A, row_of.p);
+    tri_prepare(ctx, A, scr.p, cap);
+    tri_lists(ctx, A, row_of.p, pos.p, t, cap, 0);
+    ProfScope ps(ctx, "tri_count");
+    k_tri_support<true><<<ctx->num_sms * tri_blocks_per_sm<true>(), kTriThreads, 0, ctx->stream>>>(
+        t.ost, t.ocol, t.orank, t.tstart, t.task_row, m, nullptr, ctx->d_counters, d_total, d_per_row);
+    post_launch("tri_count");
 }
 
 bool tri_applies(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M) {

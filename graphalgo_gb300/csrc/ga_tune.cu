@@ -47,8 +47,8 @@ MxmTune tune_of(int64_t warp_max, int ctas, int chunk, int64_t ratio = 16) {
 }
 
 // Candidates, the default MSA schedule first; `only` >= 0 keeps one variant
-// (its schedules only).
-std::vector<Cand> product_candidates(bool dot_ok, int only) {
+// (its schedules only). tri_ok: the operands are one symmetric 0/1 matrix.
+std::vector<Cand> product_candidates(bool dot_ok, int only, bool tri_ok = false) {
     std::vector<Cand> c;
     if (only < 0 || only == GA_MSA) {
         c.push_back({GA_MSA, MxmTune()});
@@ -65,6 +65,12 @@ std::vector<Cand> product_candidates(bool dot_ok, int only) {
         for (int chunk : {4, 8, 16}) c.push_back({GA_DOT, tune_of(32768, 0, chunk)});
     if (dot_ok && (only < 0 || only == GA_HYBRID))
         for (int64_t ratio : {4, 16, 64}) c.push_back({GA_HYBRID, tune_of(32768, 0, 8, ratio)});
+    if (tri_ok && (only < 0 || only == GA_TRI))
+        for (int order : {0, 1}) {
+            MxmTune t;
+            t.tri_order = order;
+            c.push_back({GA_TRI, t});
+        }
     return c;
 }
 
@@ -159,8 +165,20 @@ TuneEntry tune_support(ga_ctx ctx, ga_csr A, int only) {
     }
     ga_csr M = sym ? &Au : A;
     const int32_t* mre = sym ? A->rst + 1 : nullptr;
-    return pick(ctx, product_candidates(sym, only), [&](const Cand& c) {
-        if (c.algo == GA_DOT) mxm_dot_launch(ctx, A, A, A, M, sup.p, unit, mre);
+    // triangle listing: the k-truss loop's buffers (rows, mirrors, positions)
+    const bool tri_ok = sym && unit && A->dtype == GA_INT32 && (only < 0 || only == GA_TRI);
+    const size_t aux = tri_ok ? (size_t)nnz + 1 : 1;
+    DBuf<int32_t> row_of(ctx, aux), mir(ctx, aux), pos(ctx, aux);
+    DBuf<unsigned char> tscr(ctx, tri_ok ? tri_scratch_bytes(m, nnz) : 1);
+    if (tri_ok) {
+        expand_rows(ctx, A, row_of.p);
+        mirror_index(ctx, A, row_of.p, mir.p);
+    }
+    return pick(ctx, product_candidates(sym, only, tri_ok), [&](const Cand& c) {
+        if (c.algo == GA_TRI) {
+            tri_prepare(ctx, A, tscr.p, nnz);  // ranks of the candidate's order (ctx->tune)
+            tri_support_launch(ctx, A, row_of.p, mir.p, pos.p, sup.p, tscr.p, nnz, true);
+        } else if (c.algo == GA_DOT) mxm_dot_launch(ctx, A, A, A, M, sup.p, unit, mre);
         else mxm_masked_launch(ctx, c.algo, A, A, M, sup.p, scr.p, nnz, unit, mre, unit,
                                c.algo == GA_HYBRID ? A : nullptr);
     });
@@ -168,7 +186,7 @@ TuneEntry tune_support(ga_ctx ctx, ga_csr A, int only) {
 
 TuneEntry tune_product(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M, int only) {
     DBuf<unsigned char> cv(ctx, (size_t)(M->nnz + 1) * dtype_size(A->dtype));
-    return pick(ctx, product_candidates(true, only),
+    return pick(ctx, product_candidates(true, only, tri_applies(ctx, A, B, M)),
                 [&](const Cand& c) { mxm_masked_into(ctx, c.algo, A, B, M, cv.p); });
 }
 
@@ -176,6 +194,12 @@ TuneEntry tune_tc(ga_ctx ctx, ga_csr A, int only) {
     DBuf<int64_t> tot(ctx, 1);
     std::vector<Cand> all = {{GA_MSA, MxmTune()}, {GA_DOT, MxmTune()}, {GA_MCA, MxmTune()},
                              {GA_MSA, tune_of(8192, 0, 8)}, {GA_MSA, tune_of(131072, 0, 8)}};
+    if (csr_is_symmetric(ctx, A))
+        for (int order : {0, 1}) {
+            MxmTune t;
+            t.tri_order = order;
+            all.push_back({GA_TRI, t});
+        }
     std::vector<Cand> c;
     for (const Cand& x : all)
         if (only < 0 || x.algo == only) c.push_back(x);
@@ -187,9 +211,11 @@ TuneEntry tune_tc(ga_ctx ctx, ga_csr A, int only) {
 
 TuneEntry lookup_or_tune(ga_ctx ctx, int kind, ga_csr A, ga_csr B, ga_csr M, bool force, bool* cached,
                          int only = -1) {
+    // the candidate set depends on symmetry and, for triangle listing, unit values
     const bool sym = csr_is_symmetric(ctx, A);
+    const int shape = sym ? (csr_unit_values(ctx, A) ? 2 : 1) : 0;
     const TuneKey key{ctx->device, kind, bucket(A->m), bucket(A->n), bucket(A->nnz), bucket(B ? B->nnz : 0),
-                      bucket(M ? M->nnz : 0), sym ? 1 : 0, only};
+                      bucket(M ? M->nnz : 0), shape, only};
     if (!force) {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune_cache.find(key);
@@ -248,7 +274,7 @@ int ga_autotune(ga_ctx ctx, int kind, ga_csr A, ga_csr B, ga_csr M, int force, g
 int ga_autotune_variant(ga_ctx ctx, int kind, int algo, ga_csr A, ga_csr B, ga_csr M, int force,
                         ga_tune_result* out) {
     if (!ctx || !A || !out) return GA_ERR_INVALID_ARG;
-    if (algo != -1 && algo != GA_MSA && algo != GA_MCA && algo != GA_DOT && algo != GA_HYBRID)
+    if (algo != -1 && algo != GA_MSA && algo != GA_MCA && algo != GA_DOT && algo != GA_HYBRID && algo != GA_TRI)
         return GA_ERR_INVALID_ARG;
     if (kind != GA_TUNE_KTRUSS && kind != GA_TUNE_TC && kind != GA_TUNE_PRODUCT) return GA_ERR_INVALID_ARG;
     if (kind == GA_TUNE_PRODUCT && (!B || !M)) return GA_ERR_INVALID_ARG;
@@ -270,6 +296,7 @@ int ga_autotune_variant(ga_ctx ctx, int kind, int algo, ga_csr A, ga_csr B, ga_c
         out->default_ms = e.default_ms;
         out->candidates = e.candidates;
         out->cached = cached ? 1 : 0;
+        out->tri_order = e.t.tri_order;
     });
 }
 

@@ -114,10 +114,12 @@ GA_API int ga_version(int* major, int* minor);
  * GA_OPT_MXM_CTAS_PER_SM (0 = as many as fit): persistent grid size;
  * GA_OPT_DOT_CHUNK (8): mask entries per warp task of the inner-product form;
  * GA_OPT_HYBRID_RATIO (16): GA_HYBRID sends a row to the inner-product form
- * when its inner-product work times this is below its Gustavson work. */
+ * when its inner-product work times this is below its Gustavson work;
+ * GA_OPT_TRI_ORDER (0): GA_TRI ranks vertices by degree (0; power-law
+ * graphs) or by index (1; unions of small graphs). */
 enum { GA_OPT_DEVICE_LOOPS = 1, GA_OPT_PROFILE = 2, GA_OPT_FAIL_ALLOC_AFTER = 3, GA_OPT_KNN_TILED = 4,
        GA_OPT_MXM_WARP_FLOPS = 5, GA_OPT_MXM_HEAVY_FLOPS = 6, GA_OPT_MXM_CTAS_PER_SM = 7, GA_OPT_DOT_CHUNK = 8,
-       GA_OPT_HYBRID_RATIO = 9 };
+       GA_OPT_HYBRID_RATIO = 9, GA_OPT_TRI_ORDER = 10 };
 GA_API int ga_ctx_set_option(ga_ctx ctx, int option, int64_t value);
 
 /* Per-kernel timing collected while GA_OPT_PROFILE is on. Writes up to `cap`
@@ -372,10 +374,12 @@ GA_API int ga_bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t 
 
 /* -------------------------------------------------------------- autotuner */
 /* Times candidate schedules — MSA with three warp/CTA bin thresholds and
- * two grid sizes, MCA, and the inner-product form with three chunk sizes —
- * on the caller's problem (L2 flushed before each run) and keeps the fastest
- * for problems of the same signature (device, kind, half-octave size
- * buckets, symmetry) in a process-wide cache; GA_AUTO calls use it, tuning
+ * two grid sizes, MCA, the inner-product form with three chunk sizes, the
+ * hybrid form with three ratios, and triangle listing where the operands
+ * are one symmetric 0/1 matrix — on the caller's problem (L2 flushed before
+ * each run) and keeps the fastest for problems of the same signature
+ * (device, kind, half-octave size buckets, symmetry and unit values) in a
+ * process-wide cache; GA_AUTO calls use it, tuning
  * on first use. Kinds: GA_TUNE_KTRUSS (the support product C<A> = A*A of
  * k-truss), GA_TUNE_PRODUCT (A*B masked by M), GA_TUNE_TC (triangle count
  * of A). force != 0 re-tunes. Tuning launches are not counted in the work
@@ -390,9 +394,11 @@ typedef struct {
     double default_ms;      /* the default schedule (MSA) on the same problem */
     int candidates;
     int cached;             /* 1: taken from the cache, no timing run */
+    int tri_order;          /* GA_OPT_TRI_ORDER of the choice */
 } ga_tune_result;
 GA_API int ga_autotune(ga_ctx ctx, int kind, ga_csr A, ga_csr B, ga_csr M, int force, ga_tune_result* out);
-/* The same restricted to one variant (GA_MSA, GA_MCA or GA_DOT; -1: any):
+/* The same restricted to one variant (GA_MSA, GA_MCA, GA_DOT, GA_HYBRID or
+ * GA_TRI; -1: any):
  * tunes that variant's schedule only. To run it, set the result's schedule
  * with ga_ctx_set_option and call with that variant. */
 GA_API int ga_autotune_variant(ga_ctx ctx, int kind, int algo, ga_csr A, ga_csr B, ga_csr M, int force,
@@ -454,8 +460,9 @@ enum { GA_REQ_TC = 0, GA_REQ_KTRUSS = 1, GA_REQ_BC = 2 };
 typedef struct {
     int workers;                   /* worker threads (1..64); 0: 4 */
     int coalesce;                  /* 1: batch queued requests on small graphs */
-    int tc_algo;                   /* ga_algo of TC (any; GA_AUTO: tuned per graph, MSA for batched calls) */
-    int ktruss_algo;               /* ga_algo of k-truss (GA_MSA, GA_MCA, GA_HEAP, GA_DOT, GA_AUTO as for TC) */
+    int tc_algo;                   /* ga_algo of TC (any; GA_AUTO: tuned per graph, GA_TRI for batched calls) */
+    int ktruss_algo;               /* ga_algo of k-truss (GA_MSA, GA_MCA, GA_HEAP, GA_DOT, GA_HYBRID, GA_TRI,
+                                      GA_AUTO as for TC) */
     int64_t hbm_budget;            /* bytes the calls in flight may hold; 0: 80% of free memory at creation */
     int64_t coalesce_nnz;          /* graphs with at most this many stored entries are batched; 0: 2^20 */
     int64_t coalesce_max_nnz;      /* stored entries of one batched union at most; 0: 2^22 (several groups

@@ -28,7 +28,7 @@ def _graphs():
 GRAPHS = list(_graphs())
 
 
-@pytest.mark.parametrize("algo", ["dot", "msa", "mca", "heap", "naive"])
+@pytest.mark.parametrize("algo", ["dot", "msa", "mca", "heap", "naive", "tri"])
 @pytest.mark.parametrize("name,G", GRAPHS, ids=[g[0] for g in GRAPHS])
 def test_tc(ctx, algo, name, G):
     if algo == "naive" and G.m > 2000:
@@ -183,6 +183,36 @@ def _tri_graphs():
 TRI_GRAPHS = list(_tri_graphs())
 
 
+def test_tri_support_wide_rank_spans(ctx):
+    """Lists whose ranks span more than the 16,384-rank window (a graph of
+    40,000 vertices where every vertex links to random far vertices and to
+    a few hubs): members below the window are found by the binary search."""
+    rng = np.random.default_rng(31)
+    n = 40000
+    src = rng.integers(0, n, 200000)
+    dst = rng.integers(0, n, 200000)
+    hubs = rng.choice(n, 20, replace=False)
+    src = np.concatenate([src, np.repeat(hubs, 3000)])
+    dst = np.concatenate([dst, rng.integers(0, n, 60000)])
+    keep = src != dst
+    a, b = np.concatenate([src[keep], dst[keep]]), np.concatenate([dst[keep], src[keep]])
+    key = np.unique(a.astype(np.int64) * n + b)
+    r, c = (key // n).astype(np.int32), (key % n).astype(np.int32)
+    rst = np.zeros(n + 1, np.int32)
+    np.add.at(rst, r + 1, 1)
+    G = csr_from_arrays(n, np.cumsum(rst).astype(np.int32), c)
+    ref = oracle.mxm_masked(G, G, G)
+    Gd = to_device(ctx, G)
+    for order in (0, 1):
+        ctx.set_option(ga.OPT_TRI_ORDER, order)
+        try:
+            _, _, v = ga.mxm_masked("tri", Gd, Gd, Gd).download()
+            assert np.array_equal(v, np.asarray(ref, np.int32)), order
+            assert ga.tc("tri", Gd)[0] == oracle.tc_sandia(G)[0]
+        finally:
+            ctx.set_option(ga.OPT_TRI_ORDER, 0)
+
+
 @pytest.mark.parametrize("name,G", TRI_GRAPHS, ids=[g[0] for g in TRI_GRAPHS])
 def test_tri_support_product(ctx, name, G):
     """C<A> = A*A by triangle listing equals the Gustavson product bit for bit
@@ -204,9 +234,10 @@ def test_tri_support_product(ctx, name, G):
         assert wt["triangles"] == oracle.tc_sandia(G)[0]
 
 
-@pytest.mark.parametrize("device_loops", [1, 0])
-def test_tri_ktruss_with_loops_and_hubs(ctx, device_loops):
+@pytest.mark.parametrize("device_loops,order", [(1, 0), (0, 0), (1, 1)])
+def test_tri_ktruss_with_loops_and_hubs(ctx, device_loops, order):
     ctx.set_option(ga.OPT_DEVICE_LOOPS, device_loops)
+    ctx.set_option(ga.OPT_TRI_ORDER, order)
     try:
         for name, G in TRI_GRAPHS[-3:]:
             Gd = to_device(ctx, G)
@@ -218,6 +249,7 @@ def test_tri_ktruss_with_loops_and_hubs(ctx, device_loops):
                 assert np.array_equal(r, R.rst) and np.array_equal(c, R.col) and np.array_equal(v, R.val), (name, k)
     finally:
         ctx.set_option(ga.OPT_DEVICE_LOOPS, 1)
+        ctx.set_option(ga.OPT_TRI_ORDER, 0)
 
 
 def test_tri_falls_back_for_other_operands(ctx):
@@ -241,3 +273,21 @@ def test_tri_falls_back_for_other_operands(ctx):
         C, git = ga.ktruss("tri", Wd, k)
         r, c, vv = C.download()
         assert git == it and np.array_equal(c, R.col) and np.array_equal(vv, R.val)
+
+
+@pytest.mark.parametrize("name,G", TRI_GRAPHS[-3:], ids=[g[0] for g in TRI_GRAPHS[-3:]])
+def test_tri_tc_long_lists_and_loops(ctx, name, G):
+    """Triangle listing counts like the Sandia form (diagonal entries ignored,
+    per-row counts = triangles whose largest vertex is the row); a matrix
+    that is not symmetric takes the Sandia form."""
+    total, rows = oracle.tc_sandia(G)
+    got, grow = ga.tc("tri", to_device(ctx, G))
+    assert got == total and np.array_equal(grow, rows)
+    rng = np.random.default_rng(12)
+    from graphs import dense_to_csr
+    D = rng.random((90, 90)) < 0.15
+    np.fill_diagonal(D, False)
+    N = dense_to_csr(D)  # not symmetric
+    total, rows = oracle.tc_sandia(N)
+    got, grow = ga.tc("tri", to_device(ctx, N))
+    assert got == total and np.array_equal(grow, rows)

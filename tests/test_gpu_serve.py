@@ -137,7 +137,9 @@ def test_bounds_cover_allocations(ctx, gid):
     src = np.arange(min(32, m), dtype=np.int32)
     for t, run in ((ga.REQ_TC, lambda: ga.tc("msa", A, per_row=False)),
                    (ga.REQ_TC, lambda: ga.tc("dot", A, per_row=False)),
+                   (ga.REQ_TC, lambda: ga.tc("tri", A, per_row=False)),
                    (ga.REQ_KTRUSS, lambda: ga.ktruss("msa", A, 4)),
+                   (ga.REQ_KTRUSS, lambda: ga.ktruss("tri", A, 4)),
                    (ga.REQ_BC, lambda: ga.bc(A, src))):
         ctx.sync()
         base, _ = ctx.mem_stats(reset_peak=True)

@@ -21,7 +21,7 @@ def test_autotune_ktruss_cached_and_exact(ctx, rmat):
     G, A = rmat
     before = ctx.work_counters()
     r1 = ga.autotune(ga.TUNE_KTRUSS, A, force=True)
-    assert r1["algo"] in ("msa", "mca", "dot", "hybrid") and r1["cached"] == 0 and r1["candidates"] >= 5
+    assert r1["algo"] in ("msa", "mca", "dot", "hybrid", "tri") and r1["cached"] == 0 and r1["candidates"] >= 5
     assert 0 < r1["ms"] <= r1["default_ms"] + 1e-9
     r2 = ga.autotune(ga.TUNE_KTRUSS, A)
     assert r2["cached"] == 1 and r2["algo"] == r1["algo"]
@@ -36,7 +36,7 @@ def test_autotune_ktruss_cached_and_exact(ctx, rmat):
 def test_autotune_tc_and_product(ctx, rmat):
     G, A = rmat
     r = ga.autotune(ga.TUNE_TC, A, force=True)
-    assert r["algo"] in ("msa", "mca", "dot")
+    assert r["algo"] in ("msa", "mca", "dot", "tri")
     assert ga.tc("auto", A, per_row=False)[0] == oracle.tc_sandia(G)[0]
     rng = np.random.default_rng(8)
     X = random_csr(300, 200, 0.05, rng)
@@ -52,25 +52,28 @@ def test_autotune_tc_and_product(ctx, rmat):
 @pytest.mark.parametrize("opt,val", [(ga.OPT_MXM_WARP_FLOPS, 0), (ga.OPT_MXM_WARP_FLOPS, 1 << 40),
                                      (ga.OPT_MXM_HEAVY_FLOPS, 1), (ga.OPT_MXM_CTAS_PER_SM, 1),
                                      (ga.OPT_DOT_CHUNK, 1), (ga.OPT_DOT_CHUNK, 64),
-                                     (ga.OPT_HYBRID_RATIO, 0), (ga.OPT_HYBRID_RATIO, 1 << 20)])
+                                     (ga.OPT_HYBRID_RATIO, 0), (ga.OPT_HYBRID_RATIO, 1 << 20),
+                                     (ga.OPT_TRI_ORDER, 1)])
 def test_schedule_options_do_not_change_results(ctx, rmat, opt, val):
     G, A = rmat
     ref = oracle.mxm_masked(G, G, G)
     defaults = {ga.OPT_MXM_WARP_FLOPS: 32768, ga.OPT_MXM_HEAVY_FLOPS: 1 << 20, ga.OPT_MXM_CTAS_PER_SM: 0,
-                ga.OPT_DOT_CHUNK: 8, ga.OPT_HYBRID_RATIO: 16}
+                ga.OPT_DOT_CHUNK: 8, ga.OPT_HYBRID_RATIO: 16, ga.OPT_TRI_ORDER: 0}
     ctx.set_option(opt, val)
     try:
-        for algo in ("msa", "mca", "heap", "dot", "hybrid"):
+        for algo in ("msa", "mca", "heap", "dot", "hybrid", "tri"):
             assert np.array_equal(ga.mxm_masked(algo, A, A, A).download()[2], ref), algo
-        C, it = ga.ktruss("msa", A, 4)
         R, rit = oracle.ktruss(G, 4)
-        assert it == rit and np.array_equal(C.download()[1], R.col)
+        for algo in ("msa", "tri"):
+            C, it = ga.ktruss(algo, A, 4)
+            assert it == rit and np.array_equal(C.download()[1], R.col), algo
+        assert ga.tc("tri", A, per_row=False)[0] == oracle.tc_sandia(G)[0]
     finally:
         ctx.set_option(opt, defaults[opt])
 
 
 def test_bad_options_rejected(ctx):
-    for opt, val in ((ga.OPT_DOT_CHUNK, 0), (ga.OPT_MXM_CTAS_PER_SM, -1), (99, 1)):
+    for opt, val in ((ga.OPT_DOT_CHUNK, 0), (ga.OPT_MXM_CTAS_PER_SM, -1), (ga.OPT_TRI_ORDER, 2), (99, 1)):
         with pytest.raises(ga.GaError):
             ctx.set_option(opt, val)
 
