@@ -369,14 +369,16 @@ def profile_step(ga, ctx, run, algo, counters, loops):
         eo = ctr["a_entries"] / 2
         bytes_model = 8 * ctr["rows"] + 20 * eo + 4 * ctr["wedges"] + 16 * ctr["triangles"]
         tpe = profile_traffic("tri_support_rmat18.md")
+        traffic_units = ctr["a_entries"]  # the capture's DRAM bytes are per stored entry
     else:
         # products of the Gustavson kernels; list entries walked for the inner-product one
         ex = ctr["executed_dot"] if algo == "dot" else ctr["executed"]
         bytes_model = 8 * ctr["rows"] + 16 * ctr["a_entries"] + 8 * ex + 8 * ctr["mask_entries"]
         tpe = profile_traffic()
+        traffic_units = ctr["mask_entries"]
     peak, peak_kind = measured_peak_hbm()
     achieved = bytes_model / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
-    traffic = (tpe * ctr["mask_entries"] / max(1, k_launches)) if tpe is not None else None
+    traffic = (tpe * traffic_units / max(1, k_launches)) if tpe is not None else None
     return {"launches": launches, "kernel_ms": k_ms, "stats": stats, "counters": ctr,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
@@ -583,7 +585,12 @@ def run_gpu(args, dist: Dist):
         "gpu_launches": int(launches_per_step * args.steps), "clocks": clocks,
         "work": {"products_per_step": wc["products"] / args.steps,
                  "executed_products_per_step": wc["executed"] / args.steps, "k_max": kmax,
-                 "support_products_k3": per_k.get(args.kmin, {}).get("products")},
+                 "support_products_k3": per_k.get(args.kmin, {}).get("products"),
+                 "wedges_per_step": wc["wedges"] / args.steps, "triangles_per_step": wc["triangles"] / args.steps},
+        "kernel_profile": {"note": "one step with host-driven loops and CUDA events per launch (slower than "
+                                   "the timed step); summed event time per kernel scope, ms",
+                           "top": {k: round(v[1], 3) for k, v in
+                                   sorted(prof["stats"].items(), key=lambda kv: -kv[1][1])[:14]}},
         "support_variants": variants,
         "other_configs": others,
     }

@@ -176,6 +176,14 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __re
         const int ne = min(kTriTask, ub + un - p0);
         const int32_t* Ou = ocol + ub;
         const bool counted = un <= kTriCntMax;
+        // the task's entries (u, v) and v's lists, loaded before the bitmap
+        // is built so the two chains of loads overlap
+        int32_t v = 0, vs = 0, vn = 0;
+        if (lane < ne) {
+            v = __ldg(ocol + p0 + lane);
+            vs = __ldg(ost + v);
+            vn = __ldg(ost + v + 1) - vs;
+        }
         int32_t key = 0;
         int n_in = 0;
         // window: the kTriWin ranks up to O_u's highest (all of O_u when its
@@ -215,32 +223,28 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __re
         } else if (!counted) {
             key = __ldg(Ou + (int)(((int64_t)(lane + 1) * un) >> 5) - 1);
         }
-        int32_t v = 0, vs = 0, vn = 0;
-        if (lane < ne) {
-            v = __ldg(ocol + p0 + lane);
-            vs = __ldg(ost + v);
-            vn = __ldg(ost + v + 1) - vs;
-        }
         for (int e = 0; e < ne; ++e) {
             const int32_t evs = __shfl_sync(FULL, vs, e);
             const int32_t evn = __shfl_sync(FULL, vn, e);
             const int32_t ev = __shfl_sync(FULL, v, e);
             int32_t found = 0;
-            for (int32_t base = 0; base < evn; base += 32) {
-                const int32_t x = base + lane;
+            // one round of 32 wedges: the lane's wedge x of the entry, ld its
+            // loaded rank (column when the list is not counted)
+            auto probe = [&](int32_t x, int32_t ld) {
                 const bool valid = x < evn;
                 const int32_t wp = evs + x;
                 bool hit = false;
                 if (counted) {
                     // ranks above the window are above every member
-                    const int32_t b = valid ? __ldg(orank + wp) - win0 : kTriWin;
-                    if (b >= 0 && b < kTriWin) {
+                    const int32_t b = valid ? ld - win0 : kTriWin;
+                    if ((uint32_t)b < (uint32_t)kTriWin) {
                         const uint32_t wd = bits[b >> 5];
-                        if ((wd >> (b & 31)) & 1u) {
+                        const uint32_t bit = 1u << (b & 31);
+                        if (wd & bit) {
                             hit = true;
                             if (!COUNT) {
-                                const int idx = wbase[b >> 5] + __popc(wd & ((1u << (b & 31)) - 1u));
-                                atomicAdd(cnt + (idx >> 2), 1u << ((idx & 3) * 8));  // (u, w)
+                                const int idx = wbase[b >> 5] + __popc(wd & (bit - 1u));
+                                atomicAdd(cnt + (idx >> 2), 1u << ((idx & 3) << 3));  // (u, w)
                             }
                         }
                     } else if (b < 0 && below) {
@@ -253,7 +257,7 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __re
                         }
                     }
                 } else {
-                    const int32_t w = valid ? __ldg(ocol + wp) : INT32_MAX;
+                    const int32_t w = valid ? ld : INT32_MAX;
                     const int bb = warp_lower_bound(key, w);
                     if (valid && bb < 32) {
                         const int lo_b = (int)(((int64_t)bb * un) >> 5);
@@ -271,6 +275,15 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __re
                     atomicAdd(per_row + max(max(u, ev), w), 1ull);
                 }
                 found += __popc(__ballot_sync(FULL, hit));
+            };
+            // two rounds per pass, both loads issued first
+            const int32_t* src = counted ? orank : ocol;
+            for (int32_t base = 0; base < evn; base += 64) {
+                const int32_t x0 = base + lane, x1 = x0 + 32;
+                const int32_t l0 = x0 < evn ? __ldg(src + evs + x0) : 0;
+                const int32_t l1 = x1 < evn ? __ldg(src + evs + x1) : 0;
+                probe(x0, l0);
+                if (base + 32 < evn) probe(x1, l1);  // warp-uniform
             }
             if (lane == 0) {
                 wedges += (unsigned long long)evn;

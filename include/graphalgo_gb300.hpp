@@ -3,7 +3,8 @@
 //
 // It re-exposes the reference's types and signatures:
 //   spMtx<T>, denseMtx<T>                     (include/matrix.h:23-666)
-//   mxmm_msa / mxmm_mca / mxmm_heap / mxmm_naive, mxmm_msa_cmask, mxmm_spd,
+//   mxmm_msa / mxmm_mca / mxmm_heap / mxmm_naive (+ mxmm_hybrid, mxmm_tri),
+//   mxmm_msa_cmask, mxmm_spd,
 //   add_nointersect, eWiseMult, fuseEWiseMultAdd, transpose  (include/matrix_la.h)
 //   extract_lower_triangle, extract_upper_triangle, build_symm_from_lower,
 //   build_adjacency_matrix, convertType       (include/matrix.h:668-792)
@@ -331,6 +332,17 @@ template <typename T>
 void mxmm_naive(bool, const spMtx<T>& A, const spMtx<T>& B, const spMtx<T>& M, spMtx<T>& C) {
     detail::masked(GA_NAIVE, A, B, M, C);
 }
+// Not in the reference: per row the cheaper of MSA and inner products
+// (GA_HYBRID), and triangle listing (GA_TRI: C<A> = A*A of a symmetric 0/1
+// matrix, the k-truss support; other operands run GA_HYBRID). Same results.
+template <typename T>
+void mxmm_hybrid(bool, const spMtx<T>& A, const spMtx<T>& B, const spMtx<T>& M, spMtx<T>& C) {
+    detail::masked(GA_HYBRID, A, B, M, C);
+}
+template <typename T>
+void mxmm_tri(bool, const spMtx<T>& A, const spMtx<T>& B, const spMtx<T>& M, spMtx<T>& C) {
+    detail::masked(GA_TRI, A, B, M, C);
+}
 // C<!M> = A*B with a new sorted pattern (include/matrix_la.h:788-798)
 template <typename T, typename U>
 void mxmm_msa_cmask(bool, const spMtx<T>& A, const spMtx<T>& B, const spMtx<U>& M, spMtx<T>& C) {
@@ -435,7 +447,10 @@ inline ga_algo algo_of(mxmOp<int> op) {
     if (op == static_cast<mxmOp<int>>(&mxmm_mca<int, int>)) return GA_MCA;
     if (op == static_cast<mxmOp<int>>(&mxmm_heap<int>)) return GA_HEAP;
     if (op == static_cast<mxmOp<int>>(&mxmm_naive<int>)) return GA_NAIVE;
-    throw error(GA_ERR_INVALID_ARG, "mxmOp must be ga::mxmm_msa, mxmm_mca, mxmm_heap or mxmm_naive");
+    if (op == static_cast<mxmOp<int>>(&mxmm_hybrid<int>)) return GA_HYBRID;
+    if (op == static_cast<mxmOp<int>>(&mxmm_tri<int>)) return GA_TRI;
+    throw error(GA_ERR_INVALID_ARG,
+                "mxmOp must be ga::mxmm_msa, mxmm_mca, mxmm_heap, mxmm_naive, mxmm_hybrid or mxmm_tri");
 }
 }  // namespace detail
 

@@ -43,7 +43,8 @@ int main() {
 
     // triangle counting through each plugin (src/main.cpp:206-218 shapes)
     const int64_t expect_tc = or_tc_sandia((int64_t)A.m, A.Rst, A.Col, nullptr);
-    mxmOp<int> ops[] = {mxmm_msa<int>, mxmm_mca<int>, mxmm_heap<int>, mxmm_naive<int>};
+    mxmOp<int> ops[] = {mxmm_msa<int>, mxmm_mca<int>, mxmm_heap<int>, mxmm_naive<int>, mxmm_hybrid<int>,
+                        mxmm_tri<int>};
     for (mxmOp<int> op : ops) {
         int64_t t = triangle_counting_masked_sandia(A, op, true);
         EXPECT(t == expect_tc, "sandia %lld != %lld", (long long)t, (long long)expect_tc);
@@ -68,13 +69,18 @@ int main() {
     bool same = C.nz == A.nz;
     for (size_t j = 0; same && j < C.nz; ++j) same = C.Val[j] == ref[j] && C.Col[j] == A.Col[j];
     EXPECT(same, "mxmm_msa values");
+    spMtx<int> Ct;
+    mxmm_tri<int>(true, A, A, A, Ct);
+    same = Ct.nz == A.nz;
+    for (size_t j = 0; same && j < Ct.nz; ++j) same = Ct.Val[j] == ref[j] && Ct.Col[j] == A.Col[j];
+    EXPECT(same, "mxmm_tri values");
 
     // k-truss for several k with every plugin
     for (int k : {3, 4, 5}) {
         int *cr, *cc, *cv, it_ref;
         int64_t cnz;
         or_ktruss((int64_t)A.m, A.Rst, A.Col, A.Val, k, &cr, &cc, &cv, &cnz, &it_ref);
-        for (mxmOp<int> op : {ops[0], ops[1], ops[2]}) {
+        for (mxmOp<int> op : {ops[0], ops[1], ops[2], ops[4], ops[5]}) {
             int it = -1;
             spMtx<int> T = k_truss(A, k, op, true, &it);
             bool eq = (int64_t)T.nz == cnz && it == it_ref;
