@@ -146,7 +146,7 @@ __global__ void k_tri_tasklist(const int32_t* __restrict__ tstart, int64_t m, in
 // the total and, with per_row, to the row of its largest vertex index (the
 // row sums of C<L> = L·L over the strictly lower triangle L).
 template <bool COUNT>
-__global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __restrict__ ost,
+__global__ void __launch_bounds__(kTriThreads, 10) k_tri_support(const int32_t* __restrict__ ost,
                                                              const int32_t* __restrict__ ocol,
                                                              const int32_t* __restrict__ orank,
                                                              const int32_t* __restrict__ tstart,
@@ -155,15 +155,15 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __re
                                                              unsigned long long* __restrict__ ctr,
                                                              unsigned long long* __restrict__ total,
                                                              unsigned long long* __restrict__ per_row) {
-    __shared__ uint32_t bits_s[kTriThreads / 32][kTriWinWords];
-    __shared__ uint16_t wbase_s[kTriThreads / 32][kTriWinWords];
+    // per bitmap word: its member bits (x) and the member index of its first
+    // member (y), read together by one 64-bit shared load
+    __shared__ uint2 words_s[kTriThreads / 32][kTriWinWords];
     __shared__ uint32_t cnt_s[kTriThreads / 32][kTriCntWords];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    uint32_t* bits = bits_s[threadIdx.x >> 5];
-    uint16_t* wbase = wbase_s[threadIdx.x >> 5];
+    uint2* words = words_s[threadIdx.x >> 5];
     uint32_t* cnt = cnt_s[threadIdx.x >> 5];
-    for (int s = lane; s < kTriWinWords; s += 32) bits[s] = 0;
+    for (int s = lane; s < kTriWinWords; s += 32) words[s] = make_uint2(0u, 0u);
     for (int s = lane; s < kTriCntWords; s += 32) cnt[s] = 0;
     __syncwarp();
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __re
             nwords = ((hi - win0) >> 5) + 1;
             for (int t = lane; t < un; t += 32) {
                 const int32_t b = __ldg(orank + ub + t) - win0;
-                if (b >= 0) atomicOr(bits + (b >> 5), 1u << (b & 31));
+                if (b >= 0) atomicOr(&words[b >> 5].x, 1u << (b & 31));
             }
             __syncwarp();
         }
@@ -213,9 +213,9 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __re
             // member index of the first member of every bitmap word
             int run = 0;
             for (int k = 0; k < nwords; k += 32) {
-                const int c1 = __popc(bits[k + lane]);
+                const int c1 = __popc(words[k + lane].x);
                 const int incl = warp_incl_scan(c1);
-                wbase[k + lane] = (uint16_t)(run + incl - c1);
+                words[k + lane].y = (uint32_t)(run + incl - c1);
                 run += __shfl_sync(FULL, incl, 31);
             }
             n_in = run;
@@ -238,12 +238,12 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __re
                     // ranks above the window are above every member
                     const int32_t b = valid ? ld - win0 : kTriWin;
                     if ((uint32_t)b < (uint32_t)kTriWin) {
-                        const uint32_t wd = bits[b >> 5];
+                        const uint2 wd = words[b >> 5];
                         const uint32_t bit = 1u << (b & 31);
-                        if (wd & bit) {
+                        if (wd.x & bit) {
                             hit = true;
                             if (!COUNT) {
-                                const int idx = wbase[b >> 5] + __popc(wd & (bit - 1u));
+                                const int idx = (int)wd.y + __popc(wd.x & (bit - 1u));
                                 atomicAdd(cnt + (idx >> 2), 1u << ((idx & 3) << 3));  // (u, w)
                             }
                         }
@@ -293,21 +293,21 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_support(const int32_t* __re
         }
         if (counted && COUNT) {
             __syncwarp();
-            for (int s = lane; s < nwords; s += 32) bits[s] = 0;
+            for (int s = lane; s < nwords; s += 32) words[s] = make_uint2(0u, 0u);
             __syncwarp();
         } else if (counted) {
             __syncwarp();
             for (int t = lane; t < un; t += 32) {
                 const int32_t b = __ldg(orank + ub + t) - win0;
                 if (b >= 0) {
-                    const uint32_t wd = bits[b >> 5];
-                    const int idx = wbase[b >> 5] + __popc(wd & ((1u << (b & 31)) - 1u));
+                    const uint2 wd = words[b >> 5];
+                    const int idx = (int)wd.y + __popc(wd.x & ((1u << (b & 31)) - 1u));
                     const uint32_t n = (cnt[idx >> 2] >> ((idx & 3) * 8)) & 0xffu;
                     if (n) atomicAdd(sup_o + ub + t, (int32_t)n);
                 }
             }
             __syncwarp();
-            for (int s = lane; s < nwords; s += 32) bits[s] = 0;
+            for (int s = lane; s < nwords; s += 32) words[s] = make_uint2(0u, 0u);
             for (int s = lane; s < ((n_in + 3) >> 2); s += 32) cnt[s] = 0;
             __syncwarp();
         }
