@@ -283,7 +283,8 @@ def run_case(args):
 
 
 def workload_config(args, m, nnz, kmax, schedule=None):
-    return {"workload": f"k-truss sweep k={args.kmin}..{kmax} (k_max), R-MAT scale {args.scale}",
+    kmax_s = "k_max" if kmax is None else f"{kmax} (k_max)"
+    return {"workload": f"k-truss sweep k={args.kmin}..{kmax_s}, R-MAT scale {args.scale}",
             "schedule": None if schedule is None else
             {k: schedule[k] for k in ("algo", "warp_max_flops", "heavy_flops", "ctas_per_sm", "dot_chunk")},
             "graph": f"R-MAT scale {args.scale}, edge factor {args.edge_factor}, a/b/c/d=0.57/0.19/0.19/0.05, "
@@ -1095,7 +1096,8 @@ def run_reference(args, dist: Dist):
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic", "impl": "reference",
-            "config": workload_config(args, m, len(col), None),
+            "config": dict(workload_config(args, m, len(col), None),
+                           variant="oracle port of the reference's k_truss with the parallel mxmm_msa"),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 

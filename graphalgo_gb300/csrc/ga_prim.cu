@@ -162,15 +162,25 @@ bool csr_unit_values(ga_ctx ctx, ga_csr A) {
     return A->unit == 1;
 }
 
-// Pattern and values symmetric: every (i, j, v) has a (j, i, v).
+// Pattern and values symmetric: every (i, j, v) has a (j, i, v). One warp
+// per chunk of 256 consecutive entries (balanced whatever the row lengths):
+// the chunk's first and last rows by binary search of the row starts, each
+// entry's row by a search between them, its mirror by a search of row j.
+constexpr int kSymChunk = 256;
+
 template <typename T>
 __global__ void k_check_symmetric(const int32_t* __restrict__ r, const int32_t* __restrict__ c,
-                                  const T* __restrict__ v, int64_t m, int* __restrict__ flag) {
+                                  const T* __restrict__ v, int64_t m, int64_t nnz, int* __restrict__ flag) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < m; i += warps) {
+    for (int64_t ch = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch * kSymChunk < nnz; ch += warps) {
+        const int32_t q0 = (int32_t)(ch * kSymChunk);
+        const int32_t q1 = (int32_t)min(nnz, (int64_t)q0 + kSymChunk);
+        const int i0 = upper_bound_i32(r, (int)m + 1, q0) - 1;
+        const int i1 = upper_bound_i32(r, (int)m + 1, q1 - 1) - 1;
         bool bad = false;
-        for (int32_t q = r[i] + lane; q < r[i + 1]; q += 32) {
+        for (int32_t q = q0 + lane; q < q1; q += 32) {
+            const int i = i0 + upper_bound_i32(r + i0 + 1, i1 - i0, q);
             const int32_t j = c[q];
             if ((int64_t)j >= m) { bad = true; continue; }
             const int32_t jb = r[j], jn = r[j + 1] - jb;
@@ -188,8 +198,8 @@ bool csr_is_symmetric(ga_ctx ctx, ga_csr A) {
     DBuf<int> flag(ctx, 1);
     GA_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), ctx->stream));
     GA_DISPATCH_DTYPE(A->dtype, T, {
-        k_check_symmetric<T><<<grid_for(A->m * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(
-            A->rst, A->col, static_cast<const T*>(A->val), A->m, flag.p);
+        k_check_symmetric<T><<<grid_for((A->nnz + kSymChunk - 1) / kSymChunk * 32, 256, ctx->num_sms * 16), 256, 0,
+                               ctx->stream>>>(A->rst, A->col, static_cast<const T*>(A->val), A->m, A->nnz, flag.p);
     });
     post_launch("check_symmetric");
     A->sym = read_i32(ctx, flag.p) == 0 ? 1 : 0;
