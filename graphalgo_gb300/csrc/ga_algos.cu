@@ -246,14 +246,6 @@ static void tc_device(ga_ctx ctx, ga_algo algo, ga_csr A, int64_t* d_total, int6
 }
 
 // ============================================================== k-truss
-struct KtState {
-    int32_t nnz;        // nnz of C
-    int32_t t;          // iteration index
-    int32_t iters;      // reported iteration count
-    int32_t swapped;    // this iteration replaced C by the pruned matrix
-    int32_t done;
-    int32_t first_vals; // C still carries A's values (no swap yet)
-};
 
 // Rows of graphs that have finished (batched k-truss) keep every entry.
 __device__ __forceinline__ bool kt_keep_all(const int32_t* gid, const int32_t* done_g, int64_t i) {
@@ -480,7 +472,9 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
         if (algo == GA_TRI && !tri) algo = upper ? GA_HYBRID : GA_MSA;
         GA_REQUIRE(upper || (algo != GA_DOT && algo != GA_HYBRID), GA_ERR_UNSUPPORTED,
                    "k-truss with GA_DOT or GA_HYBRID needs a symmetric matrix");
-        DBuf<unsigned char> mxm_scr(ctx, tri ? tri_scratch_bytes(m, cap) : mxm_scratch_bytes(m, m, cap));
+        DBuf<unsigned char> mxm_scr(ctx, tri ? tri_kt_bytes(m, cap) : mxm_scratch_bytes(m, m, cap));
+        TriKt tk{};
+        if (tri) tri_kt_carve(mxm_scr.p, m, cap, &tk);
         const size_t aux = upper ? (size_t)cap : 1;
         DBuf<int32_t> ust(ctx, upper && !tri ? (size_t)m + 1 : 1);
         DBuf<int32_t> row_of(ctx, aux), mir(ctx, aux), pos_new(ctx, aux), trow(ctx, aux), mir_new(ctx, aux);
@@ -493,17 +487,20 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
             // date through the prunes
             k_expand_rows<<<grid_rows, 256, 0, ctx->stream>>>(C->rst, m, row_of.p);
             post_launch("kt_expand_rows");
-            k_mirror_index<<<grid_ent, 256, 0, ctx->stream>>>(C->rst, C->col, row_of.p, C->nnz, mir.p);
-            post_launch("kt_mirror_index");
+            if (tri) {
+                // rows partitioned [ranked above the row | the rest] for the whole loop
+                tri_kt_setup(ctx, C, row_of.p, mir.p, tc.p, eflag.p, tk, cap);
+            } else {
+                k_mirror_index<<<grid_ent, 256, 0, ctx->stream>>>(C->rst, C->col, row_of.p, C->nnz, mir.p);
+                post_launch("kt_mirror_index");
+            }
         }
-        if (tri) tri_prepare(ctx, C, mxm_scr.p, cap);
         auto body = [&](const LoopCtl& ctl) {
             // Tmp<C> = C*C, values aligned with C's pattern
             if (algo == GA_NAIVE) {
                 mxm_masked_into(ctx, algo, C, C, C, sup.p);
             } else if (tri) {
-                // eflag holds the orientation positions until the prune reuses it
-                tri_support_launch(ctx, C, row_of.p, mir.p, eflag.p, sup.p, mxm_scr.p, cap, true);
+                tri_kt_support(ctx, C, sup.p, tk, cap);
             } else if (upper) {
                 k_upper_start<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(C->rst, C->col, m, ust.p);
                 post_launch("kt_upper_start");
@@ -520,14 +517,24 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
             // prune: keep flags, their exclusive scan (new positions), scatter
             const int32_t* gid = batch ? batch->gid : nullptr;
             const int32_t* done_g = batch ? batch->done_g : nullptr;
-            k_kt_flags<<<grid_ent, 256, 0, ctx->stream>>>(C->rst, sup.p, m, k, cap, eflag.p, gid, done_g,
-                                                          upper ? row_of.p : nullptr, batch ? batch->kg : nullptr);
-            post_launch("kt_flags");
+            if (tri) {
+                tri_kt_flags(ctx, C, row_of.p, mir.p, sup.p, tk, cap, k, batch, eflag.p);
+            } else {
+                k_kt_flags<<<grid_ent, 256, 0, ctx->stream>>>(C->rst, sup.p, m, k, cap, eflag.p, gid, done_g,
+                                                              upper ? row_of.p : nullptr,
+                                                              batch ? batch->kg : nullptr);
+                post_launch("kt_flags");
+            }
             scan_exclusive_i32_scratch(ctx, eflag.p, eflag.p, cap, scan_scr.p);
-            k_kt_scatter<<<grid_copy, 256, 0, ctx->stream>>>(C->rst, C->col, eflag.p, m, tc.p, tr.p,
-                                                             upper ? pos_new.p : nullptr, upper ? trow.p : nullptr,
-                                                             upper ? row_of.p : nullptr);
-            post_launch("kt_scatter");
+            if (tri) {
+                tri_kt_scatter(ctx, C, eflag.p, row_of.p, tk, cap, tc.p, tr.p, pos_new.p, trow.p);
+            } else {
+                k_kt_scatter<<<grid_copy, 256, 0, ctx->stream>>>(C->rst, C->col, eflag.p, m, tc.p, tr.p,
+                                                                 upper ? pos_new.p : nullptr,
+                                                                 upper ? trow.p : nullptr,
+                                                                 upper ? row_of.p : nullptr);
+                post_launch("kt_scatter");
+            }
             if (batch) {
                 k_kt_graph_update<<<grid_for(batch->ngraphs, 128, ctx->num_sms * 4), 128, 0, ctx->stream>>>(
                     st.p, tr.p, *batch);
@@ -546,6 +553,7 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
                 k_kt_copyback_aux<<<grid_ent, 256, 0, ctx->stream>>>(st.p, trow.p, mir_new.p, row_of.p, mir.p);
                 post_launch("kt_copyback_aux");
             }
+            if (tri) tri_kt_copyback(ctx, st.p, m, pos_new.p, tk, cap);
         };
         const bool saved = ctx->device_loops;
         if (algo == GA_NAIVE) ctx->device_loops = false;  // naive allocates per call
@@ -561,6 +569,7 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
         GA_CUDA(cudaMemcpyAsync(&hs, st.p, sizeof(KtState), cudaMemcpyDeviceToHost, ctx->stream));
         GA_CUDA(cudaStreamSynchronize(ctx->stream));
         C->nnz = hs.nnz;
+        if (tri) tri_kt_finish(ctx, C, row_of.p, tk, tc.p);  // rows back in column order
         C->unit = unit ? 1 : -1;
         C->sym = upper ? 1 : -1;  // pruning a symmetric matrix by a symmetric support keeps it symmetric
         if (iters_out) *iters_out = hs.iters;

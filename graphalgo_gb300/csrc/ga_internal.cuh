@@ -209,6 +209,53 @@ struct KtBatch {
 };
 ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, const KtBatch* batch);
 
+// Device state of a k-truss loop.
+struct KtState {
+    int32_t nnz;        // nnz of C
+    int32_t t;          // iteration index
+    int32_t iters;      // reported iteration count
+    int32_t swapped;    // this iteration replaced C by the pruned matrix
+    int32_t done;
+    int32_t first_vals; // C still carries A's values (no swap yet)
+};
+
+// Triangle-listing k-truss with the orientation kept in C itself: for the
+// whole loop every row of C is stored as [entries whose column is ranked
+// above the row | the rest], both parts in column order, so each row's
+// oriented list is its first ocount entries and the prune's compaction keeps
+// the layout. Buffers (all from tri_kt_bytes):
+struct TriKt {
+    int32_t* crank;     // cap: rank of each entry's column, aligned with C
+    int32_t* tcrank;    // cap: its compacted copy
+    int32_t* ocount;    // m + 1: oriented entries per row
+    int32_t* tstart;    // m + 2: tasks per row, scanned into task starts
+    int32_t* task_row;  // cap / 32 + m + 1: row of each task
+    int32_t* dpos;      // m + 1: position of each row's diagonal entry, -1 if none
+    void* scan_scr;
+};
+size_t tri_kt_bytes(int64_t m, int64_t cap);
+void tri_kt_carve(void* scratch, int64_t m, int64_t cap, TriKt* t);
+// Before the loop: ranks, the partition of every row (tmp_col: cap entries,
+// tmp_flag: cap + 1), the mirror index in that layout, diagonal positions,
+// tasks per row. row_of must hold every entry's row.
+void tri_kt_setup(ga_ctx ctx, ga_csr C, const int32_t* row_of, int32_t* mir, int32_t* tmp_col, int32_t* tmp_flag,
+                  const TriKt& t, int64_t cap);
+// One support evaluation: counts at the oriented entries of sup (cap).
+void tri_kt_support(ga_ctx ctx, ga_csr C, int32_t* sup, const TriKt& t, int64_t cap);
+// Keep flags from the support (k, or the batch's per-graph k / finished
+// graphs), with the upper-triangle work counters.
+void tri_kt_flags(ga_ctx ctx, ga_csr C, const int32_t* row_of, const int32_t* mir, const int32_t* sup,
+                  const TriKt& t, int64_t cap, int k, const KtBatch* batch, int32_t* flag);
+// After the flags' scan (pos): compaction of C into tc / tr with rows (trow)
+// and new positions (pos_new), and of the resident arrays.
+void tri_kt_scatter(ga_ctx ctx, ga_csr C, const int32_t* pos, const int32_t* row_of, const TriKt& t, int64_t cap,
+                    int32_t* tc, int32_t* tr, int32_t* pos_new, int32_t* trow);
+// With the iteration's swap: the resident arrays follow C.
+void tri_kt_copyback(ga_ctx ctx, const KtState* st, int64_t m, const int32_t* pos_new, const TriKt& t,
+                     int64_t cap);
+// After the loop: every row back in column order.
+void tri_kt_finish(ga_ctx ctx, ga_csr C, const int32_t* row_of, const TriKt& t, int32_t* tmp_col);
+
 // Autotuned algorithm resolution: GA_AUTO becomes the cached (or freshly
 // tuned) variant, and ctx->tune its schedule; other values pass through.
 // Callers hold a TuneScope so the context's schedule is restored afterwards.

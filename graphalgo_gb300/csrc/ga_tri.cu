@@ -132,7 +132,8 @@ __global__ void k_tri_tasklist(const int32_t* __restrict__ tstart, int64_t m, in
         for (int32_t t = tstart[u]; t < tstart[u + 1]; ++t) task_row[t] = (int32_t)u;
 }
 
-// One warp per task: up to kTriTask consecutive entries (u, v) of O_u. The
+// One warp per task: up to kTriTask consecutive entries (u, v) of O_u
+// (O_u = [ost[u], ost[u+1]), or [ost[u], ost[u] + ocnt[u]) with ocnt). The
 // warp marks O_u's members of the rank window [win0, win0 + kTriWin) in its
 // bitmap (an O_u longer than kTriCntMax uses 32 bucket splitters in
 // registers and a short binary search instead). For each entry v in turn,
@@ -147,6 +148,7 @@ __global__ void k_tri_tasklist(const int32_t* __restrict__ tstart, int64_t m, in
 // row sums of C<L> = L·L over the strictly lower triangle L).
 template <bool COUNT>
 __global__ void __launch_bounds__(kTriThreads, 10) k_tri_support(const int32_t* __restrict__ ost,
+                                                             const int32_t* __restrict__ ocnt,
                                                              const int32_t* __restrict__ ocol,
                                                              const int32_t* __restrict__ orank,
                                                              const int32_t* __restrict__ tstart,
@@ -171,7 +173,7 @@ __global__ void __launch_bounds__(kTriThreads, 10) k_tri_support(const int32_t* 
     unsigned long long wedges = 0, tris = 0;
     for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ntask; c += warps) {
         const int u = task_row[c];
-        const int32_t ub = ost[u], un = ost[u + 1] - ub;
+        const int32_t ub = ost[u], un = ocnt ? ocnt[u] : ost[u + 1] - ub;
         const int32_t p0 = ub + (int32_t)(c - tstart[u]) * kTriTask;
         const int ne = min(kTriTask, ub + un - p0);
         const int32_t* Ou = ocol + ub;
@@ -182,7 +184,7 @@ __global__ void __launch_bounds__(kTriThreads, 10) k_tri_support(const int32_t* 
         if (lane < ne) {
             v = __ldg(ocol + p0 + lane);
             vs = __ldg(ost + v);
-            vn = __ldg(ost + v + 1) - vs;
+            vn = ocnt ? __ldg(ocnt + v) : __ldg(ost + v + 1) - vs;
         }
         int32_t key = 0;
         int n_in = 0;
@@ -446,7 +448,7 @@ void tri_support_launch(ga_ctx ctx, ga_csr C, const int32_t* row_of, const int32
     {
         ProfScope ps(ctx, "tri_support");
         k_tri_support<false><<<ctx->num_sms * tri_blocks_per_sm<false>(), kTriThreads, 0, ctx->stream>>>(
-            t.ost, t.ocol, t.orank, t.tstart, t.task_row, m, t.sup_o, ctx->d_counters, nullptr, nullptr);
+            t.ost, nullptr, t.ocol, t.orank, t.tstart, t.task_row, m, t.sup_o, ctx->d_counters, nullptr, nullptr);
         post_launch("tri_support");
     }
     ProfScope ps(ctx, "tri_writeback");
@@ -468,7 +470,7 @@ void tri_count(ga_ctx ctx, ga_csr A, unsigned long long* d_total, unsigned long 
     tri_lists(ctx, A, row_of.p, pos.p, t, cap, 0);
     ProfScope ps(ctx, "tri_count");
     k_tri_support<true><<<ctx->num_sms * tri_blocks_per_sm<true>(), kTriThreads, 0, ctx->stream>>>(
-        t.ost, t.ocol, t.orank, t.tstart, t.task_row, m, nullptr, ctx->d_counters, d_total, d_per_row);
+        t.ost, nullptr, t.ocol, t.orank, t.tstart, t.task_row, m, nullptr, ctx->d_counters, d_total, d_per_row);
     post_launch("tri_count");
 }
 
@@ -488,6 +490,292 @@ void tri_masked_into(ga_ctx ctx, ga_csr A, int32_t* sup) {
     mirror_index(ctx, A, row_of.p, mir.p);
     tri_prepare(ctx, A, scr.p, cap);
     tri_support_launch(ctx, A, row_of.p, mir.p, pos.p, sup, scr.p, cap, false);
+}
+
+// =============================================== resident orientation (k-truss)
+// Entry q of the unpartitioned C (column order) goes to the oriented part of
+// its row when its column is ranked above the row.
+__global__ void k_trikt_part_flags(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
+                                   const int32_t* __restrict__ row_of, const int32_t* __restrict__ rank, int64_t m,
+                                   int64_t cap, int32_t* __restrict__ flag) {
+    const int64_t cur = cr[m];
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cap; q += (int64_t)gridDim.x * blockDim.x) {
+        int32_t f = 0;
+        if (q < cur) {
+            const int32_t i = row_of[q], j = cc[q];
+            f = i != j && rank[j] > rank[i];
+        }
+        flag[q] = f;
+    }
+}
+
+// After the flags' scan: stable partition of every row (oriented part, then
+// the rest), the rank of every placed column, and per row its oriented count
+// and tasks.
+__global__ void k_trikt_part_place(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
+                                   const int32_t* __restrict__ row_of, const int32_t* __restrict__ rank,
+                                   const int32_t* __restrict__ pos, int64_t m, int32_t* __restrict__ out_col,
+                                   int32_t* __restrict__ crank, int32_t* __restrict__ ocount,
+                                   int32_t* __restrict__ ntask) {
+    const int64_t cur = cr[m];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cur || q < m; q += stride) {
+        if (q < m) {
+            const int32_t oc = pos[cr[q + 1]] - pos[cr[q]];
+            ocount[q] = oc;
+            ntask[q] = (oc + kTriTask - 1) / kTriTask;
+        }
+        if (q < cur) {
+            const int32_t i = row_of[q], rb = cr[i];
+            const int32_t before = pos[q] - pos[rb];            // oriented entries before q in its row
+            const int32_t oc = pos[cr[i + 1]] - pos[rb];
+            const bool o = pos[q + 1] != pos[q];
+            const int32_t np = o ? rb + before : rb + oc + (int32_t)(q - rb) - before;
+            const int32_t j = cc[q];
+            out_col[np] = j;
+            crank[np] = rank[j];
+        }
+    }
+}
+
+// Mirror of every entry and each row's diagonal position in the partitioned
+// layout: (j, i) lies in the oriented part of row j when i is ranked above j.
+__global__ void k_trikt_part_mirror(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
+                                    const int32_t* __restrict__ row_of, const int32_t* __restrict__ crank,
+                                    const int32_t* __restrict__ ocount, int64_t nnz, int32_t* __restrict__ mir,
+                                    int32_t* __restrict__ dpos) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t i = row_of[q], j = cc[q];
+        if (i == j) {
+            dpos[i] = (int32_t)q;
+            mir[q] = (int32_t)q;
+            continue;
+        }
+        // rank of i: the mirror's rank; q is oriented in row i iff rank(j) > rank(i)
+        const bool q_oriented = (int64_t)q - cr[i] < ocount[i];
+        const int32_t b = q_oriented ? cr[j] + ocount[j] : cr[j];  // i ranks below j: the rest of row j
+        const int32_t e = q_oriented ? cr[j + 1] : cr[j] + ocount[j];
+        mir[q] = b + lower_bound_i32(cc + b, e - b, i);
+    }
+}
+
+// Keep flags: an oriented entry's support is its count, another entry's the
+// count of its mirror (plus one per diagonal entry of its two rows); a
+// diagonal entry's support is its row's length. Work counters as for an
+// upper-triangle support product.
+__global__ void k_trikt_flags(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
+                              const int32_t* __restrict__ row_of, const int32_t* __restrict__ mir,
+                              const int32_t* __restrict__ ocount, const int32_t* __restrict__ dpos,
+                              const int32_t* __restrict__ sup, int64_t m, int64_t cap, int k,
+                              const int32_t* __restrict__ gid, const int32_t* __restrict__ done_g,
+                              const int32_t* __restrict__ kg, int32_t* __restrict__ flag,
+                              unsigned long long* __restrict__ ctr) {
+    const int64_t cur = cr[m];
+    unsigned long long prod = 0, mask = 0;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cap; q += (int64_t)gridDim.x * blockDim.x) {
+        int32_t keep = 0;
+        if (q < cur) {
+            const int32_t i = row_of[q], j = cc[q];
+            const int32_t rb = cr[i], re = cr[i + 1], oc = ocount[i];
+            int32_t s;
+            if (i == j) s = re - rb;
+            else s = sup[q - rb < oc ? q : mir[q]] + (dpos[i] >= 0) + (dpos[j] >= 0);
+            if (kg) {
+                const int g = gid[i];
+                keep = done_g[g] != 0 || s >= kg[g] - 2;
+            } else {
+                keep = s >= k - 2;
+                if (!keep && gid) keep = done_g[gid[i]] != 0;
+            }
+            // the row's largest column: the last of either part
+            const int32_t cmax = max(oc > 0 ? cc[rb + oc - 1] : -1, re > rb + oc ? cc[re - 1] : -1);
+            if (j >= i) ++mask;
+            if (cmax >= i) prod += (unsigned long long)(cr[j + 1] - cr[j]);
+        }
+        flag[q] = keep;
+    }
+    prod = warp_sum<unsigned long long>(prod);
+    mask = warp_sum<unsigned long long>(mask);
+    if ((threadIdx.x & 31) == 0) {
+        if (prod) atomicAdd(&ctr[GA_CTR_PRODUCTS], prod);
+        if (mask) atomicAdd(&ctr[GA_CTR_MASK_ENTRIES], mask);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(&ctr[GA_CTR_LAUNCHES], 1ull);
+        atomicAdd(&ctr[GA_CTR_A_ENTRIES], (unsigned long long)cur);
+        atomicAdd(&ctr[GA_CTR_ROWS], (unsigned long long)m);
+    }
+}
+
+// After the flags' scan: kept entries move to pos[q] (columns, rows, column
+// ranks), pos_new[q] is the new position or -1, the new row starts are
+// tr[i] = pos[cr[i]]; per row the oriented count shrinks to the kept
+// oriented entries (updated in place: unchanged when nothing was pruned) and
+// the next iteration's task count follows.
+__global__ void k_trikt_scatter(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
+                                const int32_t* __restrict__ pos, const int32_t* __restrict__ row_of,
+                                const int32_t* __restrict__ crank, int64_t m, int32_t* __restrict__ ocount,
+                                int32_t* __restrict__ ntask, int32_t* __restrict__ tc, int32_t* __restrict__ tr,
+                                int32_t* __restrict__ pos_new, int32_t* __restrict__ trow,
+                                int32_t* __restrict__ tcrank) {
+    const int64_t cur = cr[m];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cur || q <= m; q += stride) {
+        if (q <= m) {
+            tr[q] = pos[cr[q]];
+            if (q < m) {
+                const int32_t rb = cr[q];
+                const int32_t oc = pos[rb + ocount[q]] - pos[rb];
+                ocount[q] = oc;
+                ntask[q] = (oc + kTriTask - 1) / kTriTask;
+            }
+        }
+        if (q < cur) {
+            const int32_t d = pos[q];
+            const bool keep = pos[q + 1] != d;
+            if (keep) {
+                tc[d] = cc[q];
+                trow[d] = row_of[q];
+                tcrank[d] = crank[q];
+            }
+            pos_new[q] = keep ? d : -1;
+        }
+    }
+}
+
+__global__ void k_trikt_copyback(const KtState* st, int64_t m, const int32_t* __restrict__ pos_new,
+                                 const int32_t* __restrict__ tcrank, int32_t* __restrict__ crank,
+                                 int32_t* __restrict__ dpos) {
+    if (!st->swapped) return;
+    const int64_t nnz = st->nnz;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nnz || q < m; q += stride) {
+        if (q < nnz) crank[q] = tcrank[q];
+        if (q < m && dpos[q] >= 0) dpos[q] = pos_new[dpos[q]];
+    }
+}
+
+// Rows back in column order: an entry's place in its row is its index in its
+// part plus the entries of the other part with smaller columns.
+__global__ void k_trikt_unpart(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc,
+                               const int32_t* __restrict__ row_of, const int32_t* __restrict__ ocount, int64_t nnz,
+                               int32_t* __restrict__ out_col) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t i = row_of[q], rb = cr[i], re = cr[i + 1], oc = ocount[i];
+        const int32_t k = (int32_t)(q - rb);
+        const bool o = k < oc;
+        const int32_t ob = o ? rb + oc : rb, oe = o ? re : rb + oc;
+        const int32_t j = cc[q];
+        out_col[rb + (o ? k : k - oc) + lower_bound_i32(cc + ob, oe - ob, j)] = j;
+    }
+}
+
+namespace {
+size_t trikt_carve(void* scratch, int64_t m, int64_t cap, TriKt* t) {
+    const size_t c = (size_t)(cap > 0 ? cap : 1), r = (size_t)m + 2;
+    unsigned char* base = static_cast<unsigned char*>(scratch);
+    size_t off = 0;
+    auto take = [&](size_t count) {
+        int32_t* p = base ? reinterpret_cast<int32_t*>(base + off) : nullptr;
+        off += align256(sizeof(int32_t) * count);
+        return p;
+    };
+    TriKt s;
+    s.crank = take(c);
+    s.tcrank = take(c);
+    s.ocount = take(r);
+    s.tstart = take(r);
+    s.task_row = take(task_cap(m, cap));
+    s.dpos = take(r);
+    s.scan_scr = base ? base + off : nullptr;
+    off += align256(scan_scratch_bytes((cap > m ? cap : m) + 2));
+    if (t) *t = s;
+    return off;
+}
+}  // namespace
+
+size_t tri_kt_bytes(int64_t m, int64_t cap) { return trikt_carve(nullptr, m, cap, nullptr); }
+
+void tri_kt_carve(void* scratch, int64_t m, int64_t cap, TriKt* t) { trikt_carve(scratch, m, cap, t); }
+
+void tri_kt_setup(ga_ctx ctx, ga_csr C, const int32_t* row_of, int32_t* mir, int32_t* tmp_col, int32_t* tmp_flag,
+                  const TriKt& t, int64_t cap) {
+    const int64_t m = C->m, nnz = C->nnz;
+    // ranks by degree (or index) into task_row, which the loop fills later
+    int32_t* rank = t.task_row;
+    const int grid_v = grid_for(m, 256, ctx->num_sms * 8);
+    if (ctx->tune.tri_order == 1) {
+        k_tri_iota<<<grid_v, 256, 0, ctx->stream>>>(m, rank);
+        post_launch("tri_iota");
+    } else {
+        GA_CUDA(cudaMemsetAsync(t.tstart, 0, sizeof(int32_t) * (size_t)(m + 2), ctx->stream));
+        k_tri_deg_count<<<grid_v, 256, 0, ctx->stream>>>(C->rst, m, t.tstart);
+        post_launch("tri_deg_count");
+        scan_exclusive_i32_scratch(ctx, t.tstart, t.tstart, m + 1, t.scan_scr);
+        k_tri_rank<<<grid_v, 256, 0, ctx->stream>>>(C->rst, m, t.tstart, rank);
+        post_launch("tri_rank");
+    }
+    const int grid_ent = grid_for(cap, 256, ctx->num_sms * 16);
+    k_trikt_part_flags<<<grid_ent, 256, 0, ctx->stream>>>(C->rst, C->col, row_of, rank, m, cap, tmp_flag);
+    post_launch("trikt_part_flags");
+    scan_exclusive_i32_scratch(ctx, tmp_flag, tmp_flag, cap, t.scan_scr);
+    k_trikt_part_place<<<grid_for(m + cap, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+        C->rst, C->col, row_of, rank, tmp_flag, m, tmp_col, t.crank, t.ocount, t.tstart);
+    post_launch("trikt_part_place");
+    if (nnz) GA_CUDA(cudaMemcpyAsync(C->col, tmp_col, sizeof(int32_t) * (size_t)nnz, cudaMemcpyDeviceToDevice,
+                                     ctx->stream));
+    GA_CUDA(cudaMemsetAsync(t.dpos, 0xff, sizeof(int32_t) * (size_t)m, ctx->stream));
+    if (nnz) {
+        k_trikt_part_mirror<<<grid_for(nnz, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(
+            C->rst, C->col, row_of, t.crank, t.ocount, nnz, mir, t.dpos);
+        post_launch("trikt_part_mirror");
+    }
+}
+
+void tri_kt_support(ga_ctx ctx, ga_csr C, int32_t* sup, const TriKt& t, int64_t cap) {
+    const int64_t m = C->m;
+    {
+        ProfScope ps(ctx, "tri_orient");
+        GA_CUDA(cudaMemsetAsync(sup, 0, sizeof(int32_t) * (size_t)cap, ctx->stream));
+        scan_exclusive_i32_scratch(ctx, t.tstart, t.tstart, m, t.scan_scr);
+        k_tri_tasklist<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(t.tstart, m, t.task_row);
+        post_launch("tri_tasklist");
+    }
+    ProfScope ps(ctx, "tri_support");
+    k_tri_support<false><<<ctx->num_sms * tri_blocks_per_sm<false>(), kTriThreads, 0, ctx->stream>>>(
+        C->rst, t.ocount, C->col, t.crank, t.tstart, t.task_row, m, sup, ctx->d_counters, nullptr, nullptr);
+    post_launch("tri_support");
+}
+
+void tri_kt_flags(ga_ctx ctx, ga_csr C, const int32_t* row_of, const int32_t* mir, const int32_t* sup,
+                  const TriKt& t, int64_t cap, int k, const KtBatch* batch, int32_t* flag) {
+    k_trikt_flags<<<grid_for(cap, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(
+        C->rst, C->col, row_of, mir, t.ocount, t.dpos, sup, C->m, cap, k, batch ? batch->gid : nullptr,
+        batch ? batch->done_g : nullptr, batch ? batch->kg : nullptr, flag, ctx->d_counters);
+    post_launch("trikt_flags");
+}
+
+void tri_kt_scatter(ga_ctx ctx, ga_csr C, const int32_t* pos, const int32_t* row_of, const TriKt& t, int64_t cap,
+                    int32_t* tc, int32_t* tr, int32_t* pos_new, int32_t* trow) {
+    k_trikt_scatter<<<grid_for(C->m + cap, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+        C->rst, C->col, pos, row_of, t.crank, C->m, t.ocount, t.tstart, tc, tr, pos_new, trow, t.tcrank);
+    post_launch("trikt_scatter");
+}
+
+void tri_kt_copyback(ga_ctx ctx, const KtState* st, int64_t m, const int32_t* pos_new, const TriKt& t,
+                     int64_t cap) {
+    k_trikt_copyback<<<grid_for(m + cap, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(st, m, pos_new, t.tcrank,
+                                                                                      t.crank, t.dpos);
+    post_launch("trikt_copyback");
+}
+
+void tri_kt_finish(ga_ctx ctx, ga_csr C, const int32_t* row_of, const TriKt& t, int32_t* tmp_col) {
+    const int64_t nnz = C->nnz;
+    if (nnz == 0) return;
+    k_trikt_unpart<<<grid_for(nnz, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(C->rst, C->col, row_of, t.ocount,
+                                                                                   nnz, tmp_col);
+    post_launch("trikt_unpart");
+    GA_CUDA(cudaMemcpyAsync(C->col, tmp_col, sizeof(int32_t) * (size_t)nnz, cudaMemcpyDeviceToDevice, ctx->stream));
 }
 
 }  // namespace ga
