@@ -546,6 +546,10 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
             }
             k_kt_finalize<<<1, 32, 0, ctx->stream>>>(st.p, tr.p, m, ctl);
             post_launch("kt_finalize");
+            if (tri) {
+                tri_kt_copyback(ctx, C, st.p, tr.p, tc.p, trow.p, mir_new.p, pos_new.p, row_of.p, mir.p, tk, cap);
+                return;
+            }
             k_kt_copyback<<<grid_copy, 256, 0, ctx->stream>>>(st.p, tr.p, tc.p, m, C->rst, C->col,
                                                               static_cast<int32_t*>(C->val));
             post_launch("kt_copyback");
@@ -553,7 +557,6 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
                 k_kt_copyback_aux<<<grid_ent, 256, 0, ctx->stream>>>(st.p, trow.p, mir_new.p, row_of.p, mir.p);
                 post_launch("kt_copyback_aux");
             }
-            if (tri) tri_kt_copyback(ctx, st.p, m, pos_new.p, tk, cap);
         };
         const bool saved = ctx->device_loops;
         if (algo == GA_NAIVE) ctx->device_loops = false;  // naive allocates per call

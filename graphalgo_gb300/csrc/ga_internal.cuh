@@ -250,9 +250,11 @@ void tri_kt_flags(ga_ctx ctx, ga_csr C, const int32_t* row_of, const int32_t* mi
 // and new positions (pos_new), and of the resident arrays.
 void tri_kt_scatter(ga_ctx ctx, ga_csr C, const int32_t* pos, const int32_t* row_of, const TriKt& t, int64_t cap,
                     int32_t* tc, int32_t* tr, int32_t* pos_new, int32_t* trow);
-// With the iteration's swap: the resident arrays follow C.
-void tri_kt_copyback(ga_ctx ctx, const KtState* st, int64_t m, const int32_t* pos_new, const TriKt& t,
-                     int64_t cap);
+// With the iteration's swap: C <- the pruned matrix (tr, tc, values 1), and
+// rows, mirrors (mir_new), column ranks and diagonal positions follow it.
+void tri_kt_copyback(ga_ctx ctx, ga_csr C, const KtState* st, const int32_t* tr, const int32_t* tc,
+                     const int32_t* trow, const int32_t* mir_new, const int32_t* pos_new, int32_t* row_of,
+                     int32_t* mir, const TriKt& t, int64_t cap);
 // After the loop: every row back in column order.
 void tri_kt_finish(ga_ctx ctx, ga_csr C, const int32_t* row_of, const TriKt& t, int32_t* tmp_col);
 

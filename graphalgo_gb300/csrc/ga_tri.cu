@@ -643,15 +643,29 @@ __global__ void k_trikt_scatter(const int32_t* __restrict__ cr, const int32_t* _
     }
 }
 
-__global__ void k_trikt_copyback(const KtState* st, int64_t m, const int32_t* __restrict__ pos_new,
-                                 const int32_t* __restrict__ tcrank, int32_t* __restrict__ crank,
+// When the iteration swapped: C <- the pruned matrix (row starts, columns,
+// values 1), and the per-entry arrays (rows, mirrors, column ranks) and the
+// diagonal positions follow it; one launch for all of them.
+__global__ void k_trikt_copyback(const KtState* st, int64_t m, const int32_t* __restrict__ tr,
+                                 const int32_t* __restrict__ tc, const int32_t* __restrict__ trow,
+                                 const int32_t* __restrict__ mir_new, const int32_t* __restrict__ pos_new,
+                                 const int32_t* __restrict__ tcrank, int32_t* __restrict__ cr,
+                                 int32_t* __restrict__ cc, int32_t* __restrict__ cv, int32_t* __restrict__ row_of,
+                                 int32_t* __restrict__ mir, int32_t* __restrict__ crank,
                                  int32_t* __restrict__ dpos) {
     if (!st->swapped) return;
     const int64_t nnz = st->nnz;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nnz || q < m; q += stride) {
-        if (q < nnz) crank[q] = tcrank[q];
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nnz || q <= m; q += stride) {
+        if (q <= m) cr[q] = tr[q];
         if (q < m && dpos[q] >= 0) dpos[q] = pos_new[dpos[q]];
+        if (q < nnz) {
+            cc[q] = tc[q];
+            cv[q] = 1;
+            row_of[q] = trow[q];
+            mir[q] = mir_new[q];
+            crank[q] = tcrank[q];
+        }
     }
 }
 
@@ -762,10 +776,12 @@ void tri_kt_scatter(ga_ctx ctx, ga_csr C, const int32_t* pos, const int32_t* row
     post_launch("trikt_scatter");
 }
 
-void tri_kt_copyback(ga_ctx ctx, const KtState* st, int64_t m, const int32_t* pos_new, const TriKt& t,
-                     int64_t cap) {
-    k_trikt_copyback<<<grid_for(m + cap, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(st, m, pos_new, t.tcrank,
-                                                                                      t.crank, t.dpos);
+void tri_kt_copyback(ga_ctx ctx, ga_csr C, const KtState* st, const int32_t* tr, const int32_t* tc,
+                     const int32_t* trow, const int32_t* mir_new, const int32_t* pos_new, int32_t* row_of,
+                     int32_t* mir, const TriKt& t, int64_t cap) {
+    k_trikt_copyback<<<grid_for(C->m + cap, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+        st, C->m, tr, tc, trow, mir_new, pos_new, t.tcrank, C->rst, C->col, static_cast<int32_t*>(C->val), row_of,
+        mir, t.crank, t.dpos);
     post_launch("trikt_copyback");
 }
 
