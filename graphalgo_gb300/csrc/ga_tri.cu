@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(kTriThreads, 10) k_tri_support(const int32_t* 
             const int32_t evs = __shfl_sync(FULL, vs, e);
             const int32_t evn = __shfl_sync(FULL, vn, e);
             const int32_t ev = __shfl_sync(FULL, v, e);
-            int32_t found = 0;
+            uint32_t mine = 0;  // this lane's hits for the entry
             // one round of 32 wedges: the lane's wedge x of the entry, ld its
             // loaded rank (column when the list is not counted)
             auto probe = [&](int32_t x, int32_t ld) {
@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(kTriThreads, 10) k_tri_support(const int32_t* 
                     const int32_t w = __ldg(ocol + wp);
                     atomicAdd(per_row + max(max(u, ev), w), 1ull);
                 }
-                found += __popc(__ballot_sync(FULL, hit));
+                mine += hit ? 1u : 0u;
             };
             // two rounds per pass, both loads issued first
             const int32_t* src = counted ? orank : ocol;
@@ -287,6 +287,7 @@ __global__ void __launch_bounds__(kTriThreads, 10) k_tri_support(const int32_t* 
                 probe(x0, l0);
                 if (base + 32 < evn) probe(x1, l1);  // warp-uniform
             }
+            const int32_t found = (int32_t)__reduce_add_sync(FULL, mine);
             if (lane == 0) {
                 wedges += (unsigned long long)evn;
                 tris += (unsigned long long)found;
