@@ -231,14 +231,14 @@ __global__ void __launch_bounds__(kTriThreads, 10) k_tri_support(const int32_t* 
             const int32_t ev = __shfl_sync(FULL, v, e);
             uint32_t mine = 0;  // this lane's hits for the entry
             // one round of 32 wedges: the lane's wedge x of the entry, ld its
-            // loaded rank (column when the list is not counted)
+            // loaded rank (column when the list is not counted); INT32_MAX
+            // past the list's end, which no lookup matches
             auto probe = [&](int32_t x, int32_t ld) {
-                const bool valid = x < evn;
                 const int32_t wp = evs + x;
                 bool hit = false;
                 if (counted) {
                     // ranks above the window are above every member
-                    const int32_t b = valid ? ld - win0 : kTriWin;
+                    const int32_t b = ld - win0;
                     if ((uint32_t)b < (uint32_t)kTriWin) {
                         const uint2 wd = words[b >> 5];
                         const uint32_t bit = 1u << (b & 31);
@@ -259,9 +259,9 @@ __global__ void __launch_bounds__(kTriThreads, 10) k_tri_support(const int32_t* 
                         }
                     }
                 } else {
-                    const int32_t w = valid ? ld : INT32_MAX;
+                    const int32_t w = ld;
                     const int bb = warp_lower_bound(key, w);
-                    if (valid && bb < 32) {
+                    if (bb < 32) {
                         const int lo_b = (int)(((int64_t)bb * un) >> 5);
                         const int hi_b = (int)(((int64_t)(bb + 1) * un) >> 5);
                         const int t = lo_b + lower_bound_i32(Ou + lo_b, hi_b - lo_b, w);
@@ -282,8 +282,8 @@ __global__ void __launch_bounds__(kTriThreads, 10) k_tri_support(const int32_t* 
             const int32_t* src = counted ? orank : ocol;
             for (int32_t base = 0; base < evn; base += 64) {
                 const int32_t x0 = base + lane, x1 = x0 + 32;
-                const int32_t l0 = x0 < evn ? __ldg(src + evs + x0) : 0;
-                const int32_t l1 = x1 < evn ? __ldg(src + evs + x1) : 0;
+                const int32_t l0 = x0 < evn ? __ldg(src + evs + x0) : INT32_MAX;
+                const int32_t l1 = x1 < evn ? __ldg(src + evs + x1) : INT32_MAX;
                 probe(x0, l0);
                 if (base + 32 < evn) probe(x1, l1);  // warp-uniform
             }
