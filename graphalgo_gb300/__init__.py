@@ -40,7 +40,7 @@ TUNE_KTRUSS, TUNE_PRODUCT, TUNE_TC = 0, 1, 2
 EDGES_MIRROR, EDGES_DROP_LOOPS, EDGES_LOWER_SYMM, EDGES_UNIT = 1, 2, 4, 8
 # status codes
 OK, ERR_INVALID_ARG, ERR_INVALID_CSR, ERR_SHAPE, ERR_DTYPE, ERR_CUDA, ERR_OOM, ERR_NO_DEVICE, \
-    ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_ADMISSION = range(11)
+    ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_ADMISSION, ERR_CANCELLED = range(12)
 
 _NP = {INT32: np.int32, INT64: np.int64, FP32: np.float32, FP64: np.float64, UINT8: np.uint8}
 _DT = {np.dtype(v): k for k, v in _NP.items()}
@@ -629,7 +629,7 @@ class ServerResult(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [(n, _i64) for n in ("submitted", "completed", "failed", "rejected", "calls", "batched_calls",
                                     "batched_requests", "max_group", "max_in_flight", "budget", "reserved",
-                                    "peak_reserved", "queued")]
+                                    "peak_reserved", "queued", "cancelled")]
 
 
 def request_bytes_bound(req_type: int, m: int, nnz: int, param: int = 0) -> int:
@@ -709,6 +709,15 @@ class Server:
             lib().ga_server_release(self.handle, _i64(rid))
         return out
 
+    def cancel(self, rid: int) -> bool:
+        """Cancels a request that has not started; False when it already runs
+        or ran (it then completes normally)."""
+        rc = lib().ga_server_cancel(self.handle, _i64(rid))
+        if rc == ERR_UNSUPPORTED:
+            return False
+        _check(rc)
+        return True
+
     def drain(self, timeout: float = 0.0):
         _check(lib().ga_server_drain(self.handle, ctypes.c_double(timeout)))
 
@@ -754,6 +763,24 @@ def autotune(kind: int, A: Csr, B: Optional[Csr] = None, M: Optional[Csr] = None
     out = {n: getattr(r, n) for n, _ in TuneResult._fields_}
     out["algo"] = ALGO_NAMES.get(r.algo, r.algo)
     return out
+
+
+def tune_save(path: str) -> int:
+    """Writes the process-wide tuning cache to a file; returns the entries."""
+    n = _i64()
+    _check(lib().ga_tune_save(os.fsencode(path), ctypes.byref(n)))
+    return int(n.value)
+
+
+def tune_load(path: str) -> int:
+    """Adds a saved tuning cache's entries; returns how many."""
+    n = _i64()
+    _check(lib().ga_tune_load(os.fsencode(path), ctypes.byref(n)))
+    return int(n.value)
+
+
+def tune_clear() -> None:
+    _check(lib().ga_tune_clear())
 
 
 def apply_schedule(ctx: Context, tuned: dict) -> None:

@@ -232,6 +232,7 @@ const char* ga_status_string(int s) {
     case GA_ERR_TIMEOUT: return "device wait timed out";
     case GA_ERR_UNSUPPORTED: return "unsupported";
     case GA_ERR_ADMISSION: return "admission refused";
+    case GA_ERR_CANCELLED: return "cancelled";
     }
     return "unknown status";
 }

@@ -517,6 +517,24 @@ int ga_server_wait(ga_server srv, int64_t req_id, double timeout_s, ga_server_re
     return GA_OK;
 }
 
+int ga_server_cancel(ga_server srv, int64_t req_id) {
+    if (!srv) return GA_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    auto it = srv->reqs.find(req_id);
+    if (it == srv->reqs.end()) return GA_ERR_INVALID_ARG;
+    SrvReq* r = it->second.get();
+    auto q = std::find(srv->queue.begin(), srv->queue.end(), r);
+    if (q == srv->queue.end()) return GA_ERR_UNSUPPORTED;  // started or done: it runs to completion
+    srv->queue.erase(q);
+    r->res.status = GA_ERR_CANCELLED;
+    r->res.t_start = r->res.t_end = srv->now();
+    r->error = "cancelled before it started";
+    r->done = true;
+    srv->st.cancelled += 1;
+    srv->cv_done.notify_all();
+    return GA_OK;
+}
+
 int ga_server_release(ga_server srv, int64_t req_id) {
     if (!srv) return GA_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> lk(srv->mu);

@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <functional>
 #include <mutex>
 #include <tuple>
@@ -298,6 +299,78 @@ int ga_autotune_variant(ga_ctx ctx, int kind, int algo, ga_csr A, ga_csr B, ga_c
         out->cached = cached ? 1 : 0;
         out->tri_order = e.t.tri_order;
     });
+}
+
+// Cache file: one line per entry, "ga_tune 1" then the key's nine fields
+// (device, kind, size buckets of m, n, nnz(A), nnz(B), nnz(M), shape,
+// restriction) and the entry (variant, warp threshold, heavy threshold, CTAs
+// per SM, inner-product chunk, hybrid ratio, vertex order, its time, the
+// default's time, candidates).
+int ga_tune_save(const char* path, int64_t* entries) {
+    if (!path) return GA_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    FILE* f = fopen(path, "w");
+    if (!f) return GA_ERR_INVALID_ARG;
+    int64_t n = 0;
+    for (const auto& kv : g_tune_cache) {
+        const TuneKey& k = kv.first;
+        const TuneEntry& e = kv.second;
+        fprintf(f, "ga_tune 1 %d %d %d %d %d %d %d %d %d  %d %lld %lld %d %d %lld %d %.9g %.9g %d\n",
+                std::get<0>(k), std::get<1>(k), std::get<2>(k), std::get<3>(k), std::get<4>(k), std::get<5>(k),
+                std::get<6>(k), std::get<7>(k), std::get<8>(k), (int)e.algo, (long long)e.t.warp_max_flops,
+                (long long)e.t.heavy_flops, e.t.ctas_per_sm, e.t.dot_chunk, (long long)e.t.hybrid_ratio,
+                e.t.tri_order, e.ms, e.default_ms, e.candidates);
+        ++n;
+    }
+    const bool ok = fclose(f) == 0;
+    if (entries) *entries = n;
+    return ok ? GA_OK : GA_ERR_INVALID_ARG;
+}
+
+int ga_tune_load(const char* path, int64_t* entries) {
+    if (!path) return GA_ERR_INVALID_ARG;
+    FILE* f = fopen(path, "r");
+    if (!f) return GA_ERR_INVALID_ARG;
+    std::vector<std::pair<TuneKey, TuneEntry>> got;
+    char line[512];
+    int rc = GA_OK;
+    while (fgets(line, sizeof(line), f)) {
+        int ver = 0, k[9], algo = 0, ctas = 0, chunk = 0, order = 0, cands = 0;
+        long long warp = 0, heavy = 0, ratio = 0;
+        double ms = 0, dms = 0;
+        const int got_fields = sscanf(line, "ga_tune %d %d %d %d %d %d %d %d %d %d %d %lld %lld %d %d %lld %d %lg %lg %d",
+                                      &ver, &k[0], &k[1], &k[2], &k[3], &k[4], &k[5], &k[6], &k[7], &k[8], &algo,
+                                      &warp, &heavy, &ctas, &chunk, &ratio, &order, &ms, &dms, &cands);
+        if (got_fields != 20 || ver != 1 || algo < GA_MSA || algo > GA_TRI || algo == GA_AUTO || ctas < 0 ||
+            chunk < 1 || chunk > 4096 || ratio < 0 || (order != 0 && order != 1)) {
+            rc = GA_ERR_INVALID_ARG;  // a malformed file loads nothing
+            break;
+        }
+        TuneEntry e;
+        e.algo = (ga_algo)algo;
+        e.t.warp_max_flops = warp;
+        e.t.heavy_flops = heavy;
+        e.t.ctas_per_sm = ctas;
+        e.t.dot_chunk = chunk;
+        e.t.hybrid_ratio = ratio;
+        e.t.tri_order = order;
+        e.ms = ms;
+        e.default_ms = dms;
+        e.candidates = cands;
+        got.emplace_back(TuneKey{k[0], k[1], k[2], k[3], k[4], k[5], k[6], k[7], k[8]}, e);
+    }
+    fclose(f);
+    if (rc != GA_OK) return rc;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (const auto& kv : got) g_tune_cache[kv.first] = kv.second;
+    if (entries) *entries = (int64_t)got.size();
+    return GA_OK;
+}
+
+int ga_tune_clear(void) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache.clear();
+    return GA_OK;
 }
 
 }  // extern "C"

@@ -82,7 +82,8 @@ enum {
     GA_ERR_NO_DEVICE = 7,   /* no CUDA device / the kernels are not loadable */
     GA_ERR_TIMEOUT = 8,     /* a bounded device wait expired */
     GA_ERR_UNSUPPORTED = 9,
-    GA_ERR_ADMISSION = 10   /* request refused: HBM bound exceeded */
+    GA_ERR_ADMISSION = 10,  /* request refused: HBM bound exceeded */
+    GA_ERR_CANCELLED = 11   /* request cancelled before it started */
 };
 
 /* ------------------------------------------------------------------ context */
@@ -403,6 +404,14 @@ GA_API int ga_autotune(ga_ctx ctx, int kind, ga_csr A, ga_csr B, ga_csr M, int f
  * with ga_ctx_set_option and call with that variant. */
 GA_API int ga_autotune_variant(ga_ctx ctx, int kind, int algo, ga_csr A, ga_csr B, ga_csr M, int force,
                                ga_tune_result* out);
+/* The process-wide tuning cache as a text file (one line per problem
+ * signature and its choice), so later processes start tuned: save writes
+ * every entry, load adds the file's entries (a malformed file loads nothing
+ * and gives GA_ERR_INVALID_ARG), clear empties the cache. entries (may be
+ * NULL) receives the number written or read. */
+GA_API int ga_tune_save(const char* path, int64_t* entries);
+GA_API int ga_tune_load(const char* path, int64_t* entries);
+GA_API int ga_tune_clear(void);
 
 /* ------------------------------------------------------ batched graphs */
 /* Many independent graphs as one block-diagonal matrix: rows (and columns)
@@ -488,6 +497,7 @@ typedef struct {
     int64_t submitted, completed, failed, rejected;
     int64_t calls, batched_calls, batched_requests, max_group, max_in_flight;
     int64_t budget, reserved, peak_reserved, queued;
+    int64_t cancelled;
 } ga_server_stats;
 /* Upper bound on the device bytes of one request (type GA_REQ_*, graph of m
  * vertices and nnz stored entries; param = number of BC sources). */
@@ -516,6 +526,10 @@ GA_API int ga_server_submit(ga_server srv, int type, int graph, int k, const int
  * GA_ERR_TIMEOUT). The result's arrays stay valid until ga_server_release. */
 GA_API int ga_server_wait(ga_server srv, int64_t req_id, double timeout_s, ga_server_result* res);
 GA_API int ga_server_release(ga_server srv, int64_t req_id);
+/* Cancels a request that is still queued: it completes at once with status
+ * GA_ERR_CANCELLED (wait and release it as any other). A request that has
+ * started runs to completion: GA_ERR_UNSUPPORTED. */
+GA_API int ga_server_cancel(ga_server srv, int64_t req_id);
 /* Blocks until the queue is empty and no call is in flight. */
 GA_API int ga_server_drain(ga_server srv, double timeout_s);
 GA_API int ga_server_get_stats(ga_server srv, ga_server_stats* stats);

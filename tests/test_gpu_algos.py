@@ -49,6 +49,10 @@ def test_tc_other_forms(ctx):
     ref = np.array([int(sq[G.rst[i]:G.rst[i + 1]].sum()) >> 1 for i in range(G.m)], np.int32)
     assert np.array_equal(ga.tc_vertex("msa", Gd), ref)
     assert int(ref.sum()) == 3 * total
+    # triangle listing for the per-vertex form (C<A> = A*A of a symmetric 0/1
+    # matrix); the L*U form's operands differ, so GA_TRI runs the hybrid form
+    assert np.array_equal(ga.tc_vertex("tri", Gd), ref)
+    assert ga.tc_lu("tri", Gd) == total
 
 
 @pytest.mark.parametrize("algo", ["msa", "mca", "heap", "dot", "hybrid", "tri"])

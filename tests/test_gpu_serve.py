@@ -210,3 +210,32 @@ def test_pool_from_device_and_files(ctx, tmp_path):
         for j in (1, 2, 3):
             _same(got[i], got[3 * j + i], reqs[i][0])
     assert got[0]["tc"] > 0
+
+
+def test_cancel_queued_requests(built):
+    """Requests still queued behind a busy single worker can be cancelled:
+    they complete with GA_ERR_CANCELLED; the others run normally."""
+    with ga.Server(0, workers=1, coalesce=False) as srv:
+        for m, rst, col in POOL:
+            srv.add_graph(m, rst, col)
+        big = len(POOL) - 5  # rmat12
+        m = POOL[big][0]
+        first = [srv.submit(ga.REQ_BC, big, sources=np.arange(min(256, m), dtype=np.int32)),
+                 srv.submit(ga.REQ_KTRUSS, big, k=3)]
+        rest = [srv.submit(ga.REQ_TC, g % len(POOL)) for g in range(20)]
+        cancelled = {rid: srv.cancel(rid) for rid in reversed(rest)}
+        assert any(cancelled.values())
+        for rid in first:
+            assert srv.wait(rid)["status"] == ga.OK
+        for rid in rest:
+            r = srv.wait(rid)
+            if cancelled[rid]:
+                assert r["status"] == ga.ERR_CANCELLED and r["error"]
+            else:
+                assert r["status"] == ga.OK and r["tc"] >= 0
+        st = srv.stats()
+        assert st["cancelled"] == sum(cancelled.values())
+        # a finished request cannot be cancelled
+        done = srv.submit(ga.REQ_TC, 0)
+        srv.wait(done, release=False)
+        assert srv.cancel(done) is False

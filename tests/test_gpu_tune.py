@@ -88,3 +88,19 @@ def test_batch_auto(ctx):
     Cm, im = ga.batch_ktruss("msa", U, voff, 4)
     assert np.array_equal(ia, im)
     assert all(np.array_equal(x, y) for x, y in zip(Ca.download(), Cm.download()))
+
+
+def test_tune_cache_file_restores_choices(ctx, rmat, tmp_path):
+    """A saved cache, loaded into a cleared process cache, answers GA_AUTO
+    without re-tuning and with the same choice."""
+    G, A = rmat
+    r1 = ga.autotune(ga.TUNE_KTRUSS, A, force=True)
+    path = str(tmp_path / "tune.txt")
+    assert ga.tune_save(path) >= 1
+    ga.tune_clear()
+    assert ga.tune_load(path) >= 1
+    r2 = ga.autotune(ga.TUNE_KTRUSS, A)
+    assert r2["cached"] == 1 and r2["algo"] == r1["algo"] and r2["tri_order"] == r1["tri_order"]
+    R, it = oracle.ktruss(G, 4)
+    C, git = ga.ktruss("auto", A, 4)
+    assert git == it and np.array_equal(C.download()[1], R.col)

@@ -83,3 +83,30 @@ def test_bench_workloads_are_seeded():
         if t == ga.REQ_BC:
             m = pool[g][1]
             assert len(src) == 32 and len(set(src.tolist())) == 32 and src.max() < m
+
+
+def test_tune_cache_file_round_trip(built, tmp_path):
+    """The tuning cache file: entries load, save back unchanged, a malformed
+    file loads nothing, clear empties the cache (no GPU involved)."""
+    src = tmp_path / "tune.txt"
+    lines = ["ga_tune 1 0 0 37 37 47 0 0 2 -1  7 32768 1048576 0 8 16 0 2.5 9.25 14",
+             "ga_tune 1 0 2 25 25 35 0 0 2 -1  4 32768 1048576 0 8 16 1 0.019 0.07 7"]
+    src.write_text("\n".join(lines) + "\n")
+    ga.tune_clear()
+    assert ga.tune_load(str(src)) == 2
+    out = tmp_path / "saved.txt"
+    assert ga.tune_save(str(out)) == 2
+    saved = sorted(" ".join(l.split()) for l in out.read_text().splitlines())
+    assert saved == sorted(" ".join(l.split()) for l in lines)
+    bad = tmp_path / "bad.txt"
+    bad.write_text(lines[0] + "\nga_tune 1 0 0 1 1 1 0 0 2 -1 5 0 0 0 8 16 0 1 1 1\n")  # GA_AUTO is no choice
+    with pytest.raises(ga.GaError):
+        ga.tune_load(str(bad))
+    with pytest.raises(ga.GaError):
+        ga.tune_load(str(tmp_path / "missing.txt"))
+    ga.tune_clear()
+    assert ga.tune_save(str(out)) == 0
+
+
+def test_server_cancel_rejects_null_server(built):
+    assert ga.lib().ga_server_cancel(None, ctypes.c_int64(1)) == ga.ERR_INVALID_ARG
