@@ -587,7 +587,11 @@ def run_gpu(args, dist: Dist):
         "work": {"products_per_step": wc["products"] / args.steps,
                  "executed_products_per_step": wc["executed"] / args.steps, "k_max": kmax,
                  "support_products_k3": per_k.get(args.kmin, {}).get("products"),
-                 "wedges_per_step": wc["wedges"] / args.steps, "triangles_per_step": wc["triangles"] / args.steps},
+                 "wedges_per_step": wc["wedges"] / args.steps, "triangles_per_step": wc["triangles"] / args.steps,
+                 "note": "value counts 2 x the Gustavson products of the reference's C<C> = C*C for every "
+                         "support product (products_per_step); the triangle-listing form computes the same "
+                         "values from wedges_per_step rank-ordered lookups, the Gustavson forms from "
+                         "executed_products_per_step products"},
         "kernel_profile": {"note": "one step with host-driven loops and CUDA events per launch (slower than "
                                    "the timed step); summed event time per kernel scope, ms",
                            "top": {k: round(v[1], 3) for k, v in
