@@ -295,3 +295,25 @@ def test_tri_tc_long_lists_and_loops(ctx, name, G):
     total, rows = oracle.tc_sandia(N)
     got, grow = ga.tc("tri", to_device(ctx, N))
     assert got == total and np.array_equal(grow, rows)
+
+
+def test_tri_ktruss_degenerate_inputs(ctx):
+    """k <= 2 keeps everything; graphs without entries, with diagonal entries
+    only, or without vertices, as the oracle has them."""
+    from graphs import dense_to_csr
+    rng = np.random.default_rng(17)
+    G = random_graph(40, 0.2, rng)
+    cases = [(G, k) for k in (1, 2)]
+    cases.append((dense_to_csr(np.zeros((30, 30), bool)), 3))           # no entries
+    cases.append((dense_to_csr(np.eye(25, dtype=bool)), 3))              # diagonal only
+    cases.append((dense_to_csr(np.eye(25, dtype=bool)), 4))
+    for H, k in cases:
+        R, it = oracle.ktruss(H, k)
+        C, git = ga.ktruss("tri", to_device(ctx, H), k)
+        r, c, v = C.download()
+        assert git == it and np.array_equal(r, R.rst) and np.array_equal(c, R.col), (H.m, H.nnz, k)
+        assert np.array_equal(v, R.val)
+        assert ga.tc("tri", to_device(ctx, H))[0] == oracle.tc_sandia(H)[0]
+    E = ga.Csr.upload(ctx, 0, 0, np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0, np.int32))
+    C, git = ga.ktruss("tri", E, 3)
+    assert C.nnz == 0 and git == 0
