@@ -7,14 +7,13 @@
 // (the triangles through edge {i, j}), plus 1 for each of i and j that holds
 // a diagonal entry; C(i, i) = |N(i)| (the row's length, diagonal included).
 // Every triangle is listed once: vertices get ranks 0..m-1 in order of
-// degree (a counting sort, once per call; or their indices), each undirected edge is kept in
-// the direction of increasing rank (the oriented list O_u of u holds the
-// neighbours ranked above u, in column order), and a triangle u < v < w (by
-// rank) is found as the wedge u -> v -> w with w in O_u. Its three edges'
-// counts are raised: (u, v) by the entry's ballot total, (u, w) in shared
-// memory, (v, w) by a global atomic. The counts go back to both mirror
-// entries of every edge. Integer counts: the result is exact whatever the
-// order, and whatever order ties of degree get.
+// degree (a counting sort, once per call; or their indices), each undirected
+// edge is kept in the direction of increasing rank (the oriented list O_u of
+// u holds the neighbours ranked above u, in column order), and a triangle
+// u < v < w (by rank) is found as the wedge u -> v -> w with w in O_u. Its
+// three edges' counts are raised: (u, v) by the entry's hit total, (u, w) in
+// shared memory, (v, w) by a global atomic. Integer counts: the result is
+// exact whatever the order, and whatever order ties of degree get.
 //
 // Lookups: each warp keeps a bitmap of O_u's members in a window of kTriWin
 // ranks ending at O_u's highest rank, with per-word popcount prefixes giving
@@ -24,8 +23,9 @@
 // also be the vertex indices (GA_OPT_TRI_ORDER): then the lists of a union
 // of small graphs span fewer ranks than the window and no search is needed.
 //
-// Per evaluation (all launches read the current entry count on the device, so
-// a captured loop whose matrix shrinks can replay them):
+// A single evaluation (ga_mxm_masked, triangle counting, the autotuner) builds
+// separate oriented lists; all launches read the current entry count on the
+// device:
 //   orient     rank flags per entry, diagonal flags, work counters
 //   scan       flags -> positions in the oriented lists
 //   scatter    oriented columns and their ranks, zeroed counts, oriented row
@@ -33,6 +33,10 @@
 //   scan       tasks per row -> task starts; task list
 //   support    one warp per task
 //   writeback  counts (+ diagonal terms) to both mirror entries; C(i, i)
+// The k-truss loop keeps the orientation in C itself instead (the `trikt`
+// kernels at the end of this file): every row is stored as [oriented part |
+// the rest] for the whole loop, so an iteration is task list, support, keep
+// flags and the prune.
 #include "ga_device.cuh"
 
 namespace ga {
