@@ -360,11 +360,15 @@ __global__ void k_kt_copyback(const KtState* st, const int32_t* __restrict__ tr,
 }
 
 // Position of the first entry of row i with column >= i (rows sorted).
+// With gid / done_g (batched k-truss), rows of graphs that have finished get
+// an empty upper part: their support is not needed again (they keep every
+// entry), so the product skips them.
 __global__ void k_upper_start(const int32_t* __restrict__ cr, const int32_t* __restrict__ cc, int64_t m,
-                              int32_t* __restrict__ ust) {
+                              int32_t* __restrict__ ust, const int32_t* __restrict__ gid = nullptr,
+                              const int32_t* __restrict__ done_g = nullptr) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t b = cr[i], n = cr[i + 1] - b;
-        ust[i] = b + lower_bound_i32(cc + b, n, (int32_t)i);
+        ust[i] = kt_keep_all(gid, done_g, i) ? b + n : b + lower_bound_i32(cc + b, n, (int32_t)i);
     }
 }
 
@@ -502,7 +506,8 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
             } else if (tri) {
                 tri_kt_support(ctx, C, sup.p, tk, cap);
             } else if (upper) {
-                k_upper_start<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(C->rst, C->col, m, ust.p);
+                k_upper_start<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+                    C->rst, C->col, m, ust.p, batch ? batch->gid : nullptr, batch ? batch->done_g : nullptr);
                 post_launch("kt_upper_start");
                 Cu = *C;
                 Cu.rst = ust.p;
@@ -527,7 +532,7 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
             }
             scan_exclusive_i32_scratch(ctx, eflag.p, eflag.p, cap, scan_scr.p);
             if (tri) {
-                tri_kt_scatter(ctx, C, eflag.p, row_of.p, tk, cap, tc.p, tr.p, pos_new.p, trow.p);
+                tri_kt_scatter(ctx, C, eflag.p, row_of.p, tk, cap, tc.p, tr.p, pos_new.p, trow.p, batch);
             } else {
                 k_kt_scatter<<<grid_copy, 256, 0, ctx->stream>>>(C->rst, C->col, eflag.p, m, tc.p, tr.p,
                                                                  upper ? pos_new.p : nullptr,

@@ -247,9 +247,10 @@ void tri_kt_support(ga_ctx ctx, ga_csr C, int32_t* sup, const TriKt& t, int64_t 
 void tri_kt_flags(ga_ctx ctx, ga_csr C, const int32_t* row_of, const int32_t* mir, const int32_t* sup,
                   const TriKt& t, int64_t cap, int k, const KtBatch* batch, int32_t* flag);
 // After the flags' scan (pos): compaction of C into tc / tr with rows (trow)
-// and new positions (pos_new), and of the resident arrays.
+// and new positions (pos_new), and of the resident arrays; rows of a batch's
+// finished graphs get no tasks in the next iteration.
 void tri_kt_scatter(ga_ctx ctx, ga_csr C, const int32_t* pos, const int32_t* row_of, const TriKt& t, int64_t cap,
-                    int32_t* tc, int32_t* tr, int32_t* pos_new, int32_t* trow);
+                    int32_t* tc, int32_t* tr, int32_t* pos_new, int32_t* trow, const KtBatch* batch);
 // With the iteration's swap: C <- the pruned matrix (tr, tc, values 1), and
 // rows, mirrors (mir_new), column ranks and diagonal positions follow it.
 void tri_kt_copyback(ga_ctx ctx, ga_csr C, const KtState* st, const int32_t* tr, const int32_t* tc,

@@ -622,7 +622,8 @@ __global__ void k_trikt_scatter(const int32_t* __restrict__ cr, const int32_t* _
                                 const int32_t* __restrict__ crank, int64_t m, int32_t* __restrict__ ocount,
                                 int32_t* __restrict__ ntask, int32_t* __restrict__ tc, int32_t* __restrict__ tr,
                                 int32_t* __restrict__ pos_new, int32_t* __restrict__ trow,
-                                int32_t* __restrict__ tcrank) {
+                                int32_t* __restrict__ tcrank, const int32_t* __restrict__ gid,
+                                const int32_t* __restrict__ done_g) {
     const int64_t cur = cr[m];
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cur || q <= m; q += stride) {
@@ -632,7 +633,8 @@ __global__ void k_trikt_scatter(const int32_t* __restrict__ cr, const int32_t* _
                 const int32_t rb = cr[q];
                 const int32_t oc = pos[rb + ocount[q]] - pos[rb];
                 ocount[q] = oc;
-                ntask[q] = (oc + kTriTask - 1) / kTriTask;
+                // rows of finished graphs (batches) need no more support
+                ntask[q] = gid && done_g[gid[q]] ? 0 : (oc + kTriTask - 1) / kTriTask;
             }
         }
         if (q < cur) {
@@ -775,9 +777,10 @@ void tri_kt_flags(ga_ctx ctx, ga_csr C, const int32_t* row_of, const int32_t* mi
 }
 
 void tri_kt_scatter(ga_ctx ctx, ga_csr C, const int32_t* pos, const int32_t* row_of, const TriKt& t, int64_t cap,
-                    int32_t* tc, int32_t* tr, int32_t* pos_new, int32_t* trow) {
+                    int32_t* tc, int32_t* tr, int32_t* pos_new, int32_t* trow, const KtBatch* batch) {
     k_trikt_scatter<<<grid_for(C->m + cap, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
-        C->rst, C->col, pos, row_of, t.crank, C->m, t.ocount, t.tstart, tc, tr, pos_new, trow, t.tcrank);
+        C->rst, C->col, pos, row_of, t.crank, C->m, t.ocount, t.tstart, tc, tr, pos_new, trow, t.tcrank,
+        batch ? batch->gid : nullptr, batch ? batch->done_g : nullptr);
     post_launch("trikt_scatter");
 }
 
