@@ -389,14 +389,14 @@ def profile_step(ga, ctx, run, algo, counters, loops):
 
 
 def other_configs(ga, ctx, args):
-    """The survey's other single-GPU configurations, measured beside the
-    headline: config 1 (triangle count of a seeded Erdos-Renyi graph, n=1000,
-    9,990 edges, uint8 values; latency, bit-exact against the oracle) and
-    config 3 (batched BC on R-MAT scale 20, 64 and 256 seeded sources, FP64;
-    GTEPS = sources * nnz / 2 / t)."""
+    """The other single-GPU workloads, measured beside the headline: the
+    triangle count of a seeded Erdos-Renyi graph (n=1000, 9,990 edges, uint8
+    values; latency, bit-exact against the oracle) and batched BC on R-MAT
+    scale 20 with 64 and 256 seeded sources (FP64; GTEPS = sources * nnz / 2
+    / t)."""
     import oracle
     out = {}
-    # config 1
+    # triangle count, Erdos-Renyi n = 1000
     m, rst, col = ga.gen_er(1000, 9990, seed=args.seed)
     A8 = ga.Csr.upload(ctx, m, m, rst, col, np.ones(len(col), np.uint8))
     ref_total, ref_rows = oracle.tc_sandia(oracle.Csr(m, m, rst, col, np.ones(len(col), np.int32)))
@@ -429,7 +429,7 @@ def other_configs(ga, ctx, args):
     out["tc_er1000"] = {"triangles": ref_total, "edges": len(col) // 2, "bit_exact": True, **rec,
                         "note": "device time per call (CUDA events, 200 calls, graph resident); e2e includes "
                                 "upload, validation and the per-row download"}
-    # config 3
+    # batched BC, R-MAT scale 20
     m, rst, col = ga.gen_rmat(20, 16, 0.57, 0.19, 0.19, args.seed)
     A = ga.Csr.upload(ctx, m, m, rst, col, np.ones(len(col), np.int32))
     rng = np.random.default_rng(args.seed)
