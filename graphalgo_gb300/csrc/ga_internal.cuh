@@ -229,7 +229,7 @@ struct TriKt {
     int32_t* tcrank;    // cap: its compacted copy
     int32_t* ocount;    // m + 1: oriented entries per row
     int32_t* tstart;    // m + 2: tasks per row, scanned into task starts
-    int32_t* task_row;  // cap / 32 + m + 1: row of each task
+    int32_t* task_row;  // cap / 16 + m + 1: row of each task
     int32_t* dpos;      // m + 1: position of each row's diagonal entry, -1 if none
     void* scan_scr;
 };

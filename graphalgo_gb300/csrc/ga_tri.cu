@@ -42,7 +42,7 @@
 namespace ga {
 
 constexpr int kTriThreads = 128;
-constexpr int kTriTask = 32;                  // oriented entries per warp task (at most 32)
+constexpr int kTriTask = 16;                  // oriented entries per warp task (at most 32)
 constexpr int kTriWin = 1 << 14;              // rank window of the member bitmaps
 constexpr int kTriWinWords = kTriWin / 32;    // 512 bitmap words per warp
 constexpr int kTriCntMax = 1024;              // longest O_u counted in shared memory
