@@ -344,7 +344,9 @@ GA_API int ga_write_bin(ga_ctx ctx, ga_csr A, const char* matcode, const char* p
  * algo GA_MSA/MCA/HEAP/NAIVE: C<L> = L*L with that variant, L = strict lower
  * triangle of A, total = sum of C (triangle_counting_masked_sandia,
  * src/main.cpp:65-86); GA_DOT: the same counts by warp-level sorted-list
- * intersections. per_row (host, length m, may be NULL) receives the row sums
+ * intersections; GA_TRI: by listing every triangle once (a symmetric A; any
+ * other A takes the Sandia form with GA_HYBRID); GA_HYBRID and GA_AUTO as
+ * for the masked product. per_row (host, length m, may be NULL) receives the row sums
  * of C<L> = L*L: triangles whose largest vertex is that row. Values of A are
  * ignored (the reference CLI makes them 1, src/main.cpp:335). */
 GA_API int ga_tc(ga_ctx ctx, ga_algo algo, ga_csr A, int64_t* total, int64_t* per_row);
