@@ -13,14 +13,28 @@ msa|mca|heap|dot|hybrid runs one of the other forms);
 k starts from the (k-1)-truss, which contains it (same edge sets as starting
 from A). value = 2 * (Gustavson products of every support product, the work
 of the reference's C<M> = A*B whatever form computes it) / time, inputs
-resident in HBM, L2 flushed (256 MiB write) between steps.
+resident in HBM, L2 flushed (256 MiB write) between steps: a
+reference-equivalent rate (unit "reference-equivalent GFLOP/s"), since the
+triangle-listing form reaches the same supports with far fewer operations.
 
 e2e: the same sweep through the public API from pinned host buffers: upload
 A, run the sweep, download every k-truss (row starts and columns).
 
+parity: every k-truss the e2e sweep downloaded (iteration count, entries,
+edge-set digest) against the oracle's record of the same sweep
+(tests/golden/rmat18_sweep.json), the k = 3 truss against the oracle run
+live, TC and BC of the other configurations against the oracle.
+
 cpu_baseline / --impl reference: the oracle port of the reference's k_truss
 (oracle/oracle.c, OpenMP over all host cores) on a bounded sample of the same
-workload - the k = 3 stage from A - reported in the same unit.
+workload - the k = 3 stage from A - reported in the same unit. The reference
+arm loads nothing of the product: its graph comes from the oracle's copy of
+the generator (oracle/gen.c).
+
+The default line also carries the other configurations: the triangle count
+of an Erdos-Renyi graph (n = 1,000), batched BC on R-MAT scale 20 (64 and 256
+sources), the batched TC + 4-truss of 4,096 k-NN graphs against per-graph
+launches, and the request server against the plain sequential form.
 
 Multi-GPU: the path does not shard; --gpus N under torchrun runs N
 independent replicas (one per rank) and reports their aggregate.
@@ -44,8 +58,17 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 METRIC = "masked SpGEMM GFLOP/s & HBM % of peak; batched/served req/s, p50/p99 vs plain"
-UNIT = "GFLOP/s"
+UNIT = "reference-equivalent GFLOP/s"
 HBM_FALLBACK_GBS = 6800.0
+GOLDEN_SWEEP = os.path.join(ROOT, "tests", "golden", "rmat18_sweep.json")
+# DRAM bytes per stored entry of the dominant kernels, from one ncu capture
+# each (dram__bytes_read.sum + dram__bytes_write.sum of the launch divided by
+# its stored entries): k_tri_support on the first support product of the
+# R-MAT 18 4-truss (profiles/tri_support_rmat18.md) and k_mxm_masked<MSA> on
+# the R-MAT 18 support product (profiles/mxm_msa_rmat18_support.md). Each
+# launch of the sweep works on operands that fit in L2, so its DRAM traffic
+# is the compulsory traffic of its operands, proportional to its entries.
+DRAM_BYTES_PER_ENTRY = {"tri_support": 7.506, "mxm": 4.543}
 
 
 def parse_args():
@@ -93,6 +116,14 @@ def parse_args():
                     help="batch workload: graphs timed in the per-graph arm (0 = all)")
     ap.add_argument("--tc-algo", default=None, choices=["msa", "mca", "heap", "dot", "tri", "auto"],
                     help="TC variant (default: msa; auto for the batch workload)")
+    ap.add_argument("--batch-algo", default="auto", choices=["msa", "mca", "heap", "dot", "tri", "auto"],
+                    help="batched record: k-truss variant of the batched calls")
+    ap.add_argument("--batch-tc-algo", default="auto", choices=["msa", "mca", "heap", "dot", "tri", "auto"],
+                    help="batched record: TC variant of the batched calls")
+    ap.add_argument("--serve-requests", type=int, default=300,
+                    help="default line: requests of the light-mix serving record")
+    ap.add_argument("--serve-full-requests", type=int, default=90,
+                    help="default line: requests of the full-pool serving record (0: skip it)")
     ap.add_argument("--host-loops", action="store_true",
                     help="run the k-truss loop from the host (kernels launched one by one, e.g. for ncu)")
     args = ap.parse_args()
@@ -206,20 +237,6 @@ def measured_peak_hbm():
     return HBM_FALLBACK_GBS, "fallback"
 
 
-def profile_traffic(summary: str = "mxm_msa_rmat18_support.md"):
-    """DRAM bytes per mask entry of the dominant kernel from its committed ncu
-    summary under profiles/ (MSA, or the triangle-listing kernel), or None."""
-    p = os.path.join(ROOT, "profiles", summary)
-    try:
-        with open(p) as f:
-            for line in f:
-                if line.startswith("dram_bytes_per_mask_entry:"):
-                    return float(line.split(":", 1)[1].strip())
-    except OSError:
-        pass
-    return None
-
-
 def run_case(args):
     """Small profiling cases, --reps times each (used for ncu captures):
     `support` = the sweep's first support product C<A> = A*A; `tc` =
@@ -282,14 +299,36 @@ def run_case(args):
     ctx.close()
 
 
-def workload_config(args, m, nnz, kmax, schedule=None):
-    kmax_s = "k_max" if kmax is None else f"{kmax} (k_max)"
-    return {"workload": f"k-truss sweep k={args.kmin}..{kmax_s}, R-MAT scale {args.scale}",
-            "schedule": None if schedule is None else
-            {k: schedule[k] for k in ("algo", "warp_max_flops", "heavy_flops", "ctas_per_sm", "dot_chunk")},
+def load_sweep_golden(args):
+    """The oracle's record of the sweep (tests/golden/rmat18_sweep.json) when
+    the arguments name the same graph, else None."""
+    try:
+        with open(GOLDEN_SWEEP) as f:
+            rec = json.load(f)
+    except OSError:
+        return None
+    g = rec["graph"]
+    if (g["scale"], g["edge_factor"], g["seed"]) != (args.scale, args.edge_factor, args.seed) or args.kmin != 3:
+        return None
+    return rec
+
+
+def edge_digest(rst: np.ndarray, col: np.ndarray) -> str:
+    """BLAKE2b-128 of the row starts then the columns (little-endian int32),
+    as the golden record holds it."""
+    import hashlib
+    h = hashlib.blake2b(digest_size=16)
+    h.update(np.ascontiguousarray(rst, "<i4").tobytes())
+    h.update(np.ascontiguousarray(col, "<i4").tobytes())
+    return h.hexdigest()
+
+
+def workload_config(args, m, nnz, kmax):
+    """The workload, the same dict in both arms."""
+    return {"workload": f"k-truss sweep k={args.kmin}..k_max, R-MAT scale {args.scale}",
             "graph": f"R-MAT scale {args.scale}, edge factor {args.edge_factor}, a/b/c/d=0.57/0.19/0.19/0.05, "
                      f"seed {args.seed}, symmetrised, no loops/duplicates",
-            "vertices": m, "stored_entries": nnz, "variant": args.algo, "k_range": [args.kmin, kmax],
+            "vertices": m, "stored_entries": nnz, "k_range": [args.kmin, kmax],
             "k_start": "each k starts from the (k-1)-truss",
             "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas only"}
 
@@ -300,15 +339,16 @@ def cpu_sample(A_host, reps: int):
     oracle.build()
     threads = os.cpu_count() or 1
     oracle.set_num_threads(threads)
-    times, prod = [], 0
+    times, prod, res = [], 0, None
     for _ in range(max(1, reps)):
         t0 = time.perf_counter()
-        _, _, prod = oracle.ktruss(A_host, 3, with_products=True)
+        C, it, prod = oracle.ktruss(A_host, 3, with_products=True)
         times.append(time.perf_counter() - t0)
+        res = (C, it)
     t = statistics.median(times)
     return {"value": 2.0 * prod / t / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"k=3 stage of the sweep from A (k_truss, {prod:.4g} Gustavson products), "
-                      f"median of {len(times)} runs, {t:.3f} s each"}
+                      f"median of {len(times)} runs, {t:.3f} s each"}, res
 
 
 # --------------------------------------------------------------- GPU arm
@@ -369,13 +409,13 @@ def profile_step(ga, ctx, run, algo, counters, loops):
         # read-modify-writes
         eo = ctr["a_entries"] / 2
         bytes_model = 8 * ctr["rows"] + 20 * eo + 4 * ctr["wedges"] + 16 * ctr["triangles"]
-        tpe = profile_traffic("tri_support_rmat18.md")
+        tpe = DRAM_BYTES_PER_ENTRY["tri_support"]
         traffic_units = ctr["a_entries"]  # the capture's DRAM bytes are per stored entry
     else:
         # products of the Gustavson kernels; list entries walked for the inner-product one
         ex = ctr["executed_dot"] if algo == "dot" else ctr["executed"]
         bytes_model = 8 * ctr["rows"] + 16 * ctr["a_entries"] + 8 * ex + 8 * ctr["mask_entries"]
-        tpe = profile_traffic()
+        tpe = DRAM_BYTES_PER_ENTRY["mxm"]
         traffic_units = ctr["mask_entries"]
     peak, peak_kind = measured_peak_hbm()
     achieved = bytes_model / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
@@ -388,12 +428,33 @@ def profile_step(ga, ctx, run, algo, counters, loops):
                          "avg_launch_ms": k_ms / max(1, k_launches)}}
 
 
-def other_configs(ga, ctx, args):
+def bc_bytes_model(m, rst, col, src):
+    """Algorithmic bytes of a batched BC call under the Gustavson model of
+    the reference's algebra (betweenness_centrality.h:176-218): every source
+    s walks the stored entries of its connected component once forward
+    (Front<!Numsp> = A^T * Front: a 4-byte column and an 8-byte path count
+    per entry) and once backward (W<S[k-1]> = A * W: the same), and per
+    (vertex, source) pair reached writes its path count, reads it back,
+    writes its dependency and adds it into bc (4 x 8 bytes) plus its column
+    in the frontier (4 bytes)."""
+    import scipy.sparse as sp
+    from scipy.sparse.csgraph import connected_components
+    G = sp.csr_matrix((np.ones(len(col), np.int8), col, rst), shape=(m, m))
+    _, lab = connected_components(G, directed=False)
+    ent = np.bincount(lab, weights=np.diff(rst), minlength=lab.max() + 1)
+    ver = np.bincount(lab, minlength=lab.max() + 1)
+    e = float(ent[lab[src]].sum())
+    v = float(ver[lab[src]].sum())
+    return 2 * 12 * e + 36 * v
+
+
+def other_configs(ga, ctx, args, with_cpu: bool):
     """The other single-GPU workloads, measured beside the headline: the
     triangle count of a seeded Erdos-Renyi graph (n=1000, 9,990 edges, uint8
     values; latency, bit-exact against the oracle) and batched BC on R-MAT
     scale 20 with 64 and 256 seeded sources (FP64; GTEPS = sources * nnz / 2
-    / t)."""
+    / t), the 64-source scores checked against the FP64 oracle (1e-9
+    relative), which is also timed on all host cores as the CPU baseline."""
     import oracle
     out = {}
     # triangle count, Erdos-Renyi n = 1000
@@ -402,9 +463,12 @@ def other_configs(ga, ctx, args):
     ref_total, ref_rows = oracle.tc_sandia(oracle.Csr(m, m, rst, col, np.ones(len(col), np.int32)))
     rec = {}
     tot = ga.Dense.create(ctx, 1, 1, ga.INT64)
-    for algo in ("msa", "dot"):
-        got, rows = ga.tc(algo, A8)
-        assert got == ref_total and np.array_equal(rows, ref_rows)
+    exact = True
+    for algo in ("msa", "dot", "tri"):
+        got, rows = ga.tc(algo, A8 if algo != "tri" else ga.Csr.upload(ctx, m, m, rst, col))
+        exact = exact and got == ref_total and bool(np.array_equal(rows, ref_rows))
+        if algo == "tri":
+            continue
         reps = 200
         ctx.sync()
         ctx.timer_start()
@@ -426,16 +490,18 @@ def other_configs(ga, ctx, args):
         oracle.tc_sandia(Gh)
     rec["cpu_port_us"] = 1e6 * (time.perf_counter() - t0) / reps
     rec["cpu_port_threads"] = os.cpu_count() or 1
-    out["tc_er1000"] = {"triangles": ref_total, "edges": len(col) // 2, "bit_exact": True, **rec,
+    out["tc_er1000"] = {"triangles": ref_total, "edges": len(col) // 2, "bit_exact": exact, **rec,
                         "note": "device time per call (CUDA events, 200 calls, graph resident); e2e includes "
-                                "upload, validation and the per-row download"}
+                                "upload, validation and the per-row download; bit_exact: total and per-row "
+                                "counts of the MSA, inner-product and triangle-listing forms against the oracle"}
     # batched BC, R-MAT scale 20
     m, rst, col = ga.gen_rmat(20, 16, 0.57, 0.19, 0.19, args.seed)
     A = ga.Csr.upload(ctx, m, m, rst, col, np.ones(len(col), np.int32))
     rng = np.random.default_rng(args.seed)
+    peak, peak_kind = measured_peak_hbm()
     for ns in (64, 256):
         src = rng.choice(m, ns, replace=False).astype(np.int32)
-        ga.bc(A, src)
+        got = ga.bc(A, src)
         ms = []
         for _ in range(3):
             ctx.flush_l2()
@@ -443,9 +509,25 @@ def other_configs(ga, ctx, args):
             ga.bc(A, src)
             ms.append(ctx.timer_stop())
         t = min(ms)
-        out[f"bc_rmat20_{ns}src"] = {"ms": t, "gteps": ns * len(col) / 2 / t / 1e6, "runs_ms": ms}
+        bm = bc_bytes_model(m, rst, col, src)
+        r = {"ms": t, "gteps": ns * len(col) / 2 / t / 1e6, "runs_ms": ms, "unit": "GTEPS",
+             "roofline": {"bound": "hbm", "achieved": bm / (t * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                          "frac": bm / (t * 1e-3) / 1e9 / peak, "traffic": None, "peak_kind": peak_kind,
+                          "bytes_per_call": bm, "scope": "whole BC call (forward and backward sweeps)"}}
+        if ns == 64 and with_cpu:
+            oracle.set_num_threads(os.cpu_count() or 1)
+            Ah = oracle.Csr(m, m, rst, col, np.ones(len(col), np.int32))
+            t0 = time.perf_counter()
+            ref = oracle.bc_batch(Ah, src)
+            tc = time.perf_counter() - t0
+            rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1.0)
+            r["parity"] = {"max_rel_err": float(rel.max()), "within_1e-9": bool(rel.max() <= 1e-9),
+                           "against": "FP64 oracle (oracle.bc_batch), same sources"}
+            r["cpu_baseline"] = {"value": ns * len(col) / 2 / tc / 1e9, "unit": "GTEPS",
+                                 "cores": os.cpu_count() or 1, "kind": "port",
+                                 "sample": f"the same call ({ns} sources, FP64) by the oracle port, {tc:.2f} s"}
+        out[f"bc_rmat20_{ns}src"] = r
     return out
-
 
 
 def run_gpu(args, dist: Dist):
@@ -457,6 +539,7 @@ def run_gpu(args, dist: Dist):
     ctx.set_option(ga.OPT_DEVICE_LOOPS, loops)
     if args.hybrid_ratio is not None:
         ctx.set_option(ga.OPT_HYBRID_RATIO, args.hybrid_ratio)
+    golden = load_sweep_golden(args)
 
     m, rst, col = ga.gen_rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, args.seed)
     nnz = len(col)
@@ -506,55 +589,72 @@ def run_gpu(args, dist: Dist):
     roofline["kernel_share_of_step"] = prof["kernel_ms"] / (total_ms / args.steps) if total_ms else None
 
     # ---------------------------------------------------------- e2e
-    e2e = None
-    if not args.no_e2e:
-        rst_h = np.ascontiguousarray(rst, np.int32)
-        col_h = np.ascontiguousarray(col, np.int32)
-        val_h = np.ascontiguousarray(val, np.int32)
-        res_rst = np.empty((len(shape), m + 1), np.int32)
-        res_col = np.empty(sum(s[2] for s in shape) + 1, np.int32)
-        pinned = [rst_h, col_h, val_h, res_rst, res_col]
-        for a in pinned:
-            ga.host_register(a)
-        try:
+    # the sweep through the public API from pinned host buffers; every
+    # k-truss it downloads is then checked against the oracle's record
+    rst_h = np.ascontiguousarray(rst, np.int32)
+    col_h = np.ascontiguousarray(col, np.int32)
+    val_h = np.ascontiguousarray(val, np.int32)
+    res_rst = np.empty((len(shape), m + 1), np.int32)
+    res_col = np.empty(sum(s[2] for s in shape) + 1, np.int32)
+    pinned = [rst_h, col_h, val_h, res_rst, res_col]
+    for a in pinned:
+        ga.host_register(a)
+    e2e, got_shape = None, None
+    try:
+        d2h = 0
+
+        def sink_factory():
+            state = {"i": 0, "off": 0}
+
+            def sink(k, C):
+                nonlocal d2h
+                z = C.nnz
+                r = res_rst[state["i"]]
+                c = res_col[state["off"]:state["off"] + z]
+                # on the copy stream: overlaps with the next k's pruning
+                ga.lib().ga_csr_download_async(ctx.handle, C.handle, r.ctypes.data_as(ga._p),
+                                               c.ctypes.data_as(ga._p), None)
+                d2h += (m + 1) * 4 + z * 4
+                state["i"] += 1
+                state["off"] += z
+            return sink
+
+        e2e_ms = []
+        ctx.work_counters(reset=True)
+        dist.barrier()
+        for _ in range(1 if args.no_e2e else args.steps):
+            ctx.flush_l2()
             d2h = 0
-
-            def sink_factory():
-                state = {"i": 0, "off": 0}
-
-                def sink(k, C):
-                    nonlocal d2h
-                    z = C.nnz
-                    r = res_rst[state["i"]]
-                    c = res_col[state["off"]:state["off"] + z]
-                    # on the copy stream: overlaps with the next k's pruning
-                    ga.lib().ga_csr_download_async(ctx.handle, C.handle, r.ctypes.data_as(ga._p),
-                                                   c.ctypes.data_as(ga._p), None)
-                    d2h += (m + 1) * 4 + z * 4
-                    state["i"] += 1
-                    state["off"] += z
-                return sink
-
-            e2e_ms = []
-            ctx.work_counters(reset=True)
-            dist.barrier()
-            for _ in range(args.steps):
-                ctx.flush_l2()
-                d2h = 0
-                ctx.timer_start()
-                Ad = ga.Csr.upload(ctx, m, m, rst_h, col_h, val_h)
-                sweep(ga, ctx, Ad, args.algo, args.kmin, sink=sink_factory())
-                Ad.free()
-                ga.lib().ga_ctx_copy_sync(ctx.handle)
-                e2e_ms.append(ctx.timer_stop())
-            wce = ctx.work_counters(reset=True)
+            ctx.timer_start()
+            Ad = ga.Csr.upload(ctx, m, m, rst_h, col_h, val_h)
+            got_shape = sweep(ga, ctx, Ad, args.algo, args.kmin, sink=sink_factory())
+            Ad.free()
+            ga.lib().ga_ctx_copy_sync(ctx.handle)
+            e2e_ms.append(ctx.timer_stop())
+        wce = ctx.work_counters(reset=True)
+        if not args.no_e2e:
             e2e_t = dist.max(sum(e2e_ms))
             e2e = {"value": dist.sum(2.0 * wce["products"]) / (e2e_t * 1e-3) / 1e9, "unit": UNIT,
                    "h2d_bytes_per_step": int(rst_h.nbytes + col_h.nbytes + val_h.nbytes),
                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t / args.steps}
-        finally:
-            for a in pinned:
-                ga.host_unregister(a)
+        # digests of every downloaded k-truss
+        digests, off = [], 0
+        for i, (k, it, z) in enumerate(got_shape):
+            digests.append([k, it, z, edge_digest(res_rst[i], res_col[off:off + z])])
+            off += z
+    finally:
+        for a in pinned:
+            ga.host_unregister(a)
+    parity = {"graph_matches_record": None, "sweep_vs_oracle_record": None}
+    if golden is not None:
+        parity["graph_matches_record"] = bool(edge_digest(rst, col) == golden["graph"]["digest"])
+        gs = [list(x) for x in golden["stages"]]
+        bad = [d[0] for d, g in zip(digests, gs) if d != g]
+        parity["sweep_vs_oracle_record"] = {
+            "stages": len(gs), "compared": min(len(gs), len(digests)), "equal": not bad and len(gs) == len(digests),
+            "first_mismatch_k": bad[0] if bad else None,
+            "what": "iteration count, stored entries and BLAKE2b digest of (row starts, columns) of every "
+                    "k-truss the e2e sweep downloaded, against tests/golden/rmat18_sweep.json (CPU oracle)"}
 
     # ------------------------------------------------- support variants
     variants = {}
@@ -570,18 +670,39 @@ def run_gpu(args, dist: Dist):
         variants[algo] = {"ms": ms, "gflops": 2.0 * ctx.work_counters()["products"] / ms / 1e6}
     variants["autotune_ktruss"] = ga.autotune(ga.TUNE_KTRUSS, A)
 
-    others = other_configs(ga, ctx, args) if not args.no_other_configs else None
-
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         import oracle
-        cpu = cpu_sample(oracle.Csr(m, m, rst, col, val), args.cpu_reps)
+        cpu, (R3, it3) = cpu_sample(oracle.Csr(m, m, rst, col, val), args.cpu_reps)
+        C3, git3 = ga.ktruss(args.algo, A, 3)
+        r3, c3, v3 = C3.download()
+        C3.free()
+        parity["k3_vs_oracle_live"] = bool(git3 == it3 and np.array_equal(r3, R3.rst) and np.array_equal(c3, R3.col)
+                                           and np.array_equal(v3, R3.val))
+
+    others = other_configs(ga, ctx, args, with_cpu=dist.world == 1) if not args.no_other_configs else None
+    batch = serve = None
+    if not args.no_other_configs:
+        batch = batch_record(ga, ctx, args, dist)
+        serve = serve_record(ga, ctx, args, dist)
+    if others:
+        parity["tc_er1000_bit_exact"] = others["tc_er1000"]["bit_exact"]
+        if "parity" in others["bc_rmat20_64src"]:
+            parity["bc_rmat20_64src_max_rel_err"] = others["bc_rmat20_64src"]["parity"]["max_rel_err"]
+            parity["bc_rmat20_64src_within_1e-9"] = others["bc_rmat20_64src"]["parity"]["within_1e-9"]
+    if batch:
+        parity["batch_equal_to_plain"] = batch["plain"]["results_equal"]
+    if serve:
+        parity["serve_equal_to_plain"] = serve["results_equal"]
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": workload_config(args, m, nnz, kmax, schedule),
+        "config": workload_config(args, m, nnz, kmax),
+        "variant": args.algo, "schedule": None if schedule is None else
+        {k: schedule[k] for k in ("algo", "warp_max_flops", "heavy_flops", "ctas_per_sm", "dot_chunk")},
+        "parity": parity,
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(launches_per_step * args.steps), "clocks": clocks,
         "work": {"products_per_step": wc["products"] / args.steps,
@@ -589,15 +710,17 @@ def run_gpu(args, dist: Dist):
                  "support_products_k3": per_k.get(args.kmin, {}).get("products"),
                  "wedges_per_step": wc["wedges"] / args.steps, "triangles_per_step": wc["triangles"] / args.steps,
                  "note": "value counts 2 x the Gustavson products of the reference's C<C> = C*C for every "
-                         "support product (products_per_step); the triangle-listing form computes the same "
-                         "values from wedges_per_step rank-ordered lookups, the Gustavson forms from "
-                         "executed_products_per_step products"},
+                         "support product (products_per_step): a reference-equivalent rate; the "
+                         "triangle-listing form computes the same values from wedges_per_step rank-ordered "
+                         "lookups, the Gustavson forms from executed_products_per_step products"},
         "kernel_profile": {"note": "one step with host-driven loops and CUDA events per launch (slower than "
                                    "the timed step); summed event time per kernel scope, ms",
                            "top": {k: round(v[1], 3) for k, v in
                                    sorted(prof["stats"].items(), key=lambda kv: -kv[1][1])[:14]}},
         "support_variants": variants,
         "other_configs": others,
+        "batch": batch,
+        "serve": serve,
     }
     ctx.close()
     return line
@@ -615,49 +738,49 @@ def batch_config(args, n, nnz):
             "graphs": args.graphs, "vertices": int(n.sum()), "stored_entries": int(nnz),
             "graph": "n ~ U[32,4096], dim ~ U[4,16], points i.i.d. N(0,1), 30 nearest by Euclidean distance, "
                      f"symmetrised by union, seed {args.seed}",
-            "variant": {"tc": args.tc_algo, "ktruss": args.algo}, "k": 4,
+            "variant": {"tc": args.batch_tc_algo, "ktruss": args.batch_algo}, "k": 4,
             "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas only"}
 
 
-def run_batch(args, dist: Dist):
-    """One step = per-graph triangle counts and 4-truss of every graph of the
-    batch, as two batched calls over the block-diagonal union (resident in
-    HBM). Compared with the per-graph form on the same GPU: ga_tc and
-    ga_ktruss called graph by graph on resident per-graph handles."""
-    import graphalgo_gb300 as ga
-    from graphalgo_gb300 import build as gbuild
-    gbuild.build()
-    ctx = ga.Context(dist.local_rank)
+def batch_record(ga, ctx, args, dist: Dist, steps: int = 3, warmup: int = 1, with_profile: bool = False,
+                 cpu_budget_s: float = 5.0) -> dict:
+    """Batched TC + 4-truss of args.graphs k-NN graphs (the block-diagonal
+    union resident in HBM, GA_AUTO schedules tuned on it) against the plain
+    per-graph form on the same GPU (ga_tc + ga_ktruss graph by graph on
+    resident per-graph handles, MSA with the default schedule); results
+    compared graph by graph; e2e uploads the union and downloads the
+    results; the oracle port on a bounded sample of the graphs."""
     loops = 0 if args.host_loops else 1
     ctx.set_option(ga.OPT_DEVICE_LOOPS, loops)
     n, dim = knn_batch_sizes(args.graphs, args.seed)
     U, voff = ga.gen_knn_batch(ctx, n, dim, k=30, seed=args.seed + dist.rank)
     G = args.graphs
-    # autotuned schedules for the union (cached; GA_AUTO calls use them)
+    kt_arg = args.batch_algo
+    tc_arg = args.batch_tc_algo
     tuning = {}
-    kt_algo, tc_algo = args.algo, args.tc_algo
-    if args.algo == "auto":
+    kt_algo, tc_algo = kt_arg, tc_arg
+    if kt_arg == "auto":
         tuning["ktruss"] = ga.autotune(ga.TUNE_KTRUSS, U)
         kt_algo = tuning["ktruss"]["algo"]
-    if args.tc_algo == "auto":
+    if tc_arg == "auto":
         tuning["tc"] = ga.autotune(ga.TUNE_TC, U)
         tc_algo = tuning["tc"]["algo"]
 
     def step():
-        tcs = ga.batch_tc(args.tc_algo, U, voff)
-        C, iters = ga.batch_ktruss(args.algo, U, voff, 4)
+        tcs = ga.batch_tc(tc_arg, U, voff)
+        C, iters = ga.batch_ktruss(kt_arg, U, voff, 4)
         z = C.nnz
         C.free()
         return tcs, iters, z
 
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, warmup)):
         ref = step()
     sampler = ClockSampler(dist.local_rank)
     dist.barrier()
     ctx.sync()
     sampler.start()
     step_ms = []
-    for _ in range(args.steps):
+    for _ in range(steps):
         ctx.flush_l2()
         ctx.timer_start()
         out = step()
@@ -665,12 +788,13 @@ def run_batch(args, dist: Dist):
     ctx.sync()
     clocks = sampler.stop()
     dist.barrier()
-    assert np.array_equal(out[0], ref[0]) and np.array_equal(out[1], ref[1]) and out[2] == ref[2]
+    stable = bool(np.array_equal(out[0], ref[0]) and np.array_equal(out[1], ref[1]) and out[2] == ref[2])
     t_max = dist.max(sum(step_ms))
-    value = dist.sum(G * args.steps) / (t_max * 1e-3)
-
-    prof = profile_step(ga, ctx, step, kt_algo, lambda: ctx.work_counters(), loops)
-    prof["roofline"]["kernel_share_of_step"] = prof["kernel_ms"] / (sum(step_ms) / args.steps)
+    value = dist.sum(G * steps) / (t_max * 1e-3)
+    prof = None
+    if with_profile:
+        prof = profile_step(ga, ctx, step, kt_algo, lambda: ctx.work_counters(), loops)
+        prof["roofline"]["kernel_share_of_step"] = prof["kernel_ms"] / (sum(step_ms) / steps)
 
     # ------------------------------------------- per-graph plain launches
     rst, col, _ = U.download()
@@ -678,9 +802,8 @@ def run_batch(args, dist: Dist):
     npl = G if args.plain_graphs <= 0 else min(G, args.plain_graphs)
     pick = np.sort(np.random.default_rng(args.seed + 1).choice(G, npl, replace=False)) if npl < G else np.arange(G)
     handles = [ga.Csr.upload(ctx, m_, m_, r, c, np.ones(len(c), np.int32)) for m_, r, c in (blocks[i] for i in pick)]
-    # the plain form: the reference's default variant (MSA), default schedule
-    plain_tc_algo = args.tc_algo if args.tc_algo != "auto" else "msa"
-    plain_kt_algo = args.algo if args.algo != "auto" else "msa"
+    plain_tc_algo = tc_arg if tc_arg != "auto" else "msa"
+    plain_kt_algo = kt_arg if kt_arg != "auto" else "msa"
     for h in handles[:8]:
         ga.tc(plain_tc_algo, h, per_row=False)
         ga.ktruss(plain_kt_algo, h, 4)[0].free()
@@ -696,80 +819,92 @@ def run_batch(args, dist: Dist):
         plain_nnz += C.nnz
         C.free()
     plain_ms = ctx.timer_stop()
-    same = bool(np.array_equal(plain_tc, ref[0][pick]) and np.array_equal(plain_it, ref[1][pick])
+    same = bool(stable and np.array_equal(plain_tc, ref[0][pick]) and np.array_equal(plain_it, ref[1][pick])
                 and (npl < G or plain_nnz == ref[2]))
     for h in handles:
         h.free()
     plain_value = dist.sum(npl) / (dist.max(plain_ms) * 1e-3)
 
     # ---------------------------------------------------------- e2e
-    e2e = None
-    if not args.no_e2e:
-        rst_h = np.ascontiguousarray(rst)
-        col_h = np.ascontiguousarray(col)
-        val_h = np.ones(len(col), np.int32)
-        out_rst = np.empty(len(rst), np.int32)
-        out_col = np.empty(len(col) + 1, np.int32)
-        pinned = [rst_h, col_h, val_h, out_rst, out_col]
+    rst_h = np.ascontiguousarray(rst)
+    col_h = np.ascontiguousarray(col)
+    val_h = np.ones(len(col), np.int32)
+    out_rst = np.empty(len(rst), np.int32)
+    out_col = np.empty(len(col) + 1, np.int32)
+    pinned = [rst_h, col_h, val_h, out_rst, out_col]
+    for a in pinned:
+        ga.host_register(a)
+    try:
+        e2e_ms, d2h = [], 0
+        phases = {"upload": 0.0, "tc": 0.0, "ktruss": 0.0, "download": 0.0}
+        dist.barrier()
+        for _ in range(steps):
+            ctx.flush_l2()
+            ctx.timer_start()
+            t0 = time.perf_counter()
+            Ud = ga.Csr.upload(ctx, len(rst) - 1, len(rst) - 1, rst_h, col_h, val_h)
+            t1 = time.perf_counter()
+            tcs = ga.batch_tc(tc_arg, Ud, voff)
+            t2 = time.perf_counter()
+            C, iters = ga.batch_ktruss(kt_arg, Ud, voff, 4)
+            z = C.nnz
+            t3 = time.perf_counter()
+            ga.lib().ga_csr_download(ctx.handle, C.handle, out_rst.ctypes.data_as(ga._p),
+                                     out_col.ctypes.data_as(ga._p), None)
+            C.free()
+            Ud.free()
+            e2e_ms.append(ctx.timer_stop())
+            t4 = time.perf_counter()
+            for key, x0, x1 in (("upload", t0, t1), ("tc", t1, t2), ("ktruss", t2, t3), ("download", t3, t4)):
+                phases[key] += 1e3 * (x1 - x0) / steps
+            d2h = tcs.nbytes + iters.nbytes + out_rst.nbytes + 4 * z
+            same = same and bool(np.array_equal(tcs, ref[0]) and np.array_equal(iters, ref[1]) and z == ref[2])
+        e2e_t = dist.max(sum(e2e_ms))
+        e2e = {"value": dist.sum(G * steps) / (e2e_t * 1e-3), "unit": "graphs/s",
+               "h2d_bytes_per_step": int(rst_h.nbytes + col_h.nbytes + val_h.nbytes + voff.nbytes),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t / steps,
+               "host_phases_ms": {k: round(v, 2) for k, v in phases.items()}}
+    finally:
         for a in pinned:
-            ga.host_register(a)
-        try:
-            e2e_ms, d2h = [], 0
-            phases = {"upload": 0.0, "tc": 0.0, "ktruss": 0.0, "download": 0.0}
-            dist.barrier()
-            for _ in range(args.steps):
-                ctx.flush_l2()
-                ctx.timer_start()
-                t0 = time.perf_counter()
-                Ud = ga.Csr.upload(ctx, len(rst) - 1, len(rst) - 1, rst_h, col_h, val_h)
-                t1 = time.perf_counter()
-                tcs = ga.batch_tc(args.tc_algo, Ud, voff)
-                t2 = time.perf_counter()
-                C, iters = ga.batch_ktruss(args.algo, Ud, voff, 4)
-                z = C.nnz
-                t3 = time.perf_counter()
-                ga.lib().ga_csr_download(ctx.handle, C.handle, out_rst.ctypes.data_as(ga._p),
-                                         out_col.ctypes.data_as(ga._p), None)
-                C.free()
-                Ud.free()
-                e2e_ms.append(ctx.timer_stop())
-                t4 = time.perf_counter()
-                for key, a, b in (("upload", t0, t1), ("tc", t1, t2), ("ktruss", t2, t3), ("download", t3, t4)):
-                    phases[key] += 1e3 * (b - a) / args.steps
-                d2h = tcs.nbytes + iters.nbytes + out_rst.nbytes + 4 * z
-            e2e_t = dist.max(sum(e2e_ms))
-            e2e = {"value": dist.sum(G * args.steps) / (e2e_t * 1e-3), "unit": "graphs/s",
-                   "h2d_bytes_per_step": int(rst_h.nbytes + col_h.nbytes + val_h.nbytes + voff.nbytes),
-                   "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t / args.steps,
-                   "host_phases_ms": {k: round(v, 2) for k, v in phases.items()}}
-        finally:
-            for a in pinned:
-                ga.host_unregister(a)
-
+            ga.host_unregister(a)
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        cpu = batch_cpu_sample(blocks, args.seed)
+        cpu = batch_cpu_sample(blocks, args.seed, cpu_budget_s)
+    return {"value": value, "unit": "graphs/s", "ms_per_step": t_max / steps, "steps": steps,
+            "config": batch_config(args, n, len(col)), "clocks": clocks, "autotune": tuning,
+            "variant": {"tc": tc_algo, "ktruss": kt_algo},
+            "plain": {"value": plain_value, "unit": "graphs/s", "graphs_timed": npl, "ms": plain_ms,
+                      "results_equal": same, "speedup": value / plain_value,
+                      "form": f"ga_tc({plain_tc_algo}) + ga_ktruss({plain_kt_algo}) per graph, "
+                              "resident per-graph handles"},
+            "e2e": e2e, "e2e_speedup_vs_plain": e2e["value"] / plain_value, "cpu_baseline": cpu,
+            "work": {"triangles": int(ref[0].sum()), "truss_entries": int(ref[2]), "max_iters": int(ref[1].max())},
+            "profile": prof}
 
+
+def run_batch(args, dist: Dist):
+    """--workload batch: the batched record as the line's value."""
+    import graphalgo_gb300 as ga
+    from graphalgo_gb300 import build as gbuild
+    gbuild.build()
+    ctx = ga.Context(dist.local_rank)
+    r = batch_record(ga, ctx, args, dist, steps=args.steps, warmup=args.warmup, with_profile=True,
+                     cpu_budget_s=15.0)
+    prof = r.pop("profile")
     line = {
-        "metric": METRIC, "value": value, "unit": "graphs/s", "n_gpus": dist.world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": batch_config(args, n, len(col)),
-        "roofline": prof["roofline"], "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": int(prof["launches"] * args.steps), "clocks": clocks,
-        "autotune": tuning,
-        "plain": {"value": plain_value, "unit": "graphs/s", "graphs_timed": npl, "ms": plain_ms,
-                  "results_equal": same, "speedup": value / plain_value,
-                  "form": f"ga_tc({plain_tc_algo}) + ga_ktruss({plain_kt_algo}) per graph, resident per-graph handles"},
-        "work": {"products_per_step": prof["counters"]["products"],
-                 "triangles": int(ref[0].sum()), "truss_entries": int(ref[2]),
-                 "max_iters": int(ref[1].max())},
+        "metric": METRIC, "value": r["value"], "unit": "graphs/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic", "config": r["config"],
+        "roofline": prof["roofline"], "cpu_baseline": r["cpu_baseline"], "e2e": r["e2e"],
+        "gpu_launches": int(prof["launches"] * args.steps), "clocks": r["clocks"], "autotune": r["autotune"],
+        "variant": r["variant"], "plain": r["plain"],
+        "work": dict(r["work"], products_per_step=prof["counters"]["products"]),
     }
     ctx.close()
     return line
 
 
-def batch_cpu_sample(blocks, seed, budget_s: float = 15.0):
+def batch_cpu_sample(blocks, seed, budget_s: float = 5.0):
     """Oracle port (OpenMP, all host threads): TC + 4-truss graph by graph on
     a seeded sample of the batch's graphs until the time budget is spent."""
     import oracle
@@ -810,13 +945,13 @@ def serve_pool(args, ctx, ga):
     return pool
 
 
-def serve_requests(args, pool):
+def serve_requests(args, pool, count):
     """Request types uniform over TC / k-truss (k ~ U{3..8}) / BC (32 seeded
     sources), graphs uniform over the pool."""
     import graphalgo_gb300 as ga
-    rng = np.random.default_rng(args.seed + 7)
+    rng = np.random.default_rng(args.seed + 7 + count)
     out = []
-    for _ in range(args.requests):
+    for _ in range(count):
         g = int(rng.integers(len(pool)))
         t = int(rng.integers(3))
         m = pool[g][1]
@@ -881,20 +1016,69 @@ def serve_same(a, b):
     return True
 
 
-def run_serve(args, dist: Dist):
-    """Serving: saturated throughput (every request queued at once) of the
-    server (workers, batching) against the plain sequential form (one worker,
-    no batching) on the same requests, then Poisson arrivals at rates that
-    are multiples of the plain form's throughput, p50/p99 latency of each."""
-    import graphalgo_gb300 as ga
-    from graphalgo_gb300 import build as gbuild
-    gbuild.build()
-    ctx = ga.Context(dist.local_rank)
+def serve_classes(ga, pool, reqs, plain, srv):
+    """Per request class (type, graph): count, the plain form's summed
+    service time (t_end - t_start, one request at a time: its share of the
+    plain makespan) and p50 latency in both forms."""
+    names = {ga.REQ_TC: "tc", ga.REQ_KTRUSS: "ktruss", ga.REQ_BC: "bc"}
+    cls = {}
+    for i, (t, g, _, _) in enumerate(reqs):
+        cls.setdefault(f"{names[t]}:{pool[g][0]}", []).append(i)
+    out = {}
+    span = plain["makespan_s"]
+    for key, idx in sorted(cls.items()):
+        svc = sum(plain["results"][i]["t_end"] - plain["results"][i]["t_start"] for i in idx)
+        lat_p = [plain["results"][i]["t_end"] - plain["results"][i]["t_submit"] for i in idx]
+        lat_s = [srv["results"][i]["t_end"] - srv["results"][i]["t_submit"] for i in idx]
+        out[key] = {"requests": len(idx), "plain_service_s": round(svc, 4),
+                    "plain_share": round(svc / span, 4) if span else None,
+                    "p50_ms_plain": round(1e3 * float(np.median(lat_p)), 2),
+                    "p50_ms_server": round(1e3 * float(np.median(lat_s)), 2)}
+    return out
+
+
+def serve_mix(ga, args, pool, reqs, rates, tag):
+    """One request mix on one pool: saturated (all queued at once) server
+    against the plain form, then Poisson arrivals at multiples of the plain
+    form's rate, p50/p99 of each."""
+    al = args.serve_algo
+    plain = serve_run(ga, pool, reqs, 1, False, algo=al)
+    l0 = ga.kernel_launches()
+    srv = serve_run(ga, pool, reqs, args.workers, True, algo=al)
+    launches = ga.kernel_launches() - l0
+    same = serve_same(serve_digest(ga, reqs, plain["results"]), serve_digest(ga, reqs, srv["results"]))
+    sweep_ = []
+    rng = np.random.default_rng(args.seed + 11)
+    for f in rates:
+        lam = f * plain["req_s"]
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, len(reqs)))
+        row = {"rate_req_s": lam, "rate_x_plain": f}
+        for name, w, c in (("server", args.workers, True), ("plain", 1, False)):
+            r = serve_run(ga, pool, reqs, w, c, arrivals, algo=al)
+            row[name] = {k: r[k] for k in ("req_s", "p50_ms", "p99_ms")}
+            same = same and serve_same(serve_digest(ga, reqs, plain["results"]), serve_digest(ga, reqs, r["results"]))
+        sweep_.append(row)
+    return {"pool": tag, "graphs": [g[0] for g in pool], "requests": len(reqs),
+            "server": {k: srv[k] for k in ("req_s", "p50_ms", "p99_ms", "makespan_s")},
+            "plain": {k: plain[k] for k in ("req_s", "p50_ms", "p99_ms", "makespan_s")},
+            "speedup": srv["req_s"] / plain["req_s"], "results_equal": same,
+            "batched_calls": srv["stats"]["batched_calls"], "max_group": srv["stats"]["max_group"],
+            "gpu_launches": int(launches), "poisson": sweep_, "classes": serve_classes(ga, pool, reqs, plain, srv),
+            "d2h_bytes_per_request": srv["d2h_bytes"] / len(reqs),
+            "h2d_bytes_per_request": sum(4 * len(x[3]) for x in reqs if x[3] is not None) / len(reqs)}
+
+
+def serve_record(ga, ctx, args, dist: Dist, light_requests=None, full_requests=None, rates=(1.0, 2.0)) -> dict:
+    """The request server against the plain sequential form (one worker, no
+    batching), the same requests in both: the light mix (the pool's graphs of
+    at most 2^20 stored entries: R-MAT 10-14 and k-NN 1e3 / 1e4, where
+    per-request costs bound the rate) and the full pool (R-MAT 10-22, k-NN up
+    to 1e6, where single heavy requests do), with a per-class breakdown."""
+    light_requests = args.serve_requests if light_requests is None else light_requests
+    full_requests = args.serve_full_requests if full_requests is None else full_requests
     t_pool = time.perf_counter()
     pool = serve_pool(args, ctx, ga)
     t_pool = time.perf_counter() - t_pool
-    reqs = serve_requests(args, pool)
-    # the tuner's choices for every pool graph (process-wide cache), outside the timed runs
     tuned = {}
     t_tune = time.perf_counter()
     if args.serve_algo == "auto":
@@ -905,68 +1089,51 @@ def run_serve(args, dist: Dist):
             tuned[name] = {"ktruss": kt["algo"], "tc": tc["algo"]}
             A.free()
     t_tune = time.perf_counter() - t_tune
-    # warm-up: a few requests of each kind on the smallest graphs
-    warm = [r for r in reqs if pool[r[1]][1] <= 20000][: max(3, 3 * args.warmup)]
-    al = args.serve_algo
-    serve_run(ga, pool, warm, args.workers, True, algo=al)
+    light = [g for g in pool if len(g[3]) <= (1 << 20)]
     sampler = ClockSampler(dist.local_rank)
     sampler.start()
-    plain = serve_run(ga, pool, reqs, 1, False, algo=al)
-    l0 = ga.kernel_launches()
-    srv = serve_run(ga, pool, reqs, args.workers, True, algo=al)
-    launches = ga.kernel_launches() - l0
-    clocks = sampler.stop()
-    same = serve_same(serve_digest(ga, reqs, plain["results"]), serve_digest(ga, reqs, srv["results"]))
-    sweep = []
-    rng = np.random.default_rng(args.seed + 11)
-    for f in [float(x) for x in args.rates.split(",") if x]:
-        lam = f * plain["req_s"]
-        arrivals = np.cumsum(rng.exponential(1.0 / lam, len(reqs)))
-        row = {"rate_req_s": lam, "rate_x_plain": f}
-        for name, w, c in (("server", args.workers, True), ("plain", 1, False)):
-            r = serve_run(ga, pool, reqs, w, c, arrivals, algo=al)
-            row[name] = {k: r[k] for k in ("req_s", "p50_ms", "p99_ms")}
-        sweep.append(row)
-    # the same request mix on the pool's small graphs (<= 2^20 stored entries),
-    # where per-request overheads, not one graph's kernels, bound the rate
-    light = [g for g in pool if len(g[3]) <= (1 << 20)]
-    light_mix = None
-    if light:
-        reqs_l = serve_requests(args, light)
-        pl = serve_run(ga, light, reqs_l, 1, False, algo=al)
-        sl = serve_run(ga, light, reqs_l, args.workers, True, algo=al)
-        light_mix = {"graphs": [g[0] for g in light], "requests": len(reqs_l),
-                     "server": {k: sl[k] for k in ("req_s", "p50_ms", "p99_ms", "makespan_s")},
-                     "plain": {k: pl[k] for k in ("req_s", "p50_ms", "p99_ms", "makespan_s")},
-                     "speedup": sl["req_s"] / pl["req_s"],
-                     "results_equal": serve_same(serve_digest(ga, reqs_l, pl["results"]),
-                                                 serve_digest(ga, reqs_l, sl["results"])),
-                     "batched_calls": sl["stats"]["batched_calls"], "max_group": sl["stats"]["max_group"]}
-    value = srv["req_s"]
-    h2d = sum(4 * len(src) for (t, _, _, src) in reqs if src is not None)
+    out = {"unit": "req/s", "workers": args.workers, "variant": args.serve_algo, "tuned": tuned,
+           "pool_build_s": t_pool, "tuning_s": t_tune,
+           "graphs": {name: {"vertices": m, "stored_entries": len(col)} for name, m, _, col in pool}}
+    # warm-up: a few requests of each kind on the small graphs
+    warm = serve_requests(args, light, 12)
+    serve_run(ga, light, warm, args.workers, True, algo=args.serve_algo)
+    if light and light_requests > 0:
+        out["light_mix"] = serve_mix(ga, args, light, serve_requests(args, light, light_requests), rates, "light")
+    if full_requests > 0:
+        out["full_pool"] = serve_mix(ga, args, pool, serve_requests(args, pool, full_requests), rates[:1], "full")
+    out["clocks"] = sampler.stop()
+    lm = out.get("light_mix")
+    out["value"] = lm["server"]["req_s"] if lm else out["full_pool"]["server"]["req_s"]
+    out["speedup"] = lm["speedup"] if lm else out["full_pool"]["speedup"]
+    out["results_equal"] = all(out[k]["results_equal"] for k in ("light_mix", "full_pool") if k in out)
+    return out
+
+
+def run_serve(args, dist: Dist):
+    """--workload serve: the serving record, the light mix's server req/s as
+    the value."""
+    import graphalgo_gb300 as ga
+    from graphalgo_gb300 import build as gbuild
+    gbuild.build()
+    ctx = ga.Context(dist.local_rank)
+    r = serve_record(ga, ctx, args, dist, light_requests=args.requests, full_requests=args.requests,
+                     rates=tuple(float(x) for x in args.rates.split(",") if x))
+    main_mix = r.get("light_mix") or r["full_pool"]
     line = {
-        "metric": METRIC, "value": value, "unit": "req/s", "n_gpus": dist.world, "steps": args.requests,
-        "warmup": len(warm), "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": r["value"], "unit": "req/s", "n_gpus": dist.world, "steps": args.requests,
+        "warmup": 12, "ms_per_step": 1e3 / r["value"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic",
         "config": {"workload": f"serving {args.requests} requests (TC / k-truss k~U{{3..8}} / BC 32 sources) "
-                               f"on {len(pool)} resident graphs",
-                   "graphs": {name: {"vertices": m, "stored_entries": len(col)} for name, m, _, col in pool},
-                   "workers": args.workers, "batching": "coalesced TC / k-truss on graphs <= 2^20 entries",
-                   "hbm_budget": srv["stats"]["budget"], "l2": "inputs resident; not flushed between requests",
-                   "pool_build_s": t_pool, "variant": al, "tuned": tuned, "tuning_s": t_tune,
+                               "on the light mix and on the full pool of resident graphs",
+                   "workers": args.workers, "l2": "inputs resident; not flushed between requests",
                    "parallelism": "replicas only"},
         "roofline": None, "cpu_baseline": None,
-        "e2e": {"value": value, "unit": "req/s", "h2d_bytes_per_step": h2d / len(reqs),
-                "d2h_bytes_per_step": srv["d2h_bytes"] / len(reqs),
+        "e2e": {"value": r["value"], "unit": "req/s", "h2d_bytes_per_step": main_mix["h2d_bytes_per_request"],
+                "d2h_bytes_per_step": main_mix["d2h_bytes_per_request"],
                 "note": "requests submitted from the host, results (counts, BC scores, k-truss edge sets) "
                         "returned to host memory; graphs resident"},
-        "gpu_launches": int(launches), "clocks": clocks,
-        "saturated": {"server": {k: srv[k] for k in ("req_s", "p50_ms", "p99_ms", "makespan_s")},
-                      "plain": {k: plain[k] for k in ("req_s", "p50_ms", "p99_ms", "makespan_s")},
-                      "speedup": value / plain["req_s"], "results_equal": same,
-                      "server_stats": srv["stats"]},
-        "poisson": sweep,
-        "light_mix": light_mix,
+        "gpu_launches": main_mix["gpu_launches"], "clocks": r["clocks"], "serve": r,
     }
     ctx.close()
     return line
@@ -1074,15 +1241,21 @@ def run_ingest(args, dist: Dist):
 
 
 def run_reference(args, dist: Dist):
+    """The reference arm: the oracle port of the reference's k_truss
+    (oracle/oracle.c, the parallel MSA product, OpenMP on every host core;
+    pinned to the unmodified reference by tests/test_oracle_pin.py) on a
+    bounded sample of the sweep, the k = 3 stage from A, per step. Nothing of
+    the product is loaded: the graph comes from oracle.gen_rmat, the same
+    graph as the product's generator (tests/test_host_logic.py), and k_max
+    from the oracle's record of the whole sweep. Rank 0 only."""
     if dist.rank != 0:
         return None
-    import graphalgo_gb300 as ga  # host-side generator only (no GPU use)
-    from graphalgo_gb300 import build as gbuild
     import oracle
-    gbuild.build()
-    m, rst, col = ga.gen_rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, args.seed)
-    A = oracle.Csr(m, m, rst, col, np.ones(len(col), np.int32))
     oracle.build()
+    m, rst, col = oracle.gen_rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, args.seed)
+    A = oracle.Csr(m, m, rst, col, np.ones(len(col), np.int32))
+    golden = load_sweep_golden(args)
+    kmax = golden["stages"][-1][0] - 1 if golden else None
     threads = os.cpu_count() or 1
     oracle.set_num_threads(threads)
     prod = 0
@@ -1096,12 +1269,12 @@ def run_reference(args, dist: Dist):
     total = sum(times)
     value = 2.0 * prod * args.steps / total / 1e9
     sample = (f"k=3 stage of the k-truss sweep from A ({prod:.4g} Gustavson products) per step, "
-              f"oracle port of k_truss on {threads} host threads")
+              f"oracle port of k_truss (parallel mxmm_msa) on {threads} host threads")
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic", "impl": "reference",
-            "config": dict(workload_config(args, m, len(col), None),
-                           variant="oracle port of the reference's k_truss with the parallel mxmm_msa"),
+            "config": workload_config(args, m, len(col), kmax),
+            "variant": "oracle port of the reference's k_truss with the parallel mxmm_msa",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 

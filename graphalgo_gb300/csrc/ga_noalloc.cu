@@ -1,14 +1,16 @@
 // Allocation-free masked SpGEMM entry point.
 //
 // Some callers cannot allocate device memory at the moment they need the
-// product: code that runs while a larger CUDA graph is being captured (plain
-// cudaMalloc is not allowed during stream capture), and host applications
-// that own the whole device-memory budget through their own arena and do
-// not let libraries allocate. This entry point takes the caller's device
-// buffers for every input and output, creates no context, and keeps the
-// kernel's scratch (work queue, row lists, CTA work items) in one
-// file-scope device array of fixed size. Every GPU that loads this library
-// holds that array until the process exits.
+// product: host applications that hand the whole device-memory budget to
+// their own arena at start-up and do not let libraries allocate, and
+// latency-critical callers that cannot accept the device-wide
+// synchronisation cudaMalloc and cudaFree may cause. This entry point takes
+// the caller's device buffers for every input and output, creates no
+// context, and keeps the kernel's scratch (work queue, row lists, CTA work
+// items) in one file-scope device array of fixed size. Every GPU that loads
+// this library holds that array until the process exits. The schedule is the
+// default one (bin thresholds and grid size); tuned schedules belong to
+// contexts, which this entry point does not have.
 #include "ga_device.cuh"
 
 #include <mutex>
@@ -70,8 +72,9 @@ extern "C" int ga_mxm_masked_noalloc(void* stream, ga_algo algo, int64_t m, int6
     if (!dtype_valid(dtype)) return GA_ERR_DTYPE;
     if (m == 0 || mask_nnz == 0) return GA_OK;
     if (m >= INT32_MAX || n > INT32_MAX || k > INT32_MAX || mask_nnz > INT32_MAX) return GA_ERR_INVALID_ARG;
-    if (!a_rst || !a_val || !b_rst || !m_rst || !m_col || !c_val) return GA_ERR_INVALID_ARG;
-    if (!b_unit && !b_val) return GA_ERR_INVALID_ARG;
+    if (!a_rst || !a_col || !a_val || !b_rst || !b_col || !m_rst || !m_col || !c_val) return GA_ERR_INVALID_ARG;
+    // the sorted merge (GA_HEAP) always reads B's values
+    if ((!b_unit || algo == GA_HEAP) && !b_val) return GA_ERR_INVALID_ARG;
     // the scratch needed for this shape must fit the fixed array
     if (mxm_scratch_bytes(m, n, mask_nnz, false) > kNoAllocScratchBytes) return GA_ERR_INVALID_ARG;
     try {

@@ -226,18 +226,22 @@ GA_API int ga_mxm_masked(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M,
 GA_API int ga_mxm_masked_vals(ga_ctx ctx, ga_algo algo, ga_csr A, ga_csr B, ga_csr M, void* d_cvals);
 
 /* Allocation-free C<M> = A*B (no counterpart in the reference). For callers
- * that cannot allocate device memory when they need the product - code
- * running while a CUDA graph is being captured, where cudaMalloc is not
- * allowed, or an application that keeps the whole device-memory budget in
- * its own arena. Every argument is a device pointer the caller owns: CSR
- * arrays of A (m x k), B (k x n) and the mask M (m x n, mask_nnz entries,
- * structural), and c_val (mask_nnz values of `dtype`, aligned with M's
- * pattern). No context and no allocation: the kernel's scratch lives in one
- * fixed 16 MiB device array inside this library, which every GPU that loads
- * the library keeps until the process exits. algo is GA_MSA, GA_MCA or
- * GA_HEAP; b_unit != 0 promises that B's values are all 1 (they are then not
- * read). The work runs on `stream` (NULL: the default stream) and is not
- * synchronised. Returns GA_ERR_INVALID_ARG when the scratch this shape needs
+ * that cannot allocate device memory when they need the product: an
+ * application that hands the whole device-memory budget to its own arena at
+ * start-up and lets no library allocate, or a latency-critical caller that
+ * cannot accept the device-wide synchronisation cudaMalloc / cudaFree may
+ * cause. Every argument is a device pointer the caller owns: CSR arrays of
+ * A (m x k), B (k x n) and the mask M (m x n, mask_nnz entries, structural),
+ * and c_val (mask_nnz values of `dtype`, aligned with M's pattern). No
+ * context and no allocation: the kernel's scratch lives in one fixed 16 MiB
+ * device array inside this library, which every GPU that loads the library
+ * keeps until the process exits. algo is GA_MSA, GA_MCA or GA_HEAP, run with
+ * the default schedule (a context's tuned schedule does not apply here);
+ * b_unit != 0 promises that B's values are all 1, and GA_MSA / GA_MCA then do
+ * not read b_val (GA_HEAP always does: b_val may be NULL only for the other
+ * two). The work runs on `stream` (NULL: the default stream) and is not
+ * synchronised. Returns GA_ERR_INVALID_ARG for a NULL array and when the
+ * scratch this shape needs
  * - 256 + 4(m+1) + 16 + 16 min(m(1 + ceil(n/2^17)) + mask_nnz/4096 + 1,
  * mask_nnz + 1) bytes - exceeds 16 MiB (about 460k rows when n <= 2^17).
  * The first call on a device looks up the array's device address for that

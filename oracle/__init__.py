@@ -45,10 +45,11 @@ _SUFFIX = {np.dtype(np.int32): "i32", np.dtype(np.int64): "i64",
 def build(force: bool = False) -> str:
     """Compile liboracle.so with gcc (OpenMP on)."""
     os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
-    src = os.path.join(HERE, "oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("oracle.c", "gen.c")]
+    newest = max(os.path.getmtime(f) for f in srcs + [os.path.join(HERE, "oracle.h")])
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < newest:
         subprocess.check_call(["gcc", "-O2", "-std=c11", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off",
-                               src, "-o", LIB_PATH])
+                               *srcs, "-o", LIB_PATH])
     return LIB_PATH
 
 
@@ -72,6 +73,17 @@ def lib():
         _lib = ctypes.CDLL(LIB_PATH)
         _lib.or_tc_sandia.restype = _i64
     return _lib
+
+
+def reference_dir() -> Optional[str]:
+    """The reference source tree oracle/_ref was built from (recorded by
+    build_ref.sh), or None where it was not built."""
+    try:
+        with open(os.path.join(HERE, "_ref", "source_dir")) as f:
+            d = f.read().strip()
+    except OSError:
+        return None
+    return d if d and os.path.isdir(d) else None
 
 
 def ref_available() -> bool:
@@ -262,6 +274,22 @@ def extract_upper(A: Csr) -> Csr:
 
 def symm_from_lower(L: Csr) -> Csr:
     return _tri("symm_from_lower", L)
+
+
+def gen_rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             seed: int = 1):
+    """Seeded R-MAT graph (oracle/gen.c): (m, rst, col), the same graph as
+    the product's generator gives for the same arguments."""
+    m, z = _i64(), _i64()
+    cr, cc = _p(), _p()
+    rc = lib().or_gen_rmat(int(scale), int(edge_factor), ctypes.c_double(a), ctypes.c_double(b),
+                           ctypes.c_double(c), ctypes.c_uint64(seed), ctypes.byref(m), ctypes.byref(z),
+                           ctypes.byref(cr), ctypes.byref(cc))
+    if rc != 0:
+        raise RuntimeError(f"or_gen_rmat failed ({rc})")
+    free = lib().or_free
+    rst = _take(cr, m.value + 1, np.int32, free)
+    return int(m.value), rst, _take(cc, z.value, np.int32, free)
 
 
 def tc_sandia(A: Csr):

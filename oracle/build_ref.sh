@@ -22,4 +22,6 @@ g++ -O3 -std=c++17 -fopenmp -fPIC -shared -fsigned-char -ffp-contract=off -w \
     -I"$here/ref/stub" -I"$REF/include" -I"$REF/src" \
     "$here/ref/ref_harness.cpp" "$REF/src/mmio.cpp" \
     -o "$out/libref.so"
+# where the sources were, for the tests that read the reference's graph files
+printf '%s\n' "$REF" > "$out/source_dir"
 echo "built $out/libref.so"

@@ -83,6 +83,9 @@ OR_DECL(double, f64)
 
 /* Triangle count, Sandia form C<L> = L*L with L = strict lower triangle of A;
  * rows (optional, length m) receives the row sums of C. */
+/* Seeded R-MAT graph, the same as the product's generator (oracle/gen.c). */
+int or_gen_rmat(int scale, int edge_factor, double a, double b, double c, uint64_t seed, int64_t* m_out,
+                int64_t* nnz_out, int** rst_out, int** col_out);
 int64_t or_tc_sandia(int64_t m, const int* rst, const int* col, int64_t* rows);
 
 /* The reference CLI's reading of a Matrix Market graph file: read_mtx_to_crs,

@@ -10,9 +10,11 @@ product's generators). Outputs come from the reference's own functions:
   C<L> = L*L, k_truss (edge sets and printed iteration counts), and the
   batched BC both as shipped (FP32, sources 0..b-1) and with the reference's
   templates instantiated at double for an explicit source list.
-For the four Matrix-Market graphs shipped with the reference only the
-known answers (triangles, k-truss edge counts and iterations) are stored;
-the graphs themselves are not copied.
+For the four Matrix-Market graphs shipped with the reference (matrices of
+the SuiteSparse Matrix Collection): the known answers (triangles, k-truss
+edge counts and iterations, reference_graphs.json) and, as test inputs, each
+graph as the reference's own reader returns it (row starts, columns, values
+and type code) and after the CLI's preparation (reference_graphs.npz).
 File formats: seeded Matrix Market files written here (formats/*.mtx), the
 reference's raw reading and CLI preparation of each (formats.npz) and the
 binary files its "tobinary" action writes for them (formats/*.bin).
@@ -21,6 +23,7 @@ Element-wise: the reference's eWiseAdd and VxM on seeded operands (ewise.npz).
     python tests/golden/make_golden.py            # everything
     python tests/golden/make_golden.py formats    # the file-format fixtures only
     python tests/golden/make_golden.py ewise      # eWiseAdd / VxM fixtures only
+    python tests/golden/make_golden.py graphs     # the reference's four graphs only
 """
 from __future__ import annotations
 
@@ -36,7 +39,7 @@ sys.path.insert(0, ROOT)
 
 import oracle  # noqa: E402
 
-REF_GRAPHS = "/root/reference/graphs"
+REF_GRAPHS = os.path.join(os.environ.get("REF", "/root/reference"), "graphs")
 
 
 def csr_from_dense(D, V=None, dtype=np.int32):
@@ -225,6 +228,33 @@ def write_ewise(rng) -> list:
     return keys
 
 
+def write_reference_graphs() -> list:
+    """Each reference graph as the reference reads it (read_mtx_to_crs,
+    include/matrix.h:280-417: self-loops dropped, symmetric files mirrored;
+    float64 values) and after the CLI's preparation (build_adjacency_matrix,
+    then build_symm_from_lower(extract_lower_triangle(A)),
+    src/main.cpp:221-222)."""
+    out = {}
+    names = []
+    for g in sorted(os.listdir(REF_GRAPHS)):
+        if not g.endswith(".mtx"):
+            continue
+        name = g[:-4]
+        path = os.path.join(REF_GRAPHS, g)
+        R, code = oracle.ref_read_raw(path, "mtx")
+        out[f"{name}_raw_rst"] = R.rst
+        out[f"{name}_raw_col"] = R.col
+        out[f"{name}_raw_val"] = R.val
+        out[f"{name}_raw_n"] = np.array([R.n], np.int64)
+        out[f"{name}_matcode"] = np.frombuffer(code, np.uint8)
+        C = oracle.ref_read_cli(path, "mtx", True)
+        out[f"{name}_cli_rst"] = C.rst
+        out[f"{name}_cli_col"] = C.col
+        names.append(name)
+    np.savez_compressed(os.path.join(HERE, "reference_graphs.npz"), **out)
+    return names
+
+
 def main():
     if oracle.build_ref() is None:
         raise SystemExit("reference sources not available; cannot regenerate fixtures")
@@ -298,17 +328,20 @@ def main():
             known[g[:-4]] = {"m": G.m, "nnz": int(G.nnz), "triangles": total, "ktruss": kt}
         with open(os.path.join(HERE, "reference_graphs.json"), "w") as f:
             json.dump(known, f, indent=1)
+        write_reference_graphs()
     write_formats(np.random.default_rng(20261204))
     write_ewise(np.random.default_rng(20261205))
     print("wrote", sorted(os.listdir(HERE)))
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] in (["formats"], ["ewise"]):
+    if sys.argv[1:] in (["formats"], ["ewise"], ["graphs"]):
         if oracle.build_ref() is None:
             raise SystemExit("reference sources not available; cannot regenerate fixtures")
         if sys.argv[1] == "formats":
             print(write_formats(np.random.default_rng(20261204)))
+        elif sys.argv[1] == "graphs":
+            print(write_reference_graphs())
         else:
             print(write_ewise(np.random.default_rng(20261205)))
     else:

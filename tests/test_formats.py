@@ -15,7 +15,8 @@ from oracle import formats as F
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden")
 FMT = os.path.join(GOLD, "formats")
-REF_GRAPHS = "/root/reference/graphs"
+REF_DIR = oracle.reference_dir()
+REF_GRAPHS = os.path.join(REF_DIR, "graphs") if REF_DIR else None
 
 with open(os.path.join(GOLD, "formats.json")) as _f:
     META = json.load(_f)
@@ -78,7 +79,7 @@ def test_cli_preparation_on_sorted_rows(name):
         assert name in ("real_gen", "int_gen_dup", "int_sym_shuffled")
 
 
-@pytest.mark.skipif(not (oracle.ref_available() and os.path.isdir(REF_GRAPHS)),
+@pytest.mark.skipif(not (oracle.ref_available() and REF_GRAPHS and os.path.isdir(REF_GRAPHS)),
                     reason="reference graphs not present")
 @pytest.mark.parametrize("g", ["G43", "cage3", "iris_dataset_30NN", "yeast_30NN"])
 def test_mtx_restatement_on_reference_graphs(g):

@@ -317,3 +317,27 @@ def test_tri_ktruss_degenerate_inputs(ctx):
     E = ga.Csr.upload(ctx, 0, 0, np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0, np.int32))
     C, git = ga.ktruss("tri", E, 3)
     assert C.nnz == 0 and git == 0
+
+
+@pytest.mark.parametrize("algo", ["tri", "hybrid"])
+def test_ktruss_full_sweep_rmat16(ctx, algo):
+    """The benchmark's sweep on a smaller R-MAT graph (scale 16, edge factor
+    16): C_3 = k_truss(A, 3), then C_k = k_truss(C_{k-1}, k) until the truss
+    is empty; every k-truss (edge set, values, iteration count) equals the
+    oracle's, and the device sweep ends at the oracle's k_max."""
+    m, rst, col = ga.gen_rmat(16, 16, 0.57, 0.19, 0.19, seed=42)
+    cur_h = csr_from_arrays(m, rst, col)
+    cur_d = ga.Csr.upload(ctx, m, m, rst, col, np.ones(len(col), np.int32))
+    k = 3
+    while True:
+        R, it = oracle.ktruss(cur_h, k)
+        C, git = ga.ktruss(algo, cur_d, k)
+        r, c, v = C.download()
+        assert git == it, k
+        assert np.array_equal(r, R.rst) and np.array_equal(c, R.col) and np.array_equal(v, R.val), k
+        cur_d.free()
+        cur_h, cur_d = R, C
+        if R.nnz == 0:
+            break
+        k += 1
+    assert k > 20  # a power-law graph: a long sweep

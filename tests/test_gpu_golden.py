@@ -29,7 +29,7 @@ def _dev(ctx, data, key):
     return ga.Csr.upload(ctx, m, m, rst, data[key + "_col"], data[key + "_val"])
 
 
-@pytest.mark.parametrize("algo", ["dot", "msa", "mca", "heap", "naive"])
+@pytest.mark.parametrize("algo", ["tri", "hybrid", "dot", "msa", "mca", "heap", "naive"])
 def test_golden_tc(ctx, gold, algo):
     data, meta = gold
     for name, info in meta["graphs"].items():
@@ -38,7 +38,7 @@ def test_golden_tc(ctx, gold, algo):
         assert np.array_equal(rows, data[f"{name}_tc_rows"]), name
 
 
-@pytest.mark.parametrize("algo", ["msa", "mca", "heap", "naive"])
+@pytest.mark.parametrize("algo", ["tri", "hybrid", "dot", "msa", "mca", "heap", "naive"])
 def test_golden_ktruss(ctx, gold, algo):
     data, meta = gold
     for name, info in meta["graphs"].items():
@@ -56,7 +56,7 @@ def test_golden_square_and_bc(ctx, gold):
     data, meta = gold
     for name, info in meta["graphs"].items():
         G = _dev(ctx, data, f"{name}_A")
-        for algo in ("msa", "mca", "heap", "naive"):
+        for algo in ("msa", "mca", "heap", "naive", "dot", "hybrid", "tri"):
             assert np.array_equal(ga.mxm_masked(algo, G, G, G).download()[2], data[f"{name}_sq_val"]), (name, algo)
         ref = data[f"{name}_bc_f64"]
         got = ga.bc(G, data[f"{name}_bc_sources"])

@@ -71,10 +71,11 @@ def test_bench_workloads_are_seeded():
 
     class Args:
         seed = 42
-        requests = 300
     pool = [("g%d" % i, 100 + i, None, None) for i in range(11)]
-    reqs = bench.serve_requests(Args, pool)
+    reqs = bench.serve_requests(Args, pool, 300)
     assert len(reqs) == 300
+    again = bench.serve_requests(Args, pool, 300)
+    assert all(a[:3] == b[:3] for a, b in zip(reqs, again))
     types = np.bincount([r[0] for r in reqs], minlength=3)
     assert types.min() > 60  # uniform over TC / k-truss / BC
     for t, g, k, src in reqs:
@@ -110,3 +111,14 @@ def test_tune_cache_file_round_trip(built, tmp_path):
 
 def test_server_cancel_rejects_null_server(built):
     assert ga.lib().ga_server_cancel(None, ctypes.c_int64(1)) == ga.ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("scale,ef,seed", [(6, 4, 1), (12, 16, 4), (16, 16, 42)])
+def test_oracle_rmat_generator_matches_the_product(built, scale, ef, seed):
+    """The oracle side's R-MAT generator (oracle/gen.c, used by the reference
+    arm of bench.py so it never loads the product's library) gives the
+    product's graph bit for bit."""
+    import oracle
+    m, rst, col = ga.gen_rmat(scale, ef, 0.57, 0.19, 0.19, seed)
+    om, orst, ocol = oracle.gen_rmat(scale, ef, 0.57, 0.19, 0.19, seed)
+    assert om == m and np.array_equal(orst, rst) and np.array_equal(ocol, col)

@@ -4,8 +4,10 @@
    reference by tests/golden/make_golden.py) - runs everywhere.
 2. Against the live reference library (oracle/_ref) on fresh seeded inputs -
    runs where the reference sources were available at build time.
-3. Against the known answers on the reference's own Matrix-Market graphs -
-   runs where those graphs are present.
+3. Against the known answers on the reference's own Matrix-Market graphs,
+   from the committed copies of those graphs as the reference's reader
+   returns them (tests/golden/reference_graphs.npz) - runs everywhere; the
+   copies are checked against the files where the reference tree is present.
 """
 import json
 import os
@@ -18,7 +20,9 @@ from graphs import random_csr, random_graph
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden")
-REF_GRAPHS = "/root/reference/graphs"
+
+REF_DIR = oracle.reference_dir()
+REF_GRAPHS = os.path.join(REF_DIR, "graphs") if REF_DIR else None
 
 
 @pytest.fixture(scope="module")
@@ -130,18 +134,49 @@ def test_live_reference_graph_algorithms():
         assert np.allclose(oracle.bc_batch(G, src), oracle.ref_bc_f64(G, src), rtol=1e-12, atol=1e-12)
 
 
-@pytest.mark.skipif(not (oracle.ref_available() and os.path.isdir(REF_GRAPHS)),
-                    reason="reference graphs not present")
+def _ref_graph(z, name, what):
+    rst = z[f"{name}_{what}_rst"]
+    m = len(rst) - 1
+    col = z[f"{name}_{what}_col"]
+    val = z[f"{name}_raw_val"] if what == "raw" else np.ones(len(col), np.int32)
+    n = int(z[f"{name}_raw_n"][0]) if what == "raw" else m
+    return oracle.Csr(m, n, rst, col, val)
+
+
 def test_reference_graph_known_answers():
+    """Triangles and the whole k-truss sequence (edge counts and iteration
+    counts) of the reference's four graphs, prepared as the CLI prepares
+    them, against the answers the reference printed."""
+    from oracle import formats as F
     with open(os.path.join(GOLD, "reference_graphs.json")) as f:
         known = json.load(f)
+    z = np.load(os.path.join(GOLD, "reference_graphs.npz"))
     # the table of known answers measured on the reference (triangles, k-truss)
     assert known["G43"]["triangles"] == 1392 and known["yeast_30NN"]["triangles"] == 180175
     assert known["iris_dataset_30NN"]["triangles"] == 25972 and known["cage3"]["triangles"] == 3
+    oracle.build()
     for name, info in known.items():
-        G = oracle.ref_read_mtx(os.path.join(REF_GRAPHS, name + ".mtx"))
+        G = _ref_graph(z, name, "cli")
+        # the oracle's restatement of the CLI's preparation of the raw graph
+        L = F.lower_symmetrised(F.adjacency(_ref_graph(z, name, "raw")))
+        assert np.array_equal(L.rst, G.rst) and np.array_equal(L.col, G.col), name
         assert G.nnz == info["nnz"]
         assert oracle.tc_sandia(G)[0] == info["triangles"], name
         for k, nnz, iters in info["ktruss"]:
             C, it = oracle.ktruss(G, k)
             assert (C.nnz, it) == (nnz, iters), (name, k)
+
+
+@pytest.mark.skipif(not (oracle.ref_available() and REF_GRAPHS and os.path.isdir(REF_GRAPHS)),
+                    reason="reference graphs not present")
+def test_reference_graph_fixtures_match_files():
+    """The committed copies equal the reference's reading of its files."""
+    z = np.load(os.path.join(GOLD, "reference_graphs.npz"))
+    for name in ("G43", "cage3", "iris_dataset_30NN", "yeast_30NN"):
+        path = os.path.join(REF_GRAPHS, name + ".mtx")
+        R, code = oracle.ref_read_raw(path, "mtx")
+        assert code == z[f"{name}_matcode"].tobytes()
+        assert np.array_equal(R.rst, z[f"{name}_raw_rst"]) and np.array_equal(R.col, z[f"{name}_raw_col"])
+        assert np.array_equal(R.val.view(np.int64), z[f"{name}_raw_val"].view(np.int64))
+        C = oracle.ref_read_mtx(path)
+        assert np.array_equal(C.rst, z[f"{name}_cli_rst"]) and np.array_equal(C.col, z[f"{name}_cli_col"])

@@ -1,9 +1,10 @@
 """The allocation-free masked product, ga_mxm_masked_noalloc.
 
 It serves callers that cannot allocate device memory when they need the
-product (code running during CUDA-graph capture, applications that keep all
-device memory in their own arena): they pass device buffers for everything
-and the kernel's scratch lives in a fixed array inside the library. This
+product (applications that keep all device memory in their own arena,
+latency-critical callers that cannot accept the device synchronisation of
+cudaMalloc / cudaFree): they pass device buffers for everything and the
+kernel's scratch lives in a fixed array inside the library. This
 test calls it through the C ABI twice in a row, on the same shared scratch,
 and compares each result with the allocating entry point's
 (ga_mxm_masked), exactly - the values are integers.
@@ -73,3 +74,23 @@ def test_noalloc_rejects_shapes_beyond_its_scratch(ctx):
     assert rc == ga.ERR_INVALID_ARG
     rc = _noalloc(ctx.stream(), ga.NAIVE, m, m, m, A, A, A, A.nnz, ga.INT32, 1, _dense_ptr(out))
     assert rc == ga.ERR_UNSUPPORTED
+
+
+def test_noalloc_rejects_missing_arrays(ctx):
+    """Refused before any launch: the sorted merge reads B's values even when
+    they are all 1, so GA_HEAP with b_unit set still needs b_val; the column
+    arrays are always needed."""
+    m, rst, col = ga.gen_er(100, 300, seed=2)
+    A = ga.Csr.upload(ctx, m, m, rst, col)
+    out = _dense_ptr(ga.Dense.create(ctx, 1, A.nnz, ga.INT32))
+    f = ga.lib().ga_mxm_masked_noalloc
+    f.restype = ctypes.c_int
+    ar, ac, av = A.device_ptrs()
+
+    def call(algo, a_col, b_col, b_val):
+        return f(_p(ctx.stream()), int(algo), _i64(m), _i64(m), _i64(m), _p(ar), _p(a_col), _p(av), _p(ar),
+                 _p(b_col), _p(b_val), _p(ar), _p(ac), _i64(A.nnz), int(ga.INT32), 1, _p(out))
+
+    assert call(ga.HEAP, ac, ac, None) == ga.ERR_INVALID_ARG
+    assert call(ga.MSA, None, ac, av) == ga.ERR_INVALID_ARG
+    assert call(ga.MSA, ac, None, av) == ga.ERR_INVALID_ARG
