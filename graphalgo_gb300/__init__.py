@@ -34,7 +34,7 @@ ALGO_NAMES = {v: k for k, v in ALGOS.items()}
 # options
 OPT_DEVICE_LOOPS, OPT_PROFILE, OPT_FAIL_ALLOC_AFTER, OPT_KNN_TILED = 1, 2, 3, 4
 OPT_MXM_WARP_FLOPS, OPT_MXM_HEAVY_FLOPS, OPT_MXM_CTAS_PER_SM, OPT_DOT_CHUNK, OPT_HYBRID_RATIO = 5, 6, 7, 8, 9
-OPT_TRI_ORDER = 10
+OPT_TRI_ORDER, OPT_KT_FRONTIER = 10, 11
 TUNE_KTRUSS, TUNE_PRODUCT, TUNE_TC = 0, 1, 2
 # edge-list / file ingestion flags
 EDGES_MIRROR, EDGES_DROP_LOOPS, EDGES_LOWER_SYMM, EDGES_UNIT = 1, 2, 4, 8
@@ -487,6 +487,14 @@ def bc(A: Csr, sources: Sequence[int]) -> np.ndarray:
 
 
 # ------------------------------------------------------------- generators
+def bc_all(A: Csr, block: int) -> np.ndarray:
+    """All-source BC in blocks of `block` sources, accumulated on the device
+    (betweenness_centrality, include/betweenness_centrality.h:5-123), FP64."""
+    out = np.zeros(A.shape[0], dtype=np.float64)
+    _check(lib().ga_bc_all(A.ctx.handle, A.handle, _i64(block), _ptr(out)), A.ctx)
+    return out
+
+
 def _take_host(ptr: _p, count: int) -> np.ndarray:
     if count > 0:
         buf = (ctypes.c_int32 * count).from_address(ptr.value)

@@ -564,11 +564,13 @@ __global__ void k_bc_check_sources(const int32_t* __restrict__ src, int ns, int6
     }
 }
 
-static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t nsrc, double* d_bc) {
+// accumulate: add this batch's scores to d_bc instead of overwriting it.
+static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t nsrc, double* d_bc,
+                      bool accumulate = false) {
     GA_REQUIRE(A->m == A->n, GA_ERR_SHAPE, "non-square matrix; BC is only for square matrices");
     GA_REQUIRE(nsrc >= 0 && nsrc <= kBcMaxSources, GA_ERR_INVALID_ARG, "BC: between 0 and 1024 sources per batch");
     const int64_t m = A->m;
-    GA_CUDA(cudaMemsetAsync(d_bc, 0, sizeof(double) * (m ? m : 1), ctx->stream));
+    if (!accumulate) GA_CUDA(cudaMemsetAsync(d_bc, 0, sizeof(double) * (m ? m : 1), ctx->stream));
     if (m == 0 || nsrc == 0) return;
     const int ns = (int)nsrc;
     const int words = (ns + 31) / 32;
@@ -708,11 +710,59 @@ static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t ns
     csr_destroy(ctx, Ad);
 }
 
+__global__ void k_bc_iota(int32_t* __restrict__ out, int64_t first, int64_t n) {
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+        out[j] = (int32_t)(first + j);
+}
+
+// All-source BC (betweenness_centrality, include/betweenness_centrality.h:
+// 5-123): sources 0..m-1 in blocks of `block`, every block's scores added
+// into d_bc on the device. The reference adds each block's row sums minus
+// the block's size (:103-111), which is the block's dependency sum, as
+// bc_device computes it. A block larger than one device batch (1,024
+// sources) runs as consecutive batches of at most 1,024: BC is a sum over
+// sources, so the block size changes only the order of the additions.
+static void bc_all_device(ga_ctx ctx, ga_csr A, int64_t block, double* d_bc) {
+    GA_REQUIRE(A->m == A->n, GA_ERR_SHAPE, "non-square matrix; BC is only for square matrices");
+    GA_REQUIRE(block >= 1, GA_ERR_INVALID_ARG, "BC: the block size must be at least 1");
+    const int64_t m = A->m;
+    GA_CUDA(cudaMemsetAsync(d_bc, 0, sizeof(double) * (m ? m : 1), ctx->stream));
+    if (m == 0) return;
+    const int64_t per = std::min<int64_t>(std::min<int64_t>(block, kBcMaxSources), m);
+    DBuf<int32_t> src(ctx, (size_t)per);
+    ProfScope ps(ctx, "bc_all");
+    for (int64_t i = 0; i < m; i += block) {
+        const int64_t n = std::min(block, m - i);
+        for (int64_t j = 0; j < n; j += per) {
+            const int64_t c = std::min(per, n - j);
+            k_bc_iota<<<grid_for(c, 256, 64), 256, 0, ctx->stream>>>(src.p, i + j, c);
+            post_launch("bc_iota");
+            bc_device(ctx, A, src.p, c, d_bc, true);
+        }
+    }
+}
+
 }  // namespace ga
 
 using namespace ga;
 
 extern "C" {
+
+int ga_bc_all(ga_ctx ctx, ga_csr A, int64_t block, double* bc) {
+    if (!ctx || !A || !bc) return GA_ERR_INVALID_ARG;
+    GA_API_BODY(ctx, {
+        DBuf<double> out(ctx, A->m > 0 ? (size_t)A->m : 1);
+        bc_all_device(ctx, A, block, out.p);
+        if (A->m)
+            GA_CUDA(cudaMemcpyAsync(bc, out.p, sizeof(double) * A->m, cudaMemcpyDeviceToHost, ctx->stream));
+        GA_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int ga_bc_all_device(ga_ctx ctx, ga_csr A, int64_t block, double* d_bc) {
+    if (!ctx || !A || !d_bc) return GA_ERR_INVALID_ARG;
+    GA_API_BODY(ctx, bc_all_device(ctx, A, block, d_bc));
+}
 
 int ga_bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t nsrc, double* d_bc) {
     if (!ctx || !A || !d_bc || (nsrc > 0 && !d_sources)) return GA_ERR_INVALID_ARG;

@@ -71,6 +71,7 @@ struct ga_ctx_s {
     bool profile = false;
     int64_t fail_alloc_after = -1;  // fault injection
     bool knn_tiled = false;         // k-NN generator: tiled kernel for every graph
+    bool kt_frontier = true;        // GA_TRI k-truss: incremental support after the first listing
     ga::MxmTune tune;               // masked-product schedule
     // profiling
     std::vector<ga::PendingTiming> pending;
@@ -258,6 +259,27 @@ void tri_kt_copyback(ga_ctx ctx, ga_csr C, const KtState* st, const int32_t* tr,
                      int32_t* mir, const TriKt& t, int64_t cap);
 // After the loop: every row back in column order.
 void tri_kt_finish(ga_ctx ctx, ga_csr C, const int32_t* row_of, const TriKt& t, int32_t* tmp_col);
+
+// Frontier form of the triangle-listing k-truss of one matrix (symmetric,
+// values 1), after tri_kt_setup: the triangles are listed once, then every
+// iteration prunes the edges whose support is below k - 2 and lowers the
+// supports of the edges that shared a triangle with them. Buffers: sup, oid,
+// f0, f1, tc (cap each), flag (cap + 1), state (cap bytes), tr (m + 1), scan
+// scratch. Leaves C pruned with its rows in column order; returns the
+// reference's iteration count.
+struct TriFrontBufs {
+    int32_t* sup;
+    int32_t* flag;
+    int32_t* tr;
+    int32_t* tc;
+    int32_t* oid;
+    int32_t* f0;
+    int32_t* f1;
+    uint8_t* state;
+    void* scan_scr;
+};
+int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const int32_t* mir, const TriKt& t,
+                    int64_t cap, const TriFrontBufs& b);
 
 // Autotuned algorithm resolution: GA_AUTO becomes the cached (or freshly
 // tuned) variant, and ctx->tune its schedule; other values pass through.

@@ -38,6 +38,7 @@
 // the rest] for the whole loop, so an iteration is task list, support, keep
 // flags and the prune.
 #include "ga_device.cuh"
+#include "ga_loop.cuh"
 
 namespace ga {
 
@@ -800,6 +801,358 @@ void tri_kt_finish(ga_ctx ctx, ga_csr C, const int32_t* row_of, const TriKt& t, 
                                                                                    nnz, tmp_col);
     post_launch("trikt_unpart");
     GA_CUDA(cudaMemcpyAsync(C->col, tmp_col, sizeof(int32_t) * (size_t)nnz, cudaMemcpyDeviceToDevice, ctx->stream));
+}
+
+// ======================================== frontier k-truss (one matrix)
+// The reference's k_truss recomputes the whole support every iteration
+// (src/main.cpp:100-127). Between iterations only the triangles that lose
+// an edge change, so after one listing the loop keeps the supports and, per
+// iteration t with C_t its edges and s_t their exact supports:
+//   F_t  = edges of C_t with s_t < k - 2 (iteration 0: found by one pass over
+//          the entries; later: the edges whose support crossed below k - 2
+//          in iteration t - 1, which are exactly the ones below it);
+//   every triangle of C_t with an edge in F_t is destroyed: each of its edges
+//          outside F_t loses 1, counted once by the triangle's F_t edge with
+//          the smallest id (the position of its oriented entry); an entry
+//          (i, i) in F_t lowers every edge of row i by 1 instead, and an edge
+//          in F_t shortens its two rows, which lowers their diagonal entries;
+//   C_{t+1} = C_t minus F_t; stop when F_t is empty (iteration count t + 1)
+//          or after m iterations (count 0), as the reference does.
+// Entries never move during the loop: an edge lives at its oriented entry
+// (state alive / in F_t / gone, support), the other entry points to it
+// (oid); one compaction at the end writes the kept entries in column order.
+// A pruned edge's triangles are found by walking the shorter of its two rows
+// and binary-searching the other (in the part its rank selects), stopping
+// once its support's worth of triangles is found. Per iteration one pass
+// over the entries counts the Gustavson products of the reference's
+// Tmp<C> = C*C for the work counters (rows with an upper part: sum of the
+// degrees of their columns).
+namespace {
+
+enum : uint8_t { kAlive = 0, kDying = 1, kGone = 2 };
+
+struct TriFrontState {
+    int32_t cnt[2];   // frontier sizes; the current one is cnt[t & 1]
+    int32_t t;        // iteration
+    int32_t iters;    // reported iteration count
+    int32_t done;
+    int32_t pad;
+};
+
+struct TriFrontArgs {
+    const int32_t* cr;      // row starts (fixed during the loop)
+    const int32_t* cc;      // columns, every row as [oriented part | rest]
+    const int32_t* row_of;
+    const int32_t* mir;
+    const int32_t* crank;   // rank of each entry's column
+    const int32_t* ocount;
+    const int32_t* dpos;    // position of each row's diagonal entry, -1 if none
+    int32_t* oid;           // entry -> position of its edge's record
+    int32_t* sup;           // supports at the records
+    uint8_t* state;         // states at the records
+    int32_t* deg;           // entries of each row still in C
+    int32_t* upc;           // of those, the ones with column >= row
+    int32_t* f0;
+    int32_t* f1;
+    TriFrontState* st;
+    unsigned long long* ctr;
+    int64_t m;
+    int64_t nnz;
+    int k;
+};
+
+__device__ __forceinline__ void front_push(int32_t* buf, int32_t* cnt, int32_t x) { buf[atomicAdd(cnt, 1)] = x; }
+
+// One support unit less; the edge joins the next frontier when it drops below k - 2.
+__device__ __forceinline__ void lower_support(const TriFrontArgs& a, int32_t f, int32_t* fn, int32_t* cn) {
+    if (atomicSub(a.sup + f, 1) == a.k - 2) front_push(fn, cn, f);
+}
+
+__global__ void k_trif_init_rows(TriFrontArgs a) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t b = a.cr[i], e = a.cr[i + 1], oc = a.ocount[i];
+        a.deg[i] = e - b;
+        a.upc[i] = (oc - lower_bound_i32(a.cc + b, oc, (int32_t)i)) +
+                   (e - b - oc - lower_bound_i32(a.cc + b + oc, e - b - oc, (int32_t)i));
+    }
+}
+
+// Records of the edges (the oriented entry; a diagonal entry is its own),
+// states, the diagonal terms of the listed supports, and the first frontier.
+__global__ void k_trif_seed(TriFrontArgs a) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < a.nnz; q += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t i = a.row_of[q], j = a.cc[q];
+        const bool rec = i == j || (int64_t)q - a.cr[i] < a.ocount[i];
+        a.oid[q] = rec ? (int32_t)q : a.mir[q];
+        a.state[q] = kAlive;
+        if (i == j) {
+            if (a.deg[i] < a.k - 2) front_push(a.f0, &a.st->cnt[0], (int32_t)q);
+        } else if (rec) {
+            const int32_t s = a.sup[q] + (a.dpos[i] >= 0) + (a.dpos[j] >= 0);
+            a.sup[q] = s;
+            if (s < a.k - 2) front_push(a.f0, &a.st->cnt[0], (int32_t)q);
+        }
+    }
+}
+
+// Work counters of iteration t, as for the reference's support product of C_t.
+__global__ void k_trif_count(TriFrontArgs a) {
+    unsigned long long prod = 0, mask = 0, ent = 0;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < a.nnz; q += (int64_t)gridDim.x * blockDim.x) {
+        if (a.state[a.oid[q]] == kGone) continue;
+        const int32_t i = a.row_of[q], j = a.cc[q];
+        if (a.upc[i] > 0) prod += (unsigned long long)a.deg[j];
+        mask += j >= i;
+        ++ent;
+    }
+    prod = warp_sum<unsigned long long>(prod);
+    mask = warp_sum<unsigned long long>(mask);
+    ent = warp_sum<unsigned long long>(ent);
+    if ((threadIdx.x & 31) == 0) {
+        if (prod) atomicAdd(&a.ctr[GA_CTR_PRODUCTS], prod);
+        if (mask) atomicAdd(&a.ctr[GA_CTR_MASK_ENTRIES], mask);
+        if (ent) atomicAdd(&a.ctr[GA_CTR_A_ENTRIES], ent);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(&a.ctr[GA_CTR_LAUNCHES], 1ull);
+        atomicAdd(&a.ctr[GA_CTR_ROWS], (unsigned long long)a.m);
+    }
+}
+
+__global__ void k_trif_mark(TriFrontArgs a) {
+    const int t = a.st->t;
+    const int32_t n = a.st->cnt[t & 1];
+    const int32_t* F = (t & 1) ? a.f1 : a.f0;
+    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x)
+        a.state[F[x]] = kDying;
+}
+
+// One warp per frontier edge: its triangles in C_t, the supports they lower.
+__global__ void __launch_bounds__(128) k_trif_lower(TriFrontArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int t = a.st->t;
+    const int32_t n = a.st->cnt[t & 1];
+    const int32_t* F = (t & 1) ? a.f1 : a.f0;
+    int32_t* fn = (t & 1) ? a.f0 : a.f1;
+    int32_t* cn = &a.st->cnt[(t + 1) & 1];
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    unsigned long long probes = 0, tris = 0;
+    for (int64_t x = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; x < n; x += warps) {
+        const int32_t q = F[x];
+        const int32_t u = a.row_of[q], v = a.cc[q];
+        if (u == v) {
+            // a diagonal entry leaves: every other edge of its row loses 1
+            for (int32_t p = a.cr[u] + lane; p < a.cr[u + 1]; p += 32) {
+                if (a.cc[p] == u) continue;
+                const int32_t f = a.oid[p];
+                if (a.state[f] == kAlive) lower_support(a, f, fn, cn);
+            }
+            continue;
+        }
+        const int32_t du = a.dpos[u], dv = a.dpos[v];
+        const int target = a.sup[q] - (du >= 0 && a.state[du] != kGone) - (dv >= 0 && a.state[dv] != kGone);
+        if (target <= 0) continue;
+        const int32_t ub = a.cr[u], ue = a.cr[u + 1], vb = a.cr[v], ve = a.cr[v + 1];
+        const bool xu = ue - ub <= ve - vb;  // walk the shorter row
+        const int32_t xb = xu ? ub : vb, xe = xu ? ue : ve;
+        const int32_t y = xu ? v : u;
+        const int32_t yb = xu ? vb : ub, ye = xu ? ve : ue, yo = yb + a.ocount[y];
+        // rank of y: the entry (u, v) holds rank(v), its mirror rank(u)
+        const int32_t ry = xu ? a.crank[q] : a.crank[a.mir[q]];
+        int found = 0;
+        for (int32_t base = xb; base < xe; base += 32) {
+            const int32_t p = base + lane;
+            bool hit = false;
+            if (p < xe) {
+                ++probes;
+                const int32_t w = a.cc[p];
+                if (w != u && w != v) {
+                    const int32_t f = a.oid[p];
+                    const uint8_t sf = a.state[f];
+                    if (sf != kGone) {
+                        // w ranked above y: (y, w) is in y's oriented part
+                        const bool above = a.crank[p] > ry;
+                        const int32_t sb = above ? yb : yo, se = above ? yo : ye;
+                        const int32_t r = sb + lower_bound_i32(a.cc + sb, se - sb, w);
+                        if (r < se && a.cc[r] == w) {
+                            const int32_t g = a.oid[r];
+                            const uint8_t sg = a.state[g];
+                            if (sg != kGone) {
+                                hit = true;
+                                if (sf == kAlive && (sg == kAlive || q < g)) lower_support(a, f, fn, cn);
+                                if (sg == kAlive && (sf == kAlive || q < f)) lower_support(a, g, fn, cn);
+                            }
+                        }
+                    }
+                }
+            }
+            const int h = __popc(__ballot_sync(0xffffffffu, hit));
+            found += h;
+            if (lane == 0) tris += (unsigned long long)h;
+            if (found >= target) break;
+        }
+    }
+    probes = warp_sum<unsigned long long>(probes);
+    if (lane == 0) {
+        if (probes) atomicAdd(&a.ctr[GA_CTR_WEDGES], probes);
+        if (tris) atomicAdd(&a.ctr[GA_CTR_TRIANGLES], tris);
+    }
+}
+
+// The frontier's edges leave C_t: rows shorten, diagonal entries whose row
+// length drops below k - 2 join the next frontier.
+__global__ void k_trif_apply(TriFrontArgs a) {
+    const int t = a.st->t;
+    const int32_t n = a.st->cnt[t & 1];
+    const int32_t* F = (t & 1) ? a.f1 : a.f0;
+    int32_t* fn = (t & 1) ? a.f0 : a.f1;
+    int32_t* cn = &a.st->cnt[(t + 1) & 1];
+    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t q = F[x];
+        const int32_t u = a.row_of[q], v = a.cc[q];
+        a.state[q] = kGone;
+        if (u == v) {
+            atomicSub(a.deg + u, 1);
+            atomicSub(a.upc + u, 1);
+            continue;
+        }
+        atomicSub(a.upc + min(u, v), 1);
+        const int32_t ou = atomicSub(a.deg + u, 1), ov = atomicSub(a.deg + v, 1);
+        if (ou == a.k - 2) {
+            const int32_t d = a.dpos[u];
+            if (d >= 0 && a.state[d] == kAlive) front_push(fn, cn, d);
+        }
+        if (ov == a.k - 2) {
+            const int32_t d = a.dpos[v];
+            if (d >= 0 && a.state[d] == kAlive) front_push(fn, cn, d);
+        }
+    }
+}
+
+__global__ void k_trif_finalize(TriFrontState* st, int64_t m, LoopCtl ctl) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int t = st->t;
+    if (st->cnt[t & 1] == 0) {
+        st->iters = t + 1;
+        st->done = 1;
+    } else {
+        st->cnt[t & 1] = 0;
+        st->t = t + 1;
+        if ((int64_t)(t + 1) >= m) {
+            st->iters = 0;
+            st->done = 1;
+        }
+    }
+    loop_continue(ctl, st->done == 0);
+}
+
+__global__ void k_trif_keep(TriFrontArgs a, int64_t cap, int32_t* __restrict__ flag) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cap; q += (int64_t)gridDim.x * blockDim.x)
+        flag[q] = q < a.nnz && a.state[a.oid[q]] != kGone;
+}
+
+// After the keep flags' scan (pos): kept entries written in column order (an
+// entry's place: kept entries before it in its part, plus kept entries of
+// the other part with smaller columns), new row starts.
+__global__ void k_trif_out(TriFrontArgs a, const int32_t* __restrict__ pos, int32_t* __restrict__ tc,
+                           int32_t* __restrict__ tr) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < a.nnz || q <= a.m; q += stride) {
+        if (q <= a.m) tr[q] = pos[a.cr[q]];
+        if (q < a.nnz && pos[q + 1] != pos[q]) {
+            const int32_t i = a.row_of[q], rb = a.cr[i], re = a.cr[i + 1], ro = rb + a.ocount[i];
+            const bool o = q < ro;
+            const int32_t pb = o ? rb : ro;
+            const int32_t ob = o ? ro : rb, oe = o ? re : ro;
+            const int32_t j = a.cc[q];
+            const int32_t t = ob + lower_bound_i32(a.cc + ob, oe - ob, j);
+            tc[pos[rb] + (pos[q] - pos[pb]) + (pos[t] - pos[ob])] = j;
+        }
+    }
+}
+
+}  // namespace
+
+int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const int32_t* mir, const TriKt& t,
+                    int64_t cap, const TriFrontBufs& b) {
+    const int64_t m = C->m, nnz = C->nnz;
+    DBuf<int32_t> deg(ctx, (size_t)m + 1), upc(ctx, (size_t)m + 1);
+    DBuf<TriFrontState> st(ctx, 1);
+    GA_CUDA(cudaMemsetAsync(st.p, 0, sizeof(TriFrontState), ctx->stream));
+    TriFrontArgs a;
+    a.cr = C->rst;
+    a.cc = C->col;
+    a.row_of = row_of;
+    a.mir = mir;
+    a.crank = t.crank;
+    a.ocount = t.ocount;
+    a.dpos = t.dpos;
+    a.oid = b.oid;
+    a.sup = b.sup;
+    a.state = b.state;
+    a.deg = deg.p;
+    a.upc = upc.p;
+    a.f0 = b.f0;
+    a.f1 = b.f1;
+    a.st = st.p;
+    a.ctr = ctx->d_counters;
+    a.m = m;
+    a.nnz = nnz;
+    a.k = k;
+    const int grid_rows = grid_for(m, 256, ctx->num_sms * 8);
+    const int grid_ent = grid_for(nnz > 0 ? nnz : 1, 256, ctx->num_sms * 16);
+    const int grid_front = ctx->num_sms * 4;
+    {
+        // iteration 0's supports: one listing of every triangle
+        tri_kt_support(ctx, C, b.sup, t, cap);
+        ProfScope ps(ctx, "trif_seed");
+        k_trif_init_rows<<<grid_rows, 256, 0, ctx->stream>>>(a);
+        post_launch("trif_init_rows");
+        if (nnz) {
+            k_trif_seed<<<grid_ent, 256, 0, ctx->stream>>>(a);
+            post_launch("trif_seed");
+        }
+    }
+    auto body = [&](const LoopCtl& ctl) {
+        {
+            ProfScope ps(ctx, "trif_count");
+            if (nnz) {
+                k_trif_count<<<grid_ent, 256, 0, ctx->stream>>>(a);
+                post_launch("trif_count");
+            }
+        }
+        ProfScope ps(ctx, "trif_round");
+        k_trif_mark<<<grid_front, 256, 0, ctx->stream>>>(a);
+        post_launch("trif_mark");
+        k_trif_lower<<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(a);
+        post_launch("trif_lower");
+        k_trif_apply<<<grid_front, 256, 0, ctx->stream>>>(a);
+        post_launch("trif_apply");
+        k_trif_finalize<<<1, 32, 0, ctx->stream>>>(st.p, m, ctl);
+        post_launch("trif_finalize");
+    };
+    {
+        ProfScope ps(ctx, "ktruss_loop");
+        run_device_loop(ctx, body, m + 1);
+    }
+    // one compaction: the kept entries, rows in column order
+    ProfScope ps(ctx, "trif_compact");
+    k_trif_keep<<<grid_for(cap, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(a, cap, b.flag);
+    post_launch("trif_keep");
+    scan_exclusive_i32_scratch(ctx, b.flag, b.flag, cap, b.scan_scr);
+    k_trif_out<<<grid_for(nnz > m ? nnz : m + 1, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(a, b.flag, b.tc,
+                                                                                             b.tr);
+    post_launch("trif_out");
+    TriFrontState hs;
+    int32_t kept = 0;
+    GA_CUDA(cudaMemcpyAsync(&hs, st.p, sizeof(TriFrontState), cudaMemcpyDeviceToHost, ctx->stream));
+    GA_CUDA(cudaMemcpyAsync(&kept, b.tr + m, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    GA_CUDA(cudaMemcpyAsync(C->rst, b.tr, sizeof(int32_t) * (size_t)(m + 1), cudaMemcpyDeviceToDevice, ctx->stream));
+    GA_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (kept) GA_CUDA(cudaMemcpyAsync(C->col, b.tc, sizeof(int32_t) * (size_t)kept, cudaMemcpyDeviceToDevice,
+                                      ctx->stream));
+    C->nnz = kept;
+    return hs.iters;
 }
 
 }  // namespace ga

@@ -117,10 +117,14 @@ GA_API int ga_version(int* major, int* minor);
  * GA_OPT_HYBRID_RATIO (16): GA_HYBRID sends a row to the inner-product form
  * when its inner-product work times this is below its Gustavson work;
  * GA_OPT_TRI_ORDER (0): GA_TRI ranks vertices by degree (0; power-law
- * graphs) or by index (1; unions of small graphs). */
+ * graphs) or by index (1; unions of small graphs).
+ * GA_OPT_KT_FRONTIER (1): the GA_TRI k-truss of one matrix lists the
+ * triangles once and then, per iteration, only the triangles of the edges it
+ * prunes, lowering the supports they touch (same edge sets and iteration
+ * counts); 0 lists every triangle again in every iteration. */
 enum { GA_OPT_DEVICE_LOOPS = 1, GA_OPT_PROFILE = 2, GA_OPT_FAIL_ALLOC_AFTER = 3, GA_OPT_KNN_TILED = 4,
        GA_OPT_MXM_WARP_FLOPS = 5, GA_OPT_MXM_HEAVY_FLOPS = 6, GA_OPT_MXM_CTAS_PER_SM = 7, GA_OPT_DOT_CHUNK = 8,
-       GA_OPT_HYBRID_RATIO = 9, GA_OPT_TRI_ORDER = 10 };
+       GA_OPT_HYBRID_RATIO = 9, GA_OPT_TRI_ORDER = 10, GA_OPT_KT_FRONTIER = 11 };
 GA_API int ga_ctx_set_option(ga_ctx ctx, int option, int64_t value);
 
 /* Per-kernel timing collected while GA_OPT_PROFILE is on. Writes up to `cap`
@@ -378,6 +382,17 @@ GA_API int ga_ktruss(ga_ctx ctx, ga_algo algo, ga_csr A, int k, ga_csr* C, int* 
 GA_API int ga_bc(ga_ctx ctx, ga_csr A, const int32_t* sources, int64_t nsrc, double* bc);
 /* Device-result variant (bc: device array of length m, overwritten). */
 GA_API int ga_bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t nsrc, double* d_bc);
+/* All-source betweenness centrality (betweenness_centrality,
+ * include/betweenness_centrality.h:5-123): sources 0..m-1 in blocks of
+ * `block` (>= 1), each block's scores added into bc (host, length m) on the
+ * device, FP64. The reference adds each block's row sums minus the block's
+ * size; that is the block's dependency sum, which is what is added here.
+ * Blocks larger than 1,024 sources run as consecutive device batches of at
+ * most 1,024 (BC is a sum over sources: the block size changes only the
+ * order of the additions). GA_ERR_INVALID_ARG for block < 1. */
+GA_API int ga_bc_all(ga_ctx ctx, ga_csr A, int64_t block, double* bc);
+/* Device-result variant (bc: device array of length m, overwritten). */
+GA_API int ga_bc_all_device(ga_ctx ctx, ga_csr A, int64_t block, double* d_bc);
 
 /* -------------------------------------------------------------- autotuner */
 /* Times candidate schedules — MSA with three warp/CTA bin thresholds and

@@ -512,21 +512,16 @@ inline std::vector<float> betweenness_centrality_batch(bool, const spMtx<int>& A
     std::vector<double> d = betweenness_centrality_sources(A, src);
     return std::vector<float>(d.begin(), d.end());
 }
-// all sources in blocks of blockSize (include/betweenness_centrality.h:5-123)
+// all sources in blocks of blockSize (include/betweenness_centrality.h:5-123),
+// accumulated on the device (ga_bc_all); blockSize 0 is refused (the
+// reference would loop forever), blocks above 1,024 sources run as device
+// batches of at most 1,024 with the same sums
 inline std::vector<float> betweenness_centrality(bool, const spMtx<int>& A, size_t blockSize) {
     if (A.m != A.n) throw "non-square matrix; BC is only for square matrices";
-    if (blockSize == 0 || blockSize > 1024) blockSize = 1024;
     detail::DevCsr a = detail::upload(A);
-    std::vector<double> acc(A.m, 0.0), part(A.m);
-    std::vector<int> src;
-    for (size_t i = 0; i < A.n; i += blockSize) {
-        size_t n = std::min(A.n - i, blockSize);
-        src.resize(n);
-        for (size_t j = 0; j < n; ++j) src[j] = (int)(i + j);
-        check(ga_bc(ctx(), a.h, src.data(), (int64_t)n, part.data()));
-        for (size_t v = 0; v < A.m; ++v) acc[v] += part[v];
-    }
-    return std::vector<float>(acc.begin(), acc.end());
+    std::vector<double> bc(A.m, 0.0);
+    check(ga_bc_all(ctx(), a.h, (int64_t)blockSize, bc.data()));
+    return std::vector<float>(bc.begin(), bc.end());
 }
 
 }  // namespace ga

@@ -329,6 +329,17 @@ def bc_batch(A: Csr, sources) -> np.ndarray:
     return bc
 
 
+def bc_all(A: Csr, block: int) -> np.ndarray:
+    """FP64 all-source BC in blocks of `block` sources (betweenness_centrality.h:5-123)."""
+    bc = np.zeros(A.m, dtype=np.float64)
+    val = _c(A.val, np.int32) if A.val is not None else None
+    rc = lib().or_bc_all(_i64(A.m), _ptr(_c(A.rst, np.int32)), _ptr(_c(A.col, np.int32)), _ptr(val),
+                         _i64(block), _ptr(bc))
+    if rc != 0:
+        raise ValueError("block must be at least 1")
+    return bc
+
+
 # ----------------------------------------------------- unmodified reference
 def _ref_new(fn, dt, *args):
     cm, cn, cnz = _i64(), _i64(), _i64()
@@ -475,6 +486,14 @@ def ref_bc_f32(A: Csr, batch: int) -> np.ndarray:
     bc = np.zeros(A.m, dtype=np.float32)
     ref().ref_bc_batch_f32(_i64(A.m), _i64(A.nnz), _ptr(_c(A.rst, np.int32)), _ptr(_c(A.col, np.int32)),
                            _i64(batch), _ptr(bc))
+    return bc
+
+
+def ref_bc_all_f32(A: Csr, block: int) -> np.ndarray:
+    """The reference's betweenness_centrality as shipped (FP32, all sources)."""
+    bc = np.zeros(A.m, dtype=np.float32)
+    ref().ref_bc_all_f32(_i64(A.m), _i64(A.nnz), _ptr(_c(A.rst, np.int32)), _ptr(_c(A.col, np.int32)),
+                         _i64(block), _ptr(bc))
     return bc
 
 

@@ -676,3 +676,25 @@ int or_bc_batch(int64_t m, const int* rst, const int* col, const int* val,
     free(owner); free(av);
     return 0;
 }
+
+/* All-source BC, betweenness_centrality (include/betweenness_centrality.h:
+ * 5-123): the sources in blocks of `block` (the last block ragged), each
+ * block run as the batched algorithm over sources i..i+n-1
+ * (betweenness_centrality.h:44-54 sets Numsp's identity rows i..i+n-1 and
+ * Front = transpose(A.extractRows(i, i+n))), its row sums minus n added
+ * into bc (:103-111). FP64. */
+int or_bc_all(int64_t m, const int* rst, const int* col, const int* val, int64_t block, double* bc) {
+    if (block < 1) return -1;
+    double* part = (double*)xmalloc(sizeof(double) * (size_t)(m ? m : 1));
+    int* src = (int*)xmalloc(sizeof(int) * (size_t)(block < m ? block : (m ? m : 1)));
+    for (int64_t v = 0; v < m; ++v) bc[v] = 0.0;
+    for (int64_t i = 0; i < m; i += block) {
+        const int64_t n = m - i < block ? m - i : block;
+        for (int64_t j = 0; j < n; ++j) src[j] = (int)(i + j);
+        or_bc_batch(m, rst, col, val, n, src, part);
+        for (int64_t v = 0; v < m; ++v) bc[v] += part[v];
+    }
+    free(part);
+    free(src);
+    return 0;
+}

@@ -105,6 +105,8 @@ int or_ktruss_ex(int64_t m, const int* rst, const int* col, const int* val, int 
 
 /* Batched betweenness centrality in FP64 over an explicit source list.
  * val may be NULL (all ones). bc has length m. */
+/* All-source BC in blocks (betweenness_centrality.h:5-123), FP64. */
+int or_bc_all(int64_t m, const int* rst, const int* col, const int* val, int64_t block, double* bc);
 int or_bc_batch(int64_t m, const int* rst, const int* col, const int* val,
                 int64_t nsrc, const int* sources, double* bc);
 

@@ -373,6 +373,18 @@ int ref_bc_batch_f32(int64_t m, int64_t nnz, const int* rst, const int* col, int
     return 0;
 }
 
+// betweenness_centrality exactly as shipped: every source, in blocks of
+// blockSize (betweenness_centrality.h:5-123), FP32.
+int ref_bc_all_f32(int64_t m, int64_t nnz, const int* rst, const int* col, int64_t block, float* bc) {
+    spMtx<int> A = make_csr<int>(m, m, nnz, rst, col, nullptr);
+    std::stringstream sink;
+    auto* old = std::cerr.rdbuf(sink.rdbuf());
+    std::vector<float> r = betweenness_centrality(true, A, (size_t)block);
+    std::cerr.rdbuf(old);
+    std::memcpy(bc, r.data(), sizeof(float) * m);
+    return 0;
+}
+
 // The same batched algorithm (betweenness_centrality.h:161-228) run with the
 // reference's own templates instantiated at double and an explicit source
 // list; the dense conversion of Numsp is zero-filled (matrix.h:586-596 form).

@@ -103,8 +103,24 @@ int main() {
         EXPECT(std::fabs((double)bcf[v] - bref[v]) <= 1e-5 * std::fmax(1.0, std::fabs(bref[v])), "bc float[%zu]", v);
     }
 
-    // unknown plugins are rejected, not run on the host
+    // all-source BC in blocks (include/betweenness_centrality.h:5), a ragged
+    // last block; the reference's float result from FP64 device sums
     bool threw = false;
+    std::vector<float> ball = betweenness_centrality(true, A, 48);
+    std::vector<double> aref(A.m);
+    or_bc_all((int64_t)A.m, A.Rst, A.Col, A.Val, 48, aref.data());
+    for (size_t v = 0; v < A.m; ++v)
+        EXPECT(std::fabs((double)ball[v] - aref[v]) <= 1e-5 * std::fmax(1.0, std::fabs(aref[v])), "bc all[%zu]", v);
+    threw = false;
+    try {
+        betweenness_centrality(true, A, 0);  // the reference would never finish
+    } catch (const ga::error&) {
+        threw = true;
+    }
+    EXPECT(threw, "blockSize 0 must throw");
+
+    // unknown plugins are rejected, not run on the host
+    threw = false;
     try {
         triangle_counting_masked_sandia(A, [](bool, const spMtx<int>&, const spMtx<int>&, const spMtx<int>&,
                                               spMtx<int>&) {}, true);

@@ -341,3 +341,55 @@ def test_ktruss_full_sweep_rmat16(ctx, algo):
             break
         k += 1
     assert k > 20  # a power-law graph: a long sweep
+
+
+@pytest.mark.parametrize("device_loops", [1, 0])
+def test_tri_ktruss_frontier_equals_relisting(ctx, device_loops):
+    """The frontier form of the GA_TRI k-truss (one listing, then only the
+    triangles of the pruned edges) against the form that lists every triangle
+    in every iteration: the same edge sets and iteration counts, and the same
+    Gustavson-product, mask-entry and entry counters (the reference's work,
+    counted per iteration)."""
+    ctx.set_option(ga.OPT_DEVICE_LOOPS, device_loops)
+    graphs = [(n, G) for n, G in TRI_GRAPHS] + [("rmat14", csr_from_arrays(*ga.gen_rmat(14, 16, seed=8)))]
+    try:
+        for name, G in graphs:
+            Gd = to_device(ctx, G)
+            for k in (3, 4, 5, 8, 12):
+                out = []
+                for frontier in (1, 0):
+                    ctx.set_option(ga.OPT_KT_FRONTIER, frontier)
+                    ctx.work_counters(reset=True)
+                    C, it = ga.ktruss("tri", Gd, k)
+                    wc = ctx.work_counters(reset=True)
+                    out.append((it, C.download(), {x: wc[x] for x in ("products", "mask_entries", "a_entries",
+                                                                      "launches", "rows")}))
+                    C.free()
+                (it1, (r1, c1, v1), w1), (it0, (r0, c0, v0), w0) = out
+                assert it1 == it0, (name, k)
+                assert np.array_equal(r1, r0) and np.array_equal(c1, c0) and np.array_equal(v1, v0), (name, k)
+                assert w1 == w0, (name, k, w1, w0)
+    finally:
+        ctx.set_option(ga.OPT_KT_FRONTIER, 1)
+        ctx.set_option(ga.OPT_DEVICE_LOOPS, 1)
+
+
+def test_bc_all_sources(ctx):
+    """All-source BC (betweenness_centrality.h:5-123) accumulated on the
+    device, against the FP64 oracle's blocked form, 1e-9 relative: ragged
+    last blocks, blocks of one source, blocks above one device batch (1,024
+    sources) and above m; a directed weighted graph; block 0 refused."""
+    rng = np.random.default_rng(91)
+    G = csr_from_arrays(*ga.gen_rmat(10, 8, seed=21))
+    Gd = to_device(ctx, G)
+    ref = oracle.bc_all(G, 100)
+    for block in (100, 64, 1, 1500, 5000):
+        _bc_close(ga.bc_all(Gd, block), ref)
+    from graphs import dense_to_csr
+    D = rng.random((150, 150)) < 0.04
+    np.fill_diagonal(D, False)
+    W = dense_to_csr(D, rng.integers(1, 3, size=(150, 150)), np.int32)
+    _bc_close(ga.bc_all(to_device(ctx, W), 33), oracle.bc_all(W, 33))
+    with pytest.raises(ga.GaError) as e:
+        ga.bc_all(Gd, 0)
+    assert e.value.code == ga.ERR_INVALID_ARG

@@ -180,3 +180,31 @@ def test_reference_graph_fixtures_match_files():
         assert np.array_equal(R.val.view(np.int64), z[f"{name}_raw_val"].view(np.int64))
         C = oracle.ref_read_mtx(path)
         assert np.array_equal(C.rst, z[f"{name}_cli_rst"]) and np.array_equal(C.col, z[f"{name}_cli_col"])
+
+
+def test_bc_all_sources_pins():
+    """All-source BC (betweenness_centrality.h:5-123) by the oracle, FP64:
+    equal to the sum of its batched runs over the blocks, to exact Brandes
+    (networkx, counting ordered pairs on an undirected graph: twice its
+    unnormalised score), and, where the reference was built, to the shipped
+    FP32 reference within single precision."""
+    oracle.build()
+    rng = np.random.default_rng(41)
+    G = random_graph(120, 0.05, rng)
+    full = oracle.bc_all(G, 32)
+    acc = np.zeros(G.m)
+    for i in range(0, G.m, 32):
+        acc += oracle.bc_batch(G, np.arange(i, min(G.m, i + 32), dtype=np.int32))
+    assert np.allclose(full, acc, rtol=1e-12, atol=1e-12)
+    assert np.allclose(oracle.bc_all(G, 7), full, rtol=1e-10, atol=1e-9)  # block size: rounding only
+    nx = pytest.importorskip("networkx")
+    H = nx.Graph()
+    H.add_nodes_from(range(G.m))
+    for i in range(G.m):
+        for j in G.col[G.rst[i]:G.rst[i + 1]]:
+            H.add_edge(i, int(j))
+    exact = nx.betweenness_centrality(H, normalized=False)
+    assert np.allclose(full, [2 * exact[v] for v in range(G.m)], rtol=1e-9, atol=1e-9)
+    if oracle.ref_available():
+        ref = oracle.ref_bc_all_f32(G, 32).astype(np.float64)
+        assert np.allclose(full, ref, rtol=2e-5, atol=2e-3)
