@@ -823,20 +823,31 @@ void tri_kt_finish(ga_ctx ctx, ga_csr C, const int32_t* row_of, const TriKt& t, 
 // (oid); one compaction at the end writes the kept entries in column order.
 // A pruned edge's triangles are found by walking the shorter of its two rows
 // and binary-searching the other (in the part its rank selects), stopping
-// once its support's worth of triangles is found. Per iteration one pass
-// over the entries counts the Gustavson products of the reference's
-// Tmp<C> = C*C for the work counters (rows with an upper part: sum of the
-// degrees of their columns).
+// once its support's worth of triangles is found.
+//
+// Work counters: iteration t adds the Gustavson products of the reference's
+// Tmp<C> = C_t*C_t over the rows with an upper part, P_t = sum over entries
+// (i, j) of C_t of h(i) deg(j) (h(i): row i has a column >= i; deg: row
+// lengths) = sum_j deg(j) H(j), H(j) = entries (i, j) with h(i) = 1. P is
+// kept as a running total: an iteration changes deg and H only at the
+// endpoints of its pruned edges and, when a row loses its last upper entry
+// (once per row and call), at that row's remaining neighbours; those
+// vertices' terms are recomputed, so no iteration passes over all entries.
 namespace {
 
 enum : uint8_t { kAlive = 0, kDying = 1, kGone = 2 };
 
 struct TriFrontState {
-    int32_t cnt[2];   // frontier sizes; the current one is cnt[t & 1]
-    int32_t t;        // iteration
-    int32_t iters;    // reported iteration count
+    int32_t cnt[2];              // frontier sizes; the current one is cnt[t & 1]
+    int32_t t;                   // iteration
+    int32_t iters;               // reported iteration count
     int32_t done;
-    int32_t pad;
+    int32_t ntouch;              // vertices whose terms of P change this iteration
+    int32_t nflip;               // rows that lost their last upper entry
+    uint32_t blocks_done;        // delta kernel: blocks finished
+    unsigned long long prod;     // P_t
+    unsigned long long mask;     // entries (i, j) of C_t with j >= i
+    unsigned long long ent;      // entries of C_t
 };
 
 struct TriFrontArgs {
@@ -852,6 +863,13 @@ struct TriFrontArgs {
     uint8_t* state;         // states at the records
     int32_t* deg;           // entries of each row still in C
     int32_t* upc;           // of those, the ones with column >= row
+    uint8_t* h;             // upc > 0, as of the iteration's start
+    int32_t* H;             // per vertex: entries (i, j) of C with h(i) = 1
+    int32_t* rd;            // per vertex: entries its row lost this iteration
+    int32_t* rh;            // per vertex: what H lost this iteration
+    int32_t* mark;          // per vertex: listed in touched
+    int32_t* touched;
+    int32_t* flip;
     int32_t* f0;
     int32_t* f1;
     TriFrontState* st;
@@ -868,12 +886,21 @@ __device__ __forceinline__ void lower_support(const TriFrontArgs& a, int32_t f, 
     if (atomicSub(a.sup + f, 1) == a.k - 2) front_push(fn, cn, f);
 }
 
+__device__ __forceinline__ void touch(const TriFrontArgs& a, int32_t x) {
+    if (atomicExch(a.mark + x, 1) == 0) front_push(a.touched, &a.st->ntouch, x);
+}
+
 __global__ void k_trif_init_rows(TriFrontArgs a) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.m; i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t b = a.cr[i], e = a.cr[i + 1], oc = a.ocount[i];
+        const int32_t up = (oc - lower_bound_i32(a.cc + b, oc, (int32_t)i)) +
+                           (e - b - oc - lower_bound_i32(a.cc + b + oc, e - b - oc, (int32_t)i));
         a.deg[i] = e - b;
-        a.upc[i] = (oc - lower_bound_i32(a.cc + b, oc, (int32_t)i)) +
-                   (e - b - oc - lower_bound_i32(a.cc + b + oc, e - b - oc, (int32_t)i));
+        a.upc[i] = up;
+        a.h[i] = up > 0;
+        a.rd[i] = 0;
+        a.rh[i] = 0;
+        a.mark[i] = 0;
     }
 }
 
@@ -895,34 +922,42 @@ __global__ void k_trif_seed(TriFrontArgs a) {
     }
 }
 
-// Work counters of iteration t, as for the reference's support product of C_t.
-__global__ void k_trif_count(TriFrontArgs a) {
+// H, and P_0, the upper entries and the entries of C_0; one warp per row.
+__global__ void k_trif_init_counts(TriFrontArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     unsigned long long prod = 0, mask = 0, ent = 0;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < a.nnz; q += (int64_t)gridDim.x * blockDim.x) {
-        if (a.state[a.oid[q]] == kGone) continue;
-        const int32_t i = a.row_of[q], j = a.cc[q];
-        if (a.upc[i] > 0) prod += (unsigned long long)a.deg[j];
-        mask += j >= i;
-        ++ent;
+    for (int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < a.m; j += warps) {
+        int hs = 0;
+        for (int32_t p = a.cr[j] + lane; p < a.cr[j + 1]; p += 32) hs += a.h[a.cc[p]];
+        hs = warp_sum<int>(hs);
+        if (lane == 0) {
+            a.H[j] = hs;
+            prod += (unsigned long long)a.deg[j] * (unsigned long long)hs;
+            mask += (unsigned long long)a.upc[j];
+            ent += (unsigned long long)a.deg[j];
+        }
     }
-    prod = warp_sum<unsigned long long>(prod);
-    mask = warp_sum<unsigned long long>(mask);
-    ent = warp_sum<unsigned long long>(ent);
-    if ((threadIdx.x & 31) == 0) {
-        if (prod) atomicAdd(&a.ctr[GA_CTR_PRODUCTS], prod);
-        if (mask) atomicAdd(&a.ctr[GA_CTR_MASK_ENTRIES], mask);
-        if (ent) atomicAdd(&a.ctr[GA_CTR_A_ENTRIES], ent);
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        atomicAdd(&a.ctr[GA_CTR_LAUNCHES], 1ull);
-        atomicAdd(&a.ctr[GA_CTR_ROWS], (unsigned long long)a.m);
+    if (lane == 0) {
+        if (prod) atomicAdd(&a.st->prod, prod);
+        if (mask) atomicAdd(&a.st->mask, mask);
+        if (ent) atomicAdd(&a.st->ent, ent);
     }
 }
 
+// Start of iteration t: the work counters of its support product, and the
+// frontier marked.
 __global__ void k_trif_mark(TriFrontArgs a) {
     const int t = a.st->t;
     const int32_t n = a.st->cnt[t & 1];
     const int32_t* F = (t & 1) ? a.f1 : a.f0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(&a.ctr[GA_CTR_PRODUCTS], a.st->prod);
+        atomicAdd(&a.ctr[GA_CTR_MASK_ENTRIES], a.st->mask);
+        atomicAdd(&a.ctr[GA_CTR_A_ENTRIES], a.st->ent);
+        atomicAdd(&a.ctr[GA_CTR_LAUNCHES], 1ull);
+        atomicAdd(&a.ctr[GA_CTR_ROWS], (unsigned long long)a.m);
+    }
     for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x)
         a.state[F[x]] = kDying;
 }
@@ -986,9 +1021,9 @@ __global__ void __launch_bounds__(128) k_trif_lower(TriFrontArgs a) {
                     }
                 }
             }
-            const int h = __popc(__ballot_sync(0xffffffffu, hit));
-            found += h;
-            if (lane == 0) tris += (unsigned long long)h;
+            const int hcount = __popc(__ballot_sync(0xffffffffu, hit));
+            found += hcount;
+            if (lane == 0) tris += (unsigned long long)hcount;
             if (found >= target) break;
         }
     }
@@ -999,25 +1034,42 @@ __global__ void __launch_bounds__(128) k_trif_lower(TriFrontArgs a) {
     }
 }
 
-// The frontier's edges leave C_t: rows shorten, diagonal entries whose row
-// length drops below k - 2 join the next frontier.
+// The frontier's edges leave C_t: rows shorten (diagonal entries whose row
+// length drops below k - 2 join the next frontier), the terms of P at their
+// endpoints change, rows that lose their last upper entry are listed.
 __global__ void k_trif_apply(TriFrontArgs a) {
     const int t = a.st->t;
     const int32_t n = a.st->cnt[t & 1];
     const int32_t* F = (t & 1) ? a.f1 : a.f0;
     int32_t* fn = (t & 1) ? a.f0 : a.f1;
     int32_t* cn = &a.st->cnt[(t + 1) & 1];
+    unsigned long long mask = 0, ent = 0;
     for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
         const int32_t q = F[x];
         const int32_t u = a.row_of[q], v = a.cc[q];
         a.state[q] = kGone;
+        ++mask;
         if (u == v) {
+            ++ent;
             atomicSub(a.deg + u, 1);
-            atomicSub(a.upc + u, 1);
+            atomicAdd(a.rd + u, 1);
+            atomicSub(a.H + u, 1);  // h(u) = 1 while its diagonal entry is there
+            atomicAdd(a.rh + u, 1);
+            touch(a, u);
+            if (atomicSub(a.upc + u, 1) == 1) front_push(a.flip, &a.st->nflip, u);
             continue;
         }
-        atomicSub(a.upc + min(u, v), 1);
+        ent += 2;
         const int32_t ou = atomicSub(a.deg + u, 1), ov = atomicSub(a.deg + v, 1);
+        atomicAdd(a.rd + u, 1);
+        atomicAdd(a.rd + v, 1);
+        if (a.h[u]) { atomicSub(a.H + v, 1); atomicAdd(a.rh + v, 1); }
+        if (a.h[v]) { atomicSub(a.H + u, 1); atomicAdd(a.rh + u, 1); }
+        touch(a, u);
+        touch(a, v);
+        const int32_t lo = min(u, v);
+        if (atomicSub(a.upc + lo, 1) == 1) front_push(a.flip, &a.st->nflip, lo);
+        // a diagonal entry's support is its row's length
         if (ou == a.k - 2) {
             const int32_t d = a.dpos[u];
             if (d >= 0 && a.state[d] == kAlive) front_push(fn, cn, d);
@@ -1027,10 +1079,67 @@ __global__ void k_trif_apply(TriFrontArgs a) {
             if (d >= 0 && a.state[d] == kAlive) front_push(fn, cn, d);
         }
     }
+    mask = warp_sum<unsigned long long>(mask);
+    ent = warp_sum<unsigned long long>(ent);
+    if ((threadIdx.x & 31) == 0 && mask) {
+        atomicAdd(&a.st->mask, (unsigned long long)(-(long long)mask));
+        atomicAdd(&a.st->ent, (unsigned long long)(-(long long)ent));
+    }
 }
 
-__global__ void k_trif_finalize(TriFrontState* st, int64_t m, LoopCtl ctl) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// Rows that lost their last upper entry: h drops to 0, so every remaining
+// neighbour's H loses 1. One warp per row.
+__global__ void k_trif_flip(TriFrontArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int32_t n = a.st->nflip;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t x = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; x < n; x += warps) {
+        const int32_t i = a.flip[x];
+        if (lane == 0) a.h[i] = 0;
+        for (int32_t p = a.cr[i] + lane; p < a.cr[i + 1]; p += 32) {
+            if (a.state[a.oid[p]] == kGone) continue;
+            const int32_t j = a.cc[p];
+            atomicSub(a.H + j, 1);
+            atomicAdd(a.rh + j, 1);
+            touch(a, j);
+        }
+    }
+}
+
+// P_{t+1} = P_t + the change of deg(j) H(j) at every touched vertex; the
+// last block to finish ends the iteration (stop when F_t was empty, or
+// after m iterations) and tells the loop whether to go on.
+__global__ void __launch_bounds__(256) k_trif_delta(TriFrontArgs a, LoopCtl ctl) {
+    __shared__ long long part[8];
+    __shared__ bool last;
+    const int32_t n = a.st->ntouch;
+    long long d = 0;
+    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t j = a.touched[x];
+        const long long nd = a.deg[j], nh = a.H[j];
+        const long long od = nd + a.rd[j], oh = nh + a.rh[j];
+        d += nd * nh - od * oh;
+        a.rd[j] = 0;
+        a.rh[j] = 0;
+        a.mark[j] = 0;
+    }
+    d = warp_sum<long long>(d);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = d;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += part[w];
+        if (s) atomicAdd(&a.st->prod, (unsigned long long)s);
+        __threadfence();
+        last = atomicAdd(&a.st->blocks_done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    TriFrontState* st = a.st;
+    st->blocks_done = 0;
+    st->ntouch = 0;
+    st->nflip = 0;
     const int t = st->t;
     if (st->cnt[t & 1] == 0) {
         st->iters = t + 1;
@@ -1038,7 +1147,7 @@ __global__ void k_trif_finalize(TriFrontState* st, int64_t m, LoopCtl ctl) {
     } else {
         st->cnt[t & 1] = 0;
         st->t = t + 1;
-        if ((int64_t)(t + 1) >= m) {
+        if ((int64_t)(t + 1) >= a.m) {
             st->iters = 0;
             st->done = 1;
         }
@@ -1076,7 +1185,10 @@ __global__ void k_trif_out(TriFrontArgs a, const int32_t* __restrict__ pos, int3
 int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const int32_t* mir, const TriKt& t,
                     int64_t cap, const TriFrontBufs& b) {
     const int64_t m = C->m, nnz = C->nnz;
-    DBuf<int32_t> deg(ctx, (size_t)m + 1), upc(ctx, (size_t)m + 1);
+    const size_t mv = (size_t)m + 1;
+    DBuf<int32_t> deg(ctx, mv), upc(ctx, mv), H(ctx, mv), rd(ctx, mv), rh(ctx, mv), mark(ctx, mv), touched(ctx, mv),
+        flip(ctx, mv);
+    DBuf<uint8_t> h(ctx, mv);
     DBuf<TriFrontState> st(ctx, 1);
     GA_CUDA(cudaMemsetAsync(st.p, 0, sizeof(TriFrontState), ctx->stream));
     TriFrontArgs a;
@@ -1092,6 +1204,13 @@ int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const in
     a.state = b.state;
     a.deg = deg.p;
     a.upc = upc.p;
+    a.h = h.p;
+    a.H = H.p;
+    a.rd = rd.p;
+    a.rh = rh.p;
+    a.mark = mark.p;
+    a.touched = touched.p;
+    a.flip = flip.p;
     a.f0 = b.f0;
     a.f1 = b.f1;
     a.st = st.p;
@@ -1112,24 +1231,33 @@ int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const in
             k_trif_seed<<<grid_ent, 256, 0, ctx->stream>>>(a);
             post_launch("trif_seed");
         }
+        k_trif_init_counts<<<grid_for(m * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(a);
+        post_launch("trif_init_counts");
     }
     auto body = [&](const LoopCtl& ctl) {
         {
-            ProfScope ps(ctx, "trif_count");
-            if (nnz) {
-                k_trif_count<<<grid_ent, 256, 0, ctx->stream>>>(a);
-                post_launch("trif_count");
-            }
+            ProfScope ps(ctx, "trif_mark");
+            k_trif_mark<<<grid_front, 256, 0, ctx->stream>>>(a);
+            post_launch("trif_mark");
         }
-        ProfScope ps(ctx, "trif_round");
-        k_trif_mark<<<grid_front, 256, 0, ctx->stream>>>(a);
-        post_launch("trif_mark");
-        k_trif_lower<<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(a);
-        post_launch("trif_lower");
-        k_trif_apply<<<grid_front, 256, 0, ctx->stream>>>(a);
-        post_launch("trif_apply");
-        k_trif_finalize<<<1, 32, 0, ctx->stream>>>(st.p, m, ctl);
-        post_launch("trif_finalize");
+        {
+            ProfScope ps(ctx, "trif_lower");
+            k_trif_lower<<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(a);
+            post_launch("trif_lower");
+        }
+        {
+            ProfScope ps(ctx, "trif_apply");
+            k_trif_apply<<<grid_front, 256, 0, ctx->stream>>>(a);
+            post_launch("trif_apply");
+        }
+        {
+            ProfScope ps(ctx, "trif_flip");
+            k_trif_flip<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(a);
+            post_launch("trif_flip");
+        }
+        ProfScope ps(ctx, "trif_delta");
+        k_trif_delta<<<ctx->num_sms * 2, 256, 0, ctx->stream>>>(a, ctl);
+        post_launch("trif_delta");
     };
     {
         ProfScope ps(ctx, "ktruss_loop");
