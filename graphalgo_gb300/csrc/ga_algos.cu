@@ -494,11 +494,11 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
             if (tri) {
                 // rows partitioned [ranked above the row | the rest] for the whole loop
                 tri_kt_setup(ctx, C, row_of.p, mir.p, tc.p, eflag.p, tk, cap);
-                if (!batch && ctx->kt_frontier) {
+                if (ctx->kt_frontier) {
                     // one listing, then only the triangles of the pruned edges
                     const TriFrontBufs fb{sup.p, eflag.p, tr.p, tc.p, pos_new.p, trow.p, mir_new.p,
                                           reinterpret_cast<uint8_t*>(tk.tcrank), scan_scr.p};
-                    const int it = tri_kt_frontier(ctx, C, k, row_of.p, mir.p, tk, cap, fb);
+                    const int it = tri_kt_frontier(ctx, C, k, row_of.p, mir.p, tk, cap, fb, batch);
                     C->unit = 1;
                     C->sym = 1;
                     if (iters_out) *iters_out = it;

@@ -278,8 +278,10 @@ struct TriFrontBufs {
     uint8_t* state;
     void* scan_scr;
 };
+// With `batch`: every graph of the union with its own k, iteration count
+// (batch->iters_g) and iteration bound; the loop runs while a graph iterates.
 int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const int32_t* mir, const TriKt& t,
-                    int64_t cap, const TriFrontBufs& b);
+                    int64_t cap, const TriFrontBufs& b, const KtBatch* batch);
 
 // Autotuned algorithm resolution: GA_AUTO becomes the cached (or freshly
 // tuned) variant, and ctx->tune its schedule; other values pass through.

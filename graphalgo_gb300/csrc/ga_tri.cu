@@ -845,7 +845,9 @@ struct TriFrontState {
     int32_t ntouch;              // vertices whose terms of P change this iteration
     int32_t nflip;               // rows that lost their last upper entry
     uint32_t blocks_done;        // delta kernel: blocks finished
-    unsigned long long prod;     // P_t
+    uint32_t blocks_done_g;      // graph kernel (batches): blocks finished
+    int32_t live;                // batches: graphs still iterating
+    unsigned long long prod;     // P_t (batches: summed over the live graphs)
     unsigned long long mask;     // entries (i, j) of C_t with j >= i
     unsigned long long ent;      // entries of C_t
 };
@@ -877,13 +879,42 @@ struct TriFrontArgs {
     int64_t m;
     int64_t nnz;
     int k;
+    // batches of graphs (block-diagonal union; gid == nullptr: one matrix)
+    const int32_t* gid;     // graph of each row
+    const int32_t* kg;      // per-graph k (nullptr: k for every graph)
+    const int32_t* nvert;   // vertices per graph
+    int32_t* done_g;        // graph finished (converged, or stopped after n_g iterations)
+    int32_t* iters_g;       // reported iteration count per graph
+    int32_t* cntg;          // 2 x ngraphs: frontier elements per graph, by iteration parity
+    long long* pg;          // P per graph
+    int64_t ngraphs;
 };
 
 __device__ __forceinline__ void front_push(int32_t* buf, int32_t* cnt, int32_t x) { buf[atomicAdd(cnt, 1)] = x; }
 
+// k - 2 for the graph of row i
+__device__ __forceinline__ int kt_thr(const TriFrontArgs& a, int32_t i) {
+    return (a.kg ? a.kg[a.gid[i]] : a.k) - 2;
+}
+
+// A frontier element of row i for iteration parity par (batches also count
+// it for the row's graph).
+__device__ __forceinline__ void front_add(const TriFrontArgs& a, int32_t* buf, int32_t* cnt, int32_t x, int32_t i,
+                                          int par) {
+    front_push(buf, cnt, x);
+    if (a.gid) atomicAdd(a.cntg + par * a.ngraphs + a.gid[i], 1);
+}
+
+// Batches: the element's graph finished (a graph stopped by its iteration
+// bound keeps its edges; its queued elements are dropped).
+__device__ __forceinline__ bool kt_frozen(const TriFrontArgs& a, int32_t i) {
+    return a.gid && a.done_g[a.gid[i]];
+}
+
 // One support unit less; the edge joins the next frontier when it drops below k - 2.
-__device__ __forceinline__ void lower_support(const TriFrontArgs& a, int32_t f, int32_t* fn, int32_t* cn) {
-    if (atomicSub(a.sup + f, 1) == a.k - 2) front_push(fn, cn, f);
+__device__ __forceinline__ void lower_support(const TriFrontArgs& a, int32_t f, int32_t* fn, int32_t* cn, int par) {
+    const int32_t i = a.row_of[f];
+    if (atomicSub(a.sup + f, 1) == kt_thr(a, i)) front_add(a, fn, cn, f, i, par);
 }
 
 __device__ __forceinline__ void touch(const TriFrontArgs& a, int32_t x) {
@@ -913,11 +944,11 @@ __global__ void k_trif_seed(TriFrontArgs a) {
         a.oid[q] = rec ? (int32_t)q : a.mir[q];
         a.state[q] = kAlive;
         if (i == j) {
-            if (a.deg[i] < a.k - 2) front_push(a.f0, &a.st->cnt[0], (int32_t)q);
+            if (a.deg[i] < kt_thr(a, i)) front_add(a, a.f0, &a.st->cnt[0], (int32_t)q, i, 0);
         } else if (rec) {
             const int32_t s = a.sup[q] + (a.dpos[i] >= 0) + (a.dpos[j] >= 0);
             a.sup[q] = s;
-            if (s < a.k - 2) front_push(a.f0, &a.st->cnt[0], (int32_t)q);
+            if (s < kt_thr(a, i)) front_add(a, a.f0, &a.st->cnt[0], (int32_t)q, i, 0);
         }
     }
 }
@@ -933,7 +964,9 @@ __global__ void k_trif_init_counts(TriFrontArgs a) {
         hs = warp_sum<int>(hs);
         if (lane == 0) {
             a.H[j] = hs;
-            prod += (unsigned long long)a.deg[j] * (unsigned long long)hs;
+            const unsigned long long pj = (unsigned long long)a.deg[j] * (unsigned long long)hs;
+            prod += pj;
+            if (a.gid && pj) atomicAdd(reinterpret_cast<unsigned long long*>(a.pg + a.gid[j]), pj);
             mask += (unsigned long long)a.upc[j];
             ent += (unsigned long long)a.deg[j];
         }
@@ -943,6 +976,11 @@ __global__ void k_trif_init_counts(TriFrontArgs a) {
         if (mask) atomicAdd(&a.st->mask, mask);
         if (ent) atomicAdd(&a.st->ent, ent);
     }
+    // batches: the graphs still to iterate
+    if (a.gid)
+        for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < a.ngraphs;
+             g += (int64_t)gridDim.x * blockDim.x)
+            if (!a.done_g[g]) atomicAdd(&a.st->live, 1);
 }
 
 // Start of iteration t: the work counters of its support product, and the
@@ -958,8 +996,10 @@ __global__ void k_trif_mark(TriFrontArgs a) {
         atomicAdd(&a.ctr[GA_CTR_LAUNCHES], 1ull);
         atomicAdd(&a.ctr[GA_CTR_ROWS], (unsigned long long)a.m);
     }
-    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x)
-        a.state[F[x]] = kDying;
+    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t q = F[x];
+        if (!kt_frozen(a, a.row_of[q])) a.state[q] = kDying;
+    }
 }
 
 // One warp per frontier edge: its triangles in C_t, the supports they lower.
@@ -970,17 +1010,19 @@ __global__ void __launch_bounds__(128) k_trif_lower(TriFrontArgs a) {
     const int32_t* F = (t & 1) ? a.f1 : a.f0;
     int32_t* fn = (t & 1) ? a.f0 : a.f1;
     int32_t* cn = &a.st->cnt[(t + 1) & 1];
+    const int np = (t + 1) & 1;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     unsigned long long probes = 0, tris = 0;
     for (int64_t x = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; x < n; x += warps) {
         const int32_t q = F[x];
         const int32_t u = a.row_of[q], v = a.cc[q];
+        if (kt_frozen(a, u)) continue;
         if (u == v) {
             // a diagonal entry leaves: every other edge of its row loses 1
             for (int32_t p = a.cr[u] + lane; p < a.cr[u + 1]; p += 32) {
                 if (a.cc[p] == u) continue;
                 const int32_t f = a.oid[p];
-                if (a.state[f] == kAlive) lower_support(a, f, fn, cn);
+                if (a.state[f] == kAlive) lower_support(a, f, fn, cn, np);
             }
             continue;
         }
@@ -1014,8 +1056,8 @@ __global__ void __launch_bounds__(128) k_trif_lower(TriFrontArgs a) {
                             const uint8_t sg = a.state[g];
                             if (sg != kGone) {
                                 hit = true;
-                                if (sf == kAlive && (sg == kAlive || q < g)) lower_support(a, f, fn, cn);
-                                if (sg == kAlive && (sf == kAlive || q < f)) lower_support(a, g, fn, cn);
+                                if (sf == kAlive && (sg == kAlive || q < g)) lower_support(a, f, fn, cn, np);
+                                if (sg == kAlive && (sf == kAlive || q < f)) lower_support(a, g, fn, cn, np);
                             }
                         }
                     }
@@ -1043,10 +1085,12 @@ __global__ void k_trif_apply(TriFrontArgs a) {
     const int32_t* F = (t & 1) ? a.f1 : a.f0;
     int32_t* fn = (t & 1) ? a.f0 : a.f1;
     int32_t* cn = &a.st->cnt[(t + 1) & 1];
+    const int np = (t + 1) & 1;
     unsigned long long mask = 0, ent = 0;
     for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
         const int32_t q = F[x];
         const int32_t u = a.row_of[q], v = a.cc[q];
+        if (kt_frozen(a, u)) continue;
         a.state[q] = kGone;
         ++mask;
         if (u == v) {
@@ -1070,13 +1114,13 @@ __global__ void k_trif_apply(TriFrontArgs a) {
         const int32_t lo = min(u, v);
         if (atomicSub(a.upc + lo, 1) == 1) front_push(a.flip, &a.st->nflip, lo);
         // a diagonal entry's support is its row's length
-        if (ou == a.k - 2) {
+        if (ou == kt_thr(a, u)) {
             const int32_t d = a.dpos[u];
-            if (d >= 0 && a.state[d] == kAlive) front_push(fn, cn, d);
+            if (d >= 0 && a.state[d] == kAlive) front_add(a, fn, cn, d, u, np);
         }
-        if (ov == a.k - 2) {
+        if (ov == kt_thr(a, v)) {
             const int32_t d = a.dpos[v];
-            if (d >= 0 && a.state[d] == kAlive) front_push(fn, cn, d);
+            if (d >= 0 && a.state[d] == kAlive) front_add(a, fn, cn, d, v, np);
         }
     }
     mask = warp_sum<unsigned long long>(mask);
@@ -1106,9 +1150,10 @@ __global__ void k_trif_flip(TriFrontArgs a) {
     }
 }
 
-// P_{t+1} = P_t + the change of deg(j) H(j) at every touched vertex; the
-// last block to finish ends the iteration (stop when F_t was empty, or
-// after m iterations) and tells the loop whether to go on.
+// P_{t+1} = P_t + the change of deg(j) H(j) at every touched vertex (for a
+// batch also per graph). For one matrix, the last block to finish ends the
+// iteration (stop when F_t was empty, or after m iterations) and tells the
+// loop whether to go on; batches end it in k_trif_graphs.
 __global__ void __launch_bounds__(256) k_trif_delta(TriFrontArgs a, LoopCtl ctl) {
     __shared__ long long part[8];
     __shared__ bool last;
@@ -1118,7 +1163,9 @@ __global__ void __launch_bounds__(256) k_trif_delta(TriFrontArgs a, LoopCtl ctl)
         const int32_t j = a.touched[x];
         const long long nd = a.deg[j], nh = a.H[j];
         const long long od = nd + a.rd[j], oh = nh + a.rh[j];
-        d += nd * nh - od * oh;
+        const long long dj = nd * nh - od * oh;
+        d += dj;
+        if (a.gid && dj) atomicAdd(reinterpret_cast<unsigned long long*>(a.pg + a.gid[j]), (unsigned long long)dj);
         a.rd[j] = 0;
         a.rh[j] = 0;
         a.mark[j] = 0;
@@ -1140,6 +1187,7 @@ __global__ void __launch_bounds__(256) k_trif_delta(TriFrontArgs a, LoopCtl ctl)
     st->blocks_done = 0;
     st->ntouch = 0;
     st->nflip = 0;
+    if (a.gid) return;
     const int t = st->t;
     if (st->cnt[t & 1] == 0) {
         st->iters = t + 1;
@@ -1152,6 +1200,62 @@ __global__ void __launch_bounds__(256) k_trif_delta(TriFrontArgs a, LoopCtl ctl)
             st->done = 1;
         }
     }
+    loop_continue(ctl, st->done == 0);
+}
+
+// Batches, end of iteration t, one thread per graph: a live graph without
+// frontier elements in this iteration has converged (iteration count t + 1),
+// one that reached its bound stops with count 0 (n_g iterations, as the
+// reference's loop); both leave the live set and their P leaves the work
+// total. The last block ends the iteration; the loop goes on while a graph
+// is live.
+__global__ void __launch_bounds__(256) k_trif_graphs(TriFrontArgs a, LoopCtl ctl) {
+    __shared__ long long part[8];
+    __shared__ int lpart[8];
+    __shared__ bool last;
+    const int t = a.st->t;
+    int32_t* cnt = a.cntg + (t & 1) * a.ngraphs;
+    long long dp = 0;
+    int dl = 0;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < a.ngraphs;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t c = cnt[g];
+        cnt[g] = 0;
+        if (a.done_g[g]) continue;
+        if (c == 0 || (int64_t)(t + 1) >= a.nvert[g]) {
+            a.iters_g[g] = c == 0 ? t + 1 : 0;
+            a.done_g[g] = 1;
+            dp -= a.pg[g];
+            ++dl;
+        }
+    }
+    dp = warp_sum<long long>(dp);
+    dl = warp_sum<int>(dl);
+    if ((threadIdx.x & 31) == 0) {
+        part[threadIdx.x >> 5] = dp;
+        lpart[threadIdx.x >> 5] = dl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long s = 0;
+        int l = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            s += part[w];
+            l += lpart[w];
+        }
+        if (s) atomicAdd(&a.st->prod, (unsigned long long)s);
+        if (l) atomicSub(&a.st->live, l);
+        __threadfence();
+        last = atomicAdd(&a.st->blocks_done_g, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    TriFrontState* st = a.st;
+    st->blocks_done_g = 0;
+    st->cnt[t & 1] = 0;
+    st->t = t + 1;
+    if (st->live <= 0) st->done = 1;
     loop_continue(ctl, st->done == 0);
 }
 
@@ -1183,14 +1287,21 @@ __global__ void k_trif_out(TriFrontArgs a, const int32_t* __restrict__ pos, int3
 }  // namespace
 
 int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const int32_t* mir, const TriKt& t,
-                    int64_t cap, const TriFrontBufs& b) {
+                    int64_t cap, const TriFrontBufs& b, const KtBatch* batch) {
     const int64_t m = C->m, nnz = C->nnz;
     const size_t mv = (size_t)m + 1;
+    const int64_t ng = batch ? batch->ngraphs : 0;
     DBuf<int32_t> deg(ctx, mv), upc(ctx, mv), H(ctx, mv), rd(ctx, mv), rh(ctx, mv), mark(ctx, mv), touched(ctx, mv),
         flip(ctx, mv);
     DBuf<uint8_t> h(ctx, mv);
     DBuf<TriFrontState> st(ctx, 1);
+    DBuf<int32_t> cntg(ctx, batch ? (size_t)(2 * ng) : 1);
+    DBuf<long long> pg(ctx, batch ? (size_t)ng : 1);
     GA_CUDA(cudaMemsetAsync(st.p, 0, sizeof(TriFrontState), ctx->stream));
+    if (batch) {
+        GA_CUDA(cudaMemsetAsync(cntg.p, 0, sizeof(int32_t) * (size_t)(2 * ng), ctx->stream));
+        GA_CUDA(cudaMemsetAsync(pg.p, 0, sizeof(long long) * (size_t)ng, ctx->stream));
+    }
     TriFrontArgs a;
     a.cr = C->rst;
     a.cc = C->col;
@@ -1218,6 +1329,14 @@ int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const in
     a.m = m;
     a.nnz = nnz;
     a.k = k;
+    a.gid = batch ? batch->gid : nullptr;
+    a.kg = batch ? batch->kg : nullptr;
+    a.nvert = batch ? batch->nvert : nullptr;
+    a.done_g = batch ? batch->done_g : nullptr;
+    a.iters_g = batch ? batch->iters_g : nullptr;
+    a.cntg = batch ? cntg.p : nullptr;
+    a.pg = batch ? pg.p : nullptr;
+    a.ngraphs = ng;
     const int grid_rows = grid_for(m, 256, ctx->num_sms * 8);
     const int grid_ent = grid_for(nnz > 0 ? nnz : 1, 256, ctx->num_sms * 16);
     const int grid_front = ctx->num_sms * 4;
@@ -1231,7 +1350,7 @@ int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const in
             k_trif_seed<<<grid_ent, 256, 0, ctx->stream>>>(a);
             post_launch("trif_seed");
         }
-        k_trif_init_counts<<<grid_for(m * 32, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(a);
+        k_trif_init_counts<<<grid_for(std::max<int64_t>(m * 32, ng), 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(a);
         post_launch("trif_init_counts");
     }
     auto body = [&](const LoopCtl& ctl) {
@@ -1258,6 +1377,10 @@ int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const in
         ProfScope ps(ctx, "trif_delta");
         k_trif_delta<<<ctx->num_sms * 2, 256, 0, ctx->stream>>>(a, ctl);
         post_launch("trif_delta");
+        if (batch) {
+            k_trif_graphs<<<grid_for(ng, 256, ctx->num_sms * 2), 256, 0, ctx->stream>>>(a, ctl);
+            post_launch("trif_graphs");
+        }
     };
     {
         ProfScope ps(ctx, "ktruss_loop");

@@ -175,14 +175,48 @@ TuneEntry tune_support(ga_ctx ctx, ga_csr A, int only) {
         expand_rows(ctx, A, row_of.p);
         mirror_index(ctx, A, row_of.p, mir.p);
     }
-    return pick(ctx, product_candidates(sym, only, tri_ok), [&](const Cand& c) {
+    auto support = [&](const Cand& c) {
         if (c.algo == GA_TRI) {
             tri_prepare(ctx, A, tscr.p, nnz);  // ranks of the candidate's order (ctx->tune)
             tri_support_launch(ctx, A, row_of.p, mir.p, pos.p, sup.p, tscr.p, nnz, true);
         } else if (c.algo == GA_DOT) mxm_dot_launch(ctx, A, A, A, M, sup.p, unit, mre);
         else mxm_masked_launch(ctx, c.algo, A, A, M, sup.p, scr.p, nnz, unit, mre, unit,
                                c.algo == GA_HYBRID ? A : nullptr);
-    });
+    };
+    const std::vector<Cand> cands = product_candidates(sym, only, tri_ok);
+    if (!tri_ok || !ctx->kt_frontier) return pick(ctx, cands, support);
+    // With the frontier loop GA_TRI lists the triangles once per call, while
+    // the other forms compute the support in every iteration: whole 4-truss
+    // calls are compared. A candidate whose single support product already
+    // takes longer than the fastest GA_TRI 4-truss cannot win and is not run.
+    auto whole = [&](const Cand& c) { csr_destroy(ctx, ktruss_impl(ctx, c.algo, A, 4, nullptr, nullptr)); };
+    std::vector<Cand> finalists;
+    {
+        CounterGuard cg(ctx);
+        const MxmTune saved = ctx->tune;
+        double t_tri = INFINITY;
+        try {
+            for (const Cand& c : cands)
+                if (c.algo == GA_TRI) {
+                    ctx->tune = c.t;
+                    whole(c);
+                    t_tri = std::min(t_tri, time_once(ctx, [&] { whole(c); }));
+                    finalists.push_back(c);
+                }
+            for (const Cand& c : cands)
+                if (c.algo != GA_TRI) {
+                    ctx->tune = c.t;
+                    if (time_once(ctx, [&] { support(c); }) < t_tri) finalists.push_back(c);
+                }
+        } catch (...) {
+            ctx->tune = saved;
+            throw;
+        }
+        ctx->tune = saved;
+    }
+    TuneEntry e = pick(ctx, finalists, whole);
+    e.candidates = (int)cands.size();
+    return e;
 }
 
 TuneEntry tune_product(ga_ctx ctx, ga_csr A, ga_csr B, ga_csr M, int only) {

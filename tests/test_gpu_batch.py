@@ -201,3 +201,38 @@ def test_batch_bc_matches_single(ctx):
         assert np.all(np.abs(part - ref) <= 1e-9 * np.maximum(np.abs(ref), 1.0)), g
         orc = oracle.bc_batch(G, src)
         assert np.all(np.abs(part - orc) <= 1e-9 * np.maximum(np.abs(orc), 1.0)), g
+
+
+@pytest.mark.parametrize("device_loops", [1, 0])
+def test_batch_ktruss_frontier_per_graph_k(ctx, device_loops):
+    """The batched GA_TRI k-truss on the frontier path (one listing over the
+    union, then only the pruned edges' triangles; every graph with its own
+    k, iteration count and bound) against the batched form that lists every
+    triangle each iteration and against each graph alone: edge sets and
+    iteration counts equal, graphs without vertices or edges included."""
+    host, dev = _mixed_parts(ctx)
+    host.append(csr_from_arrays(*ga.gen_knn(500, 8, 30, seed=12)))
+    dev.append(to_device(ctx, host[-1]))
+    U, voff = ga.block_diag(ctx, dev)
+    ks = [3, 5, 4, 8, 6, 3, 7, 9]
+    ctx.set_option(ga.OPT_DEVICE_LOOPS, device_loops)
+    try:
+        out = []
+        for frontier in (1, 0):
+            ctx.set_option(ga.OPT_KT_FRONTIER, frontier)
+            C, iters = ga.batch_ktruss_k("tri", U, voff, ks)
+            cr, cc, _ = C.download()
+            out.append((list(iters), ga.split_blocks(cr, cc, voff)))
+            C.free()
+        (it1, b1), (it0, b0) = out
+        assert it1 == it0
+        for g, ((m1, r1, c1), (m0, r0, c0)) in enumerate(zip(b1, b0)):
+            assert np.array_equal(r1, r0) and np.array_equal(c1, c0), f"graph {g}"
+        for g, (G, Gd) in enumerate(zip(host, dev)):
+            C, it = ga.ktruss("tri", Gd, ks[g])
+            r, c, _ = C.download()
+            assert it1[g] == it, f"graph {g}"
+            assert np.array_equal(b1[g][1], r) and np.array_equal(b1[g][2], c), f"graph {g}"
+    finally:
+        ctx.set_option(ga.OPT_KT_FRONTIER, 1)
+        ctx.set_option(ga.OPT_DEVICE_LOOPS, 1)
