@@ -258,6 +258,12 @@ class Csr:
         _check(lib().ga_csr_device_ptrs(self.handle, ctypes.byref(r), ctypes.byref(c), ctypes.byref(v)))
         return int(r.value or 0), int(c.value or 0), int(v.value or 0)
 
+    def set_symmetric(self, symmetric: int = 1) -> None:
+        """Declares the matrix symmetric (1: the device check is skipped; a
+        false declaration gives wrong results), not symmetric (0), or
+        unknown (-1: checked again on the next use)."""
+        _check(lib().ga_csr_set_symmetric(self.ctx.handle, self.handle, int(symmetric)), self.ctx)
+
     def free(self):
         if self.handle:
             lib().ga_csr_free(self.ctx.handle, self.handle)
@@ -623,7 +629,7 @@ REQ_TC, REQ_KTRUSS, REQ_BC = 0, 1, 2
 class ServerConfig(ctypes.Structure):
     _fields_ = [("workers", _int), ("coalesce", _int), ("tc_algo", _int), ("ktruss_algo", _int),
                 ("hbm_budget", _i64), ("coalesce_nnz", _i64), ("coalesce_max_nnz", _i64),
-                ("coalesce_max_requests", _i64)]
+                ("coalesce_max_requests", _i64), ("bc_group_pairs", _i64)]
 
 
 class ServerResult(ctypes.Structure):
@@ -651,9 +657,10 @@ class Server:
 
     def __init__(self, device: int = 0, workers: int = 4, coalesce: bool = True, tc_algo="msa",
                  ktruss_algo="msa", hbm_budget: int = 0, coalesce_nnz: int = 0, coalesce_max_nnz: int = 0,
-                 coalesce_max_requests: int = 0):
+                 coalesce_max_requests: int = 0, bc_group_pairs: int = 0):
         cfg = ServerConfig(int(workers), int(bool(coalesce)), _algo(tc_algo), _algo(ktruss_algo), int(hbm_budget),
-                           int(coalesce_nnz), int(coalesce_max_nnz), int(coalesce_max_requests))
+                           int(coalesce_nnz), int(coalesce_max_nnz), int(coalesce_max_requests),
+                           int(bc_group_pairs))
         self.handle = _p()
         self.sizes = []
         _check(lib().ga_server_create(_int(device), ctypes.byref(cfg), ctypes.byref(self.handle)))

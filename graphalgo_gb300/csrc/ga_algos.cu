@@ -71,6 +71,103 @@ void run_device_loop(ga_ctx ctx, const std::function<void(const LoopCtl&)>& body
     cudaGraphDestroy(graph);
 }
 
+namespace {
+struct CachedLoop {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int* cont = nullptr;   // the loop's continue flag (host-loop mode)
+    void* args = nullptr;  // the call's parameters
+    size_t args_bytes = 0;
+    LoopCtl ctl{};
+};
+
+CachedLoop* cache_slot(ga_ctx ctx, int slot) {
+    GA_REQUIRE(slot >= 0 && slot < 4, GA_ERR_INVALID_ARG, "loop cache slot out of range");
+    if (!ctx->loop_cache[slot]) ctx->loop_cache[slot] = new CachedLoop();
+    CachedLoop* c = static_cast<CachedLoop*>(ctx->loop_cache[slot]);
+    if (!c->cont) GA_CUDA(cudaMalloc(&c->cont, sizeof(int)));
+    return c;
+}
+}  // namespace
+
+void* cached_loop_args(ga_ctx ctx, int slot, size_t bytes) {
+    CachedLoop* c = cache_slot(ctx, slot);
+    if (c->args_bytes < bytes) {
+        GA_REQUIRE(c->exec == nullptr, GA_ERR_INVALID_ARG, "loop parameters grew after capture");
+        if (c->args) GA_CUDA(cudaFree(c->args));
+        c->args = nullptr;
+        GA_CUDA(cudaMalloc(&c->args, bytes));
+        c->args_bytes = bytes;
+    }
+    return c->args;
+}
+
+void run_cached_loop(ga_ctx ctx, int slot, const std::function<void(const LoopCtl&)>& body, int64_t max_host_iters) {
+    if (!ctx->device_loops) {
+        run_device_loop(ctx, body, max_host_iters);
+        return;
+    }
+    CachedLoop* c = cache_slot(ctx, slot);
+    if (!c->exec) {
+        cudaGraph_t graph = nullptr;
+        bool capture_failed = false;
+        GA_CUDA(cudaGraphCreate(&graph, 0));
+        try {
+            c->ctl.cont = c->cont;
+            GA_CUDA(cudaGraphConditionalHandleCreate(&c->ctl.handle, graph, 1, cudaGraphCondAssignDefault));
+            c->ctl.use_handle = 1;
+            cudaGraphNodeParams cp = {};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = c->ctl.handle;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            cudaGraphNode_t node;
+            GA_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp));
+            cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
+            GA_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, bodyg, nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeRelaxed));
+            ctx->capturing = true;
+            try {
+                body(c->ctl);
+            } catch (...) {
+                ctx->capturing = false;
+                capture_failed = true;
+                cudaGraph_t dummy;
+                cudaStreamEndCapture(ctx->stream, &dummy);
+                cudaGetLastError();
+                throw;
+            }
+            ctx->capturing = false;
+            cudaGraph_t captured = nullptr;
+            GA_CUDA(cudaStreamEndCapture(ctx->stream, &captured));
+            GA_CUDA(cudaGraphInstantiate(&c->exec, graph, 0));
+            c->graph = graph;
+        } catch (...) {
+            // as in run_device_loop: a graph left by a failed capture is not destroyed
+            if (!capture_failed) cudaGraphDestroy(graph);
+            c->exec = nullptr;
+            throw;
+        }
+    }
+    {
+        ProfScope ps(ctx, "device_loop_graph");
+        GA_CUDA(cudaGraphLaunch(c->exec, ctx->stream));
+    }
+}
+
+void destroy_loop_caches(ga_ctx ctx) {
+    for (void*& p : ctx->loop_cache) {
+        CachedLoop* c = static_cast<CachedLoop*>(p);
+        if (!c) continue;
+        if (c->exec) cudaGraphExecDestroy(c->exec);
+        if (c->graph) cudaGraphDestroy(c->graph);
+        if (c->cont) cudaFree(c->cont);
+        if (c->args) cudaFree(c->args);
+        delete c;
+        p = nullptr;
+    }
+}
+
 // ==================================================== triangle counting
 constexpr int kTcThreads = 256;
 constexpr int kTcChunk = 8;  // edges (i, j) of one L row per work unit

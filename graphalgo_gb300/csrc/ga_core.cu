@@ -312,6 +312,7 @@ int ga_ctx_destroy(ga_ctx ctx) {
         cudaEventDestroy(p.stop);
     }
     for (auto ev : ctx->event_pool) cudaEventDestroy(ev);
+    ga::destroy_loop_caches(ctx);
     if (ctx->timer_start) cudaEventDestroy(ctx->timer_start);
     if (ctx->timer_stop) cudaEventDestroy(ctx->timer_stop);
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
@@ -546,6 +547,16 @@ int ga_csr_device_ptrs(ga_csr A, void** rst, void** col, void** val) {
     if (rst) *rst = A->rst;
     if (col) *col = A->col;
     if (val) *val = A->val;
+    return GA_OK;
+}
+
+int ga_csr_set_symmetric(ga_ctx ctx, ga_csr A, int symmetric) {
+    if (!ctx || !A || symmetric < -1 || symmetric > 1) return GA_ERR_INVALID_ARG;
+    if (symmetric == 1 && A->m != A->n) {
+        ctx->last_error = "a symmetric matrix is square";
+        return GA_ERR_SHAPE;
+    }
+    A->sym = symmetric;
     return GA_OK;
 }
 

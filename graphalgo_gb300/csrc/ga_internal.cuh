@@ -94,7 +94,14 @@ struct ga_ctx_s {
     std::unordered_map<void*, size_t> live;
     int64_t bytes_in_use = 0;
     int64_t bytes_peak = 0;
+    // device loops captured once and relaunched (run_cached_loop), by slot
+    void* loop_cache[4] = {};
 };
+
+namespace ga {
+// Frees the context's cached loop graphs and their device buffers.
+void destroy_loop_caches(ga_ctx ctx);
+}  // namespace ga
 
 struct ga_csr_s {
     int64_t m = 0, n = 0, nnz = 0;

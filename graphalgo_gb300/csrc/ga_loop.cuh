@@ -31,4 +31,14 @@ __device__ __forceinline__ void loop_continue(const LoopCtl& c, bool more) {
 // loop (the device-side bodies also carry their own iteration caps).
 void run_device_loop(ga_ctx ctx, const std::function<void(const LoopCtl&)>& body, int64_t max_host_iters);
 
+// The same for a body whose kernels take nothing that changes from call to
+// call except through device memory (cached_loop_args): its graph is
+// captured and instantiated on the context's first call for `slot` and only
+// relaunched afterwards. The kernel grid sizes must not depend on the call.
+void run_cached_loop(ga_ctx ctx, int slot, const std::function<void(const LoopCtl&)>& body, int64_t max_host_iters);
+// A device buffer of `bytes` kept with the slot's loop for the context's
+// lifetime: where the host writes the call's parameters before the launch.
+void* cached_loop_args(ga_ctx ctx, int slot, size_t bytes);
+enum { kLoopSlotTriFront = 0, kLoopSlotTriFrontBatch = 1 };
+
 }  // namespace ga

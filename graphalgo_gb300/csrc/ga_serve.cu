@@ -122,8 +122,7 @@ static int64_t slot_key(const SrvReq* r) {
 }
 
 // Batched BC keeps per (vertex, source) state for the whole union, so its
-// groups stay small: union vertices x sources at most this.
-constexpr int64_t kBcGroupPairs = (int64_t)1 << 22;
+// groups stay small: union vertices x (sources + 1) at most cfg.bc_group_pairs.
 constexpr int64_t kBcMaxSrc = 1024;                   // sources of one BC call
 
 // Picks the calls to run next (under the lock): the queue head and, when it
@@ -159,7 +158,10 @@ static std::vector<SrvReq*> take_group(Server* s, int64_t* reserve) {
             const int64_t m2 = um + (fresh ? g.m : 0), z2 = unz + (fresh ? g.nnz : 0);
             const int64_t ns2 = ns + (int64_t)r->sources.size();
             if (z2 > s->cfg.coalesce_max_nnz) { ++it; continue; }
-            if (r->type == GA_REQ_BC && (ns2 > kBcMaxSrc || m2 * (ns2 + 1) > kBcGroupPairs)) { ++it; continue; }
+            if (r->type == GA_REQ_BC && (ns2 > kBcMaxSrc || m2 * (ns2 + 1) > s->cfg.bc_group_pairs)) {
+                ++it;
+                continue;
+            }
             const int64_t b2 = bound_batch(head->type, m2, z2, nslots + (fresh ? 1 : 0), ns2);
             if (s->reserved + b2 > s->budget) { ++it; continue; }
             if (fresh) slots[slot_key(r)] = (int)nslots++;
@@ -363,6 +365,7 @@ int ga_server_create(int device, const ga_server_config* cfg, ga_server* out) {
     if (c.coalesce_nnz <= 0) c.coalesce_nnz = 1 << 20;
     if (c.coalesce_max_nnz <= 0) c.coalesce_max_nnz = 1 << 22;
     if (c.coalesce_max_requests <= 0) c.coalesce_max_requests = 4096;
+    if (c.bc_group_pairs <= 0) c.bc_group_pairs = (int64_t)1 << 22;
     if (c.workers > 64) return GA_ERR_INVALID_ARG;
     s->cfg = c;
     int rc = ga_ctx_create(device, nullptr, &s->home);

@@ -985,7 +985,8 @@ __global__ void k_trif_init_counts(TriFrontArgs a) {
 
 // Start of iteration t: the work counters of its support product, and the
 // frontier marked.
-__global__ void k_trif_mark(TriFrontArgs a) {
+__global__ void k_trif_mark(const TriFrontArgs* __restrict__ ap) {
+    const TriFrontArgs a = *ap;
     const int t = a.st->t;
     const int32_t n = a.st->cnt[t & 1];
     const int32_t* F = (t & 1) ? a.f1 : a.f0;
@@ -1003,7 +1004,8 @@ __global__ void k_trif_mark(TriFrontArgs a) {
 }
 
 // One warp per frontier edge: its triangles in C_t, the supports they lower.
-__global__ void __launch_bounds__(128) k_trif_lower(TriFrontArgs a) {
+__global__ void __launch_bounds__(128) k_trif_lower(const TriFrontArgs* __restrict__ ap) {
+    const TriFrontArgs a = *ap;
     const int lane = threadIdx.x & 31;
     const int t = a.st->t;
     const int32_t n = a.st->cnt[t & 1];
@@ -1079,7 +1081,8 @@ __global__ void __launch_bounds__(128) k_trif_lower(TriFrontArgs a) {
 // The frontier's edges leave C_t: rows shorten (diagonal entries whose row
 // length drops below k - 2 join the next frontier), the terms of P at their
 // endpoints change, rows that lose their last upper entry are listed.
-__global__ void k_trif_apply(TriFrontArgs a) {
+__global__ void k_trif_apply(const TriFrontArgs* __restrict__ ap) {
+    const TriFrontArgs a = *ap;
     const int t = a.st->t;
     const int32_t n = a.st->cnt[t & 1];
     const int32_t* F = (t & 1) ? a.f1 : a.f0;
@@ -1133,7 +1136,8 @@ __global__ void k_trif_apply(TriFrontArgs a) {
 
 // Rows that lost their last upper entry: h drops to 0, so every remaining
 // neighbour's H loses 1. One warp per row.
-__global__ void k_trif_flip(TriFrontArgs a) {
+__global__ void k_trif_flip(const TriFrontArgs* __restrict__ ap) {
+    const TriFrontArgs a = *ap;
     const int lane = threadIdx.x & 31;
     const int32_t n = a.st->nflip;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -1154,7 +1158,8 @@ __global__ void k_trif_flip(TriFrontArgs a) {
 // batch also per graph). For one matrix, the last block to finish ends the
 // iteration (stop when F_t was empty, or after m iterations) and tells the
 // loop whether to go on; batches end it in k_trif_graphs.
-__global__ void __launch_bounds__(256) k_trif_delta(TriFrontArgs a, LoopCtl ctl) {
+__global__ void __launch_bounds__(256) k_trif_delta(const TriFrontArgs* __restrict__ ap, LoopCtl ctl) {
+    const TriFrontArgs a = *ap;
     __shared__ long long part[8];
     __shared__ bool last;
     const int32_t n = a.st->ntouch;
@@ -1209,7 +1214,8 @@ __global__ void __launch_bounds__(256) k_trif_delta(TriFrontArgs a, LoopCtl ctl)
 // reference's loop); both leave the live set and their P leaves the work
 // total. The last block ends the iteration; the loop goes on while a graph
 // is live.
-__global__ void __launch_bounds__(256) k_trif_graphs(TriFrontArgs a, LoopCtl ctl) {
+__global__ void __launch_bounds__(256) k_trif_graphs(const TriFrontArgs* __restrict__ ap, LoopCtl ctl) {
+    const TriFrontArgs a = *ap;
     __shared__ long long part[8];
     __shared__ int lpart[8];
     __shared__ bool last;
@@ -1339,7 +1345,6 @@ int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const in
     a.ngraphs = ng;
     const int grid_rows = grid_for(m, 256, ctx->num_sms * 8);
     const int grid_ent = grid_for(nnz > 0 ? nnz : 1, 256, ctx->num_sms * 16);
-    const int grid_front = ctx->num_sms * 4;
     {
         // iteration 0's supports: one listing of every triangle
         tri_kt_support(ctx, C, b.sup, t, cap);
@@ -1353,38 +1358,45 @@ int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const in
         k_trif_init_counts<<<grid_for(std::max<int64_t>(m * 32, ng), 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(a);
         post_launch("trif_init_counts");
     }
-    auto body = [&](const LoopCtl& ctl) {
+    // The loop's kernels read the call's parameters from a device copy and
+    // have fixed grids, so the context captures the loop once per slot and
+    // relaunches it on later calls.
+    const int slot = batch ? kLoopSlotTriFrontBatch : kLoopSlotTriFront;
+    TriFrontArgs* dargs = static_cast<TriFrontArgs*>(cached_loop_args(ctx, slot, sizeof(TriFrontArgs)));
+    GA_CUDA(cudaMemcpyAsync(dargs, &a, sizeof(TriFrontArgs), cudaMemcpyHostToDevice, ctx->stream));
+    const int sms = ctx->num_sms;
+    auto body = [&, dargs, sms](const LoopCtl& ctl) {
         {
             ProfScope ps(ctx, "trif_mark");
-            k_trif_mark<<<grid_front, 256, 0, ctx->stream>>>(a);
+            k_trif_mark<<<sms * 4, 256, 0, ctx->stream>>>(dargs);
             post_launch("trif_mark");
         }
         {
             ProfScope ps(ctx, "trif_lower");
-            k_trif_lower<<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(a);
+            k_trif_lower<<<sms * 16, 128, 0, ctx->stream>>>(dargs);
             post_launch("trif_lower");
         }
         {
             ProfScope ps(ctx, "trif_apply");
-            k_trif_apply<<<grid_front, 256, 0, ctx->stream>>>(a);
+            k_trif_apply<<<sms * 4, 256, 0, ctx->stream>>>(dargs);
             post_launch("trif_apply");
         }
         {
             ProfScope ps(ctx, "trif_flip");
-            k_trif_flip<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(a);
+            k_trif_flip<<<sms * 4, 256, 0, ctx->stream>>>(dargs);
             post_launch("trif_flip");
         }
         ProfScope ps(ctx, "trif_delta");
-        k_trif_delta<<<ctx->num_sms * 2, 256, 0, ctx->stream>>>(a, ctl);
+        k_trif_delta<<<sms * 2, 256, 0, ctx->stream>>>(dargs, ctl);
         post_launch("trif_delta");
         if (batch) {
-            k_trif_graphs<<<grid_for(ng, 256, ctx->num_sms * 2), 256, 0, ctx->stream>>>(a, ctl);
+            k_trif_graphs<<<sms * 2, 256, 0, ctx->stream>>>(dargs, ctl);
             post_launch("trif_graphs");
         }
     };
     {
         ProfScope ps(ctx, "ktruss_loop");
-        run_device_loop(ctx, body, m + 1);
+        run_cached_loop(ctx, slot, body, m + 1);
     }
     // one compaction: the kept entries, rows in column order
     ProfScope ps(ctx, "trif_compact");

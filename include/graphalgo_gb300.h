@@ -203,6 +203,14 @@ GA_API int ga_csr_download_async(ga_ctx ctx, ga_csr A, int32_t* rst, int32_t* co
 GA_API int ga_ctx_copy_sync(ga_ctx ctx);
 GA_API int ga_csr_device_ptrs(ga_csr A, void** rst, void** col, void** val);
 GA_API int ga_csr_free(ga_ctx ctx, ga_csr A);
+/* Declares whether A is symmetric (pattern and values), which the
+ * triangle-listing and inner-product forms, the symmetric k-truss loop and
+ * BC otherwise check on the device once per handle (a search per entry for
+ * its mirror). symmetric = 1: no check is run; A must be symmetric (a false
+ * declaration gives wrong results). 0: A is treated as not symmetric. -1:
+ * the check runs again on the next use. No counterpart in the reference
+ * (its CLI symmetrises the graphs it reads, src/main.cpp:221-222). */
+GA_API int ga_csr_set_symmetric(ga_ctx ctx, ga_csr A, int symmetric);
 /* Deep copy, optionally converting the value type
  * (convertType, include/matrix.h:668-677). */
 GA_API int ga_csr_convert(ga_ctx ctx, ga_csr A, ga_dtype dtype, ga_csr* out);
@@ -498,6 +506,8 @@ typedef struct {
     int64_t coalesce_max_nnz;      /* stored entries of one batched union at most; 0: 2^22 (several groups
                                       keep several workers busy) */
     int64_t coalesce_max_requests; /* requests served by one batched call at most; 0: 4096 */
+    int64_t bc_group_pairs;        /* batched BC keeps state per (union vertex, source): vertices x
+                                      (sources + 1) of one group at most; 0: 2^22 */
 } ga_server_config;
 typedef struct {
     int status;                /* GA_OK, the call's error code, or GA_ERR_ADMISSION */

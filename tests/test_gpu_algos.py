@@ -393,3 +393,25 @@ def test_bc_all_sources(ctx):
     with pytest.raises(ga.GaError) as e:
         ga.bc_all(Gd, 0)
     assert e.value.code == ga.ERR_INVALID_ARG
+
+
+def test_declared_symmetry(ctx):
+    """ga_csr_set_symmetric: a symmetric graph declared symmetric skips the
+    device check and gives the same results; declared not symmetric, the
+    k-truss and BC take their general forms (same results); -1 checks
+    again; a non-square matrix cannot be declared symmetric."""
+    G = csr_from_arrays(*ga.gen_rmat(11, 16, seed=19))
+    R, it = oracle.ktruss(G, 5)
+    src = np.arange(0, 40, dtype=np.int32)
+    ref_bc = oracle.bc_batch(G, src)
+    for decl in (1, 0, -1):
+        Gd = to_device(ctx, G)
+        Gd.set_symmetric(decl)
+        C, git = ga.ktruss("tri", Gd, 5)
+        r, c, _ = C.download()
+        assert git == it and np.array_equal(r, R.rst) and np.array_equal(c, R.col), decl
+        _bc_close(ga.bc(Gd, src), ref_bc)
+    N = ga.Csr.upload(ctx, 3, 4, np.array([0, 1, 1, 1], np.int32), np.array([2], np.int32))
+    with pytest.raises(ga.GaError) as e:
+        N.set_symmetric(1)
+    assert e.value.code == ga.ERR_SHAPE
