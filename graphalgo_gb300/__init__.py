@@ -35,6 +35,7 @@ ALGO_NAMES = {v: k for k, v in ALGOS.items()}
 OPT_DEVICE_LOOPS, OPT_PROFILE, OPT_FAIL_ALLOC_AFTER, OPT_KNN_TILED = 1, 2, 3, 4
 OPT_MXM_WARP_FLOPS, OPT_MXM_HEAVY_FLOPS, OPT_MXM_CTAS_PER_SM, OPT_DOT_CHUNK, OPT_HYBRID_RATIO = 5, 6, 7, 8, 9
 OPT_TRI_ORDER, OPT_KT_FRONTIER = 10, 11
+OPT_BC_BACKWARD = 12
 TUNE_KTRUSS, TUNE_PRODUCT, TUNE_TC = 0, 1, 2
 # edge-list / file ingestion flags
 EDGES_MIRROR, EDGES_DROP_LOOPS, EDGES_LOWER_SYMM, EDGES_UNIT = 1, 2, 4, 8

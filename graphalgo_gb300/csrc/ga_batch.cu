@@ -512,25 +512,8 @@ int ga_batch_bc(ga_ctx ctx, ga_csr U, int64_t count, const int64_t* voff, const 
     if (!ctx || !U || !soff || !bc) return GA_ERR_INVALID_ARG;
     GA_API_BODY(ctx, {
         check_voff(U, count, voff);
-        GA_REQUIRE(soff[0] == 0, GA_ERR_INVALID_ARG, "batched BC: source offsets must start at 0");
-        const int64_t ns = soff[count];
-        GA_REQUIRE(ns >= 0 && (ns == 0 || sources), GA_ERR_INVALID_ARG, "batched BC: sources missing");
-        // graph g's sources, shifted to its rows of the union
-        std::vector<int32_t> global((size_t)(ns > 0 ? ns : 1));
-        for (int64_t g = 0; g < count; ++g) {
-            GA_REQUIRE(soff[g] <= soff[g + 1], GA_ERR_INVALID_ARG, "batched BC: source offsets must not decrease");
-            const int64_t mg = voff[g + 1] - voff[g];
-            for (int64_t j = soff[g]; j < soff[g + 1]; ++j) {
-                GA_REQUIRE(sources[j] >= 0 && sources[j] < mg, GA_ERR_INVALID_ARG, "batched BC: source out of range");
-                global[(size_t)j] = (int32_t)(sources[j] + voff[g]);
-            }
-        }
-        DBuf<int32_t> d_src(ctx, global.size());
         DBuf<double> d_bc(ctx, (size_t)(U->m > 0 ? U->m : 1));
-        GA_CUDA(cudaMemcpyAsync(d_src.p, global.data(), sizeof(int32_t) * global.size(), cudaMemcpyHostToDevice,
-                                ctx->stream));
-        const int rc = ga_bc_device(ctx, U, d_src.p, ns, d_bc.p);
-        if (rc != GA_OK) fail(rc, ctx->last_error);
+        bc_union_device(ctx, U, count, voff, soff, sources, d_bc.p);
         if (U->m)
             GA_CUDA(cudaMemcpyAsync(bc, d_bc.p, sizeof(double) * U->m, cudaMemcpyDeviceToHost, ctx->stream));
         GA_CUDA(cudaStreamSynchronize(ctx->stream));

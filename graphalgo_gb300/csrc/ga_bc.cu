@@ -19,8 +19,18 @@
 // bcu += acc * sigma, and bc[v] += acc * sigma (the final row sum,
 // betweenness_centrality.h:220-228, accumulated as it is produced).
 // Both sweeps run as device loops (CUDA-graph WHILE nodes).
+//
+// Source columns. Column j of the state holds source j, except in a batch
+// over the block-diagonal union of several graphs: there column j holds the
+// j-th source of every graph at once. A source only reaches the vertices of
+// its own graph, so each (vertex, column) pair still belongs to one source,
+// and the state is (union vertices) x (largest source count of a graph)
+// instead of x (all sources). The columns a graph has no source for are
+// marked visited on its vertices before the first level.
 #include "ga_device.cuh"
 #include "ga_loop.cuh"
+
+#include <algorithm>
 
 namespace ga {
 
@@ -38,6 +48,7 @@ struct BcState {
     int32_t overflow;
     int32_t mode;          // forward direction of the current level: 0 pull, 1 push
     int32_t ntouched;      // vertices reached by the current push level
+    int32_t stalled;       // a bulk copy of the backward sweep did not complete in time
     unsigned long long cur_work, next_work;  // sum over frontier rows of entries x out-degree
 };
 
@@ -45,8 +56,10 @@ struct BcArgs {
     const int32_t* atr; const int32_t* atc; const double* atv;  // A^T (in-neighbours)
     const int32_t* ar; const int32_t* ac; const double* av;     // A (out-neighbours)
     int64_t m;
-    int ns, words;                                              // sources, 32-bit words per vertex
+    int ns, words;                                              // source columns, 32-bit words per vertex
+    int nsrc;                                                   // sources (level-0 entries)
     const int32_t* sources;
+    const int32_t* scol;                                        // column of each source (nullptr: its index)
     BcState* st;
     int32_t* level_rows;    // level_rows[d] = first row of level d
     int32_t* cur_start[2];  // per vertex, per parity: first entry of its frontier row
@@ -74,12 +87,13 @@ struct BcArgs {
 constexpr unsigned long long kBcPushDiv = 8;
 
 __global__ void k_bc_init(BcArgs p) {
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < p.ns; j += gridDim.x * blockDim.x) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < p.nsrc; j += gridDim.x * blockDim.x) {
         int v = p.sources[j];
-        p.es[j] = j;
+        const int c = p.scol ? p.scol[j] : j;
+        p.es[j] = c;
         p.ev[j] = 1.0;
         p.ed[j] = 1.0;
-        atomicOr(&p.vbits[(size_t)v * p.words + (j >> 5)], 1u << (j & 31));
+        atomicOr(&p.vbits[(size_t)v * p.words + (c >> 5)], 1u << (c & 31));
         atomicAdd(&p.vcnt[v], 1);
         p.cur_start[0][v] = j;
         p.cur_len[0][v] = 1;
@@ -89,10 +103,35 @@ __global__ void k_bc_init(BcArgs p) {
 
 __global__ void k_bc_state_init(BcArgs p) {
     p.st->d = 0; p.st->depth = 0; p.st->k = 0; p.st->done = 0;
-    p.st->entries = p.ns; p.st->rows = 0; p.st->overflow = 0;
-    p.st->mode = 0; p.st->ntouched = 0;
+    p.st->entries = p.nsrc; p.st->rows = 0; p.st->overflow = 0;
+    p.st->mode = 0; p.st->ntouched = 0; p.st->stalled = 0;
     p.st->cur_work = 0; p.st->next_work = 0;
     p.level_rows[0] = 0;
+}
+
+// Batches with packed columns: on the vertices of graph g (union rows
+// [voff[g], voff[g+1])), the columns at and above its source count are
+// marked visited, so no entry is ever made there and the vertex counts as
+// reached by every column once its own sources have reached it.
+__global__ void k_bc_previsit(BcArgs p, const int64_t* __restrict__ voff, const int32_t* __restrict__ gsrc,
+                              int64_t count) {
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < p.m; v += (int64_t)gridDim.x * blockDim.x) {
+        int64_t lo = 0, hi = count;  // the graph g with voff[g] <= v < voff[g+1]
+        while (hi - lo > 1) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (voff[mid] <= v) lo = mid; else hi = mid;
+        }
+        const int have = gsrc[lo];
+        for (int w = 0; w < p.words; ++w) {
+            const int c0 = w * 32;
+            uint32_t bits = 0u;
+            if (have <= c0) bits = 0xffffffffu;
+            else if (have < c0 + 32) bits = ~((1u << (have - c0)) - 1u);
+            if (c0 + 32 > p.ns) bits &= (p.ns - c0 >= 32) ? 0xffffffffu : ((1u << (p.ns - c0)) - 1u);
+            p.vbits[(size_t)v * p.words + w] = bits;
+        }
+        p.vcnt[v] = p.ns - have;
+    }
 }
 
 // Level start: the frontier's work decides the direction.
@@ -327,7 +366,7 @@ __global__ void __launch_bounds__(kBcThreads) k_bc_push(BcArgs p) {
     if (st->done || st->mode != 1) return;
     const int d = st->d;
     const int wid = threadIdx.x >> 5;
-    const int64_t items = d == 0 ? p.ns : (int64_t)p.level_rows[d] - p.level_rows[d - 1];
+    const int64_t items = d == 0 ? p.nsrc : (int64_t)p.level_rows[d] - p.level_rows[d - 1];
     // rows of high-degree vertices: the CTA's warps split the neighbours
     for (int64_t it = blockIdx.x; it < items; it += gridDim.x) {
         int32_t u, e0, len;
@@ -418,14 +457,76 @@ __global__ void k_bc_set_w(BcArgs p, bool set) {
 
 constexpr int kBcPer = 4;  // row entries per lane per pass of the backward sweep
 
+// How the backward sweep reads the W rows of a row's level-k neighbours
+// (GA_OPT_BC_BACKWARD): 0 gathers of up to kBcHits neighbours' rows issued
+// together; 1 bulk copies of whole W rows into shared memory, two batches of
+// kBcHits rows in flight per warp (needs an even source count of at most
+// kBcBulkMaxCols and a 16-byte aligned W); 2 one neighbour at a time.
+enum { kBcBwdGather = 0, kBcBwdBulk = 1, kBcBwdSingle = 2 };
+constexpr int kBcHits = 4;
+constexpr int kBcBulkMaxCols = 128;
+constexpr long long kBcWaitCycles = 2000000000ll;  // about a second at 2 GHz
+
+// The hit lanes of one group (bit mask `hits`) in ascending order, up to
+// kBcHits of them: their neighbours and values, broadcast to the warp.
+__device__ __forceinline__ int bc_take_hits(unsigned& hits, int32_t w, double a, int32_t (&ws)[kBcHits],
+                                            double (&as)[kBcHits]) {
+    const unsigned FULL = 0xffffffffu;
+    int n = 0;
+#pragma unroll
+    for (int h = 0; h < kBcHits; ++h) {
+        ws[h] = -1;
+        as[h] = 0.0;
+        if (hits) {  // warp-uniform
+            const int src = __ffs(hits) - 1;
+            hits &= hits - 1;
+            ws[h] = __shfl_sync(FULL, w, src);
+            as[h] = __shfl_sync(FULL, a, src);
+            n = h + 1;
+        }
+    }
+    return n;
+}
+
+// Per-warp state of the bulk form: two stages of kBcHits W rows in shared
+// memory, one barrier per stage and its expected parity.
+struct BcRing {
+    double* rows;    // 2 * kBcHits rows of ns doubles
+    uint64_t* bar;   // 2 barriers
+    uint32_t phase;  // bit s: parity the next wait on stage s expects
+    bool ok;         // false once a wait ran out
+};
+
 // acc[u] += sum over out-neighbours t in [t0, t1) step `stride` (groups of
 // 32 fetched together, level-k neighbours picked by ballot) of
-// A[v][w] * W[w][s[u]].
-template <bool UNIT>
+// A[v][w] * W[w][s[u]]. The neighbours' contributions are added in the same
+// order (ascending t) in every mode.
+template <bool UNIT, int MODE>
 __device__ __forceinline__ void bc_push_range(const BcArgs& p, int32_t t0, int32_t t1, int32_t stride,
-                                              const int (&s)[kBcPer], double (&acc)[kBcPer]) {
+                                              const int (&s)[kBcPer], double (&acc)[kBcPer], BcRing& ring) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    // bulk form: the batch whose copies are in flight
+    int pend_n = 0, pend_stage = 0, next_stage = 0;
+    double pend_a[kBcHits];
+    auto consume = [&](int stage, int n, const double (&as)[kBcHits]) {
+        const bool ok = mbar_wait(ring.bar + stage, (ring.phase >> stage) & 1u, kBcWaitCycles);
+        ring.phase ^= 1u << stage;
+        if (!ok) {
+            if (lane == 0) atomicExch(&p.st->stalled, 1);
+            ring.ok = false;
+            return;
+        }
+        const double* base = ring.rows + (size_t)stage * kBcHits * p.ns;
+#pragma unroll
+        for (int h = 0; h < kBcHits; ++h) {
+            if (h >= n) break;
+            const double* row = base + (size_t)h * p.ns;
+#pragma unroll
+            for (int u = 0; u < kBcPer; ++u)
+                if (s[u] >= 0) acc[u] += as[h] * row[s[u]];
+        }
+    };
     for (int32_t g = t0; g < t1; g += stride) {
         const int32_t t = g + lane;
         int32_t w = -1;
@@ -438,30 +539,97 @@ __device__ __forceinline__ void bc_push_range(const BcArgs& p, int32_t t0, int32
             }
         }
         unsigned hits = __ballot_sync(FULL, w >= 0);
-        while (hits) {
-            const int src = __ffs(hits) - 1;
-            hits &= hits - 1;
-            const int32_t ww = __shfl_sync(FULL, w, src);
-            const double aa = __shfl_sync(FULL, a, src);
-            const double* wrow = p.W + (size_t)ww * p.ns;
+        if (MODE == kBcBwdSingle || (MODE == kBcBwdBulk && !ring.ok)) {
+            while (hits) {
+                const int src = __ffs(hits) - 1;
+                hits &= hits - 1;
+                const int32_t ww = __shfl_sync(FULL, w, src);
+                const double aa = __shfl_sync(FULL, a, src);
+                const double* wrow = p.W + (size_t)ww * p.ns;
 #pragma unroll
-            for (int u = 0; u < kBcPer; ++u)
-                if (s[u] >= 0) acc[u] += aa * wrow[s[u]];
+                for (int u = 0; u < kBcPer; ++u)
+                    if (s[u] >= 0) acc[u] += aa * wrow[s[u]];
+            }
+        } else if (MODE == kBcBwdGather) {
+            while (hits) {
+                int32_t ws[kBcHits];
+                double as[kBcHits];
+                bc_take_hits(hits, w, a, ws, as);
+                double x[kBcHits][kBcPer];
+#pragma unroll
+                for (int h = 0; h < kBcHits; ++h)
+#pragma unroll
+                    for (int u = 0; u < kBcPer; ++u)
+                        x[h][u] = (ws[h] >= 0 && s[u] >= 0) ? p.W[(size_t)ws[h] * p.ns + s[u]] : 0.0;
+#pragma unroll
+                for (int h = 0; h < kBcHits; ++h)
+                    if (ws[h] >= 0)
+#pragma unroll
+                        for (int u = 0; u < kBcPer; ++u)
+                            if (s[u] >= 0) acc[u] += as[h] * x[h][u];
+            }
+        } else {
+            while (hits) {
+                int32_t ws[kBcHits];
+                double as[kBcHits];
+                const int n = bc_take_hits(hits, w, a, ws, as);
+                // the stage is free once every lane has read its previous batch
+                __syncwarp();
+                if (lane == 0) {
+                    const uint32_t bytes = (uint32_t)p.ns * sizeof(double);
+                    double* base = ring.rows + (size_t)next_stage * kBcHits * p.ns;
+                    fence_proxy_async_smem();
+                    mbar_arrive_expect_tx(ring.bar + next_stage, bytes * (uint32_t)n);
+#pragma unroll
+                    for (int h = 0; h < kBcHits; ++h)
+                        if (h < n)
+                            bulk_copy_g2s(base + (size_t)h * p.ns, p.W + (size_t)ws[h] * p.ns, bytes,
+                                          ring.bar + next_stage);
+                }
+                if (pend_n) consume(pend_stage, pend_n, pend_a);
+                pend_n = n;
+                pend_stage = next_stage;
+#pragma unroll
+                for (int h = 0; h < kBcHits; ++h) pend_a[h] = as[h];
+                next_stage ^= 1;
+                if (!ring.ok) break;
+            }
         }
+    }
+    if (MODE == kBcBwdBulk && pend_n) {
+        if (ring.ok) consume(pend_stage, pend_n, pend_a);
+        else (void)mbar_wait(ring.bar + pend_stage, (ring.phase >> pend_stage) & 1u, kBcWaitCycles);
     }
 }
 
 // Rows of S[k-1]: acc_s = sum_w A[v][w] * W[w][s] over out-neighbours w that
 // sit at level k; bcu += acc*sigma; bc[v] += sum_s acc*sigma. Rows of heavy
 // vertices are shared by all warps of a CTA, the others take one warp.
-template <bool UNIT>
+template <bool UNIT, int MODE>
 __global__ void __launch_bounds__(kBcThreads) k_bc_backward(BcArgs p) {
     __shared__ double sacc[kBcMaxSources];
     __shared__ double s_vsum;
+    extern __shared__ __align__(16) unsigned char bsmem[];
     const int k = p.st->k;
     if (k < 1) return;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int32_t r0 = p.level_rows[k - 1], r1 = p.level_rows[k];
+    BcRing ring;
+    ring.rows = nullptr;
+    ring.bar = nullptr;
+    ring.phase = 0;
+    ring.ok = true;
+    if (MODE == kBcBwdBulk) {
+        ring.rows = reinterpret_cast<double*>(bsmem) + (size_t)wid * 2 * kBcHits * p.ns;
+        ring.bar = reinterpret_cast<uint64_t*>(bsmem + (size_t)kBcWarps * 2 * kBcHits * p.ns * sizeof(double)) +
+                   2 * wid;
+        if (lane == 0) {
+            mbar_init(ring.bar, 1);
+            mbar_init(ring.bar + 1, 1);
+            mbar_init_fence();
+        }
+        __syncwarp();
+    }
 
     // heavy rows: each warp takes every 8th group of 32 neighbours
     for (int64_t r = r0 + blockIdx.x; r < r1; r += gridDim.x) {
@@ -481,7 +649,7 @@ __global__ void __launch_bounds__(kBcThreads) k_bc_backward(BcArgs p) {
                 s[u] = e < n ? p.es[e0 + e] : -1;
                 acc[u] = 0.0;
             }
-            bc_push_range<UNIT>(p, ab + wid * 32, ae, kBcWarps * 32, s, acc);
+            bc_push_range<UNIT, MODE>(p, ab + wid * 32, ae, kBcWarps * 32, s, acc, ring);
 #pragma unroll
             for (int u = 0; u < kBcPer; ++u) {
                 const int e = base + u * 32 + lane;
@@ -518,7 +686,7 @@ __global__ void __launch_bounds__(kBcThreads) k_bc_backward(BcArgs p) {
                 s[u] = e < n ? p.es[e0 + e] : -1;
                 acc[u] = 0.0;
             }
-            bc_push_range<UNIT>(p, ab, ae, 32, s, acc);
+            bc_push_range<UNIT, MODE>(p, ab, ae, 32, s, acc, ring);
 #pragma unroll
             for (int u = 0; u < kBcPer; ++u) {
                 const int e = base + u * 32 + lane;
@@ -564,17 +732,32 @@ __global__ void k_bc_check_sources(const int32_t* __restrict__ src, int ns, int6
     }
 }
 
+// Packed source columns of a batch over a block-diagonal union (device
+// arrays): each source's column, the graphs' first rows (count + 1 of them)
+// and their source counts; ncols = the largest source count.
+struct BcPacking {
+    const int32_t* scol = nullptr;
+    const int64_t* voff = nullptr;
+    const int32_t* gsrc = nullptr;
+    int64_t count = 0;
+    int ncols = 0;
+};
+
 // accumulate: add this batch's scores to d_bc instead of overwriting it.
 static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t nsrc, double* d_bc,
-                      bool accumulate = false) {
+                      bool accumulate = false, const BcPacking* pk = nullptr) {
     GA_REQUIRE(A->m == A->n, GA_ERR_SHAPE, "non-square matrix; BC is only for square matrices");
-    GA_REQUIRE(nsrc >= 0 && nsrc <= kBcMaxSources, GA_ERR_INVALID_ARG, "BC: between 0 and 1024 sources per batch");
+    GA_REQUIRE(nsrc >= 0 && (pk || nsrc <= kBcMaxSources), GA_ERR_INVALID_ARG,
+               "BC: between 0 and 1024 sources per batch");
+    GA_REQUIRE(!pk || (pk->ncols >= 1 && pk->ncols <= kBcMaxSources), GA_ERR_INVALID_ARG,
+               "BC: between 1 and 1024 sources per graph of a batch");
     const int64_t m = A->m;
     if (!accumulate) GA_CUDA(cudaMemsetAsync(d_bc, 0, sizeof(double) * (m ? m : 1), ctx->stream));
     if (m == 0 || nsrc == 0) return;
-    const int ns = (int)nsrc;
+    const int ns = pk ? pk->ncols : (int)nsrc;  // source columns
     const int words = (ns + 31) / 32;
-    GA_REQUIRE(m * (int64_t)(ns + 1) < INT32_MAX, GA_ERR_UNSUPPORTED, "BC: m x sources exceeds the int32 entry range");
+    GA_REQUIRE(m * (int64_t)(ns + 1) + nsrc < INT32_MAX, GA_ERR_UNSUPPORTED,
+               "BC: m x sources exceeds the int32 entry range");
     ProfScope whole(ctx, "bc");
     // Values enter the algebra as FP64. All-ones values are never read (the
     // unit kernels), so A's own arrays serve; otherwise an FP64 copy. A
@@ -595,7 +778,8 @@ static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t ns
         k_bc_scan_vertices<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(Av->rst, Av->col, ATu->rst,
                                                                                         m, heavy.p, flags.p);
         post_launch("bc_scan_vertices");
-        k_bc_check_sources<<<grid_for(ns, 256, 64), 256, 0, ctx->stream>>>(d_sources, ns, m, mark.p, flags.p);
+        k_bc_check_sources<<<grid_for(nsrc, 256, 64), 256, 0, ctx->stream>>>(d_sources, (int)nsrc, m, mark.p,
+                                                                            flags.p);
         post_launch("bc_check_sources");
         int hf[2];
         GA_CUDA(cudaMemcpyAsync(hf, flags.p, sizeof(hf), cudaMemcpyDeviceToHost, ctx->stream));
@@ -605,12 +789,13 @@ static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t ns
         GA_REQUIRE(!(f & 8), GA_ERR_INVALID_ARG, "BC: source index out of range");
         GA_REQUIRE(!(f & 16), GA_ERR_INVALID_ARG, "BC: sources must be distinct");
 
-        const int64_t cap_entries = m * (int64_t)ns + ns;
+        const int64_t cap_entries = m * (int64_t)ns + nsrc;
         const int64_t cap_rows = cap_entries;
         BcArgs p;
         p.atr = ATu->rst; p.atc = ATu->col; p.atv = unit ? nullptr : static_cast<const double*>(ATu->val);
         p.ar = Av->rst; p.ac = Av->col; p.av = unit ? nullptr : static_cast<const double*>(Av->val);
         p.m = m; p.ns = ns; p.words = words; p.sources = d_sources;
+        p.nsrc = (int)nsrc; p.scol = pk ? pk->scol : nullptr;
         DBuf<BcState> st(ctx, 1);
         DBuf<int32_t> level_rows(ctx, (size_t)m + 2);
         DBuf<int32_t> cs0(ctx, m), cs1(ctx, m), cl0(ctx, m), cl1(ctx, m), vcnt(ctx, m);
@@ -645,7 +830,12 @@ static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t ns
         p.nnz = ATu->nnz;
         k_bc_state_init<<<1, 1, 0, ctx->stream>>>(p);
         post_launch("bc_state_init");
-        k_bc_init<<<grid_for(ns, 256, 64), 256, 0, ctx->stream>>>(p);
+        if (pk) {
+            k_bc_previsit<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(p, pk->voff, pk->gsrc,
+                                                                                       pk->count);
+            post_launch("bc_previsit");
+        }
+        k_bc_init<<<grid_for(nsrc, 256, 64), 256, 0, ctx->stream>>>(p);
         post_launch("bc_init");
 
         const size_t per_warp = (size_t)ns * sizeof(double) + 2 * (size_t)words * sizeof(uint32_t) +
@@ -685,11 +875,29 @@ static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t ns
         }
         {
             ProfScope ps(ctx, "bc_backward_loop");
-            auto bwd = unit ? k_bc_backward<true> : k_bc_backward<false>;
+            // the bulk form copies whole W rows: 16-byte aligned rows and at
+            // most kBcBulkMaxCols columns (its shared-memory ring)
+            int mode = ctx->bc_backward;
+            if (mode == kBcBwdBulk &&
+                (ns % 2 != 0 || ns > kBcBulkMaxCols || (reinterpret_cast<uintptr_t>(p.W) & 15u) != 0))
+                mode = kBcBwdGather;
+            void (*bwd)(BcArgs) = nullptr;
+            size_t bsmem = 0;
+            if (mode == kBcBwdBulk) {
+                bwd = unit ? k_bc_backward<true, kBcBwdBulk> : k_bc_backward<false, kBcBwdBulk>;
+                bsmem = (size_t)kBcWarps * 2 * kBcHits * ns * sizeof(double) + (size_t)kBcWarps * 2 * sizeof(uint64_t);
+                constexpr size_t max_bsmem = (size_t)kBcWarps * 2 * kBcHits * kBcBulkMaxCols * sizeof(double) +
+                                             (size_t)kBcWarps * 2 * sizeof(uint64_t);
+                GA_CUDA(cudaFuncSetAttribute(bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_bsmem));
+            } else if (mode == kBcBwdSingle) {
+                bwd = unit ? k_bc_backward<true, kBcBwdSingle> : k_bc_backward<false, kBcBwdSingle>;
+            } else {
+                bwd = unit ? k_bc_backward<true, kBcBwdGather> : k_bc_backward<false, kBcBwdGather>;
+            }
             run_device_loop(ctx, [&](const LoopCtl& ctl) {
                 k_bc_set_w<<<grid_rows, 256, 0, ctx->stream>>>(p, true);
                 post_launch("bc_set_w");
-                bwd<<<grid_rows, kBcThreads, 0, ctx->stream>>>(p);
+                bwd<<<grid_rows, kBcThreads, bsmem, ctx->stream>>>(p);
                 post_launch("bc_backward");
                 k_bc_set_w<<<grid_rows, 256, 0, ctx->stream>>>(p, false);
                 post_launch("bc_clear_w");
@@ -701,6 +909,7 @@ static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t ns
         GA_CUDA(cudaMemcpyAsync(&hs, st.p, sizeof(BcState), cudaMemcpyDeviceToHost, ctx->stream));
         GA_CUDA(cudaStreamSynchronize(ctx->stream));
         GA_REQUIRE(!hs.overflow, GA_ERR_INVALID_ARG, "BC: entry store overflow");
+        GA_REQUIRE(!hs.stalled, GA_ERR_TIMEOUT, "BC: a bulk copy of the backward sweep did not complete");
     } catch (...) {
         csr_destroy(ctx, AT);
         csr_destroy(ctx, Ad);
@@ -740,6 +949,52 @@ static void bc_all_device(ga_ctx ctx, ga_csr A, int64_t block, double* d_bc) {
             bc_device(ctx, A, src.p, c, d_bc, true);
         }
     }
+}
+
+void bc_union_device(ga_ctx ctx, ga_csr U, int64_t count, const int64_t* voff, const int64_t* soff,
+                     const int32_t* sources, double* d_bc) {
+    GA_REQUIRE(soff[0] == 0, GA_ERR_INVALID_ARG, "batched BC: source offsets must start at 0");
+    const int64_t ns = soff[count];
+    GA_REQUIRE(ns >= 0 && (ns == 0 || sources), GA_ERR_INVALID_ARG, "batched BC: sources missing");
+    // graph g's sources, shifted to its rows of the union; source j of graph
+    // g takes column j
+    std::vector<int32_t> global((size_t)(ns > 0 ? ns : 1)), col((size_t)(ns > 0 ? ns : 1));
+    std::vector<int32_t> gsrc((size_t)(count > 0 ? count : 1), 0);
+    int64_t ncols = 0;
+    for (int64_t g = 0; g < count; ++g) {
+        GA_REQUIRE(soff[g] <= soff[g + 1], GA_ERR_INVALID_ARG, "batched BC: source offsets must not decrease");
+        const int64_t mg = voff[g + 1] - voff[g];
+        GA_REQUIRE(soff[g + 1] - soff[g] <= kBcMaxSources, GA_ERR_INVALID_ARG,
+                   "batched BC: at most 1024 sources per graph");
+        for (int64_t j = soff[g]; j < soff[g + 1]; ++j) {
+            GA_REQUIRE(sources[j] >= 0 && sources[j] < mg, GA_ERR_INVALID_ARG, "batched BC: source out of range");
+            global[(size_t)j] = (int32_t)(sources[j] + voff[g]);
+            col[(size_t)j] = (int32_t)(j - soff[g]);
+        }
+        gsrc[(size_t)g] = (int32_t)(soff[g + 1] - soff[g]);
+        ncols = std::max<int64_t>(ncols, soff[g + 1] - soff[g]);
+    }
+    if (ns == 0 || U->m == 0) {
+        GA_CUDA(cudaMemsetAsync(d_bc, 0, sizeof(double) * (U->m ? U->m : 1), ctx->stream));
+        return;
+    }
+    DBuf<int32_t> d_src(ctx, global.size()), d_col(ctx, col.size()), d_gsrc(ctx, gsrc.size());
+    DBuf<int64_t> d_voff(ctx, (size_t)count + 1);
+    GA_CUDA(cudaMemcpyAsync(d_src.p, global.data(), sizeof(int32_t) * global.size(), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    GA_CUDA(cudaMemcpyAsync(d_col.p, col.data(), sizeof(int32_t) * col.size(), cudaMemcpyHostToDevice, ctx->stream));
+    GA_CUDA(cudaMemcpyAsync(d_gsrc.p, gsrc.data(), sizeof(int32_t) * gsrc.size(), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    GA_CUDA(cudaMemcpyAsync(d_voff.p, voff, sizeof(int64_t) * (count + 1), cudaMemcpyHostToDevice, ctx->stream));
+    BcPacking pk;
+    pk.scol = d_col.p;
+    pk.voff = d_voff.p;
+    pk.gsrc = d_gsrc.p;
+    pk.count = count;
+    pk.ncols = (int)ncols;
+    bc_device(ctx, U, d_src.p, ns, d_bc, false, &pk);
+    // the host vectors stay alive until the copies above are done
+    GA_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
 }  // namespace ga

@@ -412,6 +412,10 @@ int ga_ctx_set_option(ga_ctx ctx, int option, int64_t value) {
         ctx->tune.tri_order = (int)value;
         return GA_OK;
     case GA_OPT_KT_FRONTIER: ctx->kt_frontier = value != 0; return GA_OK;
+    case GA_OPT_BC_BACKWARD:
+        if (value < 0 || value > 2) break;
+        ctx->bc_backward = (int)value;
+        return GA_OK;
     }
     ctx->last_error = "unknown option";
     return GA_ERR_INVALID_ARG;

@@ -72,6 +72,7 @@ struct ga_ctx_s {
     int64_t fail_alloc_after = -1;  // fault injection
     bool knn_tiled = false;         // k-NN generator: tiled kernel for every graph
     bool kt_frontier = true;        // GA_TRI k-truss: incremental support after the first listing
+    int bc_backward = 0;            // BC backward sweep: W rows by gathers (0), bulk copies (1), one at a time (2)
     ga::MxmTune tune;               // masked-product schedule
     // profiling
     std::vector<ga::PendingTiming> pending;
@@ -357,6 +358,11 @@ bool csr_unit_values(ga_ctx ctx, ga_csr A);
 // True when A is square and every (i, j, v) has a matching (j, i, v)
 // (synchronises the stream).
 bool csr_is_symmetric(ga_ctx ctx, ga_csr A);
+// Batched BC over the block-diagonal union U of `count` graphs (host vertex
+// offsets voff), graph g with the sources [soff[g], soff[g+1]) of the host
+// array `sources` (indices within graph g); scores of U's rows into d_bc.
+void bc_union_device(ga_ctx ctx, ga_csr U, int64_t count, const int64_t* voff, const int64_t* soff,
+                     const int32_t* sources, double* d_bc);
 void scan_exclusive_i32_scratch(ga_ctx ctx, const int32_t* in, int32_t* out, int64_t n, void* scratch);
 
 // Read one device value to the host (synchronises the stream).

@@ -48,11 +48,15 @@ static int64_t bound_bc(int64_t m, int64_t nnz, int64_t ns) {
     return 40 * (m + 1) * (ns + 1) + 4 * m * words + 80 * (m + 2) + 32 * nnz + (1 << 20);
 }
 
-static int64_t bound_batch(int type, int64_t m, int64_t nnz, int64_t count, int64_t ns) {
+// ns: the union's sources; ncols: the largest source count of one graph
+// (batched BC keeps state for union vertices x ncols, plus one level-0
+// entry and its column per source).
+static int64_t bound_batch(int type, int64_t m, int64_t nnz, int64_t count, int64_t ns, int64_t ncols) {
     // union (int32 values), per-graph arrays, then the call on the union
     const int64_t u = 4 * (m + 1) + 8 * nnz + 64 * (count + 1) + 16 * (m + 2) + 4 * ns;
-    return u + (type == GA_REQ_TC ? bound_tc(m, nnz, 4) : type == GA_REQ_KTRUSS ? bound_ktruss(m, nnz)
-                                                                               : bound_bc(m, nnz, ns));
+    return u + (type == GA_REQ_TC      ? bound_tc(m, nnz, 4)
+                : type == GA_REQ_KTRUSS ? bound_ktruss(m, nnz)
+                                        : bound_bc(m, nnz, ncols) + 48 * ns + 16 * (count + 1));
 }
 
 int64_t request_bytes_bound(int type, int64_t m, int64_t nnz, int64_t param) {
@@ -121,9 +125,10 @@ static int64_t slot_key(const SrvReq* r) {
     return -r->id;
 }
 
-// Batched BC keeps per (vertex, source) state for the whole union, so its
-// groups stay small: union vertices x (sources + 1) at most cfg.bc_group_pairs.
-constexpr int64_t kBcMaxSrc = 1024;                   // sources of one BC call
+// Batched BC keeps state per (union vertex, source column), a column being
+// the j-th source of every graph: union vertices x (largest source count +
+// 1) + sources at most cfg.bc_group_pairs.
+constexpr int64_t kBcMaxSrc = 1024;                   // sources of one BC request
 
 // Picks the calls to run next (under the lock): the queue head and, when it
 // can be batched, the requests of the same type behind it. Returns the group
@@ -150,6 +155,7 @@ static std::vector<SrvReq*> take_group(Server* s, int64_t* reserve) {
         std::unordered_map<int64_t, int> slots{{slot_key(head), 0}};
         const SrvGraph& hg = s->graphs[(size_t)head->graph];
         int64_t um = hg.m, unz = hg.nnz, ns = (int64_t)head->sources.size(), nslots = 1;
+        int64_t ncols = ns;
         for (auto it = s->queue.begin(); it != s->queue.end() && (int64_t)group.size() < s->cfg.coalesce_max_requests;) {
             SrvReq* r = *it;
             if (r->type != head->type || !coalescible(s, r)) { ++it; continue; }
@@ -157,20 +163,21 @@ static std::vector<SrvReq*> take_group(Server* s, int64_t* reserve) {
             const SrvGraph& g = s->graphs[(size_t)r->graph];
             const int64_t m2 = um + (fresh ? g.m : 0), z2 = unz + (fresh ? g.nnz : 0);
             const int64_t ns2 = ns + (int64_t)r->sources.size();
+            const int64_t nc2 = std::max<int64_t>(ncols, (int64_t)r->sources.size());
             if (z2 > s->cfg.coalesce_max_nnz) { ++it; continue; }
-            if (r->type == GA_REQ_BC && (ns2 > kBcMaxSrc || m2 * (ns2 + 1) > s->cfg.bc_group_pairs)) {
+            if (r->type == GA_REQ_BC && (nc2 > kBcMaxSrc || m2 * (nc2 + 1) + ns2 > s->cfg.bc_group_pairs)) {
                 ++it;
                 continue;
             }
-            const int64_t b2 = bound_batch(head->type, m2, z2, nslots + (fresh ? 1 : 0), ns2);
+            const int64_t b2 = bound_batch(head->type, m2, z2, nslots + (fresh ? 1 : 0), ns2, nc2);
             if (s->reserved + b2 > s->budget) { ++it; continue; }
             if (fresh) slots[slot_key(r)] = (int)nslots++;
-            um = m2; unz = z2; ns = ns2;
+            um = m2; unz = z2; ns = ns2; ncols = nc2;
             *reserve = b2;
             group.push_back(r);
             it = s->queue.erase(it);
         }
-        if (group.size() > 1) *reserve = std::max(*reserve, bound_batch(head->type, um, unz, nslots, ns));
+        if (group.size() > 1) *reserve = std::max(*reserve, bound_batch(head->type, um, unz, nslots, ns, ncols));
         return group;
     }
     return group;

@@ -121,10 +121,16 @@ GA_API int ga_version(int* major, int* minor);
  * GA_OPT_KT_FRONTIER (1): the GA_TRI k-truss of one matrix lists the
  * triangles once and then, per iteration, only the triangles of the edges it
  * prunes, lowering the supports they touch (same edge sets and iteration
- * counts); 0 lists every triangle again in every iteration. */
+ * counts); 0 lists every triangle again in every iteration.
+ * GA_OPT_BC_BACKWARD (0): how BC's backward sweep reads the dependency
+ * rows W[w] of a vertex's next-level neighbours: 0 gathers, the rows of
+ * four neighbours in flight at once; 1 bulk copies (cp.async.bulk) of whole
+ * rows into shared memory, two batches of four rows in flight per warp
+ * (used for even source counts up to 128, else 0 runs); 2 one neighbour at
+ * a time. Results are the same. */
 enum { GA_OPT_DEVICE_LOOPS = 1, GA_OPT_PROFILE = 2, GA_OPT_FAIL_ALLOC_AFTER = 3, GA_OPT_KNN_TILED = 4,
        GA_OPT_MXM_WARP_FLOPS = 5, GA_OPT_MXM_HEAVY_FLOPS = 6, GA_OPT_MXM_CTAS_PER_SM = 7, GA_OPT_DOT_CHUNK = 8,
-       GA_OPT_HYBRID_RATIO = 9, GA_OPT_TRI_ORDER = 10, GA_OPT_KT_FRONTIER = 11 };
+       GA_OPT_HYBRID_RATIO = 9, GA_OPT_TRI_ORDER = 10, GA_OPT_KT_FRONTIER = 11, GA_OPT_BC_BACKWARD = 12 };
 GA_API int ga_ctx_set_option(ga_ctx ctx, int option, int64_t value);
 
 /* Per-kernel timing collected while GA_OPT_PROFILE is on. Writes up to `cap`
@@ -471,11 +477,13 @@ GA_API int ga_batch_ktruss(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, co
 GA_API int ga_batch_ktruss_k(ga_ctx ctx, ga_algo algo, ga_csr U, int64_t count, const int64_t* voff, const int* k,
                              ga_csr* C, int* iters);
 /* Batched BC over a block-diagonal union: graph g's sources are
- * sources[soff[g] .. soff[g+1]) (vertex indices within graph g; soff: host,
- * count+1 entries, at most 1,024 sources in all). No path leaves a graph,
- * so bc (host, length m of the union) holds in graph g's rows the scores
- * ga_bc gives for graph g and its sources alone (FP64, up to the order of
- * the sums). */
+ * sources[soff[g] .. soff[g+1]) (vertex indices within graph g, distinct;
+ * soff: host, count+1 entries, at most 1,024 sources per graph). No path
+ * leaves a graph, so the j-th sources of all graphs share one column of the
+ * per-(vertex, source) state: it holds union vertices x the largest source
+ * count. bc (host, length m of the union) holds in graph g's rows the
+ * scores ga_bc gives for graph g and its sources alone (FP64, up to the
+ * order of the sums). */
 GA_API int ga_batch_bc(ga_ctx ctx, ga_csr U, int64_t count, const int64_t* voff, const int64_t* soff,
                        const int32_t* sources, double* bc);
 
@@ -506,8 +514,9 @@ typedef struct {
     int64_t coalesce_max_nnz;      /* stored entries of one batched union at most; 0: 2^22 (several groups
                                       keep several workers busy) */
     int64_t coalesce_max_requests; /* requests served by one batched call at most; 0: 4096 */
-    int64_t bc_group_pairs;        /* batched BC keeps state per (union vertex, source): vertices x
-                                      (sources + 1) of one group at most; 0: 2^22 */
+    int64_t bc_group_pairs;        /* batched BC keeps state per (union vertex, source column): union
+                                      vertices x (largest source count of a request + 1) + sources
+                                      of one group at most; 0: 2^22 */
 } ga_server_config;
 typedef struct {
     int status;                /* GA_OK, the call's error code, or GA_ERR_ADMISSION */

@@ -113,6 +113,41 @@ def test_bc(ctx, device_loops):
         ctx.set_option(ga.OPT_DEVICE_LOOPS, 1)
 
 
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_bc_backward_modes(ctx, mode):
+    """GA_OPT_BC_BACKWARD: gathered W rows (0), bulk copies of whole rows
+    into shared memory (1; odd source counts and more than 128 sources fall
+    back to 0) and one neighbour at a time (2) all match the FP64 oracle; a
+    vertex with more than 1,024 neighbours (a CTA-shared row) is included."""
+    rng = np.random.default_rng(91)
+    from graphs import dense_to_csr
+    D = rng.random((300, 300)) < 0.05
+    np.fill_diagonal(D, False)
+    W = dense_to_csr(D, rng.integers(1, 4, size=(300, 300)), np.int32)
+    # a star centre with 1,500 neighbours next to an R-MAT core
+    m = 1600
+    r = list(range(1, 1501))
+    edges = [(0, j) for j in r] + [(j, 0) for j in r]
+    er = ga.gen_rmat(9, 8, seed=13)
+    rows = np.repeat(np.arange(er[0]), np.diff(er[1])) + 1000
+    edges += list(zip(rows.tolist(), (er[2] + 1000).tolist()))
+    edges += [(5, 1001), (1001, 5)]
+    E = np.array(sorted(set(edges)), dtype=np.int64)
+    rst = np.zeros(m + 1, np.int32)
+    np.add.at(rst, E[:, 0] + 1, 1)
+    S = csr_from_arrays(m, np.cumsum(rst).astype(np.int32), E[:, 1].astype(np.int32))
+    ctx.set_option(ga.OPT_BC_BACKWARD, mode)
+    try:
+        for G, counts in ((S, (64, 33, 130)), (W, (2, 40))):
+            for ns in counts:
+                src = rng.choice(G.m, ns, replace=False).astype(np.int32)
+                _bc_close(ga.bc(to_device(ctx, G), src), oracle.bc_batch(G, src))
+    finally:
+        ctx.set_option(ga.OPT_BC_BACKWARD, 0)
+    with pytest.raises(ga.GaError):
+        ctx.set_option(ga.OPT_BC_BACKWARD, 3)
+
+
 def test_bc_directed_and_weighted(ctx):
     rng = np.random.default_rng(78)
     from graphs import dense_to_csr

@@ -203,6 +203,46 @@ def test_batch_bc_matches_single(ctx):
         assert np.all(np.abs(part - orc) <= 1e-9 * np.maximum(np.abs(orc), 1.0)), g
 
 
+def test_batch_bc_uneven_source_counts(ctx):
+    """Graphs of a batch with different source counts share source columns:
+    a graph with no sources (zero scores), one with 40 (a partly used second
+    column word), one with 33, with 1 and with all its vertices; each part
+    equals the graph alone and the FP64 oracle within 1e-9."""
+    host, dev = _mixed_parts(ctx)
+    rng = np.random.default_rng(23)
+    counts = [40, 1, 33, 0, 5, 3, 120]
+    srcs = [rng.choice(G.m, min(G.m, c), replace=False) for G, c in zip(host, counts)]
+    U, voff = ga.block_diag(ctx, dev)
+    got = ga.batch_bc(U, voff, srcs)
+    for g, (G, Gd, src) in enumerate(zip(host, dev, srcs)):
+        part = got[voff[g]:voff[g + 1]]
+        if len(src) == 0:
+            assert not np.any(part), g
+            continue
+        ref = ga.bc(Gd, src)
+        assert np.all(np.abs(part - ref) <= 1e-9 * np.maximum(np.abs(ref), 1.0)), g
+        orc = oracle.bc_batch(G, src)
+        assert np.all(np.abs(part - orc) <= 1e-9 * np.maximum(np.abs(orc), 1.0)), g
+
+
+def test_batch_bc_many_graphs(ctx):
+    """More sources in all than one BC call takes (1,024): 48 k-NN graphs
+    with 32 sources each, as the request server batches them."""
+    n, dim = [int(x) for x in np.random.default_rng(5).integers(40, 400, 48)], [6] * 48
+    U, voff = ga.gen_knn_batch(ctx, n, dim, k=30, seed=31)
+    rst, col, _ = U.download()
+    rng = np.random.default_rng(8)
+    srcs = [rng.choice(m, 32, replace=False) for m in n]
+    got = ga.batch_bc(U, voff, srcs)
+    for g, (m, r, c) in enumerate(ga.split_blocks(rst, col, voff)):
+        if g % 6:
+            continue  # every sixth graph against the oracle
+        G = oracle.Csr(m, m, r, c, np.ones(len(c), np.int32))
+        orc = oracle.bc_batch(G, srcs[g].astype(np.int32))
+        part = got[voff[g]:voff[g + 1]]
+        assert np.all(np.abs(part - orc) <= 1e-9 * np.maximum(np.abs(orc), 1.0)), g
+
+
 @pytest.mark.parametrize("device_loops", [1, 0])
 def test_batch_ktruss_frontier_per_graph_k(ctx, device_loops):
     """The batched GA_TRI k-truss on the frontier path (one listing over the
