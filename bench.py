@@ -1098,9 +1098,10 @@ def serve_record(ga, ctx, args, dist: Dist, light_requests=None, full_requests=N
     out = {"unit": "req/s", "workers": args.workers, "variant": args.serve_algo, "tuned": tuned,
            "pool_build_s": t_pool, "tuning_s": t_tune,
            "graphs": {name: {"vertices": m, "stored_entries": len(col)} for name, m, _, col in pool}}
-    # warm-up: a few requests of each kind on the small graphs
+    # warm-up of both forms: a few requests of each kind on the small graphs
     warm = serve_requests(args, light, 12)
     serve_run(ga, light, warm, args.workers, True, algo=args.serve_algo)
+    serve_run(ga, light, warm, 1, False, algo=args.serve_algo)
     if light and light_requests > 0:
         out["light_mix"] = serve_mix(ga, args, light, serve_requests(args, light, light_requests), rates, "light")
     if full_requests > 0:

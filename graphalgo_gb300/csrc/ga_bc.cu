@@ -49,6 +49,7 @@ struct BcState {
     int32_t mode;          // forward direction of the current level: 0 pull, 1 push
     int32_t ntouched;      // vertices reached by the current push level
     int32_t stalled;       // a bulk copy of the backward sweep did not complete in time
+    int32_t nhrows;        // backward level: heavy rows listed in hrows
     unsigned long long cur_work, next_work;  // sum over frontier rows of entries x out-degree
 };
 
@@ -78,6 +79,7 @@ struct BcArgs {
     uint32_t* tbits;        // push levels: m x words, sources that reached each vertex
     int32_t* tlist;         // push levels: vertices reached, in order of first touch
     int32_t* tmark;         // push levels: vertex already listed
+    int32_t* hrows;         // backward level: rows of S[k-1] whose vertex has more than kBcHeavyDeg neighbours
 };
 
 // A level pushes (frontier rows scatter along their out-edges with global
@@ -104,7 +106,7 @@ __global__ void k_bc_init(BcArgs p) {
 __global__ void k_bc_state_init(BcArgs p) {
     p.st->d = 0; p.st->depth = 0; p.st->k = 0; p.st->done = 0;
     p.st->entries = p.nsrc; p.st->rows = 0; p.st->overflow = 0;
-    p.st->mode = 0; p.st->ntouched = 0; p.st->stalled = 0;
+    p.st->mode = 0; p.st->ntouched = 0; p.st->stalled = 0; p.st->nhrows = 0;
     p.st->cur_work = 0; p.st->next_work = 0;
     p.level_rows[0] = 0;
 }
@@ -306,19 +308,37 @@ __global__ void __launch_bounds__(kBcThreads) k_bc_forward(BcArgs p) {
         __syncthreads();
     }
 
+    // the rest: warp w takes the vertices w, w + W, w + 2W, ... (W warps in
+    // the grid), 32 of them at a time: each lane checks one (heavy vertices
+    // were done above; one that every source has reached, or without
+    // in-neighbours, gets an empty next row), then the warp pulls the others
+    // one by one
+    const unsigned FULL = 0xffffffffu;
     const int64_t warps = (int64_t)gridDim.x * kBcWarps;
-    for (int64_t v = (int64_t)blockIdx.x * kBcWarps + wid; v < p.m; v += warps) {
-        const int32_t ab = p.atr[v], ae = p.atr[v + 1];
-        if (ae - ab > kBcHeavyDeg) continue;  // done above
-        if (p.vcnt[v] >= p.ns) {
-            if (lane == 0) nxtL[v] = 0;
-            continue;
+    for (int64_t v0 = (int64_t)blockIdx.x * kBcWarps + wid; v0 < p.m; v0 += warps * 32) {
+        const int64_t vl = v0 + (int64_t)lane * warps;
+        int32_t lab = 0, lae = 0;
+        bool act = false;
+        if (vl < p.m) {
+            lab = p.atr[vl];
+            lae = p.atr[vl + 1];
+            if (lae - lab <= kBcHeavyDeg) {
+                act = lae > lab && p.vcnt[vl] < p.ns;
+                if (!act) nxtL[vl] = 0;
+            }
         }
-        if (lane < p.words) vis[lane] = p.vbits[(size_t)v * p.words + lane];
-        __syncwarp();
-        for (int32_t g = ab; g < ae; g += 32)
-            bc_pull_group<UNIT>(p, curS, curL, g, ae, vis, acc, touched, s_incl, s_off, s_a);
-        bc_emit_row(p, v, nxtS, nxtL, vis, acc, touched);
+        unsigned am = __ballot_sync(FULL, act);
+        while (am) {
+            const int src = __ffs(am) - 1;
+            am &= am - 1;
+            const int64_t v = v0 + (int64_t)src * warps;
+            const int32_t ab = __shfl_sync(FULL, lab, src), ae = __shfl_sync(FULL, lae, src);
+            if (lane < p.words) vis[lane] = p.vbits[(size_t)v * p.words + lane];
+            __syncwarp();
+            for (int32_t g = ab; g < ae; g += 32)
+                bc_pull_group<UNIT>(p, curS, curL, g, ae, vis, acc, touched, s_incl, s_off, s_a);
+            bc_emit_row(p, v, nxtS, nxtL, vis, acc, touched);
+        }
     }
 }
 
@@ -451,6 +471,16 @@ __global__ void k_bc_set_w(BcArgs p, bool set) {
         if (lane == 0) {
             if (set) atomicOr(&p.inlvl[v >> 5], 1u << (v & 31));
             else atomicAnd(&p.inlvl[v >> 5], ~(1u << (v & 31)));
+        }
+    }
+    // before the backward level: the heavy rows of S[k-1], listed so that
+    // the CTAs of the backward kernel can share them out
+    if (set) {
+        const int32_t q0 = p.level_rows[k - 1];
+        for (int64_t r = q0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < r0;
+             r += (int64_t)gridDim.x * blockDim.x) {
+            const int32_t v = p.rv[r];
+            if (p.ar[v + 1] - p.ar[v] > kBcHeavyDeg) p.hrows[atomicAdd(&p.st->nhrows, 1)] = (int32_t)r;
         }
     }
 }
@@ -606,7 +636,7 @@ __device__ __forceinline__ void bc_push_range(const BcArgs& p, int32_t t0, int32
 // sit at level k; bcu += acc*sigma; bc[v] += sum_s acc*sigma. Rows of heavy
 // vertices are shared by all warps of a CTA, the others take one warp.
 template <bool UNIT, int MODE>
-__global__ void __launch_bounds__(kBcThreads) k_bc_backward(BcArgs p) {
+__global__ void __launch_bounds__(kBcThreads, 3) k_bc_backward(BcArgs p) {
     __shared__ double sacc[kBcMaxSources];
     __shared__ double s_vsum;
     extern __shared__ __align__(16) unsigned char bsmem[];
@@ -631,11 +661,13 @@ __global__ void __launch_bounds__(kBcThreads) k_bc_backward(BcArgs p) {
         __syncwarp();
     }
 
-    // heavy rows: each warp takes every 8th group of 32 neighbours
-    for (int64_t r = r0 + blockIdx.x; r < r1; r += gridDim.x) {
+    // heavy rows (listed by k_bc_set_w), one per CTA at a time: its warps
+    // share the row, each warp taking every 8th group of 32 neighbours
+    const int nh = p.st->nhrows;
+    for (int hr = blockIdx.x; hr < nh; hr += gridDim.x) {
+        const int32_t r = p.hrows[hr];
         const int32_t v = p.rv[r];
         const int32_t ab = p.ar[v], ae = p.ar[v + 1];
-        if (ae - ab <= kBcHeavyDeg) continue;  // uniform over the CTA
         const int32_t e0 = p.rs[r], n = p.rl[r];
         for (int e = threadIdx.x; e < n; e += blockDim.x) sacc[e] = 0.0;
         if (threadIdx.x == 0) s_vsum = 0.0;
@@ -705,6 +737,7 @@ __global__ void __launch_bounds__(kBcThreads) k_bc_backward(BcArgs p) {
 __global__ void k_bc_backward_finalize(BcArgs p, LoopCtl ctl) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     BcState* st = p.st;
+    st->nhrows = 0;
     if (st->k >= 1) st->k -= 1;
     loop_continue(ctl, st->k >= 1);
 }
@@ -823,10 +856,10 @@ static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t ns
 
         // push-level state: touched bits, list of reached vertices, marks
         DBuf<uint32_t> tbits(ctx, (size_t)m * words);
-        DBuf<int32_t> tlist(ctx, (size_t)m), tmark(ctx, (size_t)m);
+        DBuf<int32_t> tlist(ctx, (size_t)m), tmark(ctx, (size_t)m), hrows(ctx, (size_t)m);
         GA_CUDA(cudaMemsetAsync(tbits.p, 0, sizeof(uint32_t) * m * words, ctx->stream));
         GA_CUDA(cudaMemsetAsync(tmark.p, 0, sizeof(int32_t) * m, ctx->stream));
-        p.tbits = tbits.p; p.tlist = tlist.p; p.tmark = tmark.p;
+        p.hrows = hrows.p; p.tbits = tbits.p; p.tlist = tlist.p; p.tmark = tmark.p;
         p.nnz = ATu->nnz;
         k_bc_state_init<<<1, 1, 0, ctx->stream>>>(p);
         post_launch("bc_state_init");
@@ -861,14 +894,20 @@ static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t ns
             run_device_loop(ctx, [&](const LoopCtl& ctl) {
                 k_bc_level_begin<<<1, 1, 0, ctx->stream>>>(p);
                 post_launch("bc_level_begin");
-                fwd<<<grid_fwd, kBcThreads, smem, ctx->stream>>>(p);
-                post_launch("bc_forward");
-                push<<<grid_rows, kBcThreads, 0, ctx->stream>>>(p);
-                post_launch("bc_push");
-                k_bc_push_clear<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(p);
-                post_launch("bc_push_clear");
-                k_bc_push_emit<<<grid_rows, kBcThreads, 0, ctx->stream>>>(p);
-                post_launch("bc_push_emit");
+                {
+                    ProfScope pk(ctx, "bc_forward_pull");
+                    fwd<<<grid_fwd, kBcThreads, smem, ctx->stream>>>(p);
+                    post_launch("bc_forward");
+                }
+                {
+                    ProfScope pk(ctx, "bc_forward_push");
+                    push<<<grid_rows, kBcThreads, 0, ctx->stream>>>(p);
+                    post_launch("bc_push");
+                    k_bc_push_clear<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(p);
+                    post_launch("bc_push_clear");
+                    k_bc_push_emit<<<grid_rows, kBcThreads, 0, ctx->stream>>>(p);
+                    post_launch("bc_push_emit");
+                }
                 k_bc_forward_finalize<<<1, 32, 0, ctx->stream>>>(p, ctl);
                 post_launch("bc_forward_finalize");
             }, m + 2);
@@ -897,8 +936,11 @@ static void bc_device(ga_ctx ctx, ga_csr A, const int32_t* d_sources, int64_t ns
             run_device_loop(ctx, [&](const LoopCtl& ctl) {
                 k_bc_set_w<<<grid_rows, 256, 0, ctx->stream>>>(p, true);
                 post_launch("bc_set_w");
-                bwd<<<grid_rows, kBcThreads, bsmem, ctx->stream>>>(p);
-                post_launch("bc_backward");
+                {
+                    ProfScope pk(ctx, "bc_backward");
+                    bwd<<<grid_rows, kBcThreads, bsmem, ctx->stream>>>(p);
+                    post_launch("bc_backward");
+                }
                 k_bc_set_w<<<grid_rows, 256, 0, ctx->stream>>>(p, false);
                 post_launch("bc_clear_w");
                 k_bc_backward_finalize<<<1, 32, 0, ctx->stream>>>(p, ctl);

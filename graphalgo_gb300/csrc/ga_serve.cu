@@ -372,7 +372,7 @@ int ga_server_create(int device, const ga_server_config* cfg, ga_server* out) {
     if (c.coalesce_nnz <= 0) c.coalesce_nnz = 1 << 20;
     if (c.coalesce_max_nnz <= 0) c.coalesce_max_nnz = 1 << 22;
     if (c.coalesce_max_requests <= 0) c.coalesce_max_requests = 4096;
-    if (c.bc_group_pairs <= 0) c.bc_group_pairs = (int64_t)1 << 22;
+    if (c.bc_group_pairs <= 0) c.bc_group_pairs = (int64_t)1 << 25;
     if (c.workers > 64) return GA_ERR_INVALID_ARG;
     s->cfg = c;
     int rc = ga_ctx_create(device, nullptr, &s->home);

@@ -516,7 +516,7 @@ typedef struct {
     int64_t coalesce_max_requests; /* requests served by one batched call at most; 0: 4096 */
     int64_t bc_group_pairs;        /* batched BC keeps state per (union vertex, source column): union
                                       vertices x (largest source count of a request + 1) + sources
-                                      of one group at most; 0: 2^22 */
+                                      of one group at most; 0: 2^25 */
 } ga_server_config;
 typedef struct {
     int status;                /* GA_OK, the call's error code, or GA_ERR_ADMISSION */
