@@ -18,7 +18,11 @@
 //                 slot base is kept per 32-column word). Warp rows use a
 //                 4096-bit hashed filter and a 512-entry hash table.
 //       GA_MCA  : binary search of the sorted mask row in shared memory (the
-//                 reference MCA walks the mask row, matrix_la.h:625-632);
+//                 reference MCA walks the mask row, matrix_la.h:625-632),
+//                 after a membership test that rejects the columns outside
+//                 the mask (most products of a k-truss support miss it): a
+//                 bitmap over the window (CTA items) or the 4096-bit hashed
+//                 filter (warp rows);
 //       GA_HEAP : warp-cooperative sorted merge of each B row against the
 //                 mask row (replaces the priority-queue merge,
 //                 matrix_la.h:1030-1084).
@@ -178,14 +182,16 @@ __global__ void k_row_bin(MxmArgs<T, A> p) {
 
 // ------------------------------------------------------------------ lookups
 // MODE: how a product's column finds its mask slot.
-enum { MD_DENSE = 0, MD_HASHED = 1, MD_BSEARCH = 2, MD_MERGE = 3 };
+// MD_BSEARCH: CTA items (window bitmap, then search); MD_BSEARCH_F: warp
+// rows (hashed filter, then search).
+enum { MD_DENSE = 0, MD_HASHED = 1, MD_BSEARCH = 2, MD_MERGE = 3, MD_BSEARCH_F = 4 };
 
 // The mask columns of one work item, staged in shared memory.
 struct SlotView {
-    const int32_t* mcol;    // MD_BSEARCH / MD_MERGE: sorted mask columns
-    const uint32_t* bits;   // MD_DENSE: bitmap over [lo, lo + kWinCols)
+    const int32_t* mcol;    // MD_BSEARCH(_F) / MD_MERGE: sorted mask columns
+    const uint32_t* bits;   // MD_DENSE, MD_BSEARCH: bitmap over [lo, lo + kWinCols)
     const uint16_t* wbase;  // MD_DENSE: slot of the first mask column of each bitmap word
-    const uint32_t* filt;   // MD_HASHED: 4096-bit filter of hashed columns
+    const uint32_t* filt;   // MD_HASHED, MD_BSEARCH_F: 4096-bit filter of hashed columns
     const int32_t* hkeys;   // MD_HASHED: open-addressing table (2^kWarpTblBits)
     const uint8_t* hslot;
     int ns;
@@ -217,6 +223,13 @@ __device__ __forceinline__ int slot_of(const SlotView& v, int32_t c) {
         }
     } else {
         if (c < v.lo || c > v.hi) return -1;
+        if (MD == MD_BSEARCH) {
+            const uint32_t d = (uint32_t)(c - v.lo);
+            if (!((v.bits[d >> 5] >> (d & 31)) & 1u)) return -1;
+        } else if (MD == MD_BSEARCH_F) {
+            const uint32_t f = hash_col(c) >> (32 - kFilterBits);
+            if (!((v.filt[f >> 5] >> (f & 31)) & 1u)) return -1;
+        }
         const int pos = lower_bound_i32(v.mcol, v.ns, c);
         return (pos < v.ns && v.mcol[pos] == c) ? pos : -1;
     }
@@ -446,22 +459,25 @@ __device__ __forceinline__ void merge_row(const MxmArgs<T, A>& p, int32_t bs, in
 template <int MD, typename A>
 struct MxmSmem {
     static constexpr bool dense = MD == MD_DENSE;
+    static constexpr bool filt = MD == MD_BSEARCH;  // bitmap / hashed filter in front of the search
     // CTA phase
     static constexpr size_t off_acc = 0;
     static constexpr size_t off_lbs = off_acc + (size_t)kCtaSlots * sizeof(A);
     static constexpr size_t off_lend = off_lbs + (size_t)kLongCap * 4;
     static constexpr size_t off_lchunk = off_lend + (size_t)kLongCap * 4;
     static constexpr size_t off_la = off_lchunk + (size_t)(kLongCap + 8) * 4;
-    static constexpr size_t off_key = off_la + (size_t)kLongCap * sizeof(A);  // bits+wbase or mcol
+    static constexpr size_t off_key = off_la + (size_t)kLongCap * sizeof(A);  // bits+wbase, bits+mcol or mcol
     static constexpr size_t off_wbase = off_key + (size_t)kWinWords * 4;
-    static constexpr size_t cta_bytes =
-        dense ? off_wbase + (size_t)kWinWords * 2 : off_key + (size_t)kCtaSlots * 4;
+    static constexpr size_t off_fcol = off_key + (size_t)kWinWords * 4;  // MCA: mcol after the bitmap
+    static constexpr size_t cta_bytes = dense  ? off_wbase + (size_t)kWinWords * 2
+                                        : filt ? off_fcol + (size_t)kCtaSlots * 4
+                                               : off_key + (size_t)kCtaSlots * 4;
     // warp phase (per warp): acc, hashed filter + table (MSA) or mcol (others)
     static constexpr size_t w_acc = 0;
     static constexpr size_t w_filt = w_acc + (size_t)kWarpSlots * sizeof(A);
     static constexpr size_t w_hkeys = w_filt + (size_t)(1 << kFilterBits) / 8;
     static constexpr size_t w_hslot = w_hkeys + (size_t)(1 << kWarpTblBits) * 4;
-    static constexpr size_t w_mcol = w_filt;
+    static constexpr size_t w_mcol = filt ? w_filt + (size_t)(1 << kFilterBits) / 8 : w_filt;
     static constexpr size_t warp_one =
         dense ? w_hslot + (size_t)(1 << kWarpTblBits) : w_mcol + (size_t)kWarpSlots * 4;
     static constexpr size_t warp_bytes = warp_one * kMxmWarps;
@@ -476,7 +492,9 @@ __global__ void __launch_bounds__(kMxmThreads, 3) k_mxm_masked(MxmArgs<T, A> p) 
     extern __shared__ __align__(16) unsigned char smem[];
     using SM = MxmSmem<MD, A>;
     constexpr bool DENSE = MD == MD_DENSE;
-    constexpr int WMD = DENSE ? MD_HASHED : MD;  // warp-row lookup
+    constexpr bool FILT = MD == MD_BSEARCH;   // MCA: membership filters in front of the search
+    constexpr bool BITS = DENSE || FILT;      // CTA items keep a window bitmap
+    constexpr int WMD = DENSE ? MD_HASHED : FILT ? MD_BSEARCH_F : MD;  // warp-row lookup
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     unsigned char* scr = smem + SM::region;
@@ -495,8 +513,8 @@ __global__ void __launch_bounds__(kMxmThreads, 3) k_mxm_masked(MxmArgs<T, A> p) 
         A* la = reinterpret_cast<A*>(smem + SM::off_la);
         uint32_t* bits = reinterpret_cast<uint32_t*>(smem + SM::off_key);
         uint16_t* wbase = reinterpret_cast<uint16_t*>(smem + SM::off_wbase);
-        int32_t* mcol = reinterpret_cast<int32_t*>(smem + SM::off_key);
-        if (DENSE)
+        int32_t* mcol = reinterpret_cast<int32_t*>(smem + (FILT ? SM::off_fcol : SM::off_key));
+        if (BITS)
             for (int t = threadIdx.x; t < kWinWords; t += blockDim.x) bits[t] = 0u;
         const int nheavy = p.q->heavy_count;
         const int ncta = nheavy + p.q->normal_count;
@@ -526,6 +544,10 @@ __global__ void __launch_bounds__(kMxmThreads, 3) k_mxm_masked(MxmArgs<T, A> p) 
                     if (s == 0 || ((uint32_t)(__ldg(gcol + s - 1) - v.lo) >> 5) != (d >> 5)) wbase[d >> 5] = (uint16_t)s;
                 } else {
                     mcol[s] = c;
+                    if (FILT) {
+                        const uint32_t d = (uint32_t)(c - v.lo);
+                        atomicOr(&bits[d >> 5], 1u << (d & 31));
+                    }
                 }
             }
             __syncthreads();
@@ -585,7 +607,7 @@ __global__ void __launch_bounds__(kMxmThreads, 3) k_mxm_masked(MxmArgs<T, A> p) 
             __syncthreads();
             for (int s = threadIdx.x; s < ns; s += blockDim.x) {
                 p.cv[mb + s0 + s] = from_acc<T, A>(acc[s]);
-                if (DENSE) bits[(uint32_t)(__ldg(gcol + s) - v.lo) >> 5] = 0u;
+                if (BITS) bits[(uint32_t)(__ldg(gcol + s) - v.lo) >> 5] = 0u;
             }
             __syncthreads();
         }
@@ -601,10 +623,10 @@ __global__ void __launch_bounds__(kMxmThreads, 3) k_mxm_masked(MxmArgs<T, A> p) 
         int32_t* mcol = reinterpret_cast<int32_t*>(base + SM::w_mcol);
         constexpr int FW = (1 << kFilterBits) / 32;
         constexpr int TBL = 1 << kWarpTblBits;
-        if (DENSE) {
+        if (DENSE || FILT)
             for (int t = lane; t < FW; t += 32) filt[t] = 0u;
+        if (DENSE)
             for (int t = lane; t < TBL; t += 32) hkeys[t] = kEmpty;
-        }
         __syncwarp();
         const int nwarp = p.q->warp_count;
         while (true) {
@@ -630,6 +652,10 @@ __global__ void __launch_bounds__(kMxmThreads, 3) k_mxm_masked(MxmArgs<T, A> p) 
                     hash_insert<uint8_t>(hkeys, hslot, kWarpTblBits, c, (uint8_t)s);
                 } else {
                     mcol[s] = c;
+                    if (FILT) {
+                        const uint32_t f = hash_col(c) >> (32 - kFilterBits);
+                        atomicOr(&filt[f >> 5], 1u << (f & 31));
+                    }
                 }
             }
             __syncwarp();
@@ -648,10 +674,10 @@ __global__ void __launch_bounds__(kMxmThreads, 3) k_mxm_masked(MxmArgs<T, A> p) 
             }
             __syncwarp();
             for (int s = lane; s < mi; s += 32) p.cv[mb + s] = from_acc<T, A>(acc[s]);
-            if (DENSE) {
+            if (DENSE || FILT)
                 for (int t = lane; t < FW; t += 32) filt[t] = 0u;
+            if (DENSE)
                 for (int t = lane; t < TBL; t += 32) hkeys[t] = kEmpty;
-            }
             __syncwarp();
         }
     }
