@@ -450,8 +450,10 @@ __device__ __forceinline__ void merge_row(const MxmArgs<T, A>& p, int32_t bs, in
         const int32_t yr = __shfl_sync(FULL, y, r & 31);
         if (r < 32 && yr == x && x != INT32_MAX)
             atomic_add_acc<A>(&acc[yc + r], av * to_acc<T, A>(__ldg(p.bv + xb + lane)));
-        const int32_t x31 = __shfl_sync(FULL, x, 31);
-        if (x31 <= y31) xb += 32; else yc += 32;
+        // the chunk whose last element is smaller moves on; for B that is its
+        // last stored element (past the row's end the lanes hold INT32_MAX)
+        const int32_t xl = __shfl_sync(FULL, x, min(31, be - 1 - xb));
+        if (xl <= y31) xb += 32; else yc += 32;
     }
 }
 
