@@ -69,6 +69,9 @@ GOLDEN_SWEEP = os.path.join(ROOT, "tests", "golden", "rmat18_sweep.json")
 # launch of the sweep works on operands that fit in L2, so its DRAM traffic
 # is the compulsory traffic of its operands, proportional to its entries.
 DRAM_BYTES_PER_ENTRY = {"tri_support": 7.506, "mxm": 4.543}
+# DRAM bytes per pruned edge of the frontier k-truss kernel k_trif_lower,
+# from its ncu capture (None until one exists: no traffic figure).
+DRAM_BYTES_PER_FRONT_EDGE = None
 
 
 def parse_args():
@@ -94,9 +97,10 @@ def parse_args():
     ap.add_argument("--no-other-configs", action="store_true",
                     help="skip the TC (Erdos-Renyi n=1000) and BC (R-MAT 20) measurements")
     ap.add_argument("--cpu-reps", type=int, default=2)
-    ap.add_argument("--case", choices=["support", "tc", "bc", "ktruss", "batch"], default=None,
+    ap.add_argument("--case", choices=["support", "tc", "bc", "ktruss", "sweep", "batch"], default=None,
                     help="profiling case instead of the benchmark, --reps times: support product, TC, BC, "
-                         "4-truss from A, or batched TC + 4-truss of --graphs k-NN graphs")
+                         "4-truss from A, the k-truss sweep from A, or batched TC + 4-truss of --graphs k-NN "
+                         "graphs")
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--sources", type=int, default=64)
     ap.add_argument("--ingest-scale", type=int, default=20, help="ingest workload: R-MAT scale of the file")
@@ -241,8 +245,10 @@ def run_case(args):
     """Small profiling cases, --reps times each (used for ncu captures):
     `support` = the sweep's first support product C<A> = A*A; `tc` =
     triangle count with the dot-product kernel; `bc` = batched BC over
-    --sources seeded sources; `ktruss` = 4-truss from A (all on the bench's
-    R-MAT graph); `batch` = batched TC + 4-truss of --graphs k-NN graphs."""
+    --sources seeded sources; `ktruss` = 4-truss from A; `sweep` = the
+    k-truss sweep k = --kmin ... from A, with the library's kernel launches
+    per sweep (all on the bench's R-MAT graph); `batch` = batched TC +
+    4-truss of --graphs k-NN graphs."""
     import graphalgo_gb300 as ga
     from graphalgo_gb300 import build as gbuild
     gbuild.build()
@@ -291,6 +297,12 @@ def run_case(args):
             ms = ctx.timer_stop()
             rec = {"ktruss_ms": ms, "iters": it, "nnz": C.nnz, "products": ctx.work_counters()["products"]}
             C.free()
+        elif args.case == "sweep":
+            l0 = ga.kernel_launches()
+            shape = sweep(ga, ctx, A, args.algo, args.kmin)
+            ms = ctx.timer_stop()
+            rec = {"sweep_ms": ms, "stages": len(shape), "iterations": int(sum(s[1] for s in shape)),
+                   "launches": ga.kernel_launches() - l0, "products": ctx.work_counters()["products"]}
         else:
             ga.bc(A, src)
             ms = ctx.timer_stop()
@@ -353,38 +365,44 @@ def cpu_sample(A_host, reps: int):
 
 # --------------------------------------------------------------- GPU arm
 def sweep(ga, ctx, A, algo, kmin, sink=None, per_k=None):
-    """k-truss sweep from A: C_k = k_truss(C_{k-1}, k) until the truss is empty."""
-    cur, k, out = A, kmin, []
-    while True:
+    """k-truss sweep from A: C_k = k_truss(C_{k-1}, k) until the truss is
+    empty, through ga.ktruss_sweep (with triangle listing one device-resident
+    state for the whole sweep). Each C_k is freed once the next one exists,
+    so a download of it (sink) overlaps with the next k."""
+    out, prev = [], None
+    if per_k is not None:
+        ctx.work_counters(reset=True)
+    for k, C, it in ga.ktruss_sweep(algo, A, kmin):
+        out.append((k, it, C.nnz))
         if per_k is not None:
-            ctx.work_counters(reset=True)
-        C, it = ga.ktruss(algo, cur, k)
-        nnz = C.nnz
-        out.append((k, it, nnz))
-        if per_k is not None:
-            per_k[k] = ctx.work_counters()
+            per_k[k] = ctx.work_counters(reset=True)
         if sink is not None:
             sink(k, C)
-        if cur is not A:
-            cur.free()
-        cur = C
-        if nnz == 0:
-            break
-        k += 1
-    if cur is not A:
-        cur.free()
+        if prev is not None:
+            prev.free()
+        prev = C
+    if prev is not None:
+        prev.free()
     return out
 
 
 def profile_step(ga, ctx, run, algo, counters, loops):
     """Runs one step with host-driven loops and per-kernel timing; returns the
-    launch count and the roofline of the masked-SpGEMM kernel.
+    launch count and the roofline of the step's dominant kernel.
 
-    achieved = algorithmic bytes of the Gustavson model with int32 values
-    (s = 4): 4(m+1)*2 + nnz(A)*(4+4) + nnz(A)*8 + P*(4+4) + nnz(M)*4 +
-    nnz(C)*4, P being the products the kernel processed (the support of a
-    symmetric C evaluates its upper triangle and mirrors it), divided by the
-    kernel's summed event time."""
+    Gustavson variants: achieved = algorithmic bytes of the Gustavson model
+    with int32 values (s = 4): 4(m+1)*2 + nnz(A)*(4+4) + nnz(A)*8 + P*(4+4) +
+    nnz(M)*4 + nnz(C)*4, P being the products the kernel processed (the
+    support of a symmetric C evaluates its upper triangle and mirrors it),
+    divided by the kernel's summed event time. Triangle listing (the sweep
+    lists the triangles once and then prunes by frontier): the frontier
+    kernel k_trif_lower, 48 bytes per pruned edge (its frontier slot, row,
+    column, diagonal positions, support, both rows' bounds, the oriented
+    count and rank of the far row), 34 bytes per probed row entry (column,
+    record position, state and rank of the entry, about four binary-search
+    steps in the other row, the found entry's record position and state) and
+    16 bytes per destroyed triangle (two 4-byte support read-modify-writes),
+    over its summed event time."""
     ctx.set_option(ga.OPT_DEVICE_LOOPS, 0)
     ctx.set_option(ga.OPT_PROFILE, 1)
     ctx.reset_kernel_stats()
@@ -399,18 +417,12 @@ def profile_step(ga, ctx, run, algo, counters, loops):
     ctx.set_option(ga.OPT_PROFILE, 0)
     ctx.set_option(ga.OPT_DEVICE_LOOPS, loops)
     kname = {"msa": "mxm_msa", "mca": "mxm_mca", "heap": "mxm_heap_merge", "dot": "mxm_dot",
-             "hybrid": "mxm_msa", "tri": "tri_support"}[algo]
+             "hybrid": "mxm_msa", "tri": "trif_lower"}[algo]
     k_launches, k_ms = stats.get(kname, (0, 0.0))
     if algo == "tri":
-        # triangle listing: oriented row starts and task starts (4 bytes each
-        # per row), per oriented entry (half the stored entries of a graph
-        # without loops) its column, its list bounds and one 4-byte count
-        # read-modify-write, per wedge its column, per triangle two 4-byte
-        # read-modify-writes
-        eo = ctr["a_entries"] / 2
-        bytes_model = 8 * ctr["rows"] + 20 * eo + 4 * ctr["wedges"] + 16 * ctr["triangles"]
-        tpe = DRAM_BYTES_PER_ENTRY["tri_support"]
-        traffic_units = ctr["a_entries"]  # the capture's DRAM bytes are per stored entry
+        bytes_model = 48 * ctr["front_edges"] + 34 * ctr["front_probes"] + 16 * ctr["front_triangles"]
+        tpe = DRAM_BYTES_PER_FRONT_EDGE
+        traffic_units = ctr["front_edges"]  # the capture's DRAM bytes are per pruned edge
     else:
         # products of the Gustavson kernels; list entries walked for the inner-product one
         ex = ctr["executed_dot"] if algo == "dot" else ctr["executed"]
@@ -712,10 +724,15 @@ def run_gpu(args, dist: Dist):
                  "executed_products_per_step": wc["executed"] / args.steps, "k_max": kmax,
                  "support_products_k3": per_k.get(args.kmin, {}).get("products"),
                  "wedges_per_step": wc["wedges"] / args.steps, "triangles_per_step": wc["triangles"] / args.steps,
+                 "frontier_edges_per_step": wc["front_edges"] / args.steps,
+                 "frontier_probes_per_step": wc["front_probes"] / args.steps,
+                 "frontier_triangles_per_step": wc["front_triangles"] / args.steps,
                  "note": "value counts 2 x the Gustavson products of the reference's C<C> = C*C for every "
-                         "support product (products_per_step): a reference-equivalent rate; the "
-                         "triangle-listing form computes the same values from wedges_per_step rank-ordered "
-                         "lookups, the Gustavson forms from executed_products_per_step products"},
+                         "support product of every k (products_per_step): a reference-equivalent rate, not "
+                         "arithmetic executed. The triangle-listing sweep lists the triangles once "
+                         "(wedges_per_step rank-ordered lookups) and then, k after k and iteration after "
+                         "iteration, walks only the triangles of the edges it prunes (frontier_*); the "
+                         "Gustavson forms execute executed_products_per_step products"},
         "kernel_profile": {"note": "one step with host-driven loops and CUDA events per launch (slower than "
                                    "the timed step); summed event time per kernel scope, ms",
                            "top": {k: round(v[1], 3) for k, v in

@@ -178,12 +178,14 @@ class Context:
         """Masked-SpGEMM work since the last reset: Gustavson products P of the
         requested products, mask entries, launches, A entries, rows, the
         products the Gustavson kernels processed, and the list entries the
-        inner-product kernels walked, and the wedges and triangles of the
-        triangle-listing form (device counters)."""
-        out = (ctypes.c_int64 * 9)()
+        inner-product kernels walked, the wedges and triangles of the
+        triangle-listing form, and the pruned edges, probed row entries and
+        destroyed triangles of the frontier k-truss (device counters)."""
+        out = (ctypes.c_int64 * 12)()
         _check(lib().ga_ctx_work_counters(self.handle, out, int(bool(reset))), self)
         return dict(zip(("products", "mask_entries", "launches", "a_entries", "rows", "executed", "executed_dot",
-                         "wedges", "triangles"), (int(x) for x in out)))
+                         "wedges", "triangles", "front_edges", "front_probes", "front_triangles"),
+                        (int(x) for x in out)))
 
     def flush_l2(self):
         _check(lib().ga_ctx_flush_l2(self.handle), self)
@@ -484,6 +486,23 @@ def ktruss(algo, A: Csr, k: int) -> Tuple[Csr, int]:
     it = _int()
     _check(lib().ga_ktruss(A.ctx.handle, _algo(algo), A.handle, int(k), ctypes.byref(h), ctypes.byref(it)), A.ctx)
     return Csr(A.ctx, h), int(it.value)
+
+
+def ktruss_sweep(algo, A: Csr, kmin: int = 3):
+    """k-truss sweep from A: yields (k, C_k, iterations) for k = kmin,
+    kmin + 1, ... until C_k is empty (the empty C_k included), each C_k equal
+    to ktruss(algo, C_{k-1}, k). The caller frees each C_k."""
+    h = _p()
+    _check(lib().ga_ktruss_sweep_begin(A.ctx.handle, _algo(algo), A.handle, int(kmin), ctypes.byref(h)), A.ctx)
+    try:
+        while True:
+            c, k, it = _p(), _int(), _int()
+            _check(lib().ga_ktruss_sweep_next(h, ctypes.byref(c), ctypes.byref(k), ctypes.byref(it)), A.ctx)
+            if not c:
+                return
+            yield int(k.value), Csr(A.ctx, c), int(it.value)
+    finally:
+        lib().ga_ktruss_sweep_free(h)
 
 
 def bc(A: Csr, sources: Sequence[int]) -> np.ndarray:

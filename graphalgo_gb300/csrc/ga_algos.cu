@@ -4,6 +4,8 @@
 #include "ga_device.cuh"
 #include "ga_loop.cuh"
 
+#include <memory>
+
 namespace ga {
 
 // ============================================================ loop driver
@@ -695,11 +697,149 @@ ga_csr ktruss_impl(ga_ctx ctx, ga_algo algo, ga_csr A, int k, int* iters_out, co
     return C;
 }
 
+// ------------------------------------------------------------ k-truss sweep
+// C_k = k-truss of A for k = kmin, kmin + 1, ... until C_k is empty, each
+// C_k equal to k_truss(C_{k-1}, k) (src/main.cpp:90-146). For a symmetric
+// 0/1 matrix with triangle listing the frontier state stays on the device
+// from one k to the next: the triangles are listed once for the whole
+// sweep, and each k starts from the supports the previous k left. Otherwise
+// every k is one ga_ktruss call on the previous result.
+struct KtSweep {
+    ga_ctx ctx = nullptr;
+    ga_algo algo = GA_MSA;
+    int k = 0;
+    bool finished = false;
+    ga_csr cur = nullptr;  // stage by stage: the next k's input
+    bool fused = false;
+    ga_csr W = nullptr;    // fused: A's copy, rows partitioned for the whole sweep
+    int64_t cap = 0;
+    DBuf<int32_t> sup, eflag, tr, tc, row_of, mir, oid, f0, f1;
+    DBuf<uint8_t> state;
+    DBuf<unsigned char> scan_scr, tri_scr;
+    TriKt tk{};
+    std::unique_ptr<TriFront> front;
+
+    ~KtSweep() {
+        front.reset();
+        if (cur) csr_destroy(ctx, cur);
+        if (W) csr_destroy(ctx, W);
+    }
+
+    void begin(ga_algo a, ga_csr A, int kmin) {
+        GA_REQUIRE(A->m == A->n, GA_ERR_SHAPE, "k-truss needs a square matrix");
+        GA_REQUIRE(A->dtype == GA_INT32, GA_ERR_DTYPE, "k-truss needs int32 values (spMtx<int>)");
+        algo = a;
+        k = kmin;
+        const int64_t m = A->m;
+        ga_algo r = GA_MSA;
+        {
+            TuneScope tscope(ctx);
+            r = resolve_ktruss_algo(ctx, a, A);
+        }
+        fused = r == GA_TRI && ctx->kt_frontier && m > 0 && A->nnz > 0 && csr_is_symmetric(ctx, A) &&
+                csr_unit_values(ctx, A);
+        if (!fused) {
+            cur = copy_csr(ctx, A, GA_INT32);
+            return;
+        }
+        W = copy_csr(ctx, A, GA_INT32);
+        cap = W->nnz;
+        sup = DBuf<int32_t>(ctx, (size_t)cap);
+        eflag = DBuf<int32_t>(ctx, (size_t)cap + 1);
+        tr = DBuf<int32_t>(ctx, (size_t)m + 1);
+        tc = DBuf<int32_t>(ctx, (size_t)cap);
+        row_of = DBuf<int32_t>(ctx, (size_t)cap);
+        mir = DBuf<int32_t>(ctx, (size_t)cap);
+        oid = DBuf<int32_t>(ctx, (size_t)cap);
+        f0 = DBuf<int32_t>(ctx, (size_t)cap);
+        f1 = DBuf<int32_t>(ctx, (size_t)cap);
+        state = DBuf<uint8_t>(ctx, (size_t)cap);
+        scan_scr = DBuf<unsigned char>(ctx, scan_scratch_bytes(cap + 1));
+        tri_scr = DBuf<unsigned char>(ctx, tri_kt_bytes(m, cap));
+        tri_kt_carve(tri_scr.p, m, cap, &tk);
+        expand_rows(ctx, W, row_of.p);
+        tri_kt_setup(ctx, W, row_of.p, mir.p, tc.p, eflag.p, tk, cap);
+        const TriFrontBufs fb{sup.p, eflag.p, tr.p, tc.p, oid.p, f0.p, f1.p, state.p, scan_scr.p};
+        front.reset(new TriFront(ctx, W, row_of.p, mir.p, tk, cap, fb, nullptr));
+    }
+
+    // The next C_k (owned by the caller), or nullptr after the empty one.
+    ga_csr next(int* k_out, int* iters) {
+        if (k_out) *k_out = k;
+        if (iters) *iters = 0;
+        if (finished) return nullptr;
+        ga_csr out = nullptr;
+        int it = 0;
+        if (fused) {
+            front->run(k);
+            const int64_t kept = front->compact(&it);
+            const int64_t m = W->m;
+            out = csr_alloc(ctx, m, m, kept, GA_INT32);
+            try {
+                GA_CUDA(cudaMemcpyAsync(out->rst, tr.p, sizeof(int32_t) * (size_t)(m + 1), cudaMemcpyDeviceToDevice,
+                                        ctx->stream));
+                if (kept)
+                    GA_CUDA(cudaMemcpyAsync(out->col, tc.p, sizeof(int32_t) * (size_t)kept, cudaMemcpyDeviceToDevice,
+                                            ctx->stream));
+                fill_ones(ctx, out->val, kept, GA_INT32);
+            } catch (...) {
+                csr_destroy(ctx, out);
+                throw;
+            }
+            out->unit = 1;
+            out->sym = 1;
+        } else {
+            ga_csr res = ktruss_impl(ctx, algo, cur, k, &it, nullptr);
+            csr_destroy(ctx, cur);
+            cur = res;
+            out = copy_csr(ctx, res, GA_INT32);
+            out->unit = res->unit;
+            out->sym = res->sym;
+        }
+        if (iters) *iters = it;
+        if (out->nnz == 0) finished = true;
+        ++k;
+        return out;
+    }
+};
+
 }  // namespace ga
+
+struct ga_kt_sweep_s : ga::KtSweep {};
 
 using namespace ga;
 
 extern "C" {
+
+int ga_ktruss_sweep_begin(ga_ctx ctx, ga_algo algo, ga_csr A, int kmin, ga_kt_sweep* sweep) {
+    if (!ctx || !A || !sweep) return GA_ERR_INVALID_ARG;
+    *sweep = nullptr;
+    ga_kt_sweep_s* s = nullptr;
+    GA_API_BODY(ctx, {
+        s = new ga_kt_sweep_s();
+        s->ctx = ctx;
+        try {
+            s->begin(algo, A, kmin);
+        } catch (...) {
+            delete s;
+            throw;
+        }
+        *sweep = s;
+    });
+}
+
+int ga_ktruss_sweep_next(ga_kt_sweep sweep, ga_csr* C, int* k, int* iters) {
+    if (!sweep || !C) return GA_ERR_INVALID_ARG;
+    *C = nullptr;
+    ga_ctx ctx = sweep->ctx;
+    GA_API_BODY(ctx, *C = sweep->next(k, iters));
+}
+
+int ga_ktruss_sweep_free(ga_kt_sweep sweep) {
+    if (!sweep) return GA_OK;
+    ga_ctx ctx = sweep->ctx;
+    GA_API_BODY(ctx, delete sweep);
+}
 
 int ga_tc_device(ga_ctx ctx, ga_algo algo, ga_csr A, int64_t* d_total, int64_t* d_per_row) {
     if (!ctx || !A || !d_total) return GA_ERR_INVALID_ARG;

@@ -290,6 +290,26 @@ struct TriFrontBufs {
 // (batch->iters_g) and iteration bound; the loop runs while a graph iterates.
 int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const int32_t* mir, const TriKt& t,
                     int64_t cap, const TriFrontBufs& b, const KtBatch* batch);
+// The same state kept between calls: run(k) iterates for one k (the first
+// call lists the triangles; a later call, one matrix only, takes a larger k
+// and continues from the supports the previous k left, so a sweep k = kmin,
+// kmin + 1, ... lists the triangles once); compact() writes the kept
+// entries, rows in column order, to b.tc / b.tr and returns their number and
+// the iteration count of the last run (one host synchronisation).
+class TriFront {
+public:
+    TriFront(ga_ctx ctx, ga_csr C, const int32_t* row_of, const int32_t* mir, const TriKt& t, int64_t cap,
+             const TriFrontBufs& b, const KtBatch* batch);
+    ~TriFront();
+    TriFront(const TriFront&) = delete;
+    TriFront& operator=(const TriFront&) = delete;
+    void run(int k);
+    int64_t compact(int* iters);
+
+private:
+    struct Impl;
+    Impl* impl_;
+};
 
 // Autotuned algorithm resolution: GA_AUTO becomes the cached (or freshly
 // tuned) variant, and ctx->tune its schedule; other values pass through.

@@ -40,6 +40,8 @@
 #include "ga_device.cuh"
 #include "ga_loop.cuh"
 
+#include <cstddef>
+
 namespace ga {
 
 constexpr int kTriThreads = 128;
@@ -50,17 +52,37 @@ constexpr int kTriCntMax = 1024;              // longest O_u counted in shared m
 constexpr int kTriCntWords = kTriCntMax / 4;  // byte counters, four per word
 
 // ------------------------------------------------------------------ ranks
+// Degrees repeat a lot (a power-law graph has many vertices of degree 0, 1,
+// 2, ...), so the lanes of a warp that share a degree are grouped
+// (__match_any_sync) and one of them updates the bucket for the group.
 __global__ void k_tri_deg_count(const int32_t* __restrict__ cr, int64_t m, int32_t* __restrict__ hist) {
-    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < m; v += (int64_t)gridDim.x * blockDim.x)
-        atomicAdd(hist + (cr[v + 1] - cr[v]), 1);
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); b < m; b += stride) {
+        const int64_t v = b + lane;
+        const int32_t d = v < m ? cr[v + 1] - cr[v] : -1;
+        const unsigned grp = __match_any_sync(0xffffffffu, d);
+        if (d >= 0 && lane == __ffs(grp) - 1) atomicAdd(hist + d, __popc(grp));
+    }
 }
 
 // After the scan of the degree histogram: rank = next free place of the
-// vertex's degree bucket.
+// vertex's degree bucket (a group of lanes with one degree reserves its
+// places with one atomic).
 __global__ void k_tri_rank(const int32_t* __restrict__ cr, int64_t m, int32_t* __restrict__ next,
                            int32_t* __restrict__ rank) {
-    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < m; v += (int64_t)gridDim.x * blockDim.x)
-        rank[v] = atomicAdd(next + (cr[v + 1] - cr[v]), 1);
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); b < m; b += stride) {
+        const int64_t v = b + lane;
+        const int32_t d = v < m ? cr[v + 1] - cr[v] : -1;
+        const unsigned grp = __match_any_sync(0xffffffffu, d);
+        const int leader = __ffs(grp) - 1;
+        int32_t base = 0;
+        if (d >= 0 && lane == leader) base = atomicAdd(next + d, __popc(grp));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (d >= 0) rank[v] = base + __popc(grp & ((1u << lane) - 1u));
+    }
 }
 
 __global__ void k_tri_iota(int64_t m, int32_t* __restrict__ rank) {
@@ -953,6 +975,18 @@ __global__ void k_trif_seed(TriFrontArgs a) {
     }
 }
 
+// A later k of a sweep (one matrix): the edges left by the previous k have
+// exact supports in C, so the first frontier of the new k is the live
+// records below the new k - 2 (a diagonal record: its row's length).
+__global__ void k_trif_reseed(TriFrontArgs a) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < a.nnz; q += (int64_t)gridDim.x * blockDim.x) {
+        if (a.oid[q] != (int32_t)q || a.state[q] != kAlive) continue;
+        const int32_t i = a.row_of[q];
+        const int32_t s = a.cc[q] == i ? a.deg[i] : a.sup[q];
+        if (s < kt_thr(a, i)) front_push(a.f0, &a.st->cnt[0], (int32_t)q);
+    }
+}
+
 // H, and P_0, the upper entries and the entries of C_0; one warp per row.
 __global__ void k_trif_init_counts(TriFrontArgs a) {
     const int lane = threadIdx.x & 31;
@@ -1014,11 +1048,12 @@ __global__ void __launch_bounds__(128) k_trif_lower(const TriFrontArgs* __restri
     int32_t* cn = &a.st->cnt[(t + 1) & 1];
     const int np = (t + 1) & 1;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    unsigned long long probes = 0, tris = 0;
+    unsigned long long probes = 0, tris = 0, edges = 0;
     for (int64_t x = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; x < n; x += warps) {
         const int32_t q = F[x];
         const int32_t u = a.row_of[q], v = a.cc[q];
         if (kt_frozen(a, u)) continue;
+        if (lane == 0) ++edges;
         if (u == v) {
             // a diagonal entry leaves: every other edge of its row loses 1
             for (int32_t p = a.cr[u] + lane; p < a.cr[u + 1]; p += 32) {
@@ -1073,8 +1108,9 @@ __global__ void __launch_bounds__(128) k_trif_lower(const TriFrontArgs* __restri
     }
     probes = warp_sum<unsigned long long>(probes);
     if (lane == 0) {
-        if (probes) atomicAdd(&a.ctr[GA_CTR_WEDGES], probes);
-        if (tris) atomicAdd(&a.ctr[GA_CTR_TRIANGLES], tris);
+        if (edges) atomicAdd(&a.ctr[GA_CTR_FRONT_EDGES], edges);
+        if (probes) atomicAdd(&a.ctr[GA_CTR_FRONT_PROBES], probes);
+        if (tris) atomicAdd(&a.ctr[GA_CTR_FRONT_TRIANGLES], tris);
     }
 }
 
@@ -1292,130 +1328,182 @@ __global__ void k_trif_out(TriFrontArgs a, const int32_t* __restrict__ pos, int3
 
 }  // namespace
 
-int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const int32_t* mir, const TriKt& t,
-                    int64_t cap, const TriFrontBufs& b, const KtBatch* batch) {
-    const int64_t m = C->m, nnz = C->nnz;
-    const size_t mv = (size_t)m + 1;
-    const int64_t ng = batch ? batch->ngraphs : 0;
-    DBuf<int32_t> deg(ctx, mv), upc(ctx, mv), H(ctx, mv), rd(ctx, mv), rh(ctx, mv), mark(ctx, mv), touched(ctx, mv),
-        flip(ctx, mv);
-    DBuf<uint8_t> h(ctx, mv);
-    DBuf<TriFrontState> st(ctx, 1);
-    DBuf<int32_t> cntg(ctx, batch ? (size_t)(2 * ng) : 1);
-    DBuf<long long> pg(ctx, batch ? (size_t)ng : 1);
-    GA_CUDA(cudaMemsetAsync(st.p, 0, sizeof(TriFrontState), ctx->stream));
-    if (batch) {
-        GA_CUDA(cudaMemsetAsync(cntg.p, 0, sizeof(int32_t) * (size_t)(2 * ng), ctx->stream));
-        GA_CUDA(cudaMemsetAsync(pg.p, 0, sizeof(long long) * (size_t)ng, ctx->stream));
-    }
+struct TriFront::Impl {
+    ga_ctx ctx;
+    ga_csr C;
+    TriKt t;
+    int64_t cap;
+    TriFrontBufs b;
+    const KtBatch* batch;
+    int64_t ng;
+    DBuf<int32_t> deg, upc, H, rd, rh, mark, touched, flip;
+    DBuf<uint8_t> h;
+    DBuf<TriFrontState> st;
+    DBuf<int32_t> cntg;
+    DBuf<long long> pg;
     TriFrontArgs a;
-    a.cr = C->rst;
-    a.cc = C->col;
-    a.row_of = row_of;
-    a.mir = mir;
-    a.crank = t.crank;
-    a.ocount = t.ocount;
-    a.dpos = t.dpos;
-    a.oid = b.oid;
-    a.sup = b.sup;
-    a.state = b.state;
-    a.deg = deg.p;
-    a.upc = upc.p;
-    a.h = h.p;
-    a.H = H.p;
-    a.rd = rd.p;
-    a.rh = rh.p;
-    a.mark = mark.p;
-    a.touched = touched.p;
-    a.flip = flip.p;
-    a.f0 = b.f0;
-    a.f1 = b.f1;
-    a.st = st.p;
-    a.ctr = ctx->d_counters;
-    a.m = m;
-    a.nnz = nnz;
-    a.k = k;
-    a.gid = batch ? batch->gid : nullptr;
-    a.kg = batch ? batch->kg : nullptr;
-    a.nvert = batch ? batch->nvert : nullptr;
-    a.done_g = batch ? batch->done_g : nullptr;
-    a.iters_g = batch ? batch->iters_g : nullptr;
-    a.cntg = batch ? cntg.p : nullptr;
-    a.pg = batch ? pg.p : nullptr;
-    a.ngraphs = ng;
-    const int grid_rows = grid_for(m, 256, ctx->num_sms * 8);
-    const int grid_ent = grid_for(nnz > 0 ? nnz : 1, 256, ctx->num_sms * 16);
-    {
-        // iteration 0's supports: one listing of every triangle
-        tri_kt_support(ctx, C, b.sup, t, cap);
-        ProfScope ps(ctx, "trif_seed");
-        k_trif_init_rows<<<grid_rows, 256, 0, ctx->stream>>>(a);
-        post_launch("trif_init_rows");
-        if (nnz) {
-            k_trif_seed<<<grid_ent, 256, 0, ctx->stream>>>(a);
-            post_launch("trif_seed");
-        }
-        k_trif_init_counts<<<grid_for(std::max<int64_t>(m * 32, ng), 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(a);
-        post_launch("trif_init_counts");
-    }
-    // The loop's kernels read the call's parameters from a device copy and
-    // have fixed grids, so the context captures the loop once per slot and
-    // relaunches it on later calls.
-    const int slot = batch ? kLoopSlotTriFrontBatch : kLoopSlotTriFront;
-    TriFrontArgs* dargs = static_cast<TriFrontArgs*>(cached_loop_args(ctx, slot, sizeof(TriFrontArgs)));
-    GA_CUDA(cudaMemcpyAsync(dargs, &a, sizeof(TriFrontArgs), cudaMemcpyHostToDevice, ctx->stream));
-    const int sms = ctx->num_sms;
-    auto body = [&, dargs, sms](const LoopCtl& ctl) {
-        {
-            ProfScope ps(ctx, "trif_mark");
-            k_trif_mark<<<sms * 4, 256, 0, ctx->stream>>>(dargs);
-            post_launch("trif_mark");
-        }
-        {
-            ProfScope ps(ctx, "trif_lower");
-            k_trif_lower<<<sms * 16, 128, 0, ctx->stream>>>(dargs);
-            post_launch("trif_lower");
-        }
-        {
-            ProfScope ps(ctx, "trif_apply");
-            k_trif_apply<<<sms * 4, 256, 0, ctx->stream>>>(dargs);
-            post_launch("trif_apply");
-        }
-        {
-            ProfScope ps(ctx, "trif_flip");
-            k_trif_flip<<<sms * 4, 256, 0, ctx->stream>>>(dargs);
-            post_launch("trif_flip");
-        }
-        ProfScope ps(ctx, "trif_delta");
-        k_trif_delta<<<sms * 2, 256, 0, ctx->stream>>>(dargs, ctl);
-        post_launch("trif_delta");
+    bool first = true;
+
+    Impl(ga_ctx ctx_, ga_csr C_, const int32_t* row_of, const int32_t* mir, const TriKt& t_, int64_t cap_,
+         const TriFrontBufs& b_, const KtBatch* batch_)
+        : ctx(ctx_), C(C_), t(t_), cap(cap_), b(b_), batch(batch_), ng(batch_ ? batch_->ngraphs : 0),
+          deg(ctx_, (size_t)C_->m + 1), upc(ctx_, (size_t)C_->m + 1), H(ctx_, (size_t)C_->m + 1),
+          rd(ctx_, (size_t)C_->m + 1), rh(ctx_, (size_t)C_->m + 1), mark(ctx_, (size_t)C_->m + 1),
+          touched(ctx_, (size_t)C_->m + 1), flip(ctx_, (size_t)C_->m + 1), h(ctx_, (size_t)C_->m + 1),
+          st(ctx_, 1), cntg(ctx_, batch_ ? (size_t)(2 * batch_->ngraphs) : 1),
+          pg(ctx_, batch_ ? (size_t)batch_->ngraphs : 1) {
+        GA_CUDA(cudaMemsetAsync(st.p, 0, sizeof(TriFrontState), ctx->stream));
         if (batch) {
-            k_trif_graphs<<<sms * 2, 256, 0, ctx->stream>>>(dargs, ctl);
-            post_launch("trif_graphs");
+            GA_CUDA(cudaMemsetAsync(cntg.p, 0, sizeof(int32_t) * (size_t)(2 * ng), ctx->stream));
+            GA_CUDA(cudaMemsetAsync(pg.p, 0, sizeof(long long) * (size_t)ng, ctx->stream));
         }
-    };
-    {
+        a.cr = C->rst;
+        a.cc = C->col;
+        a.row_of = row_of;
+        a.mir = mir;
+        a.crank = t.crank;
+        a.ocount = t.ocount;
+        a.dpos = t.dpos;
+        a.oid = b.oid;
+        a.sup = b.sup;
+        a.state = b.state;
+        a.deg = deg.p;
+        a.upc = upc.p;
+        a.h = h.p;
+        a.H = H.p;
+        a.rd = rd.p;
+        a.rh = rh.p;
+        a.mark = mark.p;
+        a.touched = touched.p;
+        a.flip = flip.p;
+        a.f0 = b.f0;
+        a.f1 = b.f1;
+        a.st = st.p;
+        a.ctr = ctx->d_counters;
+        a.m = C->m;
+        a.nnz = C->nnz;
+        a.k = 0;
+        a.gid = batch ? batch->gid : nullptr;
+        a.kg = batch ? batch->kg : nullptr;
+        a.nvert = batch ? batch->nvert : nullptr;
+        a.done_g = batch ? batch->done_g : nullptr;
+        a.iters_g = batch ? batch->iters_g : nullptr;
+        a.cntg = batch ? cntg.p : nullptr;
+        a.pg = batch ? pg.p : nullptr;
+        a.ngraphs = ng;
+    }
+
+    void run(int k) {
+        const int64_t m = a.m, nnz = a.nnz;
+        a.k = k;
+        const int grid_ent = grid_for(nnz > 0 ? nnz : 1, 256, ctx->num_sms * 16);
+        if (first) {
+            first = false;
+            // iteration 0's supports: one listing of every triangle
+            tri_kt_support(ctx, C, b.sup, t, cap);
+            ProfScope ps(ctx, "trif_seed");
+            k_trif_init_rows<<<grid_for(m, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(a);
+            post_launch("trif_init_rows");
+            if (nnz) {
+                k_trif_seed<<<grid_ent, 256, 0, ctx->stream>>>(a);
+                post_launch("trif_seed");
+            }
+            k_trif_init_counts<<<grid_for(std::max<int64_t>(m * 32, ng), 256, ctx->num_sms * 16), 256, 0,
+                                 ctx->stream>>>(a);
+            post_launch("trif_init_counts");
+        } else {
+            GA_REQUIRE(!batch, GA_ERR_INVALID_ARG, "a batched frontier k-truss runs one k");
+            // a new k: the loop state restarts (the running work totals stay)
+            ProfScope ps(ctx, "trif_seed");
+            GA_CUDA(cudaMemsetAsync(st.p, 0, offsetof(TriFrontState, live), ctx->stream));
+            if (nnz) {
+                k_trif_reseed<<<grid_ent, 256, 0, ctx->stream>>>(a);
+                post_launch("trif_reseed");
+            }
+        }
+        // The loop's kernels read the call's parameters from a device copy and
+        // have fixed grids, so the context captures the loop once per slot and
+        // relaunches it on later calls.
+        const int slot = batch ? kLoopSlotTriFrontBatch : kLoopSlotTriFront;
+        TriFrontArgs* dargs = static_cast<TriFrontArgs*>(cached_loop_args(ctx, slot, sizeof(TriFrontArgs)));
+        GA_CUDA(cudaMemcpyAsync(dargs, &a, sizeof(TriFrontArgs), cudaMemcpyHostToDevice, ctx->stream));
+        const int sms = ctx->num_sms;
+        const bool batched = batch != nullptr;
+        ga_ctx c = ctx;
+        auto body = [c, dargs, sms, batched](const LoopCtl& ctl) {
+            {
+                ProfScope ps(c, "trif_mark");
+                k_trif_mark<<<sms * 4, 256, 0, c->stream>>>(dargs);
+                post_launch("trif_mark");
+            }
+            {
+                ProfScope ps(c, "trif_lower");
+                k_trif_lower<<<sms * 16, 128, 0, c->stream>>>(dargs);
+                post_launch("trif_lower");
+            }
+            {
+                ProfScope ps(c, "trif_apply");
+                k_trif_apply<<<sms * 4, 256, 0, c->stream>>>(dargs);
+                post_launch("trif_apply");
+            }
+            {
+                ProfScope ps(c, "trif_flip");
+                k_trif_flip<<<sms * 4, 256, 0, c->stream>>>(dargs);
+                post_launch("trif_flip");
+            }
+            ProfScope ps(c, "trif_delta");
+            k_trif_delta<<<sms * 2, 256, 0, c->stream>>>(dargs, ctl);
+            post_launch("trif_delta");
+            if (batched) {
+                k_trif_graphs<<<sms * 2, 256, 0, c->stream>>>(dargs, ctl);
+                post_launch("trif_graphs");
+            }
+        };
         ProfScope ps(ctx, "ktruss_loop");
         run_cached_loop(ctx, slot, body, m + 1);
     }
-    // one compaction: the kept entries, rows in column order
-    ProfScope ps(ctx, "trif_compact");
-    k_trif_keep<<<grid_for(cap, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(a, cap, b.flag);
-    post_launch("trif_keep");
-    scan_exclusive_i32_scratch(ctx, b.flag, b.flag, cap, b.scan_scr);
-    k_trif_out<<<grid_for(nnz > m ? nnz : m + 1, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(a, b.flag, b.tc,
-                                                                                             b.tr);
-    post_launch("trif_out");
-    TriFrontState hs;
-    int32_t kept = 0;
-    GA_CUDA(cudaMemcpyAsync(&hs, st.p, sizeof(TriFrontState), cudaMemcpyDeviceToHost, ctx->stream));
-    GA_CUDA(cudaMemcpyAsync(&kept, b.tr + m, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+
+    int64_t compact(int* iters) {
+        const int64_t m = a.m, nnz = a.nnz;
+        ProfScope ps(ctx, "trif_compact");
+        k_trif_keep<<<grid_for(cap, 256, ctx->num_sms * 16), 256, 0, ctx->stream>>>(a, cap, b.flag);
+        post_launch("trif_keep");
+        scan_exclusive_i32_scratch(ctx, b.flag, b.flag, cap, b.scan_scr);
+        k_trif_out<<<grid_for(nnz > m ? nnz : m + 1, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(a, b.flag, b.tc,
+                                                                                                 b.tr);
+        post_launch("trif_out");
+        TriFrontState hs;
+        int32_t kept = 0;
+        GA_CUDA(cudaMemcpyAsync(&hs, st.p, sizeof(TriFrontState), cudaMemcpyDeviceToHost, ctx->stream));
+        GA_CUDA(cudaMemcpyAsync(&kept, b.tr + m, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        GA_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (iters) *iters = hs.iters;
+        return kept;
+    }
+};
+
+TriFront::TriFront(ga_ctx ctx, ga_csr C, const int32_t* row_of, const int32_t* mir, const TriKt& t, int64_t cap,
+                   const TriFrontBufs& b, const KtBatch* batch)
+    : impl_(new Impl(ctx, C, row_of, mir, t, cap, b, batch)) {}
+
+TriFront::~TriFront() { delete impl_; }
+
+void TriFront::run(int k) { impl_->run(k); }
+
+int64_t TriFront::compact(int* iters) { return impl_->compact(iters); }
+
+int tri_kt_frontier(ga_ctx ctx, ga_csr C, int k, const int32_t* row_of, const int32_t* mir, const TriKt& t,
+                    int64_t cap, const TriFrontBufs& b, const KtBatch* batch) {
+    TriFront f(ctx, C, row_of, mir, t, cap, b, batch);
+    f.run(k);
+    int iters = 0;
+    const int64_t kept = f.compact(&iters);
+    const int64_t m = C->m;
     GA_CUDA(cudaMemcpyAsync(C->rst, b.tr, sizeof(int32_t) * (size_t)(m + 1), cudaMemcpyDeviceToDevice, ctx->stream));
-    GA_CUDA(cudaStreamSynchronize(ctx->stream));
     if (kept) GA_CUDA(cudaMemcpyAsync(C->col, b.tc, sizeof(int32_t) * (size_t)kept, cudaMemcpyDeviceToDevice,
                                       ctx->stream));
     C->nnz = kept;
-    return hs.iters;
+    return iters;
 }
 
 }  // namespace ga

@@ -163,12 +163,15 @@ GA_API int ga_ctx_mem_stats(ga_ctx ctx, int64_t* in_use, int64_t* peak, int rese
  * triangle of a symmetric matrix and mirrors it), and the list entries the
  * inner-product intersections walked (DOT, and the hybrid form's
  * inner-product rows), and for GA_TRI the wedges it looked up and the
- * triangles it found. They feed the GFLOP/s (2P)
+ * triangles it found; for the frontier k-truss (GA_TRI, after its one
+ * listing) the pruned edges whose triangles it walked, the row entries it
+ * probed and the triangles it destroyed. They feed the GFLOP/s (2P)
  * and byte models. out has GA_CTR_COUNT entries; reset != 0 zeroes them
  * after reading. Synchronises the stream. */
 enum { GA_CTR_PRODUCTS = 0, GA_CTR_MASK_ENTRIES = 1, GA_CTR_LAUNCHES = 2, GA_CTR_A_ENTRIES = 3,
        GA_CTR_ROWS = 4, GA_CTR_EXECUTED = 5, GA_CTR_EXECUTED_DOT = 6, GA_CTR_WEDGES = 7,
-       GA_CTR_TRIANGLES = 8, GA_CTR_COUNT = 9 };
+       GA_CTR_TRIANGLES = 8, GA_CTR_FRONT_EDGES = 9, GA_CTR_FRONT_PROBES = 10, GA_CTR_FRONT_TRIANGLES = 11,
+       GA_CTR_COUNT = 12 };
 GA_API int ga_ctx_work_counters(ga_ctx ctx, int64_t* out, int reset);
 
 /* Kernel launches issued by this library in this process so far (counted on
@@ -387,6 +390,22 @@ GA_API int ga_tc_vertex(ga_ctx ctx, ga_algo algo, ga_csr A, int32_t* per_vertex)
  * the reference prints (0 if it did not converge within m iterations).
  * A must be int32. */
 GA_API int ga_ktruss(ga_ctx ctx, ga_algo algo, ga_csr A, int k, ga_csr* C, int* iters);
+
+/* k-truss sweep: C_k for k = kmin, kmin + 1, ... until C_k is empty, each
+ * C_k and its iteration count equal to ga_ktruss(C_{k-1}, k) (the
+ * reference's k_truss, src/main.cpp:90-146, applied to the previous
+ * result). ga_ktruss_sweep_next returns the next C_k (the caller frees it)
+ * with its k and iteration count, and *C = NULL once the empty truss has
+ * been returned. With GA_TRI (or GA_AUTO choosing it) on a symmetric matrix
+ * of unit values the k-truss state stays on the device from one k to the
+ * next: the triangles are listed once for the whole sweep and each k starts
+ * from the supports the previous k left; other cases run one ga_ktruss per
+ * k. A is copied by ga_ktruss_sweep_begin; free the sweep before its
+ * context. No counterpart in the reference (its CLI runs one k per call). */
+typedef struct ga_kt_sweep_s* ga_kt_sweep;
+GA_API int ga_ktruss_sweep_begin(ga_ctx ctx, ga_algo algo, ga_csr A, int kmin, ga_kt_sweep* sweep);
+GA_API int ga_ktruss_sweep_next(ga_kt_sweep sweep, ga_csr* C, int* k, int* iters);
+GA_API int ga_ktruss_sweep_free(ga_kt_sweep sweep);
 
 /* Batched betweenness centrality (betweenness_centrality_batch,
  * include/betweenness_centrality.h:125-237) for an explicit list of distinct

@@ -378,6 +378,66 @@ def test_ktruss_full_sweep_rmat16(ctx, algo):
     assert k > 20  # a power-law graph: a long sweep
 
 
+@pytest.mark.parametrize("algo", ["tri", "msa"])
+@pytest.mark.parametrize("device_loops", [1, 0])
+def test_ktruss_sweep_api(ctx, algo, device_loops):
+    """ga_ktruss_sweep (with triangle listing one device-resident state for
+    the whole sweep; otherwise one ga_ktruss per k) against the oracle run
+    stage by stage on R-MAT 14: every k-truss (edge set, values, iteration
+    count) equal, the same k_max, and the same Gustavson-product count as the
+    stage-by-stage ga_ktruss calls. A sweep can start at k <= 2 (nothing
+    pruned) and on a matrix without entries."""
+    ctx.set_option(ga.OPT_DEVICE_LOOPS, device_loops)
+    try:
+        m, rst, col = ga.gen_rmat(14, 16, 0.57, 0.19, 0.19, seed=5)
+        A = ga.Csr.upload(ctx, m, m, rst, col, np.ones(len(col), np.int32))
+        cur_h = csr_from_arrays(m, rst, col)
+        ctx.work_counters(reset=True)
+        got = []
+        for k, C, it in ga.ktruss_sweep(algo, A, 2):
+            r, c, v = C.download()
+            C.free()
+            got.append((k, it, r, c, v))
+        products_sweep = ctx.work_counters(reset=True)["products"]
+        ks = [g[0] for g in got]
+        assert ks == list(range(2, 2 + len(got))) and len(got) > 10
+        for k, it, r, c, v in got:
+            R, rit = oracle.ktruss(cur_h, k)
+            assert it == rit, k
+            assert np.array_equal(r, R.rst) and np.array_equal(c, R.col) and np.array_equal(v, R.val), k
+            cur_h = R
+        assert got[-1][2][-1] == 0 and all(g[2][-1] > 0 for g in got[:-1])
+        # the same work counted as the stage-by-stage calls
+        cur = A
+        for k in ks:
+            C, _ = ga.ktruss(algo, cur, k)
+            if cur is not A:
+                cur.free()
+            cur = C
+        cur.free()
+        assert ctx.work_counters(reset=True)["products"] == products_sweep
+        # diagonal entries: a diagonal entry's support is its row's length
+        rng = np.random.default_rng(4)
+        from graphs import dense_to_csr
+        U = np.triu(rng.random((80, 80)) < 0.3, 1)
+        D = U | U.T
+        D[np.arange(0, 80, 3), np.arange(0, 80, 3)] = True
+        G = dense_to_csr(D)
+        cur_h = G
+        for k, C, it in ga.ktruss_sweep(algo, to_device(ctx, G), 3):
+            R, rit = oracle.ktruss(cur_h, k)
+            r, c, _ = C.download()
+            assert it == rit and np.array_equal(r, R.rst) and np.array_equal(c, R.col), k
+            cur_h = R
+        assert cur_h.nnz == 0
+        E = ga.Csr.upload(ctx, 5, 5, np.zeros(6, np.int32), np.zeros(0, np.int32), np.zeros(0, np.int32))
+        out = [(k, C.nnz, it) for k, C, it in ga.ktruss_sweep(algo, E, 3)]
+        C0, it0 = ga.ktruss(algo, E, 3)
+        assert out == [(3, 0, it0)], out
+    finally:
+        ctx.set_option(ga.OPT_DEVICE_LOOPS, 1)
+
+
 @pytest.mark.parametrize("device_loops", [1, 0])
 def test_tri_ktruss_frontier_equals_relisting(ctx, device_loops):
     """The frontier form of the GA_TRI k-truss (one listing, then only the
