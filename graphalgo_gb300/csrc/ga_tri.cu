@@ -866,6 +866,7 @@ struct TriFrontState {
     int32_t done;
     int32_t ntouch;              // vertices whose terms of P change this iteration
     int32_t nflip;               // rows that lost their last upper entry
+    int32_t nseg;                // segments of long rows listed this iteration
     uint32_t blocks_done;        // delta kernel: blocks finished
     uint32_t blocks_done_g;      // graph kernel (batches): blocks finished
     int32_t live;                // batches: graphs still iterating
@@ -896,6 +897,9 @@ struct TriFrontArgs {
     int32_t* flip;
     int32_t* f0;
     int32_t* f1;
+    int2* seg;              // segments of long rows: (frontier slot, segment)
+    int32_t* efound;        // per frontier slot: triangles its segments found
+    int64_t segcap;
     TriFrontState* st;
     unsigned long long* ctr;
     int64_t m;
@@ -965,12 +969,20 @@ __global__ void k_trif_seed(TriFrontArgs a) {
         const bool rec = i == j || (int64_t)q - a.cr[i] < a.ocount[i];
         a.oid[q] = rec ? (int32_t)q : a.mir[q];
         a.state[q] = kAlive;
+        // one matrix: a record of the first frontier is marked at once
+        // (batches mark theirs in k_trif_mark)
         if (i == j) {
-            if (a.deg[i] < kt_thr(a, i)) front_add(a, a.f0, &a.st->cnt[0], (int32_t)q, i, 0);
+            if (a.deg[i] < kt_thr(a, i)) {
+                front_add(a, a.f0, &a.st->cnt[0], (int32_t)q, i, 0);
+                if (!a.gid) a.state[q] = kDying;
+            }
         } else if (rec) {
             const int32_t s = a.sup[q] + (a.dpos[i] >= 0) + (a.dpos[j] >= 0);
             a.sup[q] = s;
-            if (s < kt_thr(a, i)) front_add(a, a.f0, &a.st->cnt[0], (int32_t)q, i, 0);
+            if (s < kt_thr(a, i)) {
+                front_add(a, a.f0, &a.st->cnt[0], (int32_t)q, i, 0);
+                if (!a.gid) a.state[q] = kDying;
+            }
         }
     }
 }
@@ -983,7 +995,10 @@ __global__ void k_trif_reseed(TriFrontArgs a) {
         if (a.oid[q] != (int32_t)q || a.state[q] != kAlive) continue;
         const int32_t i = a.row_of[q];
         const int32_t s = a.cc[q] == i ? a.deg[i] : a.sup[q];
-        if (s < kt_thr(a, i)) front_push(a.f0, &a.st->cnt[0], (int32_t)q);
+        if (s < kt_thr(a, i)) {
+            front_push(a.f0, &a.st->cnt[0], (int32_t)q);
+            a.state[q] = kDying;
+        }
     }
 }
 
@@ -1017,8 +1032,25 @@ __global__ void k_trif_init_counts(TriFrontArgs a) {
             if (!a.done_g[g]) atomicAdd(&a.st->live, 1);
 }
 
-// Start of iteration t: the work counters of its support product, and the
-// frontier marked.
+// The reference's work for one iteration's support product C_t * C_t (its
+// Gustavson products, mask and stored entries), added to the context's
+// counters by one thread.
+__device__ __forceinline__ void trif_count_iteration(const TriFrontArgs& a) {
+    atomicAdd(&a.ctr[GA_CTR_PRODUCTS], a.st->prod);
+    atomicAdd(&a.ctr[GA_CTR_MASK_ENTRIES], a.st->mask);
+    atomicAdd(&a.ctr[GA_CTR_A_ENTRIES], a.st->ent);
+    atomicAdd(&a.ctr[GA_CTR_LAUNCHES], 1ull);
+    atomicAdd(&a.ctr[GA_CTR_ROWS], (unsigned long long)a.m);
+}
+
+// One matrix, before a k's first iteration (whose frontier the seed marked):
+// that iteration's counters. Later iterations are counted by k_trif_delta.
+__global__ void k_trif_begin(TriFrontArgs a) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) trif_count_iteration(a);
+}
+
+// Batches, start of iteration t: the work counters of its support product,
+// and the frontier marked.
 __global__ void k_trif_mark(const TriFrontArgs* __restrict__ ap) {
     const TriFrontArgs a = *ap;
     const int t = a.st->t;
@@ -1037,10 +1069,98 @@ __global__ void k_trif_mark(const TriFrontArgs* __restrict__ ap) {
     }
 }
 
+// Rows of at most this many entries are staged in shared memory (columns
+// and record positions) before the probes search them.
+constexpr int kTrifStage = 512;
+// An edge whose shorter row has more than kTrifSplit entries is walked in
+// segments of kTrifSeg entries by separate warps (k_trif_lower_seg).
+constexpr int kTrifSplit = 128;
+constexpr int kTrifSeg = 64;
+
+// A frontier edge (u, v) to walk: the shorter row x, the other row y with
+// its oriented part [yb, yo) and the rest [yo, ye), y's rank, and the
+// triangles the edge is in (its support without the diagonal terms).
+struct TrifEdge {
+    int32_t q, u, v, xb, xe, yb, yo, ye, ry;
+    int target;
+};
+
+__device__ __forceinline__ TrifEdge trif_edge(const TriFrontArgs& a, int32_t q, int32_t u, int32_t v) {
+    TrifEdge e;
+    e.q = q;
+    e.u = u;
+    e.v = v;
+    const int32_t du = a.dpos[u], dv = a.dpos[v];
+    e.target = a.sup[q] - (du >= 0 && a.state[du] != kGone) - (dv >= 0 && a.state[dv] != kGone);
+    const int32_t ub = a.cr[u], ue = a.cr[u + 1], vb = a.cr[v], ve = a.cr[v + 1];
+    const bool xu = ue - ub <= ve - vb;  // walk the shorter row
+    e.xb = xu ? ub : vb;
+    e.xe = xu ? ue : ve;
+    const int32_t y = xu ? v : u;
+    e.yb = xu ? vb : ub;
+    e.ye = xu ? ve : ue;
+    e.yo = e.yb + a.ocount[y];
+    // rank of y: the entry (u, v) holds rank(v), its mirror rank(u)
+    e.ry = xu ? a.crank[q] : a.crank[a.mir[q]];
+    return e;
+}
+
+// Entry p of row x looked up in row y (scol / soid: y's columns and record
+// positions indexed from yb); loads only, so that a lane's lookups of
+// several entries overlap. A hit is the triangle (u, v, w): f and g are the
+// records of its other two edges (u or v, w) and (y, w), with their states.
+struct TrifHit {
+    int32_t f, g;
+    uint8_t sf, sg;
+    bool hit;
+};
+
+__device__ __forceinline__ TrifHit trif_find(const TriFrontArgs& a, const TrifEdge& e, int32_t p, const int32_t* scol,
+                                             const int32_t* soid) {
+    TrifHit h;
+    h.hit = false;
+    h.f = h.g = 0;
+    h.sf = h.sg = kGone;
+    const int32_t w = a.cc[p];
+    if (w == e.u || w == e.v) return h;
+    h.f = a.oid[p];
+    h.sf = a.state[h.f];
+    if (h.sf == kGone) return h;
+    // w ranked above y: (y, w) is in y's oriented part
+    const bool above = a.crank[p] > e.ry;
+    const int32_t sb = above ? 0 : e.yo - e.yb, se = above ? e.yo - e.yb : e.ye - e.yb;
+    const int32_t r = sb + lower_bound_i32(scol + sb, se - sb, w);
+    if (r >= se || scol[r] != w) return h;
+    h.g = soid[r];
+    h.sg = a.state[h.g];
+    h.hit = h.sg != kGone;
+    return h;
+}
+
+// A hit lowers the supports of the triangle's other two edges, each once
+// (the frontier edge with the smallest record position owns a triangle with
+// two frontier edges).
+__device__ __forceinline__ void trif_apply_hit(const TriFrontArgs& a, const TrifEdge& e, const TrifHit& h, int32_t* fn,
+                                               int32_t* cn, int np) {
+    if (!h.hit) return;
+    if (h.sf == kAlive && (h.sg == kAlive || e.q < h.g)) lower_support(a, h.f, fn, cn, np);
+    if (h.sg == kAlive && (h.sf == kAlive || e.q < h.f)) lower_support(a, h.g, fn, cn, np);
+}
+
 // One warp per frontier edge: its triangles in C_t, the supports they lower.
-__global__ void __launch_bounds__(128) k_trif_lower(const TriFrontArgs* __restrict__ ap) {
+// The warp walks the shorter row x of the edge and looks each entry up in
+// the other row y: in y's part that the entry's rank selects, binary-searched
+// in shared memory when y has at most kTrifStage entries (its columns and
+// record positions copied there first, coalesced), else in global memory.
+// A row x longer than kTrifSplit is listed as segments for
+// k_trif_lower_seg instead (while the segment list has room).
+__global__ void __launch_bounds__(128, 8) k_trif_lower(const TriFrontArgs* __restrict__ ap) {
+    __shared__ int32_t s_col[4][kTrifStage];
+    __shared__ int32_t s_oid[4][kTrifStage];
     const TriFrontArgs a = *ap;
     const int lane = threadIdx.x & 31;
+    int32_t* ycol = s_col[threadIdx.x >> 5];
+    int32_t* yoid = s_oid[threadIdx.x >> 5];
     const int t = a.st->t;
     const int32_t n = a.st->cnt[t & 1];
     const int32_t* F = (t & 1) ? a.f1 : a.f0;
@@ -1063,52 +1183,106 @@ __global__ void __launch_bounds__(128) k_trif_lower(const TriFrontArgs* __restri
             }
             continue;
         }
-        const int32_t du = a.dpos[u], dv = a.dpos[v];
-        const int target = a.sup[q] - (du >= 0 && a.state[du] != kGone) - (dv >= 0 && a.state[dv] != kGone);
-        if (target <= 0) continue;
-        const int32_t ub = a.cr[u], ue = a.cr[u + 1], vb = a.cr[v], ve = a.cr[v + 1];
-        const bool xu = ue - ub <= ve - vb;  // walk the shorter row
-        const int32_t xb = xu ? ub : vb, xe = xu ? ue : ve;
-        const int32_t y = xu ? v : u;
-        const int32_t yb = xu ? vb : ub, ye = xu ? ve : ue, yo = yb + a.ocount[y];
-        // rank of y: the entry (u, v) holds rank(v), its mirror rank(u)
-        const int32_t ry = xu ? a.crank[q] : a.crank[a.mir[q]];
-        int found = 0;
-        for (int32_t base = xb; base < xe; base += 32) {
-            const int32_t p = base + lane;
-            bool hit = false;
-            if (p < xe) {
-                ++probes;
-                const int32_t w = a.cc[p];
-                if (w != u && w != v) {
-                    const int32_t f = a.oid[p];
-                    const uint8_t sf = a.state[f];
-                    if (sf != kGone) {
-                        // w ranked above y: (y, w) is in y's oriented part
-                        const bool above = a.crank[p] > ry;
-                        const int32_t sb = above ? yb : yo, se = above ? yo : ye;
-                        const int32_t r = sb + lower_bound_i32(a.cc + sb, se - sb, w);
-                        if (r < se && a.cc[r] == w) {
-                            const int32_t g = a.oid[r];
-                            const uint8_t sg = a.state[g];
-                            if (sg != kGone) {
-                                hit = true;
-                                if (sf == kAlive && (sg == kAlive || q < g)) lower_support(a, f, fn, cn, np);
-                                if (sg == kAlive && (sf == kAlive || q < f)) lower_support(a, g, fn, cn, np);
-                            }
-                        }
-                    }
-                }
+        const TrifEdge e = trif_edge(a, q, u, v);
+        if (e.target <= 0) continue;
+        if (e.xe - e.xb > kTrifSplit) {
+            // segments for k_trif_lower_seg: (frontier slot, segment)
+            const int nseg = (e.xe - e.xb + kTrifSeg - 1) / kTrifSeg;
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&a.st->nseg, nseg);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if ((int64_t)base + nseg <= a.segcap) {
+                if (lane == 0) a.efound[x] = 0;
+                for (int j = lane; j < nseg; j += 32) a.seg[base + j] = make_int2((int32_t)x, j);
+                continue;
             }
-            const int hcount = __popc(__ballot_sync(0xffffffffu, hit));
+            // no room: holes in the list are marked, the warp walks the row
+            for (int64_t j = base + lane; j < a.segcap && j < (int64_t)base + nseg; j += 32)
+                a.seg[j] = make_int2(-1, 0);
+        }
+        const bool staged = e.ye - e.yb <= kTrifStage;
+        if (staged) {
+            __syncwarp();  // the previous edge's lookups are done
+            for (int32_t i = lane; i < e.ye - e.yb; i += 32) {
+                ycol[i] = a.cc[e.yb + i];
+                yoid[i] = a.oid[e.yb + i];
+            }
+            __syncwarp();
+        }
+        const int32_t* scol = staged ? ycol : a.cc + e.yb;
+        const int32_t* soid = staged ? yoid : a.oid + e.yb;
+        // 32 entries per pass, stopping once the edge's triangles are found
+        // (two entries per lane per pass were slower: the later stop wastes
+        // more lookups than the overlap gains)
+        int found = 0;
+        for (int32_t base = e.xb; base < e.xe; base += 32) {
+            const int32_t p = base + lane;
+            TrifHit h;
+            h.hit = false;
+            if (p < e.xe) {
+                ++probes;
+                h = trif_find(a, e, p, scol, soid);
+                trif_apply_hit(a, e, h, fn, cn, np);
+            }
+            const int hcount = __popc(__ballot_sync(0xffffffffu, h.hit));
             found += hcount;
             if (lane == 0) tris += (unsigned long long)hcount;
-            if (found >= target) break;
+            if (found >= e.target) break;
         }
     }
     probes = warp_sum<unsigned long long>(probes);
     if (lane == 0) {
         if (edges) atomicAdd(&a.ctr[GA_CTR_FRONT_EDGES], edges);
+        if (probes) atomicAdd(&a.ctr[GA_CTR_FRONT_PROBES], probes);
+        if (tris) atomicAdd(&a.ctr[GA_CTR_FRONT_TRIANGLES], tris);
+    }
+}
+
+// The segments k_trif_lower listed, one warp each: kTrifSeg entries of a
+// long row x looked up in y in global memory. The edge's triangles found so
+// far are counted in efound (per frontier slot); a segment stops once they
+// reach the edge's total.
+__global__ void __launch_bounds__(128, 8) k_trif_lower_seg(const TriFrontArgs* __restrict__ ap) {
+    const TriFrontArgs a = *ap;
+    const int lane = threadIdx.x & 31;
+    const int t = a.st->t;
+    const int32_t* F = (t & 1) ? a.f1 : a.f0;
+    int32_t* fn = (t & 1) ? a.f0 : a.f1;
+    int32_t* cn = &a.st->cnt[(t + 1) & 1];
+    const int np = (t + 1) & 1;
+    const int64_t ns = min((int64_t)a.st->nseg, a.segcap);
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    unsigned long long probes = 0, tris = 0;
+    for (int64_t sx = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; sx < ns; sx += warps) {
+        const int2 sg = a.seg[sx];
+        if (sg.x < 0) continue;
+        const int32_t q = F[sg.x];
+        const TrifEdge e = trif_edge(a, q, a.row_of[q], a.cc[q]);
+        if (*(volatile int32_t*)(a.efound + sg.x) >= e.target) continue;
+        const int32_t s0 = e.xb + sg.y * kTrifSeg, s1 = min(e.xe, s0 + kTrifSeg);
+        const int32_t* scol = a.cc + e.yb;
+        const int32_t* soid = a.oid + e.yb;
+        for (int32_t base = s0; base < s1; base += 32) {
+            const int32_t p = base + lane;
+            TrifHit h;
+            h.hit = false;
+            if (p < s1) {
+                ++probes;
+                h = trif_find(a, e, p, scol, soid);
+                trif_apply_hit(a, e, h, fn, cn, np);
+            }
+            const int hcount = __popc(__ballot_sync(0xffffffffu, h.hit));
+            int before = 0;
+            if (lane == 0) {
+                tris += (unsigned long long)hcount;
+                before = hcount ? atomicAdd(a.efound + sg.x, hcount) : *(volatile int32_t*)(a.efound + sg.x);
+            }
+            before = __shfl_sync(0xffffffffu, before, 0);
+            if (before + hcount >= e.target) break;
+        }
+    }
+    probes = warp_sum<unsigned long long>(probes);
+    if (lane == 0) {
         if (probes) atomicAdd(&a.ctr[GA_CTR_FRONT_PROBES], probes);
         if (tris) atomicAdd(&a.ctr[GA_CTR_FRONT_TRIANGLES], tris);
     }
@@ -1199,6 +1373,15 @@ __global__ void __launch_bounds__(256) k_trif_delta(const TriFrontArgs* __restri
     __shared__ long long part[8];
     __shared__ bool last;
     const int32_t n = a.st->ntouch;
+    if (!a.gid) {
+        // one matrix: the next frontier is complete, so its edges are marked
+        // here instead of by a marking kernel at the next iteration's start
+        const int t = a.st->t;
+        const int32_t nn = a.st->cnt[(t + 1) & 1];
+        const int32_t* Fn = (t & 1) ? a.f0 : a.f1;
+        for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < nn; x += (int64_t)gridDim.x * blockDim.x)
+            a.state[Fn[x]] = kDying;
+    }
     long long d = 0;
     for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
         const int32_t j = a.touched[x];
@@ -1228,6 +1411,7 @@ __global__ void __launch_bounds__(256) k_trif_delta(const TriFrontArgs* __restri
     st->blocks_done = 0;
     st->ntouch = 0;
     st->nflip = 0;
+    st->nseg = 0;
     if (a.gid) return;
     const int t = st->t;
     if (st->cnt[t & 1] == 0) {
@@ -1241,6 +1425,7 @@ __global__ void __launch_bounds__(256) k_trif_delta(const TriFrontArgs* __restri
             st->done = 1;
         }
     }
+    if (!st->done) trif_count_iteration(a);
     loop_continue(ctl, st->done == 0);
 }
 
@@ -1341,6 +1526,8 @@ struct TriFront::Impl {
     DBuf<TriFrontState> st;
     DBuf<int32_t> cntg;
     DBuf<long long> pg;
+    DBuf<int2> seg;
+    DBuf<int32_t> efound;
     TriFrontArgs a;
     bool first = true;
 
@@ -1351,7 +1538,8 @@ struct TriFront::Impl {
           rd(ctx_, (size_t)C_->m + 1), rh(ctx_, (size_t)C_->m + 1), mark(ctx_, (size_t)C_->m + 1),
           touched(ctx_, (size_t)C_->m + 1), flip(ctx_, (size_t)C_->m + 1), h(ctx_, (size_t)C_->m + 1),
           st(ctx_, 1), cntg(ctx_, batch_ ? (size_t)(2 * batch_->ngraphs) : 1),
-          pg(ctx_, batch_ ? (size_t)batch_->ngraphs : 1) {
+          pg(ctx_, batch_ ? (size_t)batch_->ngraphs : 1),
+          seg(ctx_, (size_t)std::max<int64_t>(cap_ / 8, 4096)), efound(ctx_, (size_t)cap_) {
         GA_CUDA(cudaMemsetAsync(st.p, 0, sizeof(TriFrontState), ctx->stream));
         if (batch) {
             GA_CUDA(cudaMemsetAsync(cntg.p, 0, sizeof(int32_t) * (size_t)(2 * ng), ctx->stream));
@@ -1378,6 +1566,9 @@ struct TriFront::Impl {
         a.flip = flip.p;
         a.f0 = b.f0;
         a.f1 = b.f1;
+        a.seg = seg.p;
+        a.efound = efound.p;
+        a.segcap = (int64_t)seg.count;
         a.st = st.p;
         a.ctr = ctx->d_counters;
         a.m = C->m;
@@ -1421,6 +1612,10 @@ struct TriFront::Impl {
                 post_launch("trif_reseed");
             }
         }
+        if (!batch) {
+            k_trif_begin<<<1, 32, 0, ctx->stream>>>(a);
+            post_launch("trif_begin");
+        }
         // The loop's kernels read the call's parameters from a device copy and
         // have fixed grids, so the context captures the loop once per slot and
         // relaunches it on later calls.
@@ -1431,7 +1626,7 @@ struct TriFront::Impl {
         const bool batched = batch != nullptr;
         ga_ctx c = ctx;
         auto body = [c, dargs, sms, batched](const LoopCtl& ctl) {
-            {
+            if (batched) {
                 ProfScope ps(c, "trif_mark");
                 k_trif_mark<<<sms * 4, 256, 0, c->stream>>>(dargs);
                 post_launch("trif_mark");
@@ -1440,6 +1635,8 @@ struct TriFront::Impl {
                 ProfScope ps(c, "trif_lower");
                 k_trif_lower<<<sms * 16, 128, 0, c->stream>>>(dargs);
                 post_launch("trif_lower");
+                k_trif_lower_seg<<<sms * 16, 128, 0, c->stream>>>(dargs);
+                post_launch("trif_lower_seg");
             }
             {
                 ProfScope ps(c, "trif_apply");
