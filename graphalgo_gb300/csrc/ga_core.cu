@@ -101,6 +101,7 @@ ga_csr csr_alloc(ga_ctx ctx, int64_t m, int64_t n, int64_t nnz, ga_dtype dt) {
 
 void csr_destroy(ga_ctx ctx, ga_csr A) {
     if (!A) return;
+    if (A->copied) cudaEventDestroy(A->copied);
     dfree(ctx, A->rst);
     dfree(ctx, A->col);
     dfree(ctx, A->val);
@@ -568,9 +569,9 @@ int ga_csr_free(ga_ctx ctx, ga_csr A) {
     if (!ctx) return GA_ERR_INVALID_ARG;
     if (!A) return GA_OK;
     GA_API_BODY(ctx, {
-        // a download still in flight on the copy stream finishes before the
-        // stream-ordered free
-        if (ctx->copy_stream) GA_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->copy_done, 0));
+        // a download of this handle still in flight on the copy stream
+        // finishes before the stream-ordered free
+        if (A->copied) GA_CUDA(cudaStreamWaitEvent(ctx->stream, A->copied, 0));
         csr_destroy(ctx, A);
     });
 }
@@ -594,6 +595,8 @@ int ga_csr_download_async(ga_ctx ctx, ga_csr A, int32_t* rst, int32_t* col, void
             GA_CUDA(cudaMemcpyAsync(val, A->val, dtype_size(A->dtype) * A->nnz, cudaMemcpyDeviceToHost,
                                     ctx->copy_stream));
         GA_CUDA(cudaEventRecord(ctx->copy_done, ctx->copy_stream));
+        if (!A->copied) GA_CUDA(cudaEventCreateWithFlags(&A->copied, cudaEventDisableTiming));
+        GA_CUDA(cudaEventRecord(A->copied, ctx->copy_stream));
     });
 }
 

@@ -113,6 +113,7 @@ struct ga_csr_s {
     size_t cap = 0;  // allocated entries of col/val
     int unit = -1;   // all values equal 1: -1 unknown, 0 no, 1 yes
     int sym = -1;    // pattern and values symmetric: -1 unknown, 0 no, 1 yes
+    cudaEvent_t copied = nullptr;  // the handle's last download on the copy stream
 };
 
 struct ga_dense_s {
