@@ -69,9 +69,12 @@ GOLDEN_SWEEP = os.path.join(ROOT, "tests", "golden", "rmat18_sweep.json")
 # launch of the sweep works on operands that fit in L2, so its DRAM traffic
 # is the compulsory traffic of its operands, proportional to its entries.
 DRAM_BYTES_PER_ENTRY = {"tri_support": 7.506, "mxm": 4.543}
-# DRAM bytes per pruned edge of the frontier k-truss kernel k_trif_lower,
-# from its ncu capture (None until one exists: no traffic figure).
-DRAM_BYTES_PER_FRONT_EDGE = None
+# DRAM bytes per pruned edge of the frontier pruning kernels (k_trif_lower +
+# k_trif_lower_seg): dram__bytes_read.sum + dram__bytes_write.sum summed over
+# every launch of one R-MAT 18 sweep (ncu with --cache-control none, so the
+# caches stay warm as in the timed step: 2,983.7 MB) over its 3,805,777
+# pruned edges (profiles/trif_lower_rmat18_sweep.md).
+DRAM_BYTES_PER_FRONT_EDGE = 784.0
 
 
 def parse_args():
@@ -103,6 +106,9 @@ def parse_args():
                          "graphs")
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--sources", type=int, default=64)
+    ap.add_argument("--bc-backward", type=int, default=None, choices=[0, 1, 2],
+                    help="BC case: how the backward sweep reads W rows (GA_OPT_BC_BACKWARD: 0 gathers, "
+                         "1 bulk copies, 2 one neighbour at a time)")
     ap.add_argument("--ingest-scale", type=int, default=20, help="ingest workload: R-MAT scale of the file")
     ap.add_argument("--workload", choices=["ktruss-sweep", "batch", "serve", "ingest"], default="ktruss-sweep",
                     help="ktruss-sweep: the R-MAT k-truss sweep; batch: TC + 4-truss of many k-NN graphs; "
@@ -256,6 +262,8 @@ def run_case(args):
     ctx.set_option(ga.OPT_DEVICE_LOOPS, 0 if args.host_loops else 1)
     if args.hybrid_ratio is not None:
         ctx.set_option(ga.OPT_HYBRID_RATIO, args.hybrid_ratio)
+    if args.bc_backward is not None:
+        ctx.set_option(ga.OPT_BC_BACKWARD, args.bc_backward)
     if args.case == "batch":
         n, dim = knn_batch_sizes(args.graphs, args.seed)
         U, voff = ga.gen_knn_batch(ctx, n, dim, k=30, seed=args.seed)
@@ -273,6 +281,7 @@ def run_case(args):
         return
     m, rst, col = ga.gen_rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, args.seed)
     A = ga.Csr.upload(ctx, m, m, rst, col, np.ones(len(col), np.int32))
+    A.set_symmetric(1)  # symmetrised by construction
     rng = np.random.default_rng(args.seed)
     src = rng.choice(m, min(args.sources, m), replace=False).astype(np.int32)
     for _ in range(args.reps):
@@ -605,10 +614,9 @@ def run_gpu(args, dist: Dist):
     # k-truss it downloads is then checked against the oracle's record
     rst_h = np.ascontiguousarray(rst, np.int32)
     col_h = np.ascontiguousarray(col, np.int32)
-    val_h = np.ascontiguousarray(val, np.int32)
     res_rst = np.empty((len(shape), m + 1), np.int32)
     res_col = np.empty(sum(s[2] for s in shape) + 1, np.int32)
-    pinned = [rst_h, col_h, val_h, res_rst, res_col]
+    pinned = [rst_h, col_h, res_rst, res_col]
     for a in pinned:
         ga.host_register(a)
     e2e, got_shape = None, None
@@ -638,7 +646,9 @@ def run_gpu(args, dist: Dist):
             ctx.flush_l2()
             d2h = 0
             ctx.timer_start()
-            Ad = ga.Csr.upload(ctx, m, m, rst_h, col_h, val_h)
+            # the pattern only: an adjacency matrix's values are all 1 (the
+            # reference CLI's build_adjacency_matrix), set on the device
+            Ad = ga.Csr.upload(ctx, m, m, rst_h, col_h)
             Ad.set_symmetric(1)  # symmetrised by construction, as the reference CLI's graphs are
             got_shape = sweep(ga, ctx, Ad, args.algo, args.kmin, sink=sink_factory())
             Ad.free()
@@ -648,10 +658,11 @@ def run_gpu(args, dist: Dist):
         if not args.no_e2e:
             e2e_t = dist.max(sum(e2e_ms))
             e2e = {"value": dist.sum(2.0 * wce["products"]) / (e2e_t * 1e-3) / 1e9, "unit": UNIT,
-                   "h2d_bytes_per_step": int(rst_h.nbytes + col_h.nbytes + val_h.nbytes),
+                   "h2d_bytes_per_step": int(rst_h.nbytes + col_h.nbytes),
                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t / args.steps,
-                   "note": "per step: upload of A from pinned host memory (validated on the device, declared "
-                           "symmetric with ga_csr_set_symmetric), the sweep, every k-truss downloaded"}
+                   "note": "per step: upload of A's pattern from pinned host memory (values all 1, set on the "
+                           "device; validated on the device, declared symmetric with ga_csr_set_symmetric), "
+                           "the sweep, every k-truss downloaded"}
         # digests of every downloaded k-truss
         digests, off = [], 0
         for i, (k, it, z) in enumerate(got_shape):
@@ -848,10 +859,9 @@ def batch_record(ga, ctx, args, dist: Dist, steps: int = 3, warmup: int = 1, wit
     # ---------------------------------------------------------- e2e
     rst_h = np.ascontiguousarray(rst)
     col_h = np.ascontiguousarray(col)
-    val_h = np.ones(len(col), np.int32)
     out_rst = np.empty(len(rst), np.int32)
     out_col = np.empty(len(col) + 1, np.int32)
-    pinned = [rst_h, col_h, val_h, out_rst, out_col]
+    pinned = [rst_h, col_h, out_rst, out_col]
     for a in pinned:
         ga.host_register(a)
     try:
@@ -862,7 +872,8 @@ def batch_record(ga, ctx, args, dist: Dist, steps: int = 3, warmup: int = 1, wit
             ctx.flush_l2()
             ctx.timer_start()
             t0 = time.perf_counter()
-            Ud = ga.Csr.upload(ctx, len(rst) - 1, len(rst) - 1, rst_h, col_h, val_h)
+            Ud = ga.Csr.upload(ctx, len(rst) - 1, len(rst) - 1, rst_h, col_h)  # values all 1, set on the device
+            Ud.set_symmetric(1)  # k-NN graphs symmetrised by union
             t1 = time.perf_counter()
             tcs = ga.batch_tc(tc_arg, Ud, voff)
             t2 = time.perf_counter()
@@ -881,7 +892,7 @@ def batch_record(ga, ctx, args, dist: Dist, steps: int = 3, warmup: int = 1, wit
             same = same and bool(np.array_equal(tcs, ref[0]) and np.array_equal(iters, ref[1]) and z == ref[2])
         e2e_t = dist.max(sum(e2e_ms))
         e2e = {"value": dist.sum(G * steps) / (e2e_t * 1e-3), "unit": "graphs/s",
-               "h2d_bytes_per_step": int(rst_h.nbytes + col_h.nbytes + val_h.nbytes + voff.nbytes),
+               "h2d_bytes_per_step": int(rst_h.nbytes + col_h.nbytes + voff.nbytes),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_t / steps,
                "host_phases_ms": {k: round(v, 2) for k, v in phases.items()}}
     finally:

@@ -43,8 +43,9 @@ struct BcState {
     int32_t depth;    // number of non-empty levels (forward result)
     int32_t k;        // backward level
     int32_t done;
-    int32_t entries;  // entries appended so far (store size)
-    int32_t rows;     // frontier rows appended so far
+    // entries appended so far (store size, low 32 bits) and frontier rows
+    // appended so far (high 32 bits): one atomic reserves both
+    unsigned long long er;
     int32_t overflow;
     int32_t mode;          // forward direction of the current level: 0 pull, 1 push
     int32_t ntouched;      // vertices reached by the current push level
@@ -105,7 +106,7 @@ __global__ void k_bc_init(BcArgs p) {
 
 __global__ void k_bc_state_init(BcArgs p) {
     p.st->d = 0; p.st->depth = 0; p.st->k = 0; p.st->done = 0;
-    p.st->entries = p.nsrc; p.st->rows = 0; p.st->overflow = 0;
+    p.st->er = (unsigned long long)p.nsrc; p.st->overflow = 0;
     p.st->mode = 0; p.st->ntouched = 0; p.st->stalled = 0; p.st->nhrows = 0;
     p.st->cur_work = 0; p.st->next_work = 0;
     p.level_rows[0] = 0;
@@ -204,9 +205,11 @@ __device__ __forceinline__ void bc_pull_group(const BcArgs& p, const int32_t* cu
 }
 
 // Appends v's new frontier row (its touched sources, in source order) by one
-// warp; resets acc/touched.
+// warp; resets acc/touched. Lane 0 adds the row's next-level work (entries x
+// out-degree) to `work`, which the caller adds to the level total once.
 __device__ __forceinline__ void bc_emit_row(const BcArgs& p, int64_t v, int32_t* nxtS, int32_t* nxtL,
-                                            const uint32_t* vis, double* acc, uint32_t* touched) {
+                                            const uint32_t* vis, double* acc, uint32_t* touched,
+                                            unsigned long long& work) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const uint32_t word = lane < p.words ? touched[lane] : 0u;
@@ -219,15 +222,16 @@ __device__ __forceinline__ void bc_emit_row(const BcArgs& p, int64_t v, int32_t*
     }
     int start = 0;
     if (lane == 0) {
-        start = atomicAdd(&p.st->entries, count);
-        const int r = atomicAdd(&p.st->rows, 1);
+        const unsigned long long old = atomicAdd(&p.st->er, (1ull << 32) | (unsigned long long)count);
+        start = (int)(old & 0xffffffffull);
+        const int r = (int)(old >> 32);
         if ((int64_t)start + count > p.cap_entries || (int64_t)r >= p.cap_rows) {
             atomicExch(&p.st->overflow, 1);
             start = -1;
         } else {
             p.rv[r] = (int32_t)v; p.rs[r] = start; p.rl[r] = count;
             p.vcnt[v] += count;
-            atomicAdd(&p.st->next_work, (unsigned long long)count * (unsigned long long)(p.ar[v + 1] - p.ar[v]));
+            work += (unsigned long long)count * (unsigned long long)(p.ar[v + 1] - p.ar[v]);
         }
         nxtS[v] = start;
         nxtL[v] = start < 0 ? 0 : count;
@@ -279,6 +283,7 @@ __global__ void __launch_bounds__(kBcThreads) k_bc_forward(BcArgs p) {
     region(0, acc0, touched0, vis0, i0, o0, a0);
 
     if (p.st->done || p.st->mode != 0) return;
+    unsigned long long work = 0;  // lane 0: next-level work of the rows this warp emits
     const int d = p.st->d;
     const int par = d & 1;
     const int32_t* curS = p.cur_start[par];
@@ -301,7 +306,7 @@ __global__ void __launch_bounds__(kBcThreads) k_bc_forward(BcArgs p) {
             for (int32_t g = ab + wid * 32; g < ae; g += kBcWarps * 32)
                 bc_pull_group<UNIT>(p, curS, curL, g, ae, vis0, acc0, touched0, s_incl, s_off, s_a);
             __syncthreads();
-            if (wid == 0) bc_emit_row(p, v, nxtS, nxtL, vis0, acc0, touched0);
+            if (wid == 0) bc_emit_row(p, v, nxtS, nxtL, vis0, acc0, touched0, work);
         } else if (threadIdx.x == 0) {
             nxtL[v] = 0;
         }
@@ -337,9 +342,10 @@ __global__ void __launch_bounds__(kBcThreads) k_bc_forward(BcArgs p) {
             __syncwarp();
             for (int32_t g = ab; g < ae; g += 32)
                 bc_pull_group<UNIT>(p, curS, curL, g, ae, vis, acc, touched, s_incl, s_off, s_a);
-            bc_emit_row(p, v, nxtS, nxtL, vis, acc, touched);
+            bc_emit_row(p, v, nxtS, nxtL, vis, acc, touched, work);
         }
     }
+    if (lane == 0 && work) atomicAdd(&p.st->next_work, work);
 }
 
 // Push level, one frontier row (vertex u, entries [e0, e0+len)) and the
@@ -425,12 +431,14 @@ __global__ void __launch_bounds__(kBcThreads) k_bc_push_emit(BcArgs p) {
     int32_t* nxtL = p.cur_len[par ^ 1];
     const int n = st->ntouched;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    unsigned long long work = 0;  // lane 0: next-level work of the rows this warp emits
     for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
         const int32_t w = p.tlist[i];
         bc_emit_row(p, w, nxtS, nxtL, p.vbits + (size_t)w * p.words, p.W + (size_t)w * p.ns,
-                    p.tbits + (size_t)w * p.words);
+                    p.tbits + (size_t)w * p.words, work);
         if (lane == 0) p.tmark[w] = 0;
     }
+    if (lane == 0 && work) atomicAdd(&p.st->next_work, work);
 }
 
 __global__ void k_bc_forward_finalize(BcArgs p, LoopCtl ctl) {
@@ -439,11 +447,12 @@ __global__ void k_bc_forward_finalize(BcArgs p, LoopCtl ctl) {
     bool more = false;
     if (!st->done) {
         const int d = st->d;
-        if (st->overflow || st->rows == p.level_rows[d]) {
+        const int32_t rows = (int32_t)(st->er >> 32);
+        if (st->overflow || rows == p.level_rows[d]) {
             st->depth = d;
             st->done = 1;
         } else {
-            p.level_rows[d + 1] = st->rows;
+            p.level_rows[d + 1] = rows;
             st->d = d + 1;
             if ((int64_t)st->d > p.m) { st->depth = st->d; st->done = 1; }
             else more = true;

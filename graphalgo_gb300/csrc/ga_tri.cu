@@ -1306,22 +1306,21 @@ __global__ void k_trif_apply(const TriFrontArgs* __restrict__ ap) {
         if (kt_frozen(a, u)) continue;
         a.state[q] = kGone;
         ++mask;
+        // deg and H keep their values from the iteration's start; the losses
+        // are counted in rd and rh and applied by k_trif_delta
         if (u == v) {
             ++ent;
-            atomicSub(a.deg + u, 1);
             atomicAdd(a.rd + u, 1);
-            atomicSub(a.H + u, 1);  // h(u) = 1 while its diagonal entry is there
-            atomicAdd(a.rh + u, 1);
+            atomicAdd(a.rh + u, 1);  // h(u) = 1 while its diagonal entry is there
             touch(a, u);
             if (atomicSub(a.upc + u, 1) == 1) front_push(a.flip, &a.st->nflip, u);
             continue;
         }
         ent += 2;
-        const int32_t ou = atomicSub(a.deg + u, 1), ov = atomicSub(a.deg + v, 1);
-        atomicAdd(a.rd + u, 1);
-        atomicAdd(a.rd + v, 1);
-        if (a.h[u]) { atomicSub(a.H + v, 1); atomicAdd(a.rh + v, 1); }
-        if (a.h[v]) { atomicSub(a.H + u, 1); atomicAdd(a.rh + u, 1); }
+        // the row lengths before this entry left
+        const int32_t ou = a.deg[u] - atomicAdd(a.rd + u, 1), ov = a.deg[v] - atomicAdd(a.rd + v, 1);
+        if (a.h[u]) atomicAdd(a.rh + v, 1);
+        if (a.h[v]) atomicAdd(a.rh + u, 1);
         touch(a, u);
         touch(a, v);
         const int32_t lo = min(u, v);
@@ -1357,7 +1356,6 @@ __global__ void k_trif_flip(const TriFrontArgs* __restrict__ ap) {
         for (int32_t p = a.cr[i] + lane; p < a.cr[i + 1]; p += 32) {
             if (a.state[a.oid[p]] == kGone) continue;
             const int32_t j = a.cc[p];
-            atomicSub(a.H + j, 1);
             atomicAdd(a.rh + j, 1);
             touch(a, j);
         }
@@ -1385,11 +1383,13 @@ __global__ void __launch_bounds__(256) k_trif_delta(const TriFrontArgs* __restri
     long long d = 0;
     for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
         const int32_t j = a.touched[x];
-        const long long nd = a.deg[j], nh = a.H[j];
-        const long long od = nd + a.rd[j], oh = nh + a.rh[j];
+        const long long od = a.deg[j], oh = a.H[j];
+        const long long nd = od - a.rd[j], nh = oh - a.rh[j];
         const long long dj = nd * nh - od * oh;
         d += dj;
         if (a.gid && dj) atomicAdd(reinterpret_cast<unsigned long long*>(a.pg + a.gid[j]), (unsigned long long)dj);
+        a.deg[j] = (int32_t)nd;
+        a.H[j] = (int32_t)nh;
         a.rd[j] = 0;
         a.rh[j] = 0;
         a.mark[j] = 0;
