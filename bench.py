@@ -548,6 +548,34 @@ def other_configs(ga, ctx, args, with_cpu: bool):
                                  "cores": os.cpu_count() or 1, "kind": "port",
                                  "sample": f"the same call ({ns} sources, FP64) by the oracle port, {tc:.2f} s"}
         out[f"bc_rmat20_{ns}src"] = r
+    # the masked product itself on the same graph (31.4M entries: operands
+    # larger than L2), C<A> = A*A with int32 values, default schedule, per
+    # Gustavson variant against the survey's byte model 8(m+1) + 16 nnz(A) +
+    # 8 P + 4 nnz(M) + 4 nnz(C); triangle listing (which performs no
+    # Gustavson products) by time only
+    nnz = len(col)
+    mx = {}
+    for algo in ("msa", "hybrid", "mca", "tri"):
+        ga.mxm_masked(algo, A, A, A).free()
+        best, prods = None, 0
+        for _ in range(2):
+            ctx.work_counters(reset=True)
+            ctx.flush_l2()
+            ctx.timer_start()
+            C = ga.mxm_masked(algo, A, A, A)
+            t = ctx.timer_stop()
+            C.free()
+            prods = ctx.work_counters(reset=True)["products"]
+            best = t if best is None else min(best, t)
+        rec = {"ms": best, "reference_equivalent_gflops": 2.0 * prods / best / 1e6}
+        if algo != "tri":
+            bm = 8 * (m + 1) + 16 * nnz + 8 * prods + 4 * nnz + 4 * nnz
+            rec["roofline"] = {"bound": "hbm", "achieved": bm / (best * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                               "frac": bm / (best * 1e-3) / 1e9 / peak, "bytes_per_call": bm,
+                               "peak_kind": peak_kind, "traffic": None}
+        mx[algo] = rec
+    out["mxm_rmat20"] = {"product": "C<A> = A*A (the k-truss support), R-MAT scale 20, int32 values",
+                         "gustavson_products": prods, "variants": mx}
     return out
 
 

@@ -756,11 +756,34 @@ struct KtSweep {
         state = DBuf<uint8_t>(ctx, (size_t)cap);
         scan_scr = DBuf<unsigned char>(ctx, scan_scratch_bytes(cap + 1));
         tri_scr = DBuf<unsigned char>(ctx, tri_kt_bytes(m, cap));
-        tri_kt_carve(tri_scr.p, m, cap, &tk);
+        setup_front();
+    }
+
+    // The frontier state on W (its rows partitioned by rank, its mirror
+    // index; the first run lists W's triangles). The buffers keep the size
+    // of the sweep's first matrix; a rebuilt W is smaller.
+    void setup_front() {
+        cap = W->nnz;
+        tri_kt_carve(tri_scr.p, W->m, cap, &tk);
         expand_rows(ctx, W, row_of.p);
         tri_kt_setup(ctx, W, row_of.p, mir.p, tc.p, eflag.p, tk, cap);
         const TriFrontBufs fb{sup.p, eflag.p, tr.p, tc.p, oid.p, f0.p, f1.p, state.p, scan_scr.p};
         front.reset(new TriFront(ctx, W, row_of.p, mir.p, tk, cap, fb, nullptr));
+    }
+
+    // Entries never move inside the state, so once a k-truss keeps at most
+    // half of W's entries the state is rebuilt on it: every per-k pass (the
+    // reseed, the keep flags, the output) then runs over the live entries,
+    // at the price of one listing of the smaller graph.
+    void maybe_rebuild(ga_csr Ck) {
+        if (Ck->nnz == 0 || Ck->nnz * 2 > W->nnz) return;
+        front.reset();
+        ga_csr nw = copy_csr(ctx, Ck, GA_INT32);
+        nw->unit = 1;
+        nw->sym = 1;
+        csr_destroy(ctx, W);
+        W = nw;
+        setup_front();
     }
 
     // The next C_k (owned by the caller), or nullptr after the empty one.
@@ -788,6 +811,7 @@ struct KtSweep {
             }
             out->unit = 1;
             out->sym = 1;
+            maybe_rebuild(out);
         } else {
             ga_csr res = ktruss_impl(ctx, algo, cur, k, &it, nullptr);
             csr_destroy(ctx, cur);
