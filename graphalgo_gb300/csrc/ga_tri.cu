@@ -1076,6 +1076,10 @@ constexpr int kTrifStage = 512;
 // segments of kTrifSeg entries by separate warps (k_trif_lower_seg).
 constexpr int kTrifSplit = 128;
 constexpr int kTrifSeg = 64;
+// Grids of the loop's kernels, per SM: the pruning kernels (128 threads)
+// and the passes over the frontier (256 threads).
+constexpr int kTrifLowerCtas = 8;
+constexpr int kTrifPassCtas = 2;
 
 // A frontier edge (u, v) to walk: the shorter row x, the other row y with
 // its oriented part [yb, yo) and the rest [yo, ye), y's rank, and the
@@ -1633,19 +1637,19 @@ struct TriFront::Impl {
             }
             {
                 ProfScope ps(c, "trif_lower");
-                k_trif_lower<<<sms * 16, 128, 0, c->stream>>>(dargs);
+                k_trif_lower<<<sms * kTrifLowerCtas, 128, 0, c->stream>>>(dargs);
                 post_launch("trif_lower");
-                k_trif_lower_seg<<<sms * 16, 128, 0, c->stream>>>(dargs);
+                k_trif_lower_seg<<<sms * kTrifLowerCtas, 128, 0, c->stream>>>(dargs);
                 post_launch("trif_lower_seg");
             }
             {
                 ProfScope ps(c, "trif_apply");
-                k_trif_apply<<<sms * 4, 256, 0, c->stream>>>(dargs);
+                k_trif_apply<<<sms * kTrifPassCtas, 256, 0, c->stream>>>(dargs);
                 post_launch("trif_apply");
             }
             {
                 ProfScope ps(c, "trif_flip");
-                k_trif_flip<<<sms * 4, 256, 0, c->stream>>>(dargs);
+                k_trif_flip<<<sms * kTrifPassCtas, 256, 0, c->stream>>>(dargs);
                 post_launch("trif_flip");
             }
             ProfScope ps(c, "trif_delta");
