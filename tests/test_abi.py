@@ -46,6 +46,10 @@ def test_null_arguments_are_rejected(built):
     assert L.ga_ctx_create(0, None, None) == ga.ERR_INVALID_ARG
     assert L.ga_csr_free(None, None) == ga.ERR_INVALID_ARG
     assert L.ga_mxm_masked(None, 0, None, None, None, None) == ga.ERR_INVALID_ARG
+    assert L.ga_ktruss_sweep_begin(None, 0, None, 3, None) == ga.ERR_INVALID_ARG
+    assert L.ga_ktruss_sweep_next(None, None, None, None) == ga.ERR_INVALID_ARG
+    assert L.ga_ktruss_sweep_free(None) == ga.OK
+    assert L.ga_csr_set_symmetric(None, None, 1) == ga.ERR_INVALID_ARG
 
 
 def _check_graph(m, rst, col):
