@@ -773,10 +773,11 @@ def run_gpu(args, dist: Dist):
                  "frontier_triangles_per_step": wc["front_triangles"] / args.steps,
                  "note": "value counts 2 x the Gustavson products of the reference's C<C> = C*C for every "
                          "support product of every k (products_per_step): a reference-equivalent rate, not "
-                         "arithmetic executed. The triangle-listing sweep lists the triangles once "
-                         "(wedges_per_step rank-ordered lookups) and then, k after k and iteration after "
-                         "iteration, walks only the triangles of the edges it prunes (frontier_*); the "
-                         "Gustavson forms execute executed_products_per_step products"},
+                         "arithmetic executed. The triangle-listing sweep lists the triangles of A once, and "
+                         "again each time a k-truss keeps at most half of the listed graph's entries "
+                         "(wedges_per_step rank-ordered lookups in all), and otherwise, k after k and "
+                         "iteration after iteration, walks only the triangles of the edges it prunes "
+                         "(frontier_*); the Gustavson forms execute executed_products_per_step products"},
         "kernel_profile": {"note": "one step with host-driven loops and CUDA events per launch (slower than "
                                    "the timed step); summed event time per kernel scope, ms",
                            "top": {k: round(v[1], 3) for k, v in
