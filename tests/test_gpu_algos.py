@@ -510,3 +510,36 @@ def test_declared_symmetry(ctx):
     with pytest.raises(ga.GaError) as e:
         N.set_symmetric(1)
     assert e.value.code == ga.ERR_SHAPE
+
+
+def test_ktruss_sweep_rmat18_matches_oracle_record(ctx):
+    """The benchmark's own workload through ga_ktruss_sweep: R-MAT scale 18
+    (edge factor 16, seed 42), k = 3 ... until empty; every k-truss's
+    iteration count, entry count and BLAKE2b digest of (row starts, columns)
+    equal the oracle's record of the same sweep (tests/golden/rmat18_sweep.json,
+    made by tests/golden/make_sweep.py), and the sweep ends where it ends."""
+    import hashlib
+    import json
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "rmat18_sweep.json")
+    with open(path) as f:
+        rec = json.load(f)
+    g = rec["graph"]
+    m, rst, col = ga.gen_rmat(g["scale"], g["edge_factor"], *g["abc"], seed=g["seed"])
+    assert m == g["vertices"] and len(col) == g["stored_entries"]
+
+    def digest(r, c):
+        h = hashlib.blake2b(digest_size=16)
+        h.update(np.ascontiguousarray(r, "<i4").tobytes())
+        h.update(np.ascontiguousarray(c, "<i4").tobytes())
+        return h.hexdigest()
+
+    assert digest(rst, col) == g["digest"]
+    A = ga.Csr.upload(ctx, m, m, rst, col)
+    got = []
+    for k, C, it in ga.ktruss_sweep("tri", A, 3):
+        z = C.nnz
+        r, c, _ = C.download()
+        C.free()
+        got.append([k, it, z, digest(r, c[:z])])
+    assert got == [list(s) for s in rec["stages"]]
