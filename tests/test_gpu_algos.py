@@ -3,6 +3,8 @@
 TC totals, per-row counts and k-truss edge sets are bit-exact; BC scores
 (FP64) agree within 1e-9 relative (absolute floor 1e-9).
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -543,3 +545,23 @@ def test_ktruss_sweep_rmat18_matches_oracle_record(ctx):
         C.free()
         got.append([k, it, z, digest(r, c[:z])])
     assert got == [list(s) for s in rec["stages"]]
+
+
+def test_bc_rmat20_64_sources_against_oracle(ctx):
+    """Config 3 at its full size: batched BC on R-MAT scale 20 (edge factor
+    16, seed 42) with 64 seeded sources, every score within 1e-9 relative of
+    the FP64 oracle (OpenMP on the host cores), in all three forms of the
+    backward sweep."""
+    m, rst, col = ga.gen_rmat(20, 16, 0.57, 0.19, 0.19, seed=42)
+    G = csr_from_arrays(m, rst, col)
+    src = np.random.default_rng(42).choice(m, 64, replace=False).astype(np.int32)
+    oracle.set_num_threads(os.cpu_count() or 1)
+    ref = oracle.bc_batch(G, src)
+    A = ga.Csr.upload(ctx, m, m, rst, col)
+    A.set_symmetric(1)
+    try:
+        for mode in (0, 1, 2):
+            ctx.set_option(ga.OPT_BC_BACKWARD, mode)
+            _bc_close(ga.bc(A, src), ref)
+    finally:
+        ctx.set_option(ga.OPT_BC_BACKWARD, 0)
