@@ -72,9 +72,9 @@ DRAM_BYTES_PER_ENTRY = {"tri_support": 7.506, "mxm": 4.543}
 # DRAM bytes per pruned edge of the frontier pruning kernels (k_trif_lower +
 # k_trif_lower_seg): dram__bytes_read.sum + dram__bytes_write.sum summed over
 # every launch of one R-MAT 18 sweep (ncu with --cache-control none, so the
-# caches stay warm as in the timed step: 2,983.7 MB) over its 3,805,777
+# caches stay warm as in the timed step: 1,721.0 MB) over its 3,805,777
 # pruned edges (profiles/trif_lower_rmat18_sweep.md).
-DRAM_BYTES_PER_FRONT_EDGE = 784.0
+DRAM_BYTES_PER_FRONT_EDGE = 452.2
 
 
 def parse_args():
