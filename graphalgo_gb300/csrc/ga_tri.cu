@@ -1349,21 +1349,36 @@ __global__ void k_trif_apply(const TriFrontArgs* __restrict__ ap) {
 
 // Rows that lost their last upper entry: h drops to 0, so every remaining
 // neighbour's H loses 1. One warp per row.
+// H(j) loses 1 here directly, and P loses deg(j) (the row length at the
+// iteration's start): k_trif_delta's term for a touched j, computed from
+// this H, then misses exactly that; a j that nothing else touched changes
+// by exactly that. So the flipped rows' neighbours are neither touched nor
+// counted in rh.
 __global__ void k_trif_flip(const TriFrontArgs* __restrict__ ap) {
     const TriFrontArgs a = *ap;
     const int lane = threadIdx.x & 31;
     const int32_t n = a.st->nflip;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    long long d = 0;  // this lane's part of the change of P
     for (int64_t x = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; x < n; x += warps) {
         const int32_t i = a.flip[x];
         if (lane == 0) a.h[i] = 0;
+        long long di = 0;
         for (int32_t p = a.cr[i] + lane; p < a.cr[i + 1]; p += 32) {
             if (a.state[a.oid[p]] == kGone) continue;
             const int32_t j = a.cc[p];
-            atomicAdd(a.rh + j, 1);
-            touch(a, j);
+            atomicSub(a.H + j, 1);
+            di -= a.deg[j];
         }
+        if (a.gid) {
+            // the neighbours of row i are in i's graph
+            const long long gi = warp_sum<long long>(di);
+            if (lane == 0 && gi) atomicAdd(reinterpret_cast<unsigned long long*>(a.pg + a.gid[i]), (unsigned long long)gi);
+        }
+        d += di;
     }
+    d = warp_sum<long long>(d);
+    if (lane == 0 && d) atomicAdd(&a.st->prod, (unsigned long long)d);
 }
 
 // P_{t+1} = P_t + the change of deg(j) H(j) at every touched vertex (for a
