@@ -165,7 +165,9 @@ bool csr_unit_values(ga_ctx ctx, ga_csr A) {
 // Pattern and values symmetric: every (i, j, v) has a (j, i, v). One warp
 // per chunk of 256 consecutive entries (balanced whatever the row lengths):
 // the chunk's first and last rows by binary search of the row starts, each
-// entry's row by a search between them, its mirror by a search of row j.
+// entry's row by a search between them. Only the entries above the diagonal
+// search their mirror (in row j); the entries below it are counted, and the
+// two counts must agree, which halves the searches.
 constexpr int kSymChunk = 256;
 
 template <typename T>
@@ -179,15 +181,30 @@ __global__ void k_check_symmetric(const int32_t* __restrict__ r, const int32_t* 
         const int i0 = upper_bound_i32(r, (int)m + 1, q0) - 1;
         const int i1 = upper_bound_i32(r, (int)m + 1, q1 - 1) - 1;
         bool bad = false;
+        int upper = 0, lower = 0;
         for (int32_t q = q0 + lane; q < q1; q += 32) {
             const int i = i0 + upper_bound_i32(r + i0 + 1, i1 - i0, q);
             const int32_t j = c[q];
             if ((int64_t)j >= m) { bad = true; continue; }
+            if (j < i) {
+                ++lower;
+                continue;
+            }
+            if (j == i) continue;
+            // an entry above the diagonal: its mirror must be there, with the
+            // same value (searched in row j, which for a power-law graph is
+            // usually the shorter row: hubs have the low indices)
+            ++upper;
             const int32_t jb = r[j], jn = r[j + 1] - jb;
             const int pos = lower_bound_i32(c + jb, jn, (int32_t)i);
             if (pos >= jn || c[jb + pos] != (int32_t)i || !(v[jb + pos] == v[q])) bad = true;
         }
         if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flag, 1);
+        // every upper entry has a distinct lower mirror; equal counts then
+        // give every lower entry an upper one
+        upper = warp_sum<int>(upper);
+        lower = warp_sum<int>(lower);
+        if (lane == 0 && upper != lower) atomicAdd(flag + 1, upper - lower);
     }
 }
 
@@ -195,14 +212,18 @@ bool csr_is_symmetric(ga_ctx ctx, ga_csr A) {
     if (A->sym >= 0) return A->sym == 1;
     if (A->m != A->n) return false;
     if (A->nnz == 0) return true;
-    DBuf<int> flag(ctx, 1);
-    GA_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), ctx->stream));
+    // flag[0]: a missing or different mirror; flag[1]: upper minus lower entries
+    DBuf<int> flag(ctx, 2);
+    GA_CUDA(cudaMemsetAsync(flag.p, 0, 2 * sizeof(int), ctx->stream));
     GA_DISPATCH_DTYPE(A->dtype, T, {
         k_check_symmetric<T><<<grid_for((A->nnz + kSymChunk - 1) / kSymChunk * 32, 256, ctx->num_sms * 16), 256, 0,
                                ctx->stream>>>(A->rst, A->col, static_cast<const T*>(A->val), A->m, A->nnz, flag.p);
     });
     post_launch("check_symmetric");
-    A->sym = read_i32(ctx, flag.p) == 0 ? 1 : 0;
+    int h[2];
+    GA_CUDA(cudaMemcpyAsync(h, flag.p, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    GA_CUDA(cudaStreamSynchronize(ctx->stream));
+    A->sym = h[0] == 0 && h[1] == 0 ? 1 : 0;
     return A->sym == 1;
 }
 

@@ -84,6 +84,36 @@ def test_ktruss_dot_needs_symmetric(ctx):
     assert e.value.code == ga.ERR_UNSUPPORTED
 
 
+def test_symmetry_check_cases(ctx):
+    """The device symmetry check searches the mirror of each entry above the
+    diagonal and compares the counts above and below it: a symmetric matrix
+    passes (diagonal entries allowed); an extra entry below the diagonal, an
+    extra entry above it, or one value that differs from its mirror's makes
+    it not symmetric (GA_DOT k-truss refuses it)."""
+    rng = np.random.default_rng(12)
+    from graphs import dense_to_csr
+    D = rng.random((300, 300)) < 0.05
+    D = D | D.T
+    np.fill_diagonal(D, False)
+    D[7, 7] = True
+    V = rng.integers(1, 9, size=(300, 300))
+    V = np.triu(V) + np.triu(V, 1).T
+    i, j = [(a, b) for a, b in zip(*np.nonzero(D)) if a > b][5]
+    lower, upper, val = D.copy(), D.copy(), V.copy()
+    lower[j, i] = False  # (i, j) below the diagonal loses its mirror
+    upper[i, j] = False  # (j, i) above the diagonal loses its mirror
+    val[i, j] += 1
+    G = dense_to_csr(D, V)
+    R, it = oracle.ktruss(G, 3)
+    C, git = ga.ktruss("dot", to_device(ctx, G), 3)
+    r, c, v = C.download()
+    assert git == it and np.array_equal(r, R.rst) and np.array_equal(c, R.col) and np.array_equal(v, R.val)
+    for M, W in ((lower, V), (upper, V), (D, val)):
+        with pytest.raises(ga.GaError) as e:
+            ga.ktruss("dot", to_device(ctx, dense_to_csr(M, W)), 3)
+        assert e.value.code == ga.ERR_UNSUPPORTED
+
+
 def test_ktruss_naive_and_trivial_k(ctx):
     G = csr_from_arrays(*ga.gen_knn(300, 4, 30, seed=9))
     Gd = to_device(ctx, G)
