@@ -23,9 +23,15 @@
 //                 the mask (most products of a k-truss support miss it): a
 //                 bitmap over the window (CTA items) or the 4096-bit hashed
 //                 filter (warp rows);
-//       GA_HEAP : warp-cooperative sorted merge of each B row against the
-//                 mask row (replaces the priority-queue merge,
-//                 matrix_la.h:1030-1084).
+//       GA_HEAP : sorted merge of each B row against the mask row
+//                 (replaces the priority-queue merge,
+//                 matrix_la.h:1030-1084): lanes take 32 A entries; a B row
+//                 with few entries inside the window is merged by its lane,
+//                 a longer one is cut into 32 slices merged by one lane
+//                 each (the mask side gallops), and a B row far longer
+//                 than the mask row is merged by the whole warp, 32
+//                 columns against 32, galloping over the B runs that
+//                 cannot meet the mask.
 //     Work distribution inside a CTA item: warps take the row's A entries 32
 //     at a time; B rows of up to kLongSeg entries (32 when the A row is too
 //     short to occupy every warp) are flattened over the
@@ -425,20 +431,56 @@ __device__ __forceinline__ void stream_row(const MxmArgs<T, A>& p, const SlotVie
     if (jt + lane < j1) add_product<MD, A>(v, acc, __ldg(p.bc + jt + lane), a * bval<VM, T, A>(p, jt + lane));
 }
 
+// First index in [lo, hi) of a sorted array whose value is >= key (hi if
+// none), found by the whole warp with 32 probes per step: the first step
+// probes the ends of the next 32 runs of 32 entries (a short skip costs two
+// steps), later steps split what is left 32 ways. GLOBAL: the array is in
+// global memory (read-only path), else in shared memory. Warp-uniform
+// arguments and result.
+template <bool GLOBAL>
+__device__ __forceinline__ int32_t warp_lower_bound(const int32_t* a, int32_t lo, int32_t hi, int32_t key) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int64_t step = 32;
+    // the answer lies in [lo, hi]; hi itself when every entry below it is < key
+    while (hi - lo > 32) {
+        const int64_t idx = (int64_t)lo + (int64_t)(lane + 1) * step - 1;
+        const bool lt = idx < hi && (GLOBAL ? __ldg(a + idx) : a[idx]) < key;
+        const int cnt = __popc(__ballot_sync(FULL, lt));
+        if (cnt == 32) {
+            lo = (int32_t)min((int64_t)hi, (int64_t)lo + 32 * step);
+        } else {
+            lo = (int32_t)((int64_t)lo + cnt * step);
+            hi = (int32_t)min((int64_t)hi, (int64_t)lo + step - 1);
+        }
+        step = ((int64_t)(hi - lo) + 31) >> 5;
+    }
+    const bool lt = lo + lane < hi && (GLOBAL ? __ldg(a + lo + lane) : a[lo + lane]) < key;
+    return lo + __popc(__ballot_sync(FULL, lt));
+}
+
 // Warp-cooperative sorted merge of B row [bs, be) against the item's sorted
-// mask columns; matches add a*b into the slot accumulator.
+// mask columns; matches add a*b into the slot accumulator. Each step ranks
+// 32 B entries against 32 mask columns; the side whose run ends first moves
+// past what it resolved, and when the entry 64 ahead on that side is still
+// below the other side's first unresolved value, it gallops there by a warp
+// search instead of walking (a hub B row against a short mask row costs a
+// few searches per mask column, not a pass over the hub). Returns the B
+// entries it compared.
 template <typename T, typename A>
-__device__ __forceinline__ void merge_row(const MxmArgs<T, A>& p, int32_t bs, int32_t be, A av, const SlotView& v,
-                                          A* acc) {
+__device__ __forceinline__ int32_t merge_row(const MxmArgs<T, A>& p, int32_t bs, int32_t be, A av,
+                                             const SlotView& v, A* acc) {
     const int lane = threadIdx.x & 31;
     const unsigned FULL = 0xffffffffu;
-    if (bs >= be) return;
-    const int32_t x0 = __ldg(p.bc + bs);
-    int yc = lower_bound_i32(v.mcol, v.ns, x0);
-    int32_t xb = bs;
+    if (bs >= be) return 0;
+    int32_t yc = warp_lower_bound<false>(v.mcol, 0, v.ns, __ldg(p.bc + bs));
+    int32_t xb = bs, seen = 0;
     while (xb < be && yc < v.ns) {
         const int32_t x = (xb + lane < be) ? __ldg(p.bc + xb + lane) : INT32_MAX;
+        const int32_t xp = (xb + 63 < be) ? __ldg(p.bc + xb + 63) : INT32_MAX;  // end of the next B run
         const int32_t y = (yc + lane < v.ns) ? v.mcol[yc + lane] : INT32_MAX;
+        const int32_t yp = (yc + 63 < v.ns) ? v.mcol[yc + 63] : INT32_MAX;  // end of the next mask run
+        seen += min(32, be - xb);
         int r = 0;
 #pragma unroll
         for (int step = 16; step >= 1; step >>= 1) {
@@ -450,11 +492,122 @@ __device__ __forceinline__ void merge_row(const MxmArgs<T, A>& p, int32_t bs, in
         const int32_t yr = __shfl_sync(FULL, y, r & 31);
         if (r < 32 && yr == x && x != INT32_MAX)
             atomic_add_acc<A>(&acc[yc + r], av * to_acc<T, A>(__ldg(p.bv + xb + lane)));
-        // the chunk whose last element is smaller moves on; for B that is its
-        // last stored element (past the row's end the lanes hold INT32_MAX)
+        // the run whose last element is smaller is resolved; for B that is
+        // its last stored element (past the row's end the lanes hold INT32_MAX)
         const int32_t xl = __shfl_sync(FULL, x, min(31, be - 1 - xb));
-        if (xl <= y31) xb += 32; else yc += 32;
+        if (xl <= y31) {
+            // mask columns <= xl are resolved too; yu: the first one above
+            const unsigned gt = __ballot_sync(FULL, y > xl);
+            if (gt == 0u) {
+                xb += 32;
+                yc += 32;
+            } else {
+                const int f = __ffs(gt) - 1;
+                const int32_t yu = __shfl_sync(FULL, y, f);
+                yc += f;
+                xb = xp < yu ? warp_lower_bound<true>(p.bc, xb + 64, be, yu) : xb + 32;
+            }
+        } else {
+            // B entries <= y31 are resolved; xu: the first one above
+            const int g = __ffs(__ballot_sync(FULL, x > y31)) - 1;
+            const int32_t xu = __shfl_sync(FULL, x, g);
+            xb += g;
+            yc = yp < xu ? warp_lower_bound<false>(v.mcol, yc + 64, v.ns, xu) : yc + 32;
+        }
     }
+    return seen;
+}
+
+// One lane's sorted merge of B row [bs, be) against the mask columns: a
+// binary search places the first B column, then the mask position gallops
+// (doubling steps, then a binary search) to the first column >= each next
+// B column.
+template <typename T, typename A>
+__device__ __forceinline__ void lane_merge(const MxmArgs<T, A>& p, int32_t bs, int32_t be, A av, const SlotView& v,
+                                           A* acc) {
+    const int32_t* mc = v.mcol;
+    const int32_t ns = v.ns;
+    int32_t xn = __ldg(p.bc + bs);
+    int32_t yc = lower_bound_i32(mc, ns, xn);
+    if (yc >= ns) return;
+    for (int32_t j = bs; j < be; ++j) {
+        const int32_t x = xn;
+        if (j + 1 < be) xn = __ldg(p.bc + j + 1);
+        if (mc[yc] < x) {
+            int32_t b = 1;
+            while (yc + b < ns && mc[yc + b] < x) b <<= 1;
+            // mc[yc + b/2] < x; mc[yc + b] >= x unless past the end
+            int32_t lo = yc + (b >> 1) + 1, hi = min(ns, yc + b);
+            while (lo < hi) {
+                const int32_t mid = (lo + hi) >> 1;
+                if (mc[mid] < x) lo = mid + 1; else hi = mid;
+            }
+            yc = lo;
+            if (yc >= ns) break;
+        }
+        if (mc[yc] == x) atomic_add_acc<A>(&acc[yc], av * to_acc<T, A>(__ldg(p.bv + j)));
+    }
+}
+
+// The lane's share of B entries [j0, j1) cut into 32 contiguous slices,
+// merged against the mask by one lane each.
+template <typename T, typename A>
+__device__ __forceinline__ void merge_slices(const MxmArgs<T, A>& p, int32_t j0, int32_t j1, A av, const SlotView& v,
+                                             A* acc) {
+    const int32_t per = (j1 - j0 + 31) >> 5;
+    const int32_t s0 = j0 + (threadIdx.x & 31) * per, s1 = min(j1, s0 + per);
+    if (s0 < s1) lane_merge<T, A>(p, s0, s1, av, v, acc);
+}
+
+// Merge variant, 32 A entries at a time (lane l takes entry t0 + l). A B
+// row whose part inside [lo, hi] has at most kLaneMerge entries is merged by
+// its own lane. In a CTA item (PUSH) one with more than kMergePiece entries
+// is listed for the CTA, which cuts it into pieces that all warps share.
+// The others are merged by the whole warp afterwards, one at a time: cut
+// into 32 slices (merge_slices); or, when a B row is more than kMergeRatio
+// times longer than the mask row, by the warp-cooperative merge (which
+// gallops over the long B row). Returns the B entries compared
+// (warp-uniform; listed rows are counted where their pieces are merged).
+constexpr int kLaneMerge = 8;
+constexpr int kMergeRatio = 8;
+constexpr int kMergePiece = 256;
+template <typename T, typename A, bool PUSH>
+__device__ __forceinline__ int64_t merge_group(const MxmArgs<T, A>& p, int32_t t0, int32_t ae, bool clip,
+                                               const SlotView& v, A* acc, int* s_nlong, int32_t* s_lbs,
+                                               int32_t* s_lend, A* s_la) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int32_t t = t0 + lane;
+    int32_t bs = 0, be = 0;
+    A av = (A)0;
+    if (t < ae) {
+        b_range(p, t, clip, v.lo, v.hi, bs, be);
+        av = to_acc<T, A>(__ldg(p.av + t));
+        if (PUSH && be - bs > kMergePiece) {
+            const int slot = atomicAdd(s_nlong, 1);
+            if (slot < kLongCap) {
+                s_lbs[slot] = bs;
+                s_lend[slot] = be;
+                s_la[slot] = av;
+                be = bs;
+            }
+        }
+    }
+    const bool wide = be - bs > kLaneMerge;
+    if (!wide && bs < be) lane_merge<T, A>(p, bs, be, av, v, acc);
+    int64_t seen = warp_sum<int64_t>(wide ? 0 : be - bs);
+    for (unsigned w = __ballot_sync(FULL, wide); w; w &= w - 1) {
+        const int l = __ffs(w) - 1;
+        const int32_t s = __shfl_sync(FULL, bs, l), e = __shfl_sync(FULL, be, l);
+        const A a = __shfl_sync(FULL, av, l);
+        if ((int64_t)v.ns * kMergeRatio < (int64_t)(e - s)) {
+            seen += merge_row<T, A>(p, s, e, a, v, acc);
+        } else {
+            merge_slices<T, A>(p, s, e, a, v, acc);
+            seen += e - s;
+        }
+    }
+    return seen;
 }
 
 // Shared-memory layout per variant (MD of the CTA phase: MD_DENSE for MSA).
@@ -558,12 +711,13 @@ __global__ void __launch_bounds__(kMxmThreads, 3) k_mxm_masked(MxmArgs<T, A> p) 
             const bool clip = ns < mi || p.mre != nullptr;
             const int32_t ab = p.ar[i], ae = p.ar[i + 1];
             if (MD == MD_MERGE) {
-                for (int32_t t = ab + wid; t < ae; t += kMxmWarps) {
-                    int32_t bs, be;
-                    b_range(p, t, clip, v.lo, v.hi, bs, be);
-                    merge_row<T, A>(p, bs, be, to_acc<T, A>(__ldg(p.av + t)), v, acc);
-                    executed += (unsigned long long)(be - bs);
-                }
+                // phase A: groups of up to 32 A entries, small enough that
+                // every warp gets one when the row is short; B rows longer
+                // than kMergePiece listed
+                const int32_t gsz = min(32, (ae - ab + kMxmWarps - 1) / kMxmWarps);
+                for (int32_t g = ab + wid * gsz; g < ae; g += kMxmWarps * gsz)
+                    executed += (unsigned long long)merge_group<T, A, true>(p, g, min(ae, g + gsz), clip, v, acc,
+                                                                            &s_nlong, lbs, lend, la);
             } else {
                 // phase A: short B rows flattened per warp, long ones listed
                 // (an A row too short to give every warp 32 entries lists
@@ -572,7 +726,9 @@ __global__ void __launch_bounds__(kMxmThreads, 3) k_mxm_masked(MxmArgs<T, A> p) 
                 for (int32_t g = ab + wid * 32; g < ae; g += kMxmWarps * 32)
                     executed += (unsigned long long)group_products<MD, VM, T, A, true>(
                         p, g, ae, clip, v, acc, s_incl, s_off, s_a, &s_nlong, lbs, lend, la, long_seg);
-                __syncthreads();
+            }
+            __syncthreads();
+            {
                 // phase B: long B rows cut into kChunk pieces shared by all warps
                 const int nlong = min(s_nlong, kLongCap);
                 if (nlong > 0) {
@@ -601,7 +757,8 @@ __global__ void __launch_bounds__(kMxmThreads, 3) k_mxm_masked(MxmArgs<T, A> p) 
                         const int seg = upper_bound_i32(lchunk + 1, nlong, c);
                         const int32_t j0 = lbs[seg] + (c - lchunk[seg]) * kChunk;
                         const int32_t j1 = min(lend[seg], j0 + kChunk);
-                        stream_row<MD, VM, T, A>(p, v, acc, j0, j1, la[seg]);
+                        if (MD == MD_MERGE) merge_slices<T, A>(p, j0, j1, la[seg], v, acc);
+                        else stream_row<MD, VM, T, A>(p, v, acc, j0, j1, la[seg]);
                         executed += (unsigned long long)(j1 - j0);
                     }
                 }
@@ -663,12 +820,9 @@ __global__ void __launch_bounds__(kMxmThreads, 3) k_mxm_masked(MxmArgs<T, A> p) 
             __syncwarp();
             const int32_t ab = p.ar[i], ae = p.ar[i + 1];
             if (MD == MD_MERGE) {
-                for (int32_t t = ab; t < ae; ++t) {
-                    int32_t bs, be;
-                    b_range(p, t, clip, v.lo, v.hi, bs, be);
-                    merge_row<T, A>(p, bs, be, to_acc<T, A>(__ldg(p.av + t)), v, acc);
-                    executed += (unsigned long long)(be - bs);
-                }
+                for (int32_t g = ab; g < ae; g += 32)
+                    executed += (unsigned long long)merge_group<T, A, false>(p, g, ae, clip, v, acc, nullptr,
+                                                                             nullptr, nullptr, nullptr);
             } else {
                 for (int32_t g = ab; g < ae; g += 32)
                     executed += (unsigned long long)group_products<WMD, VM, T, A, false>(
