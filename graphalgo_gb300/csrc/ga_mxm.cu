@@ -521,31 +521,42 @@ __device__ __forceinline__ int32_t merge_row(const MxmArgs<T, A>& p, int32_t bs,
 // One lane's sorted merge of B row [bs, be) against the mask columns: a
 // binary search places the first B column, then the mask position gallops
 // (doubling steps, then a binary search) to the first column >= each next
-// B column.
+// B column. B columns are loaded four at a time, the next four while the
+// current ones are merged.
 template <typename T, typename A>
 __device__ __forceinline__ void lane_merge(const MxmArgs<T, A>& p, int32_t bs, int32_t be, A av, const SlotView& v,
                                            A* acc) {
     const int32_t* mc = v.mcol;
     const int32_t ns = v.ns;
-    int32_t xn = __ldg(p.bc + bs);
-    int32_t yc = lower_bound_i32(mc, ns, xn);
+    int32_t xn[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) xn[q] = bs + q < be ? __ldg(p.bc + bs + q) : INT32_MAX;
+    int32_t yc = lower_bound_i32(mc, ns, xn[0]);
     if (yc >= ns) return;
-    for (int32_t j = bs; j < be; ++j) {
-        const int32_t x = xn;
-        if (j + 1 < be) xn = __ldg(p.bc + j + 1);
-        if (mc[yc] < x) {
-            int32_t b = 1;
-            while (yc + b < ns && mc[yc + b] < x) b <<= 1;
-            // mc[yc + b/2] < x; mc[yc + b] >= x unless past the end
-            int32_t lo = yc + (b >> 1) + 1, hi = min(ns, yc + b);
-            while (lo < hi) {
-                const int32_t mid = (lo + hi) >> 1;
-                if (mc[mid] < x) lo = mid + 1; else hi = mid;
-            }
-            yc = lo;
-            if (yc >= ns) break;
+    for (int32_t j = bs; j < be; j += 4) {
+        int32_t x[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            x[q] = xn[q];
+            xn[q] = j + 4 + q < be ? __ldg(p.bc + j + 4 + q) : INT32_MAX;
         }
-        if (mc[yc] == x) atomic_add_acc<A>(&acc[yc], av * to_acc<T, A>(__ldg(p.bv + j)));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (j + q >= be) break;
+            if (mc[yc] < x[q]) {
+                int32_t b = 1;
+                while (yc + b < ns && mc[yc + b] < x[q]) b <<= 1;
+                // mc[yc + b/2] < x; mc[yc + b] >= x unless past the end
+                int32_t lo = yc + (b >> 1) + 1, hi = min(ns, yc + b);
+                while (lo < hi) {
+                    const int32_t mid = (lo + hi) >> 1;
+                    if (mc[mid] < x[q]) lo = mid + 1; else hi = mid;
+                }
+                yc = lo;
+                if (yc >= ns) return;
+            }
+            if (mc[yc] == x[q]) atomic_add_acc<A>(&acc[yc], av * to_acc<T, A>(__ldg(p.bv + j + q)));
+        }
     }
 }
 
