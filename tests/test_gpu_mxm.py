@@ -90,6 +90,24 @@ def test_masked_long_rows_and_hubs(ctx, algo):
     assert np.array_equal(C.download()[2], ref)
 
 
+def test_masked_support_rmat18_all_variants(ctx):
+    """The bench's support product C<A> = A*A on R-MAT 18 (edge factor 16,
+    seed 42: rows of up to 25,000 entries, so CTA items over several windows,
+    hub B rows and warp rows all occur), with unit values and with values
+    1..3: every variant equal to the oracle."""
+    m, rst, col = ga.gen_rmat(18, 16, seed=42)
+    rng = np.random.default_rng(18)
+    for vals in (np.ones(len(col), np.int32), rng.integers(1, 4, len(col)).astype(np.int32)):
+        A = oracle.Csr(m, m, rst, col, vals)
+        ref = oracle.mxm_masked(A, A, A)
+        Ad = to_device(ctx, A)
+        algos = ["msa", "mca", "heap", "dot", "hybrid"] + (["tri"] if vals[0] == 1 and np.all(vals == 1) else [])
+        for algo in algos:
+            C = ga.mxm_masked(algo, Ad, Ad, Ad)
+            assert np.array_equal(C.download()[2], ref), algo
+            C.free()
+
+
 @pytest.mark.parametrize("algo", ALGOS)
 def test_masked_square_graphs(ctx, algo):
     rng = np.random.default_rng(21)
