@@ -4,10 +4,10 @@ It serves callers that cannot allocate device memory when they need the
 product (applications that keep all device memory in their own arena,
 latency-critical callers that cannot accept the device synchronisation of
 cudaMalloc / cudaFree): they pass device buffers for everything and the
-kernel's scratch lives in a fixed array inside the library. This
-test calls it through the C ABI twice in a row, on the same shared scratch,
-and compares each result with the allocating entry point's
-(ga_mxm_masked), exactly - the values are integers.
+kernel's scratch lives in a fixed array inside the library. These
+tests call it through the C ABI twice in a row, on the same shared scratch,
+and inside a captured CUDA graph, and compare each result with the
+allocating entry point's (ga_mxm_masked), exactly - the values are integers.
 """
 import ctypes
 
@@ -94,3 +94,32 @@ def test_noalloc_rejects_missing_arrays(ctx):
     assert call(ga.HEAP, ac, ac, None) == ga.ERR_INVALID_ARG
     assert call(ga.MSA, None, ac, av) == ga.ERR_INVALID_ARG
     assert call(ga.MSA, ac, None, av) == ga.ERR_INVALID_ARG
+
+
+def test_noalloc_captured_in_a_cuda_graph(ctx):
+    """After one eager call (the per-device setup), the call is captured into
+    a CUDA graph on a caller's stream (nothing in it allocates or
+    synchronises, which capture refuses); the graph, replayed twice into an
+    output reset before each replay, gives ga_mxm_masked's values."""
+    torch = pytest.importorskip("torch")
+    m, rst, col = ga.gen_rmat(11, 16, seed=33)
+    A = ga.Csr.upload(ctx, m, m, rst, col)
+    expected = ga.mxm_masked(ga.MSA, A, A, A).download()[2]
+    nnz = A.nnz
+    out = torch.full((nnz,), -7, dtype=torch.int32, device="cuda")
+    s = torch.cuda.Stream()
+    ctx.sync()
+    torch.cuda.synchronize()
+    assert _noalloc(s.cuda_stream, ga.MSA, m, m, m, A, A, A, nnz, ga.INT32, 1, out.data_ptr()) == ga.OK
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), expected)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        rc = _noalloc(s.cuda_stream, ga.MSA, m, m, m, A, A, A, nnz, ga.INT32, 1, out.data_ptr())
+    assert rc == ga.OK
+    for _ in range(2):
+        out.fill_(-7)
+        torch.cuda.synchronize()
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy(), expected)
