@@ -54,7 +54,8 @@ typedef enum {
 typedef enum {
     GA_MSA = 0,   /* mxmm_msa,   include/matrix_la.h:700-749 */
     GA_MCA = 1,   /* mxmm_mca,   include/matrix_la.h:586-641 */
-    GA_HEAP = 2,  /* mxmm_heap,  include/matrix_la.h:1013-1084 (a warp-cooperative sorted merge here) */
+    GA_HEAP = 2,  /* mxmm_heap,  include/matrix_la.h:1013-1084 (sorted merges of B rows with the mask row
+                     here: by a lane, by 32 lanes over slices, or by the whole warp, galloping) */
     GA_NAIVE = 3, /* mxmm_naive, include/matrix_la.h:1139-1277 */
     GA_DOT = 4,   /* inner-product form: each mask entry (i,j) is A_i . (B^T)_j by warp
                      sorted-list intersection (B^T built on the fly unless B is
@@ -160,7 +161,9 @@ GA_API int ga_ctx_mem_stats(ga_ctx ctx, int64_t* in_use, int64_t* peak, int rese
  * (i,k) of nnz(B_k) (the work of the reference's C<M> = A*B), mask entries,
  * launches, A entries, rows, and the products the kernels actually processed
  * (fewer than P when a k-truss support product only evaluates the upper
- * triangle of a symmetric matrix and mirrors it), and the list entries the
+ * triangle of a symmetric matrix and mirrors it; for HEAP the B entries its
+ * merges compared, the galloping merges skipping runs that cannot meet the
+ * mask), and the list entries the
  * inner-product intersections walked (DOT, and the hybrid form's
  * inner-product rows), and for GA_TRI the wedges it looked up and the
  * triangles it found; for the frontier k-truss (GA_TRI, after its one
